@@ -1,0 +1,341 @@
+"""Benchmark: lnL evaluations per second of the DNA GTR+Gamma4 workload
+(128 taxa, Yule tree with Exp(mean 0.05) branch lengths, 100,000 sites, 2% of
+tip cells missing) on one GB300, FP32 partials with per-site scaling.
+
+A step is one full likelihood evaluation through the C ABI: P(t) for every
+edge and category (FP64 eigen form), the post-order pass over all sites and
+the compensated reduction of the site log-likelihoods to one number.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+Prints one JSON line.  Multi-GPU runs (torchrun, one rank per GPU) are
+independent replicas of the workload: the path does not shard within one
+evaluation here, so there is no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "cfg2"
+SEED = 2
+FALLBACK_HBM_GBS = 6800.0
+FALLBACK_BF16_TFLOPS = 1900.0
+SM_COUNT = 152
+FP32_LANES_PER_SM = 128
+
+
+def algorithmic_bytes_per_site(n_tips: int, S: int, C: int, b: int) -> int:
+    """Bytes one lnL evaluation must move per site in a level-by-level pass:
+    internal-child partials read, 1-byte tip codes, each internal node's
+    partials written plus a 4-byte scaler."""
+    n_int = n_tips - 1
+    internal_child_edges = n_int - 1
+    return internal_child_edges * S * C * b + n_tips * 1 + n_int * (S * C * b + 4)
+
+
+def algorithmic_flops_per_site(n_tips: int, S: int, C: int) -> int:
+    """2 flops per multiply-add of every internal-child P(t) product, plus the
+    per-node combine; tip children are table look-ups."""
+    n_int = n_tips - 1
+    return (n_int - 1) * 2 * C * S * S + n_int * C * S
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return FALLBACK_HBM_GBS, FALLBACK_BF16_TFLOPS, "fallback"
+
+
+def load_traffic():
+    """DRAM bytes per launch of the post-order kernel from the committed ncu
+    summary of this workload (None when no capture has been summarised)."""
+    p = os.path.join(ROOT, "profiles", "prune4_dna_gtr_g4_128x100k.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                rows.append((float(f[0]), float(f[1]), f[3:7]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_port_seconds(w, n_sites_sample: int, threads: int) -> float:
+    """The oracle port of the reference path on a bounded sample of sites:
+    P(t) rebuilt by Taylor-plus-20-squarings for every (site, edge,
+    category), as simpleML::branch_likelihood does."""
+    from oracle import oracle as O
+    teff = O.effective_lengths(w.left, w.right, w.bl, root_dist0=1e-30)
+    t0 = time.perf_counter()
+    O.loglik(w.left, w.right, np.ascontiguousarray(w.masks[:, :n_sites_sample]), teff, w.Q, w.freqs,
+             w.cat_rates, w.cat_weights, p_mode=O.P_TAYLOR20, per_site_pmat=True, threads=threads)
+    return time.perf_counter() - t0
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("PLK_BENCH_GLOO") is None else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(world, x: float, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU path on the host cores: the oracle port (the
+    reference's sources do not travel to the GPU host) on all threads, each
+    step a bounded sample of the same workload."""
+    if rank != 0:
+        return
+    from phylommand_gb300 import synth
+    w = synth.make(WORKLOAD, seed=SEED)
+    threads = os.cpu_count() or 1
+    sample = max(threads * 40, 256)
+    for _ in range(args.warmup):
+        cpu_port_seconds(w, sample, threads)
+    secs = [cpu_port_seconds(w, sample, threads) for _ in range(args.steps)]
+    per_eval = (sum(secs) / len(secs)) * (w.n_sites / sample)
+    value = 1.0 / per_eval
+    line = {
+        "impl": "reference", "metric": "lnL evals/s", "value": value, "unit": "evals/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(w),
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} of {w.n_sites} sites per step, {threads} threads, P(t) rebuilt per "
+                                   f"(site, edge, category) by the reference's Taylor-plus-20-squarings; "
+                                   f"time scaled linearly to all sites"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gsite_node_updates_per_s": value * (w.n_tips - 1) * w.n_sites / 1e9,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(w):
+    return {"workload": "DNA GTR+Gamma4, 128-taxon Yule tree, 100,000 sites, 2% missing cells",
+            "n_taxa": w.n_tips, "n_sites": w.n_sites, "n_states": w.n_states, "n_categories": len(w.cat_rates),
+            "alpha": w.alpha, "branch_lengths": "Exp(mean 0.05)", "seed": w.seed,
+            "p_matrix": "FP64 eigen form", "partials": "FP32, per-site power-of-two scaling",
+            "site_sum": "FP64 compensated", "parallelism": "replicas"}
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from phylommand_gb300 import plk, synth
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = synth.make(WORKLOAD, seed=SEED)
+    h = plk.Handle(local)
+    h.set_alignment(w.masks, w.n_states)
+    h.set_tree(w.left, w.right, w.bl)
+    h.set_rate_model(False)
+    h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
+    stream = torch.cuda.Stream(device=dev)
+    h.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # larger than the 129 MB L2
+
+    lnl64 = h.loglik(plk.PLK_FP64)
+    for _ in range(max(args.warmup, 3)):
+        h.loglik_async(plk.PLK_FP32S)
+    lnl32 = h.loglik_result()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    h.set_profiling(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[k].record(stream)
+        h.loglik_async(plk.PLK_FP32S)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    kern_ms, n_evals = h.kernel_times(reset=True)
+    h.set_profiling(False)
+    lnl_timed = h.loglik_result()
+    max_ms = reduce_max(world, dev_ms, dev)
+    value = world * args.steps / (max_ms / 1e3)
+
+    # end to end through the C ABI with host buffers: upload the alignment,
+    # tree and model from pinned host memory, evaluate, read the lnL back
+    h.set_stream(None)
+    pinned = torch.empty(w.masks.shape, dtype=torch.int32, pin_memory=True)
+    masks_pinned = pinned.numpy().view(np.uint32)
+    masks_pinned[...] = w.masks
+    h2d = masks_pinned.nbytes + w.left.nbytes + w.right.nbytes + w.bl.nbytes + w.Q.nbytes + w.freqs.nbytes \
+        + w.cat_rates.nbytes + w.cat_weights.nbytes
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(2):
+        h.set_alignment(masks_pinned, w.n_states)
+        h.loglik(plk.PLK_FP32S)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h.set_alignment(masks_pinned, w.n_states)
+        h.set_tree(w.left, w.right, w.bl)
+        h.set_rate_model(False)
+        h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
+        lnl_e2e = h.loglik(plk.PLK_FP32S)
+    e2e_s = reduce_max(world, time.perf_counter() - t0, dev)
+    e2e_value = world * e2e_steps / e2e_s
+    h.close()
+
+    if rank != 0:
+        return
+    hbm_peak, _, peak_src = load_peaks()
+    bytes_per_launch = algorithmic_bytes_per_site(w.n_tips, w.n_states, len(w.cat_rates), 4) * w.n_sites
+    flops_per_launch = algorithmic_flops_per_site(w.n_tips, w.n_states, len(w.cat_rates)) * w.n_sites
+    prune_ms = kern_ms[1] / max(n_evals, 1)
+    achieved = bytes_per_launch / (prune_ms / 1e3) / 1e9
+    fp32_peak_mhz = clk["sm_max_mhz"] if clk else 2070.0
+    fp32_peak = SM_COUNT * FP32_LANES_PER_SM * 2 * fp32_peak_mhz * 1e6 / 1e12
+    fp32_achieved = flops_per_launch / (prune_ms / 1e3) / 1e12
+
+    # CPU baseline: the reference's algorithm (oracle port), one core, on a
+    # bounded sample of this workload
+    sample = 1200
+    cpu_s = cpu_port_seconds(w, sample, 1)
+    cpu_value = 1.0 / (cpu_s * w.n_sites / sample)
+
+    # error of the timed FP32 result against the FP64 oracle
+    from oracle import oracle as O
+    teff = plk.effective_lengths(w.left, w.right, w.bl, False)
+    orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights, p_mode=O.P_EXACT,
+                   threads=os.cpu_count() or 1)
+    line = {
+        "metric": "lnL evals/s", "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded simulation of the workload's shapes)",
+        "config": {**workload_config(w), "l2": "flushed before every step (256 MiB write, outside the events)"},
+        "gsite_node_updates_per_s": value * (w.n_tips - 1) * w.n_sites / 1e9,
+        "wall_s_timed_region": wall,
+        "kernel_ms_per_eval": {"pmat": kern_ms[0] / max(n_evals, 1), "postorder": prune_ms,
+                               "reduce": kern_ms[2] / max(n_evals, 1)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": load_traffic(),
+                     "kernel": "prune4_kernel (post-order pass)",
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "peak_source": peak_src,
+                     "note": "algorithmic bytes of a level-by-level pass; this kernel keeps partials on chip"},
+        "roofline_fp32": {"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                          "frac": fp32_achieved / fp32_peak,
+                          "peak_source": f"derived: {SM_COUNT} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
+                                         f"{fp32_peak_mhz:.0f} MHz"},
+        "cpu_baseline": {"value": cpu_value, "unit": "evals/s", "cores": 1, "kind": "port",
+                         "sample": f"{sample} of {w.n_sites} sites, P(t) rebuilt per (site, edge, category) by the "
+                                   f"reference's Taylor-plus-20-squarings, scaled linearly to all sites"},
+        "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 12,
+                "path": "plk_set_alignment + plk_set_tree + plk_set_rate_model + plk_set_model + plk_loglik"},
+        "gpu_launches": 3 * args.steps,
+        "error_vs_fp64_oracle": {"abs": abs(lnl_timed - orc.lnl), "rel": abs(lnl_timed - orc.lnl) / abs(orc.lnl),
+                                 "fp64_engine_rel": abs(lnl64 - orc.lnl) / abs(orc.lnl),
+                                 "e2e_rel": abs(lnl_e2e - orc.lnl) / abs(orc.lnl)},
+        "clocks": clk,
+    }
+    del lnl32
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    world, rank, local = (1, 0, 0) if args.impl == "reference" else dist_setup(args.gpus)
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,185 @@
+/* plk.h — C ABI of the GB300 phylogenetic likelihood engine (libplk.so).
+ *
+ * The engine replaces the likelihood path of phylommand's treeator:
+ *   simpleML::set_char            src/simpleML.h:41-57           -> plk_set_alignment
+ *   tree::tree_file_parser result src/tree.cpp:69-237            -> plk_set_tree
+ *   rate_model (time slices, clade rates)
+ *                                 src/rate_model.cpp:103-127,
+ *                                 src/rate_model.h:64-67         -> plk_set_rate_model
+ *   sub_model Q / P(t)            src/sub_model.cpp:99-127,
+ *                                 src/marth/marth.cpp:129-140    -> plk_q_matrix, plk_set_model
+ *   simpleML::calculate_log_likelihood
+ *                                 src/simpleML.h:58-90,
+ *                                 src/simpleML.cpp:127-197       -> plk_loglik
+ *   simpleML::get_log_likelihood_from_root
+ *                                 src/simpleML.h:123-141         -> plk_loglik, plk_site_loglik
+ *   simpleML::draw_normalized_likelihood_on_nodes
+ *                                 src/simpleML.cpp:199-231       -> plk_node_states
+ *   opt_function (the NLopt objective)
+ *                                 src/treeator.cpp:1122-1129     -> plk_loglik per call
+ *
+ * Conventions
+ *  - All arrays are caller-owned host memory, copied in on every plk_set_*;
+ *    the handle owns every device buffer.  No device pointer escapes.
+ *  - Every entry point returns a plk_status (0 = success, negative = error)
+ *    and never throws; plk_last_error() gives the message of the last failure.
+ *  - A handle is used from one host thread at a time (as the reference's
+ *    simpleML object is); several handles may coexist, each on its own stream.
+ *  - Tree: nodes 0..n_tips-1 are the tips, tip i being row i of the alignment;
+ *    left[v] / right[v] are child ids or -1.  The root is the one node that is
+ *    nobody's child.  branch_length[v] is the length of the edge above v.
+ *    A node with one child follows the reference: its vector is the child's
+ *    transported vector.
+ *  - State sets: bit s of a mask means state s is allowed (the reference's
+ *    bitset<24>); a gap or unknown is the all-states mask.
+ */
+#ifndef PLK_H
+#define PLK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLK_API_VERSION 1
+
+typedef struct plk_handle plk_handle;
+typedef int plk_status;
+
+/* status codes */
+#define PLK_OK 0
+#define PLK_ERR_ARG (-1)      /* bad argument (sizes, ids, values) */
+#define PLK_ERR_ALLOC (-2)    /* device or host allocation failed */
+#define PLK_ERR_CUDA (-3)     /* a CUDA call failed */
+#define PLK_ERR_STATE (-4)    /* call order: e.g. plk_loglik before plk_set_tree */
+#define PLK_ERR_TIMEOUT (-5)  /* a bounded device wait gave up */
+#define PLK_ERR_NUMERIC (-6)  /* non-finite likelihood */
+#define PLK_ERR_TIP (-7)      /* a tip cell allows no state (simpleML::check_nodes) */
+#define PLK_ERR_NODEV (-8)    /* no CUDA device */
+#define PLK_ERR_UNSUPPORTED (-9)
+
+/* arithmetic of the partial vectors */
+#define PLK_FP64 0   /* plain: FP64 partials, reference operation order */
+#define PLK_FP32S 1  /* fast: FP32 partials, per-site power-of-two scaling,
+                        FP64 P(t), scaler logs and compensated site sum */
+
+/* construction of P(t) = exp(Q t) */
+#define PLK_P_TAYLOR20 0 /* the reference's (I + Q t / 2^20)^(2^20),
+                            src/marth/marth.cpp:129-140, same operation order */
+#define PLK_P_EXACT 1    /* exp(Q t): eigendecomposition for a reversible Q
+                            (FP64 Jacobi on the host, FP64 P on the device),
+                            scaling and squaring for a non-reversible Q */
+
+/* node-state outputs */
+#define PLK_NODES_COND 0     /* per site, sum_k w_k L_k[s] / sum over s of the
+                                post-order conditional vector (the intent of
+                                simpleML::draw_normalized_likelihood_on_nodes) */
+#define PLK_NODES_MARGINAL 1 /* per site, normalised marginal posterior from a
+                                pre-order pass (absent in the reference) */
+
+/* ---- handle ------------------------------------------------------------ */
+/* Create a handle on CUDA device `device`. */
+plk_status plk_create(plk_handle** out, int device);
+/* Free the handle and every device buffer it owns.  NULL is accepted. */
+void plk_destroy(plk_handle* h);
+/* Message of the last failed call on h (or of the last failed plk_create
+ * when h is NULL).  Valid until the next call on h. */
+const char* plk_last_error(const plk_handle* h);
+const char* plk_status_string(plk_status s);
+int plk_api_version(void);
+
+/* ---- inputs ------------------------------------------------------------ */
+/* Alignment: masks[tip * n_sites + site], bit s = state s allowed;
+ * 1 <= n_states <= 24 (the reference's bitset<SIZE=24>, src/constants.h:25).
+ * Replaces simpleML::set_char for every (tip, site). */
+plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states,
+                             const uint32_t* masks);
+
+/* Tree topology and raw branch lengths (see the conventions above). */
+plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* right,
+                        const double* branch_length);
+
+/* Branch-length modifiers of rate_model (src/rate_model.cpp:103-127), applied
+ * on the host to give the effective length of every edge as
+ * simpleML::calculate_likelihood does (src/simpleML.cpp:127-184):
+ *   t_eff(v) = time_mod(bl(v), (float)dist(parent)) * clade_rate(clade of parent)
+ * root_quirk = 1 reproduces the reference exactly: the recursion starts at a
+ * root distance of 0, so every edge whose parent lies at distance 0 (the two
+ * root-child edges at least) gets length 0.  root_quirk = 0 gives every edge
+ * its own length.  n_cut time slices: cut_off[i] (ascending), cut_rate[i].
+ * clade_of_node[v] >= 0 marks v as MRCA of clade number clade_of_node[v]
+ * (may be NULL); clade_rate[c] for c < n_clades.  Default after plk_set_tree:
+ * root_quirk = 1, no slices, no clades. */
+plk_status plk_set_rate_model(plk_handle* h, int root_quirk, int n_cut, const float* cut_off,
+                              const float* cut_rate, const int* clade_of_node, int n_clades,
+                              const float* clade_rate);
+
+/* Substitution model.  Q is row-major n_states x n_states (rows sum to 0);
+ * root_weights[s] weights the root vector (the frequencies for a reversible
+ * model, all 1 for a non-reversible one, src/simpleML.h:128-135).  For
+ * reversible = 1 and p_mode = PLK_P_EXACT, Q must satisfy
+ * root_weights[i] Q[i][j] = root_weights[j] Q[j][i].  Rate categories: n_cats
+ * rates r_k multiply every effective length; weights w_k mix the site
+ * likelihoods.  n_cats = 1, r = w = 1 is the reference's model. */
+plk_status plk_set_model(plk_handle* h, int n_states, const double* Q,
+                         const double* root_weights, int reversible, int n_cats,
+                         const double* cat_rates, const double* cat_weights, int p_mode);
+
+/* ---- evaluation ---------------------------------------------------------- */
+/* Total log-likelihood (sites summed with a compensated sum).  Builds P(t)
+ * for every edge and category on the device, runs the post-order pass, and
+ * reduces on the device; one device-to-host copy of 8 bytes. */
+plk_status plk_loglik(plk_handle* h, int precision, double* lnl_out);
+/* plk_loglik split in two: enqueue the whole evaluation on the handle's
+ * stream without waiting, then fetch (waits for the stream).  Lets a caller
+ * overlap host work with the device or queue evaluations back to back. */
+plk_status plk_loglik_async(plk_handle* h, int precision);
+plk_status plk_loglik_result(plk_handle* h, double* lnl_out);
+/* Run the handle's work on an existing CUDA stream (a cudaStream_t passed as
+ * void*); NULL returns to the handle's own stream. */
+plk_status plk_set_stream(plk_handle* h, void* cuda_stream);
+/* Kernel timing: with profiling on, every evaluation records CUDA events on
+ * the handle's stream around its P(t), post-order and reduction kernels.
+ * plk_kernel_times waits for the stream and returns the summed milliseconds
+ * of each phase (ms_out[3]) over the evaluations recorded since the last
+ * reset, and their number. */
+plk_status plk_set_profiling(plk_handle* h, int on);
+plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int reset);
+/* Per-site log-likelihoods of the last plk_loglik (n_sites doubles). */
+plk_status plk_site_loglik(plk_handle* h, double* out);
+/* Node-state output for every internal node: out[(rank * n_sites + site) *
+ * n_states + s], internal nodes ranked in post-order (left subtree, right
+ * subtree, node), the order draw_normalized_likelihood_on_nodes visits them. */
+plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out);
+/* Number of internal nodes of the current tree (rows of plk_node_states). */
+int plk_n_internal(const plk_handle* h);
+
+/* ---- host helpers (FP64, no device work) ---------------------------------- */
+/* Q as sub_model::calc_Q_matrix (src/sub_model.cpp:99-114): off-diagonal
+ * Q[i][j] = rates[rate_spec[pos(i,j)]] * (reversible ? freq_j : 1), diagonal =
+ * -row sum; pos as sub_model::get_rate_pos (src/sub_model.cpp:3-29): upper
+ * triangle row-major for reversible models.  freqs holds n_states - 1 values
+ * (the last is 1 - their sum, src/sub_model.cpp:44-53) or NULL for 1/n. */
+plk_status plk_q_matrix(int n_states, int reversible, const unsigned* rate_spec,
+                        const double* rates, const double* freqs, double* Q_out);
+/* P(t) on the host with the engine's own FP64 code (either p_mode). */
+plk_status plk_pmat_host(int n_states, const double* Q, const double* root_weights,
+                         int reversible, double t, int p_mode, double* P_out);
+/* Mean rates of K equal-probability categories of a mean-1 Gamma(alpha)
+ * (Yang 1994). */
+plk_status plk_discrete_gamma(double alpha, int K, double* rates_out);
+/* Effective length of the edge above every node under a rate model, as
+ * plk_set_rate_model defines it (the handle uses this same function).
+ * clade_of_node may be NULL. */
+plk_status plk_effective_lengths(int n_nodes, const int* left, const int* right,
+                                 const double* branch_length, int root_quirk, int n_cut,
+                                 const float* cut_off, const float* cut_rate,
+                                 const int* clade_of_node, int n_clades, const float* clade_rate,
+                                 double* t_eff_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PLK_H */

@@ -1,0 +1,648 @@
+// C ABI of libplk (include/plk.h): argument checks, host-side preparation,
+// device buffers and kernel sequencing.  Host code only; kernels live in
+// plk_kernels.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "plk_internal.h"
+
+using namespace plk;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// Owning device allocation that only grows.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = n;
+        return cudaSuccess;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct plk_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // alignment
+    bool have_aln = false;
+    int n_tips = 0, n_sites = 0, S = 0;
+    bool bad_tip = false;
+    int n_codes = 0;
+    std::vector<uint32_t> code_mask;
+    DevBuf d_codes, d_code_mask;
+    // tree
+    bool have_tree = false;
+    int n_nodes = 0, tree_tips = 0, root = -1;
+    std::vector<int> left, right, post, rank;
+    std::vector<double> bl;
+    Program prog;
+    DevBuf d_ops, d_order, d_left, d_right, d_rank;
+    // rate model
+    bool root_quirk = true;
+    std::vector<float> cut_off, cut_rate, clade_rate;
+    std::vector<int> clade_of_node;
+    std::vector<double> t_eff;
+    bool teff_dirty = true;
+    DevBuf d_teff;
+    // substitution model
+    bool have_model = false;
+    int C = 1, p_kind = 0, reversible = 1;
+    std::vector<double> Q, root_w, cat_rate, cat_w, lam, L, R;
+    DevBuf d_Q, d_rootw, d_catr, d_catw, d_lam, d_L, d_R;
+    // P(t) and tip tables
+    DevBuf d_P64, d_P32, d_tip64, d_tip32;
+    // results and scratch
+    DevBuf d_site_lnl, d_block, d_lnl, d_work, d_cond, d_outside, d_nodes_out;
+    DevBuf d_mask_raw, d_flag;
+    bool have_lnl = false;
+    bool lnl_pending = false;
+    // streams: own_stream is created with the handle; stream is the active one
+    cudaStream_t own_stream = nullptr;
+    // kernel timing (plk_set_profiling)
+    bool profiling = false;
+    struct EvSet { cudaEvent_t e[4]; };
+    std::vector<EvSet> evs;
+    size_t ev_used = 0;
+    ~plk_handle() {
+        for (auto& s : evs)
+            for (auto& e : s.e) cudaEventDestroy(e);
+    }
+};
+
+namespace {
+
+plk_status fail(plk_handle* h, plk_status s, const std::string& msg) {
+    if (h) h->err = msg;
+    else g_create_error = msg;
+    return s;
+}
+
+plk_status cuda_fail(plk_handle* h, cudaError_t e, const char* what) {
+    const plk_status s = (e == cudaErrorMemoryAllocation) ? PLK_ERR_ALLOC : PLK_ERR_CUDA;
+    return fail(h, s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PLK_CUDA(h, expr, what)                          \
+    do {                                                 \
+        cudaError_t _e = (expr);                         \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, what); \
+    } while (0)
+
+template <typename T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess) return e;
+    if (v.empty()) return cudaSuccess;
+    return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+}
+
+plk_status ready(plk_handle* h) {
+    if (!h) return PLK_ERR_ARG;
+    if (!h->have_aln) return fail(h, PLK_ERR_STATE, "no alignment set (plk_set_alignment)");
+    if (!h->have_tree) return fail(h, PLK_ERR_STATE, "no tree set (plk_set_tree)");
+    if (!h->have_model) return fail(h, PLK_ERR_STATE, "no model set (plk_set_model)");
+    if (h->tree_tips != h->n_tips)
+        return fail(h, PLK_ERR_ARG, "tree has " + std::to_string(h->tree_tips) + " tips, alignment has " +
+                                        std::to_string(h->n_tips) + " rows");
+    if (h->S != (int)std::lround(std::sqrt((double)h->Q.size())))
+        return fail(h, PLK_ERR_ARG, "model and alignment state counts differ");
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    return PLK_OK;
+}
+
+plk_status refresh_teff(plk_handle* h) {
+    if (!h->teff_dirty) return PLK_OK;
+    h->t_eff.assign(h->n_nodes, 0.0);
+    effective_lengths(h->n_nodes, h->left.data(), h->right.data(), h->root, h->bl.data(), h->root_quirk,
+                      h->cut_off, h->cut_rate, h->clade_of_node, h->clade_rate, h->t_eff.data());
+    PLK_CUDA(h, upload(h->d_teff, h->t_eff, h->stream), "upload effective lengths");
+    h->teff_dirty = false;
+    return PLK_OK;
+}
+
+plk_status build_pmats(plk_handle* h) {
+    plk_status s = refresh_teff(h);
+    if (s != PLK_OK) return s;
+    const size_t SS = (size_t)h->S * h->S;
+    const size_t np = (size_t)h->n_nodes * h->C * SS;
+    const size_t nt = (size_t)h->n_tips * h->C * h->n_codes * h->S;
+    PLK_CUDA(h, h->d_P64.ensure(np * sizeof(double)), "allocate P");
+    PLK_CUDA(h, h->d_P32.ensure(np * sizeof(float)), "allocate P");
+    PLK_CUDA(h, h->d_tip64.ensure(nt * sizeof(double)), "allocate tip tables");
+    PLK_CUDA(h, h->d_tip32.ensure(nt * sizeof(float)), "allocate tip tables");
+    DeviceModel m{};
+    m.S = h->S; m.C = h->C; m.n_nodes = h->n_nodes; m.n_tips = h->n_tips; m.n_codes = h->n_codes;
+    m.t_eff = h->d_teff.as<double>(); m.cat_rate = h->d_catr.as<double>(); m.Q = h->d_Q.as<double>();
+    m.eig_lam = h->d_lam.as<double>(); m.eig_L = h->d_L.as<double>(); m.eig_R = h->d_R.as<double>();
+    m.code_mask = h->d_code_mask.as<uint32_t>();
+    m.P64 = h->d_P64.as<double>(); m.P32 = h->d_P32.as<float>();
+    m.tip64 = h->d_tip64.as<double>(); m.tip32 = h->d_tip32.as<float>();
+    PLK_CUDA(h, launch_pmat(m, h->p_kind, h->stream), "P(t) kernel launch");
+    return PLK_OK;
+}
+
+PruneArgs prune_args(plk_handle* h, int precision) {
+    PruneArgs a{};
+    const bool fp64 = precision == PLK_FP64;
+    a.ops = h->d_ops.as<Op>();
+    a.n_ops = (int)h->prog.ops.size();
+    a.max_depth = h->prog.max_depth;
+    a.codes = h->d_codes.as<uint8_t>();
+    a.site_stride = h->n_sites;
+    a.n_sites = h->n_sites;
+    a.n_codes = h->n_codes;
+    a.C = h->C;
+    a.P = fp64 ? (const void*)h->d_P64.p : (const void*)h->d_P32.p;
+    a.tipT = fp64 ? (const void*)h->d_tip64.p : (const void*)h->d_tip32.p;
+    a.root_w = h->d_rootw.as<double>();
+    a.cat_w = h->d_catw.as<double>();
+    a.site_lnl = h->d_site_lnl.as<double>();
+    a.block_sum = h->d_block.as<double>();
+    a.order = h->d_order.as<int>();
+    a.left = h->d_left.as<int>();
+    a.right = h->d_right.as<int>();
+    a.rank = h->d_rank.as<int>();
+    a.n_int = (int)h->post.size();
+    a.n_tips = h->n_tips;
+    return a;
+}
+
+bool fused_kernel_applies(const plk_handle* h, int precision) {
+    if (h->S != 4 || h->C > 8) return false;
+    const int cm = h->C == 1 ? 1 : (h->C <= 4 ? 4 : 8);
+    const size_t ops_bytes = (h->prog.ops.size() * sizeof(Op) + 31) & ~(size_t)31;
+    const size_t stack = (size_t)std::max(h->prog.max_depth, 1) * cm * (precision == PLK_FP64 ? 32 : 16) * 128;
+    return ops_bytes + stack <= 227 * 1024;
+}
+
+// Runs the post-order pass (P(t) already built); store != null asks for the
+// conditional vectors of every internal node in *store.
+plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* after_prune = nullptr) {
+    const size_t tsz = precision == PLK_FP64 ? sizeof(double) : sizeof(float);
+    const size_t vec_bytes = (size_t)h->post.size() * h->C * h->n_sites * h->S * tsz;
+    const int blocks = (h->n_sites + 127) / 128;
+    PLK_CUDA(h, h->d_site_lnl.ensure(sizeof(double) * h->n_sites), "allocate site lnL");
+    PLK_CUDA(h, h->d_block.ensure(sizeof(double) * 2 * blocks), "allocate block sums");
+    PLK_CUDA(h, h->d_lnl.ensure(sizeof(double)), "allocate lnL");
+    PruneArgs a = prune_args(h, precision);
+    const bool fused = fused_kernel_applies(h, precision);
+    if (!fused) {
+        PLK_CUDA(h, h->d_work.ensure(vec_bytes), "allocate work vectors");
+        a.work = h->d_work.p;
+        a.cond = h->d_work.p;
+    } else if (store) {
+        PLK_CUDA(h, h->d_cond.ensure(vec_bytes), "allocate node vectors");
+        a.cond = h->d_cond.p;
+    }
+    int nb = 0;
+    PLK_CUDA(h, launch_prune(a, h->S, precision, store != nullptr, &nb, h->stream), "post-order kernel launch");
+    if (after_prune) PLK_CUDA(h, cudaEventRecord(*after_prune, h->stream), "cudaEventRecord");
+    PLK_CUDA(h, launch_reduce(a.block_sum, nb, h->d_lnl.as<double>(), h->stream), "reduce kernel launch");
+    if (store) *store = a.cond;
+    return PLK_OK;
+}
+
+bool finite_masks(uint32_t m, int S) {
+    const uint32_t all = S >= 32 ? 0xffffffffu : ((1u << S) - 1u);
+    return (m & all) != 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plk_api_version(void) { return PLK_API_VERSION; }
+
+const char* plk_status_string(plk_status s) {
+    switch (s) {
+        case PLK_OK: return "ok";
+        case PLK_ERR_ARG: return "bad argument";
+        case PLK_ERR_ALLOC: return "allocation failed";
+        case PLK_ERR_CUDA: return "CUDA error";
+        case PLK_ERR_STATE: return "call order (missing input)";
+        case PLK_ERR_TIMEOUT: return "bounded device wait gave up";
+        case PLK_ERR_NUMERIC: return "non-finite likelihood";
+        case PLK_ERR_TIP: return "a tip cell allows no state";
+        case PLK_ERR_NODEV: return "no CUDA device";
+        case PLK_ERR_UNSUPPORTED: return "unsupported configuration";
+        default: return "unknown status";
+    }
+}
+
+const char* plk_last_error(const plk_handle* h) {
+    return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+plk_status plk_create(plk_handle** out, int device) {
+    if (!out) return fail(nullptr, PLK_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(nullptr, PLK_ERR_NODEV, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= n) return fail(nullptr, PLK_ERR_ARG, "device index out of range");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(nullptr, PLK_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    plk_handle* h = new (std::nothrow) plk_handle();
+    if (!h) return fail(nullptr, PLK_ERR_ALLOC, "host allocation failed");
+    h->device = device;
+    e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(nullptr, PLK_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    h->stream = h->own_stream;
+    *out = h;
+    return PLK_OK;
+}
+
+void plk_destroy(plk_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+}
+
+plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states, const uint32_t* masks) {
+    if (!h) return PLK_ERR_ARG;
+    if (n_tips < 1 || n_sites < 1 || n_states < 1 || n_states > kMaxStates || !masks)
+        return fail(h, PLK_ERR_ARG, "alignment needs n_tips >= 1, n_sites >= 1, 1 <= n_states <= 24");
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    const uint32_t all = (n_states >= 32) ? 0xffffffffu : ((1u << n_states) - 1u);
+    const size_t n_cells = (size_t)n_tips * n_sites;
+    std::vector<uint32_t> table;
+    bool bad = false;
+    if (n_states <= 4) {
+        // small alphabets: the code is the state set itself, encoded on the
+        // device straight from the caller's masks
+        for (uint32_t c = 0; c < (1u << n_states); ++c) table.push_back(c);
+        PLK_CUDA(h, h->d_mask_raw.ensure(n_cells * sizeof(uint32_t)), "allocate mask staging");
+        PLK_CUDA(h, h->d_codes.ensure(n_cells), "allocate tip codes");
+        PLK_CUDA(h, h->d_flag.ensure(sizeof(int)), "allocate flag");
+        PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks, n_cells * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream),
+                 "upload masks");
+        PLK_CUDA(h, cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "clear flag");
+        PLK_CUDA(h, launch_encode_small(h->d_mask_raw.as<uint32_t>(), n_cells, all, h->d_codes.as<uint8_t>(),
+                                        h->d_flag.as<int>(), h->stream),
+                 "encode kernel launch");
+        int flag = 0;
+        PLK_CUDA(h, cudaMemcpyAsync(&flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
+        PLK_CUDA(h, upload(h->d_code_mask, table, h->stream), "upload code table");
+        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "encode tip codes");
+        bad = flag != 0;
+    } else {
+        std::vector<uint8_t> codes(n_cells);
+        std::map<uint32_t, int> index;
+        for (size_t i = 0; i < codes.size(); ++i) {
+            const uint32_t m = masks[i] & all;
+            if (m == 0) bad = true;
+            auto it = index.find(m);
+            int c;
+            if (it == index.end()) {
+                c = (int)table.size();
+                if (c >= kMaxCodes) return fail(h, PLK_ERR_UNSUPPORTED, "more than 256 distinct tip state sets");
+                index.emplace(m, c);
+                table.push_back(m);
+            } else c = it->second;
+            codes[i] = (uint8_t)c;
+        }
+        PLK_CUDA(h, upload(h->d_codes, codes, h->stream), "upload tip codes");
+        PLK_CUDA(h, upload(h->d_code_mask, table, h->stream), "upload code table");
+        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "upload tip codes");
+    }
+    h->n_tips = n_tips;
+    h->n_sites = n_sites;
+    h->S = n_states;
+    h->n_codes = (int)table.size();
+    h->code_mask = table;
+    h->bad_tip = bad;
+    h->have_aln = true;
+    h->have_lnl = false;
+    return PLK_OK;
+}
+
+plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* right, const double* bl) {
+    if (!h) return PLK_ERR_ARG;
+    if (n_nodes < 2 || !left || !right || !bl) return fail(h, PLK_ERR_ARG, "tree needs n_nodes >= 2 and three arrays");
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    int n_leaves = 0;
+    for (int v = 0; v < n_nodes; ++v)
+        if (left[v] < 0 && right[v] < 0) ++n_leaves;
+    std::vector<int> post, rank;
+    int root = -1;
+    std::string err;
+    if (!check_tree(n_leaves, n_nodes, left, right, &root, &post, &rank, &err)) return fail(h, PLK_ERR_ARG, err);
+    for (int v = 0; v < n_nodes; ++v)
+        if (!std::isfinite(bl[v])) return fail(h, PLK_ERR_ARG, "non-finite branch length at node " + std::to_string(v));
+    h->left.assign(left, left + n_nodes);
+    h->right.assign(right, right + n_nodes);
+    h->bl.assign(bl, bl + n_nodes);
+    h->post = post;
+    h->rank = rank;
+    h->root = root;
+    h->n_nodes = n_nodes;
+    h->tree_tips = n_leaves;
+    h->prog = build_program(n_leaves, n_nodes, left, right, root, rank);
+    PLK_CUDA(h, upload(h->d_ops, h->prog.ops, h->stream), "upload program");
+    PLK_CUDA(h, upload(h->d_order, post, h->stream), "upload order");
+    PLK_CUDA(h, upload(h->d_left, h->left, h->stream), "upload tree");
+    PLK_CUDA(h, upload(h->d_right, h->right, h->stream), "upload tree");
+    PLK_CUDA(h, upload(h->d_rank, rank, h->stream), "upload tree");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "upload tree");
+    // default rate model: the reference's empty rate_model
+    h->root_quirk = true;
+    h->cut_off.clear();
+    h->cut_rate.clear();
+    h->clade_of_node.clear();
+    h->clade_rate.clear();
+    h->teff_dirty = true;
+    h->have_tree = true;
+    h->have_lnl = false;
+    return PLK_OK;
+}
+
+plk_status plk_set_rate_model(plk_handle* h, int root_quirk, int n_cut, const float* cut_off,
+                              const float* cut_rate, const int* clade_of_node, int n_clades,
+                              const float* clade_rate) {
+    if (!h) return PLK_ERR_ARG;
+    if (!h->have_tree) return fail(h, PLK_ERR_STATE, "set the tree before the rate model");
+    if (n_cut < 0 || n_clades < 0 || (n_cut > 0 && (!cut_off || !cut_rate)) || (n_clades > 0 && !clade_rate))
+        return fail(h, PLK_ERR_ARG, "bad rate model arrays");
+    for (int i = 1; i < n_cut; ++i)
+        if (cut_off[i] < cut_off[i - 1]) return fail(h, PLK_ERR_ARG, "cut-offs must ascend");
+    h->root_quirk = root_quirk != 0;
+    h->cut_off.assign(cut_off, cut_off + n_cut);
+    h->cut_rate.assign(cut_rate, cut_rate + n_cut);
+    h->clade_rate.assign(clade_rate, clade_rate + n_clades);
+    if (clade_of_node) {
+        h->clade_of_node.assign(clade_of_node, clade_of_node + h->n_nodes);
+        for (int c : h->clade_of_node)
+            if (c >= n_clades) return fail(h, PLK_ERR_ARG, "clade number without a rate");
+    } else h->clade_of_node.clear();
+    h->teff_dirty = true;
+    h->have_lnl = false;
+    return PLK_OK;
+}
+
+plk_status plk_set_model(plk_handle* h, int S, const double* Q, const double* root_w, int reversible,
+                         int n_cats, const double* cat_rates, const double* cat_weights, int p_mode) {
+    if (!h) return PLK_ERR_ARG;
+    if (S < 1 || S > kMaxStates || !Q || !root_w) return fail(h, PLK_ERR_ARG, "model needs 1 <= n_states <= 24, Q and root weights");
+    if (n_cats < 1 || n_cats > kMaxCats || !cat_rates || !cat_weights)
+        return fail(h, PLK_ERR_ARG, "model needs 1 <= n_cats <= 16 with rates and weights");
+    if (p_mode != PLK_P_TAYLOR20 && p_mode != PLK_P_EXACT) return fail(h, PLK_ERR_ARG, "unknown p_mode");
+    for (int i = 0; i < S * S; ++i)
+        if (!std::isfinite(Q[i])) return fail(h, PLK_ERR_ARG, "non-finite Q entry");
+    for (int k = 0; k < n_cats; ++k)
+        if (!(cat_rates[k] >= 0.0) || !std::isfinite(cat_rates[k]) || !std::isfinite(cat_weights[k]))
+            return fail(h, PLK_ERR_ARG, "bad category rate or weight");
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    h->Q.assign(Q, Q + S * S);
+    h->root_w.assign(root_w, root_w + S);
+    h->cat_rate.assign(cat_rates, cat_rates + n_cats);
+    h->cat_w.assign(cat_weights, cat_weights + n_cats);
+    h->C = n_cats;
+    h->reversible = reversible;
+    h->lam.assign(S, 0.0);
+    h->L.assign((size_t)S * S, 0.0);
+    h->R.assign((size_t)S * S, 0.0);
+    if (p_mode == PLK_P_TAYLOR20) h->p_kind = 0;
+    else if (reversible) {
+        if (!reversible_eigen(S, Q, root_w, h->lam.data(), h->L.data(), h->R.data()))
+            return fail(h, PLK_ERR_ARG, "eigen form needs positive root weights (frequencies)");
+        h->p_kind = 1;
+    } else h->p_kind = 2;
+    PLK_CUDA(h, upload(h->d_Q, h->Q, h->stream), "upload model");
+    PLK_CUDA(h, upload(h->d_rootw, h->root_w, h->stream), "upload model");
+    PLK_CUDA(h, upload(h->d_catr, h->cat_rate, h->stream), "upload model");
+    PLK_CUDA(h, upload(h->d_catw, h->cat_w, h->stream), "upload model");
+    PLK_CUDA(h, upload(h->d_lam, h->lam, h->stream), "upload model");
+    PLK_CUDA(h, upload(h->d_L, h->L, h->stream), "upload model");
+    PLK_CUDA(h, upload(h->d_R, h->R, h->stream), "upload model");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "upload model");
+    h->have_model = true;
+    h->have_lnl = false;
+    return PLK_OK;
+}
+
+plk_status plk_loglik_async(plk_handle* h, int precision) {
+    plk_status s = ready(h);
+    if (s != PLK_OK) return s;
+    if (precision != PLK_FP64 && precision != PLK_FP32S) return fail(h, PLK_ERR_ARG, "unknown precision");
+    h->lnl_pending = false;
+    if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
+    plk_handle::EvSet* ev = nullptr;
+    if (h->profiling) {
+        if (h->ev_used == h->evs.size()) {
+            plk_handle::EvSet e{};
+            for (auto& x : e.e) PLK_CUDA(h, cudaEventCreate(&x), "cudaEventCreate");
+            h->evs.push_back(e);
+        }
+        ev = &h->evs[h->ev_used++];
+        PLK_CUDA(h, cudaEventRecord(ev->e[0], h->stream), "cudaEventRecord");
+    }
+    if ((s = build_pmats(h)) != PLK_OK) return s;
+    if (ev) PLK_CUDA(h, cudaEventRecord(ev->e[1], h->stream), "cudaEventRecord");
+    if ((s = run_prune(h, precision, nullptr, ev ? &ev->e[2] : nullptr)) != PLK_OK) return s;
+    if (ev) PLK_CUDA(h, cudaEventRecord(ev->e[3], h->stream), "cudaEventRecord");
+    h->lnl_pending = true;
+    return PLK_OK;
+}
+
+plk_status plk_loglik_result(plk_handle* h, double* lnl_out) {
+    if (!h) return PLK_ERR_ARG;
+    if (!lnl_out) return fail(h, PLK_ERR_ARG, "lnl_out is NULL");
+    *lnl_out = 0.0;
+    if (!h->lnl_pending) return fail(h, PLK_ERR_STATE, "no evaluation enqueued (plk_loglik_async)");
+    double v = 0.0;
+    PLK_CUDA(h, cudaMemcpyAsync(&v, h->d_lnl.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy lnL");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "likelihood kernels");
+    h->lnl_pending = false;
+    *lnl_out = v;
+    h->have_lnl = true;
+    if (!std::isfinite(v)) return fail(h, PLK_ERR_NUMERIC, "log-likelihood is not finite");
+    return PLK_OK;
+}
+
+plk_status plk_loglik(plk_handle* h, int precision, double* lnl_out) {
+    if (!h) return PLK_ERR_ARG;
+    if (!lnl_out) return fail(h, PLK_ERR_ARG, "lnl_out is NULL");
+    *lnl_out = 0.0;
+    plk_status s = plk_loglik_async(h, precision);
+    if (s != PLK_OK) return s;
+    return plk_loglik_result(h, lnl_out);
+}
+
+plk_status plk_set_stream(plk_handle* h, void* stream) {
+    if (!h) return PLK_ERR_ARG;
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "switch stream");
+    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    return PLK_OK;
+}
+
+plk_status plk_set_profiling(plk_handle* h, int on) {
+    if (!h) return PLK_ERR_ARG;
+    h->profiling = on != 0;
+    h->ev_used = 0;
+    return PLK_OK;
+}
+
+plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int reset) {
+    if (!h || !ms_out) return PLK_ERR_ARG;
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "kernel timing");
+    double tot[3] = {0, 0, 0};
+    for (size_t i = 0; i < h->ev_used; ++i)
+        for (int p = 0; p < 3; ++p) {
+            float ms = 0.f;
+            PLK_CUDA(h, cudaEventElapsedTime(&ms, h->evs[i].e[p], h->evs[i].e[p + 1]), "cudaEventElapsedTime");
+            tot[p] += ms;
+        }
+    for (int p = 0; p < 3; ++p) ms_out[p] = tot[p];
+    if (n_evals) *n_evals = (int)h->ev_used;
+    if (reset) h->ev_used = 0;
+    return PLK_OK;
+}
+
+plk_status plk_site_loglik(plk_handle* h, double* out) {
+    if (!h) return PLK_ERR_ARG;
+    if (!out) return fail(h, PLK_ERR_ARG, "out is NULL");
+    if (!h->have_lnl) return fail(h, PLK_ERR_STATE, "no likelihood computed yet (plk_loglik)");
+    PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    PLK_CUDA(h, cudaMemcpyAsync(out, h->d_site_lnl.p, sizeof(double) * h->n_sites, cudaMemcpyDeviceToHost, h->stream), "copy site lnL");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "copy site lnL");
+    return PLK_OK;
+}
+
+int plk_n_internal(const plk_handle* h) { return h ? (int)h->post.size() : 0; }
+
+plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) {
+    plk_status s = ready(h);
+    if (s != PLK_OK) return s;
+    if (!out) return fail(h, PLK_ERR_ARG, "out is NULL");
+    if (mode != PLK_NODES_COND && mode != PLK_NODES_MARGINAL) return fail(h, PLK_ERR_ARG, "unknown node-state mode");
+    if (precision != PLK_FP64 && precision != PLK_FP32S) return fail(h, PLK_ERR_ARG, "unknown precision");
+    if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
+    if ((s = build_pmats(h)) != PLK_OK) return s;
+    void* cond = nullptr;
+    if ((s = run_prune(h, precision, &cond)) != PLK_OK) return s;
+    const int n_int = (int)h->post.size();
+    const size_t out_n = (size_t)n_int * h->n_sites * h->S;
+    PLK_CUDA(h, h->d_nodes_out.ensure(out_n * sizeof(double)), "allocate node output");
+    if (mode == PLK_NODES_COND) {
+        PLK_CUDA(h, launch_cond_normalise(cond, h->d_catw.as<double>(), n_int, h->C, h->n_sites, h->S, precision,
+                                          h->d_nodes_out.as<double>(), h->stream),
+                 "normalise kernel launch");
+    } else {
+        const size_t tsz = precision == PLK_FP64 ? sizeof(double) : sizeof(float);
+        PLK_CUDA(h, h->d_outside.ensure((size_t)n_int * h->C * h->n_sites * h->S * tsz), "allocate outside vectors");
+        PreorderArgs p{};
+        const bool fp64 = precision == PLK_FP64;
+        p.order = h->d_order.as<int>(); p.left = h->d_left.as<int>(); p.right = h->d_right.as<int>();
+        p.rank = h->d_rank.as<int>(); p.n_int = n_int; p.n_tips = h->n_tips; p.n_sites = h->n_sites;
+        p.n_codes = h->n_codes; p.S = h->S; p.C = h->C; p.codes = h->d_codes.as<uint8_t>();
+        p.site_stride = h->n_sites;
+        p.P = fp64 ? (const void*)h->d_P64.p : (const void*)h->d_P32.p;
+        p.tipT = fp64 ? (const void*)h->d_tip64.p : (const void*)h->d_tip32.p;
+        p.root_w = h->d_rootw.as<double>(); p.cat_w = h->d_catw.as<double>();
+        p.cond = cond; p.outside = h->d_outside.p; p.out = h->d_nodes_out.as<double>();
+        PLK_CUDA(h, launch_preorder(p, precision, h->stream), "pre-order kernel launch");
+    }
+    PLK_CUDA(h, cudaMemcpyAsync(out, h->d_nodes_out.p, out_n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy node states");
+    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "node-state kernels");
+    h->have_lnl = true;
+    return PLK_OK;
+}
+
+plk_status plk_q_matrix(int n, int reversible, const unsigned* spec, const double* rates, const double* freqs,
+                        double* Q_out) {
+    if (n < 1 || n > kMaxStates || !spec || !rates || !Q_out) return fail(nullptr, PLK_ERR_ARG, "bad arguments to plk_q_matrix");
+    q_matrix(n, reversible != 0, spec, rates, freqs, Q_out);
+    return PLK_OK;
+}
+
+plk_status plk_pmat_host(int n, const double* Q, const double* root_w, int reversible, double t, int p_mode,
+                         double* P_out) {
+    if (n < 1 || n > kMaxStates || !Q || !P_out) return fail(nullptr, PLK_ERR_ARG, "bad arguments to plk_pmat_host");
+    if (p_mode == PLK_P_TAYLOR20) {
+        pmat_taylor20_host(n, Q, t, P_out);
+        return PLK_OK;
+    }
+    if (p_mode != PLK_P_EXACT) return fail(nullptr, PLK_ERR_ARG, "unknown p_mode");
+    if (reversible) {
+        if (!root_w) return fail(nullptr, PLK_ERR_ARG, "reversible eigen form needs root weights");
+        std::vector<double> lam(n), L((size_t)n * n), R((size_t)n * n);
+        if (!reversible_eigen(n, Q, root_w, lam.data(), L.data(), R.data()))
+            return fail(nullptr, PLK_ERR_ARG, "eigen form needs positive frequencies");
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                double acc = 0.0;
+                for (int m = 0; m < n; ++m) acc += L[i * n + m] * std::exp(lam[m] * t) * R[m * n + j];
+                P_out[i * n + j] = acc;
+            }
+        return PLK_OK;
+    }
+    pmat_series_host(n, Q, t, P_out);
+    return PLK_OK;
+}
+
+plk_status plk_discrete_gamma(double alpha, int K, double* rates_out) {
+    if (!(alpha > 0.0) || !std::isfinite(alpha) || K < 1 || K > kMaxCats || !rates_out)
+        return fail(nullptr, PLK_ERR_ARG, "discrete Gamma needs alpha > 0 and 1 <= K <= 16");
+    discrete_gamma(alpha, K, rates_out);
+    return PLK_OK;
+}
+
+plk_status plk_effective_lengths(int n_nodes, const int* left, const int* right, const double* bl,
+                                 int root_quirk, int n_cut, const float* cut_off, const float* cut_rate,
+                                 const int* clade_of_node, int n_clades, const float* clade_rate,
+                                 double* out) {
+    if (n_nodes < 2 || !left || !right || !bl || !out || n_cut < 0 || n_clades < 0 ||
+        (n_cut > 0 && (!cut_off || !cut_rate)) || (n_clades > 0 && !clade_rate))
+        return fail(nullptr, PLK_ERR_ARG, "bad arguments to plk_effective_lengths");
+    int n_leaves = 0;
+    for (int v = 0; v < n_nodes; ++v)
+        if (left[v] < 0 && right[v] < 0) ++n_leaves;
+    std::vector<int> post, rank;
+    int root = -1;
+    std::string err;
+    if (!check_tree(n_leaves, n_nodes, left, right, &root, &post, &rank, &err)) return fail(nullptr, PLK_ERR_ARG, err);
+    std::vector<float> co(cut_off, cut_off + n_cut), cr(cut_rate, cut_rate + n_cut);
+    std::vector<float> crt(clade_rate, clade_rate + n_clades);
+    std::vector<int> con;
+    if (clade_of_node) con.assign(clade_of_node, clade_of_node + n_nodes);
+    effective_lengths(n_nodes, left, right, root, bl, root_quirk != 0, co, cr, con, crt, out);
+    return PLK_OK;
+}
+
+}  // extern "C"

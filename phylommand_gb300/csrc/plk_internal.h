@@ -1,0 +1,141 @@
+// Internal declarations shared by the host code (plk_api.cpp, plk_host.cpp)
+// and the device code (plk_kernels.cu) of libplk.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/plk.h"
+
+namespace plk {
+
+constexpr int kMaxStates = 24;   // bitset<SIZE=24> in the reference (src/constants.h:25)
+constexpr int kMaxCats = 16;
+constexpr int kMaxCodes = 256;   // distinct tip state-sets per alignment (1 byte per cell)
+
+// Source of one child vector in a post-order op.
+constexpr int kSrcAcc = -1;    // the previous op's result, still in registers
+constexpr int kSrcPop = -2;    // popped from the per-thread spill stack
+constexpr int kSrcNone = -3;   // no second child (unary node)
+
+// One internal node of the post-order program.  A thread walks the ops in
+// order for its site(s); s0/s1 >= 0 name a tip (its id), else kSrc*.
+// e0/e1 are the child node ids whose edge P(t) applies.
+struct Op {
+    int node;   // node id
+    int rank;   // post-order rank (left subtree, right subtree, node)
+    int e0, e1; // child ids (e1 = -1 for a unary node)
+    int s0, s1; // sources of the two child vectors
+    int push;   // 1: push the result onto the spill stack
+    int pad;
+};
+static_assert(sizeof(Op) == 32, "Op is 32 bytes");
+
+// Post-order program: ops plus the deepest spill stack it needs.
+struct Program {
+    std::vector<Op> ops;
+    int max_depth = 0;
+};
+
+// ---- host model math (plk_host.cpp) --------------------------------------
+unsigned rate_pos(unsigned n, bool tr, unsigned row, unsigned col);
+void q_matrix(int n, bool tr, const unsigned* spec, const double* rates, const double* freqs,
+              double* Q);
+// Symmetric eigendecomposition by cyclic Jacobi rotations: A = V diag(w) V^T.
+void jacobi_eigen(int n, const double* A, double* w, double* V);
+// Eigen system of a reversible Q with weights pi: Q = L diag(lam) R with
+// L = D^-1/2 V, R = V^T D^1/2 (D = diag(pi)).
+bool reversible_eigen(int n, const double* Q, const double* pi, double* lam, double* L,
+                      double* R);
+void pmat_taylor20_host(int n, const double* Q, double t, double* P);
+void pmat_series_host(int n, const double* Q, double t, double* P);
+void discrete_gamma(double alpha, int K, double* rates);
+// Effective branch lengths (rate_model over the tree, src/rate_model.cpp:103-127).
+void effective_lengths(int n_nodes, const int* left, const int* right, int root,
+                       const double* bl, bool root_quirk, const std::vector<float>& cut_off,
+                       const std::vector<float>& cut_rate, const std::vector<int>& clade_of_node,
+                       const std::vector<float>& clade_rate, double* t_eff);
+// Checks the tree; fills root, internal post-order and rank; message on error.
+bool check_tree(int n_tips, int n_nodes, const int* left, const int* right, int* root,
+                std::vector<int>* internal_postorder, std::vector<int>* rank, std::string* err);
+// Register-allocated post-order program (Sethi-Ullman child order).
+Program build_program(int n_tips, int n_nodes, const int* left, const int* right, int root,
+                      const std::vector<int>& rank);
+
+// ---- device launches (plk_kernels.cu) -------------------------------------
+struct DeviceModel {
+    int S, C, n_nodes, n_tips, n_codes;
+    const double* t_eff;      // [n_nodes]
+    const double* cat_rate;   // [C]
+    const double* Q;          // [S*S]
+    const double* eig_lam;    // [S]
+    const double* eig_L;      // [S*S]
+    const double* eig_R;      // [S*S]
+    const uint32_t* code_mask;// [n_codes]
+    double* P64;              // [n_nodes][C][S][S]
+    float* P32;               // [n_nodes][C][S][S]
+    double* tip64;            // [n_tips][C][n_codes][S]
+    float* tip32;             // [n_tips][C][n_codes][S]
+};
+// p_kind: 0 taylor20, 1 eigen (reversible), 2 series (non-reversible)
+cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st);
+
+struct PruneArgs {
+    const Op* ops;
+    int n_ops;
+    int max_depth;
+    const uint8_t* codes;      // [n_tips][site_stride]
+    int site_stride;
+    int n_sites;
+    int n_codes;
+    int C;
+    const void* P;             // T [n_nodes][C][S][S]
+    const void* tipT;          // T [n_tips][C][n_codes][S]
+    const double* root_w;      // [S]
+    const double* cat_w;       // [C]
+    double* site_lnl;          // [n_sites]
+    double* block_sum;         // [2 * n_blocks] (sum, compensation)
+    void* cond;                // T [n_int][C][n_sites][S] or null
+    void* work;                // T scratch of the generic kernel [n_int][C][n_sites][S]
+    // topology for the generic kernel (device arrays)
+    const int* order;          // internal nodes in post-order [n_int]
+    const int* left;           // [n_nodes]
+    const int* right;          // [n_nodes]
+    const int* rank;           // [n_nodes], -1 for tips
+    int n_int;
+    int n_tips;
+};
+// Chooses the kernel for (S, C, precision); returns the number of blocks used
+// for the partial sums in *n_blocks.
+cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, int* n_blocks,
+                         cudaStream_t st);
+cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cudaStream_t st);
+// codes[i] = masks[i] & all (alphabets of <= 4 states); *bad |= 1 if a cell is empty.
+cudaError_t launch_encode_small(const uint32_t* masks, size_t n, uint32_t all, uint8_t* codes, int* bad,
+                                cudaStream_t st);
+
+struct PreorderArgs {
+    const int* order;   // internal nodes in post-order [n_int]
+    const int* left;
+    const int* right;
+    const int* rank;    // [n_nodes], -1 for tips
+    int n_int, n_tips, n_sites, n_codes, S, C;
+    const uint8_t* codes;
+    int site_stride;
+    const void* P;
+    const void* tipT;
+    const double* root_w;
+    const double* cat_w;
+    const void* cond;   // T [n_int][C][n_sites][S]
+    void* outside;      // T [n_int][C][n_sites][S]
+    double* out;        // [n_int][n_sites][S] normalised
+};
+cudaError_t launch_preorder(const PreorderArgs& a, int precision, cudaStream_t st);
+cudaError_t launch_cond_normalise(const void* cond, const double* cat_w, int n_int, int C,
+                                  int n_sites, int S, int precision, double* out,
+                                  cudaStream_t st);
+
+}  // namespace plk

@@ -1,0 +1,772 @@
+// Device code of libplk (sm_103a).
+//
+//  pmat_kernel      P(t) for every (edge, category): the reference's
+//                   Taylor-plus-20-squarings (src/marth/marth.cpp:129-140),
+//                   an eigen form for reversible Q, or scaling-and-squaring
+//                   for non-reversible Q; FP64, plus FP32 copies and the
+//                   per-tip-edge lookup tables (P times each tip state set).
+//  prune4_kernel    post-order pass for 4 states (src/simpleML.cpp:127-197):
+//                   one thread per site walks the whole register-allocated
+//                   op list; partial vectors live in registers, spills in a
+//                   per-thread shared-memory stack; per-site power-of-two
+//                   scaling; root reduction (src/simpleML.h:123-141) fused;
+//                   compensated block sums of the per-site lnL.
+//  prune_generic    the same pass for any state count (<= 24), vectors in a
+//                   global work buffer.
+//  preorder_kernel  outside vectors from the root down and normalised
+//                   marginal posteriors (absent in the reference).
+//  reduce_kernel    compensated (TwoSum) sum of the block partial sums.
+#include <cstdio>
+
+#include "plk_internal.h"
+
+namespace plk {
+
+namespace {
+
+constexpr int kPruneThreads = 128;
+
+template <typename T>
+struct alignas(4 * sizeof(T)) V4 {
+    T v[4];
+};
+
+// ---- arithmetic helpers: EXACT keeps every multiply and add separately
+// rounded in the reference's order; otherwise FMA chains.
+template <typename T>
+__device__ __forceinline__ T mul_rn(T a, T b);
+template <>
+__device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+template <>
+__device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b);
+template <>
+__device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
+template <>
+__device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+    s = __dadd_rn(a, b);
+    const double bb = __dsub_rn(s, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+
+template <typename T>
+__device__ __forceinline__ T scale_threshold();
+template <>
+__device__ __forceinline__ float scale_threshold<float>() { return 5.421010862427522e-20f; }  // 2^-64
+template <>
+__device__ __forceinline__ double scale_threshold<double>() { return 8.636168555094445e-78; }  // 2^-256
+
+}  // namespace
+
+// =========================================================================
+// P(t)
+// =========================================================================
+__global__ void pmat_kernel(DeviceModel m, int p_kind) {
+    const int v = blockIdx.x / m.C, k = blockIdx.x % m.C;
+    const int S = m.S, SS = S * S;
+    extern __shared__ double pm_smem[];
+    double* A = pm_smem;
+    double* B = pm_smem + SS;
+    double* X = pm_smem + 2 * SS;  // eigen exponentials / series term
+    const double t = __dmul_rn(m.t_eff[v], m.cat_rate[k]);
+    if (p_kind == 0) {
+        // A = I + (Q t) / 2^20, then 20 squarings with prod[i][j] summed
+        // over k ascending from 0, every operation rounded on its own.
+        for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+            const int i = idx / S, j = idx % S;
+            const double q = __ddiv_rn(__dmul_rn(m.Q[idx], t), 1048576.0);
+            A[idx] = (i == j) ? __dadd_rn(1.0, q) : q;
+        }
+        __syncthreads();
+        for (int it = 0; it < 20; ++it) {
+            for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+                const int i = idx / S, j = idx % S;
+                double acc = __dmul_rn(A[i * S], A[j]);
+                for (int kk = 1; kk < S; ++kk) acc = __dadd_rn(acc, __dmul_rn(A[i * S + kk], A[kk * S + j]));
+                B[idx] = acc;
+            }
+            __syncthreads();
+            double* tmp = A; A = B; B = tmp;
+        }
+    } else if (p_kind == 1) {
+        for (int i = threadIdx.x; i < S; i += blockDim.x) X[i] = exp(m.eig_lam[i] * t);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+            const int i = idx / S, j = idx % S;
+            double acc = 0.0;
+            for (int mm = 0; mm < S; ++mm) acc = fma(m.eig_L[i * S + mm] * X[mm], m.eig_R[mm * S + j], acc);
+            A[idx] = acc;
+        }
+        __syncthreads();
+    } else {
+        // scaling and squaring: A0 = Q t 2^-s with ||A0|| <= 1/8, Taylor to 18
+        __shared__ int s_sq;
+        if (threadIdx.x == 0) {
+            double norm = 0.0;
+            for (int i = 0; i < S; ++i) {
+                double r = 0.0;
+                for (int j = 0; j < S; ++j) r += fabs(m.Q[i * S + j] * t);
+                norm = fmax(norm, r);
+            }
+            int s = 0;
+            while (norm > 0.125 && s < 1000) { norm *= 0.5; ++s; }
+            s_sq = s;
+        }
+        __syncthreads();
+        const int s = s_sq;
+        const double f = ldexp(t, -s);
+        double* term = X;   // needs SS doubles
+        for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+            const int i = idx / S, j = idx % S;
+            term[idx] = (i == j) ? 1.0 : 0.0;
+            A[idx] = term[idx];
+        }
+        __syncthreads();
+        for (int mm = 1; mm <= 18; ++mm) {
+            for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+                const int i = idx / S, j = idx % S;
+                double acc = 0.0;
+                for (int kk = 0; kk < S; ++kk) acc = fma(term[i * S + kk], m.Q[kk * S + j] * f, acc);
+                B[idx] = acc / mm;
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+                term[idx] = B[idx];
+                A[idx] += B[idx];
+            }
+            __syncthreads();
+        }
+        for (int it = 0; it < s; ++it) {
+            for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+                const int i = idx / S, j = idx % S;
+                double acc = 0.0;
+                for (int kk = 0; kk < S; ++kk) acc = fma(A[i * S + kk], A[kk * S + j], acc);
+                B[idx] = acc;
+            }
+            __syncthreads();
+            double* tmp = A; A = B; B = tmp;
+        }
+    }
+    const size_t base = ((size_t)v * m.C + k) * SS;
+    for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
+        m.P64[base + idx] = A[idx];
+        m.P32[base + idx] = (float)A[idx];
+    }
+    if (v < m.n_tips) {
+        // table[code][i] = sum over allowed j (ascending) of P[i][j]: what
+        // branch_likelihood gives for a 0/1 tip vector (0 * P adds nothing).
+        const size_t tb = ((size_t)v * m.C + k) * m.n_codes * S;
+        for (int idx = threadIdx.x; idx < m.n_codes * S; idx += blockDim.x) {
+            const int c = idx / S, i = idx % S;
+            const uint32_t mask = m.code_mask[c];
+            double acc = 0.0;
+            bool first = true;
+            for (int j = 0; j < S; ++j)
+                if ((mask >> j) & 1u) {
+                    acc = first ? A[i * S + j] : __dadd_rn(acc, A[i * S + j]);
+                    first = false;
+                }
+            m.tip64[tb + idx] = acc;
+            m.tip32[tb + idx] = (float)acc;
+        }
+    }
+}
+
+cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st) {
+    const int SS = m.S * m.S;
+    const size_t smem = sizeof(double) * (size_t)(3 * SS);
+    const int threads = SS >= 256 ? 256 : (SS >= 64 ? 64 : 32);
+    pmat_kernel<<<m.n_nodes * m.C, threads, smem, st>>>(m, p_kind);
+    return cudaGetLastError();
+}
+
+// =========================================================================
+// Post-order pass, 4 states
+// =========================================================================
+namespace {
+
+template <typename T, bool EXACT>
+__device__ __forceinline__ void matvec4(const T* __restrict__ Pm, const T x[4], T out[4]) {
+    const V4<T>* rows = reinterpret_cast<const V4<T>*>(Pm);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const V4<T> r = rows[i];
+        if (EXACT) {
+            T acc = mul_rn(x[0], r.v[0]);
+            acc = add_rn(acc, mul_rn(x[1], r.v[1]));
+            acc = add_rn(acc, mul_rn(x[2], r.v[2]));
+            acc = add_rn(acc, mul_rn(x[3], r.v[3]));
+            out[i] = acc;
+        } else {
+            T acc = x[0] * r.v[0];
+            acc = fma(x[1], r.v[1], acc);
+            acc = fma(x[2], r.v[2], acc);
+            acc = fma(x[3], r.v[3], acc);
+            out[i] = acc;
+        }
+    }
+}
+
+template <typename T, int CM, bool EXACT, bool STORE>
+__global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
+    extern __shared__ __align__(32) unsigned char pr_smem[];
+    Op* s_ops = reinterpret_cast<Op*>(pr_smem);
+    V4<T>* s_stack = reinterpret_cast<V4<T>*>(pr_smem + (((size_t)a.n_ops * sizeof(Op) + 31) & ~(size_t)31));
+    for (int i = threadIdx.x; i < a.n_ops; i += blockDim.x) s_ops[i] = a.ops[i];
+    __syncthreads();
+
+    const int C = a.C;
+    const int site = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = site < a.n_sites;
+    const int cs = site;
+    const T* __restrict__ P = static_cast<const T*>(a.P);
+    const T* __restrict__ tipT = static_cast<const T*>(a.tipT);
+    const uint8_t* __restrict__ codes = a.codes;
+    T acc[CM][4];
+#pragma unroll
+    for (int k = 0; k < CM; ++k)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[k][i] = T(1);
+    int scale_e = 0;
+    int sp = 0;
+    const int nthr = blockDim.x;
+
+    for (int o = 0; valid && o < a.n_ops; ++o) {
+        const Op op = s_ops[o];
+        T d0[CM][4], d1[CM][4];
+        // ---- first child vector
+        if (op.s0 >= 0) {
+            const int code = codes[(size_t)op.s0 * a.site_stride + cs];
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) {
+                    const V4<T> tv = *reinterpret_cast<const V4<T>*>(
+                        tipT + (((size_t)op.s0 * C + k) * a.n_codes + code) * 4);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) d0[k][i] = tv.v[i];
+                }
+        } else {
+            if (op.s0 == kSrcPop) --sp;
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) {
+                    T x[4];
+                    if (op.s0 == kSrcPop) {
+                        const V4<T> sv = s_stack[((size_t)sp * CM + k) * nthr + threadIdx.x];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) x[i] = sv.v[i];
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) x[i] = acc[k][i];
+                    }
+                    matvec4<T, EXACT>(P + ((size_t)op.e0 * C + k) * 16, x, d0[k]);
+                }
+        }
+        // ---- second child vector
+        if (op.s1 >= 0) {
+            const int code = codes[(size_t)op.s1 * a.site_stride + cs];
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) {
+                    const V4<T> tv = *reinterpret_cast<const V4<T>*>(
+                        tipT + (((size_t)op.s1 * C + k) * a.n_codes + code) * 4);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) d1[k][i] = tv.v[i];
+                }
+        } else if (op.s1 == kSrcAcc) {
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) matvec4<T, EXACT>(P + ((size_t)op.e1 * C + k) * 16, acc[k], d1[k]);
+        }
+        // ---- combine: left assigns, right multiplies (commutative)
+        if (op.s1 == kSrcNone) {
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[k][i] = d0[k][i];
+        } else {
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[k][i] = EXACT ? mul_rn(d0[k][i], d1[k][i]) : d0[k][i] * d1[k][i];
+        }
+        // ---- per-site power-of-two scaling (exact)
+        T mx = T(0);
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+            if (k < C)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) mx = fmax(mx, acc[k][i]);
+        if (mx < scale_threshold<T>() && mx > T(0)) {
+            int e;
+            frexp(mx, &e);
+            const T f = ldexp(T(1), -e);
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[k][i] *= f;
+            scale_e += e;
+        }
+        if (STORE) {
+            T* cond = static_cast<T*>(a.cond);
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) {
+                    V4<T> w;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) w.v[i] = acc[k][i];
+                    *reinterpret_cast<V4<T>*>(cond + (((size_t)op.rank * C + k) * a.n_sites + site) * 4) = w;
+                }
+        }
+        if (op.push) {
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) {
+                    V4<T> w;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) w.v[i] = acc[k][i];
+                    s_stack[((size_t)sp * CM + k) * nthr + threadIdx.x] = w;
+                }
+            ++sp;
+        }
+    }
+    // ---- root: sum_k w_k sum_s L[s] * root_w[s]
+    double lsum = 0.0;
+#pragma unroll
+    for (int k = 0; k < CM; ++k)
+        if (k < C) {
+            double lk;
+            if (EXACT) {
+                lk = __dmul_rn((double)acc[k][0], a.root_w[0]);
+#pragma unroll
+                for (int s = 1; s < 4; ++s) lk = __dadd_rn(lk, __dmul_rn((double)acc[k][s], a.root_w[s]));
+                lsum = (k == 0) ? __dmul_rn(a.cat_w[0], lk) : __dadd_rn(lsum, __dmul_rn(a.cat_w[k], lk));
+            } else {
+                lk = (double)acc[k][0] * a.root_w[0];
+#pragma unroll
+                for (int s = 1; s < 4; ++s) lk = fma((double)acc[k][s], a.root_w[s], lk);
+                lsum = fma(a.cat_w[k], lk, lsum);
+            }
+        }
+    const double lnl = valid ? log(lsum) + (double)scale_e * 0.69314718055994530942 : 0.0;
+    if (valid) a.site_lnl[site] = lnl;
+    // ---- compensated block reduction
+    double s = valid ? lnl : 0.0, c = 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double os = __shfl_down_sync(0xffffffffu, s, off);
+        const double oc = __shfl_down_sync(0xffffffffu, c, off);
+        double ns, e;
+        two_sum(s, os, ns, e);
+        s = ns;
+        c = c + oc + e;
+    }
+    __shared__ double red_s[32], red_c[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        s = lane < nw ? red_s[lane] : 0.0;
+        c = lane < nw ? red_c[lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double os = __shfl_down_sync(0xffffffffu, s, off);
+            const double oc = __shfl_down_sync(0xffffffffu, c, off);
+            double ns, e;
+            two_sum(s, os, ns, e);
+            s = ns;
+            c = c + oc + e;
+        }
+        if (lane == 0) {
+            a.block_sum[2 * blockIdx.x] = s;
+            a.block_sum[2 * blockIdx.x + 1] = c;
+        }
+    }
+}
+
+}  // namespace
+
+// =========================================================================
+// Post-order pass, any state count: vectors in a global work buffer laid
+// out [rank][k][site][S]; one thread per site.
+// =========================================================================
+namespace {
+
+struct GenericArgs {
+    PruneArgs a;
+    const int* order;
+    const int* left;
+    const int* right;
+    const int* rank;
+    int n_int, n_tips, S;
+};
+
+template <typename T, bool EXACT>
+__device__ __forceinline__ void child_vec_generic(const GenericArgs& g, int v, int k, int site,
+                                                  int cs, const T* work, const T* P, T* out) {
+    const PruneArgs& a = g.a;
+    const int S = g.S, C = a.C;
+    if (v < g.n_tips) {
+        const int code = a.codes[(size_t)v * a.site_stride + cs];
+        const T* tv = static_cast<const T*>(a.tipT) + (((size_t)v * C + k) * a.n_codes + code) * S;
+        for (int i = 0; i < S; ++i) out[i] = tv[i];
+        return;
+    }
+    const T* x = work + (((size_t)g.rank[v] * C + k) * a.n_sites + site) * S;
+    const T* Pm = P + ((size_t)v * C + k) * S * S;
+    for (int i = 0; i < S; ++i) {
+        T acc;
+        if (EXACT) {
+            acc = mul_rn(x[0], Pm[i * S]);
+            for (int j = 1; j < S; ++j) acc = add_rn(acc, mul_rn(x[j], Pm[i * S + j]));
+        } else {
+            acc = x[0] * Pm[i * S];
+            for (int j = 1; j < S; ++j) acc = fma(x[j], Pm[i * S + j], acc);
+        }
+        out[i] = acc;
+    }
+}
+
+template <typename T, bool EXACT>
+__global__ void __launch_bounds__(kPruneThreads) prune_generic_kernel(GenericArgs g) {
+    const PruneArgs& a = g.a;
+    const int S = g.S, C = a.C;
+    const int site = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = site < a.n_sites;
+    const int cs = valid ? site : a.n_sites - 1;
+    T* work = static_cast<T*>(a.work);
+    const T* P = static_cast<const T*>(a.P);
+    int scale_e = 0;
+    T d0[kMaxStates], d1[kMaxStates];
+    for (int r = 0; valid && r < g.n_int; ++r) {
+        const int u = g.order[r];
+        const int l = g.left[u], rr = g.right[u];
+        T mx = T(0);
+        for (int k = 0; k < C; ++k) {
+            T* dst = work + (((size_t)r * C + k) * a.n_sites + cs) * S;
+            const int c0 = l >= 0 ? l : rr;
+            const int c1 = l >= 0 ? rr : -1;
+            child_vec_generic<T, EXACT>(g, c0, k, cs, cs, work, P, d0);
+            if (c1 >= 0) {
+                child_vec_generic<T, EXACT>(g, c1, k, cs, cs, work, P, d1);
+                for (int i = 0; i < S; ++i) d0[i] = EXACT ? mul_rn(d0[i], d1[i]) : d0[i] * d1[i];
+            }
+            for (int i = 0; i < S; ++i) mx = fmax(mx, d0[i]);
+            for (int i = 0; i < S; ++i) dst[i] = d0[i];
+        }
+        if (mx < scale_threshold<T>() && mx > T(0)) {
+            int e;
+            frexp(mx, &e);
+            const T f = ldexp(T(1), -e);
+            for (int k = 0; k < C; ++k) {
+                T* dst = work + (((size_t)r * C + k) * a.n_sites + cs) * S;
+                for (int i = 0; i < S; ++i) dst[i] *= f;
+            }
+            scale_e += e;
+        }
+    }
+    double lnl = 0.0;
+    if (valid) {
+        const int r = g.n_int - 1;
+        double lsum = 0.0;
+        for (int k = 0; k < C; ++k) {
+            const T* R = work + (((size_t)r * C + k) * a.n_sites + site) * S;
+            double lk;
+            if (EXACT) {
+                lk = __dmul_rn((double)R[0], a.root_w[0]);
+                for (int s = 1; s < S; ++s) lk = __dadd_rn(lk, __dmul_rn((double)R[s], a.root_w[s]));
+                lsum = (k == 0) ? __dmul_rn(a.cat_w[0], lk) : __dadd_rn(lsum, __dmul_rn(a.cat_w[k], lk));
+            } else {
+                lk = (double)R[0] * a.root_w[0];
+                for (int s = 1; s < S; ++s) lk = fma((double)R[s], a.root_w[s], lk);
+                lsum = fma(a.cat_w[k], lk, lsum);
+            }
+        }
+        lnl = log(lsum) + (double)scale_e * 0.69314718055994530942;
+        a.site_lnl[site] = lnl;
+    }
+    double s = lnl, c = 0.0;
+    for (int off = 16; off > 0; off >>= 1) {
+        const double os = __shfl_down_sync(0xffffffffu, s, off);
+        const double oc = __shfl_down_sync(0xffffffffu, c, off);
+        double ns, e;
+        two_sum(s, os, ns, e);
+        s = ns;
+        c = c + oc + e;
+    }
+    __shared__ double red_s[32], red_c[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        s = lane < nw ? red_s[lane] : 0.0;
+        c = lane < nw ? red_c[lane] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) {
+            const double os = __shfl_down_sync(0xffffffffu, s, off);
+            const double oc = __shfl_down_sync(0xffffffffu, c, off);
+            double ns, e;
+            two_sum(s, os, ns, e);
+            s = ns;
+            c = c + oc + e;
+        }
+        if (lane == 0) {
+            a.block_sum[2 * blockIdx.x] = s;
+            a.block_sum[2 * blockIdx.x + 1] = c;
+        }
+    }
+}
+
+}  // namespace
+
+template <typename T, int CM, bool EXACT>
+static cudaError_t launch_prune4(const PruneArgs& a, bool store, int blocks, cudaStream_t st) {
+    const size_t ops_bytes = ((size_t)a.n_ops * sizeof(Op) + 31) & ~(size_t)31;
+    const size_t stack_bytes = (size_t)(a.max_depth > 0 ? a.max_depth : 1) * CM * sizeof(V4<T>) * kPruneThreads;
+    const size_t smem = ops_bytes + stack_bytes;
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    cudaError_t err;
+    if (store) {
+        auto kern = prune4_kernel<T, CM, EXACT, true>;
+        err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+        kern<<<blocks, kPruneThreads, smem, st>>>(a);
+    } else {
+        auto kern = prune4_kernel<T, CM, EXACT, false>;
+        err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+        kern<<<blocks, kPruneThreads, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, int* n_blocks,
+                         cudaStream_t st) {
+    const int blocks = (a.n_sites + kPruneThreads - 1) / kPruneThreads;
+    *n_blocks = blocks;
+    const bool fp64 = precision == PLK_FP64;
+    if (S == 4 && a.C <= 8) {
+        const size_t ops_bytes = ((size_t)a.n_ops * sizeof(Op) + 31) & ~(size_t)31;
+        const int cm = a.C == 1 ? 1 : (a.C <= 4 ? 4 : 8);
+        const size_t stack_bytes = (size_t)(a.max_depth > 0 ? a.max_depth : 1) * cm *
+                                   (fp64 ? 32 : 16) * kPruneThreads;
+        if (ops_bytes + stack_bytes <= 227 * 1024) {
+            if (fp64) {
+                if (cm == 1) return launch_prune4<double, 1, true>(a, store, blocks, st);
+                if (cm == 4) return launch_prune4<double, 4, true>(a, store, blocks, st);
+                return launch_prune4<double, 8, true>(a, store, blocks, st);
+            }
+            if (cm == 1) return launch_prune4<float, 1, false>(a, store, blocks, st);
+            if (cm == 4) return launch_prune4<float, 4, false>(a, store, blocks, st);
+            return launch_prune4<float, 8, false>(a, store, blocks, st);
+        }
+    }
+    if (a.work == nullptr) return cudaErrorInvalidValue;
+    GenericArgs g{a, a.order, a.left, a.right, a.rank, a.n_int, a.n_tips, S};
+    if (fp64) prune_generic_kernel<double, true><<<blocks, kPruneThreads, 0, st>>>(g);
+    else prune_generic_kernel<float, false><<<blocks, kPruneThreads, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+// =========================================================================
+// Tip encoding for alphabets of <= 4 states: the code is the state set
+// itself; a cell with no allowed state raises the flag (check_nodes).
+// =========================================================================
+__global__ void encode_small_kernel(const uint32_t* __restrict__ masks, size_t n, uint32_t all,
+                                    uint8_t* __restrict__ codes, int* __restrict__ bad) {
+    const size_t n4 = n / 4;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    int any_bad = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const uint4 m = reinterpret_cast<const uint4*>(masks)[i];
+        const uint32_t a = m.x & all, b = m.y & all, c = m.z & all, d = m.w & all;
+        any_bad |= (a == 0) | (b == 0) | (c == 0) | (d == 0);
+        reinterpret_cast<uchar4*>(codes)[i] = make_uchar4((uint8_t)a, (uint8_t)b, (uint8_t)c, (uint8_t)d);
+    }
+    for (size_t i = n4 * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t a = masks[i] & all;
+        any_bad |= (a == 0);
+        codes[i] = (uint8_t)a;
+    }
+    if (__any_sync(0xffffffffu, any_bad) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+cudaError_t launch_encode_small(const uint32_t* masks, size_t n, uint32_t all, uint8_t* codes, int* bad,
+                                cudaStream_t st) {
+    const int threads = 256;
+    size_t blocks = (n / 4 + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    encode_small_kernel<<<(unsigned)blocks, threads, 0, st>>>(masks, n, all, codes, bad);
+    return cudaGetLastError();
+}
+
+// =========================================================================
+// Final compensated reduction of the block sums
+// =========================================================================
+__global__ void reduce_kernel(const double* __restrict__ bs, int n, double* out) {
+    double s = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double ns, e;
+        two_sum(s, bs[2 * i], ns, e);
+        s = ns;
+        c = c + bs[2 * i + 1] + e;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double os = __shfl_down_sync(0xffffffffu, s, off);
+        const double oc = __shfl_down_sync(0xffffffffu, c, off);
+        double ns, e;
+        two_sum(s, os, ns, e);
+        s = ns;
+        c = c + oc + e;
+    }
+    __shared__ double rs[32], rc[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { rs[warp] = s; rc[warp] = c; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        s = lane < nw ? rs[lane] : 0.0;
+        c = lane < nw ? rc[lane] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) {
+            const double os = __shfl_down_sync(0xffffffffu, s, off);
+            const double oc = __shfl_down_sync(0xffffffffu, c, off);
+            double ns, e;
+            two_sum(s, os, ns, e);
+            s = ns;
+            c = c + oc + e;
+        }
+        if (lane == 0) out[0] = s + c;
+    }
+}
+
+cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cudaStream_t st) {
+    reduce_kernel<<<1, 256, 0, st>>>(block_sum, n_blocks, out);
+    return cudaGetLastError();
+}
+
+// =========================================================================
+// Node-state outputs
+// =========================================================================
+template <typename T>
+__global__ void cond_normalise_kernel(const T* __restrict__ cond, const double* __restrict__ cat_w,
+                                      int n_int, int C, int n_sites, int S, double* __restrict__ out) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)n_int * n_sites) return;
+    const int r = (int)(idx / n_sites), site = (int)(idx % n_sites);
+    double v[kMaxStates];
+    double tot = 0.0;
+    for (int s = 0; s < S; ++s) {
+        double acc = 0.0;
+        for (int k = 0; k < C; ++k) acc += cat_w[k] * (double)cond[(((size_t)r * C + k) * n_sites + site) * S + s];
+        v[s] = acc;
+        tot += acc;
+    }
+    for (int s = 0; s < S; ++s) out[idx * S + s] = v[s] / tot;
+}
+
+cudaError_t launch_cond_normalise(const void* cond, const double* cat_w, int n_int, int C,
+                                  int n_sites, int S, int precision, double* out,
+                                  cudaStream_t st) {
+    const size_t n = (size_t)n_int * n_sites;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    if (precision == PLK_FP64)
+        cond_normalise_kernel<double><<<blocks, threads, 0, st>>>(static_cast<const double*>(cond), cat_w, n_int, C, n_sites, S, out);
+    else
+        cond_normalise_kernel<float><<<blocks, threads, 0, st>>>(static_cast<const float*>(cond), cat_w, n_int, C, n_sites, S, out);
+    return cudaGetLastError();
+}
+
+// Pre-order pass: Out(root) = root weights; for an internal child v of u with
+// sibling w, Out(v)[b] = sum_a Out(u)[a] * D_w[a] * P_v[a][b], D_w = P_w x_w.
+// Marginal(u)[s] ∝ sum_k w_k Out(u)[k][s] Cond(u)[k][s].  Vectors are
+// rescaled by powers of two (a common factor per node and site cancels in
+// the normalisation).
+template <typename T>
+__global__ void __launch_bounds__(128) preorder_kernel(PreorderArgs a) {
+    const int site = blockIdx.x * blockDim.x + threadIdx.x;
+    if (site >= a.n_sites) return;
+    const int S = a.S, C = a.C;
+    const T* cond = static_cast<const T*>(a.cond);
+    T* outside = static_cast<T*>(a.outside);
+    const T* P = static_cast<const T*>(a.P);
+    const T* tipT = static_cast<const T*>(a.tipT);
+    T o[kMaxStates], dw[kMaxStates], tmp[kMaxStates];
+    double marg[kMaxStates];
+    for (int r = a.n_int - 1; r >= 0; --r) {
+        const int u = a.order[r];
+        for (int s = 0; s < S; ++s) marg[s] = 0.0;
+        for (int k = 0; k < C; ++k) {
+            const T* cu = cond + (((size_t)r * C + k) * a.n_sites + site) * S;
+            const T* ou = outside + (((size_t)r * C + k) * a.n_sites + site) * S;
+            for (int s = 0; s < S; ++s) {
+                const T os = (r == a.n_int - 1) ? (T)a.root_w[s] : ou[s];
+                marg[s] += a.cat_w[k] * (double)os * (double)cu[s];
+            }
+        }
+        double tot = 0.0;
+        for (int s = 0; s < S; ++s) tot += marg[s];
+        for (int s = 0; s < S; ++s) a.out[((size_t)r * a.n_sites + site) * S + s] = marg[s] / tot;
+        const int kids[2] = {a.left[u], a.right[u]};
+        for (int c = 0; c < 2; ++c) {
+            const int v = kids[c], w = kids[1 - c];
+            if (v < 0 || v < a.n_tips) continue;
+            const int rv = a.rank[v];
+            T mx = T(0);
+            for (int k = 0; k < C; ++k) {
+                const T* ou = outside + (((size_t)r * C + k) * a.n_sites + site) * S;
+                for (int s = 0; s < S; ++s) o[s] = (r == a.n_int - 1) ? (T)a.root_w[s] : ou[s];
+                if (w >= 0) {
+                    if (w < a.n_tips) {
+                        const int code = a.codes[(size_t)w * a.site_stride + site];
+                        const T* tv = tipT + (((size_t)w * C + k) * a.n_codes + code) * S;
+                        for (int i = 0; i < S; ++i) dw[i] = tv[i];
+                    } else {
+                        const T* x = cond + (((size_t)a.rank[w] * C + k) * a.n_sites + site) * S;
+                        const T* Pw = P + ((size_t)w * C + k) * S * S;
+                        for (int i = 0; i < S; ++i) {
+                            T acc = T(0);
+                            for (int j = 0; j < S; ++j) acc = fma(x[j], Pw[i * S + j], acc);
+                            dw[i] = acc;
+                        }
+                    }
+                    for (int i = 0; i < S; ++i) tmp[i] = o[i] * dw[i];
+                } else {
+                    for (int i = 0; i < S; ++i) tmp[i] = o[i];
+                }
+                const T* Pv = P + ((size_t)v * C + k) * S * S;
+                T* ov = outside + (((size_t)rv * C + k) * a.n_sites + site) * S;
+                for (int b = 0; b < S; ++b) {
+                    T acc = T(0);
+                    for (int i = 0; i < S; ++i) acc = fma(tmp[i], Pv[i * S + b], acc);
+                    ov[b] = acc;
+                    mx = fmax(mx, acc);
+                }
+            }
+            if (mx < scale_threshold<T>() && mx > T(0)) {
+                int e;
+                frexp(mx, &e);
+                const T f = ldexp(T(1), -e);
+                for (int k = 0; k < C; ++k) {
+                    T* ov = outside + (((size_t)rv * C + k) * a.n_sites + site) * S;
+                    for (int b = 0; b < S; ++b) ov[b] *= f;
+                }
+            }
+        }
+    }
+}
+
+cudaError_t launch_preorder(const PreorderArgs& a, int precision, cudaStream_t st) {
+    const int threads = 128;
+    const int blocks = (a.n_sites + threads - 1) / threads;
+    if (precision == PLK_FP64) preorder_kernel<double><<<blocks, threads, 0, st>>>(a);
+    else preorder_kernel<float><<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace plk

@@ -1,0 +1,259 @@
+"""ctypes binding of libplk (include/plk.h).
+
+The engine itself is the C ABI; this module only marshals numpy arrays across
+it.  Loading fails loudly when ``lib/libplk.so`` has not been built: there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libplk.so")
+
+PLK_OK = 0
+PLK_ERR_ARG = -1
+PLK_ERR_ALLOC = -2
+PLK_ERR_CUDA = -3
+PLK_ERR_STATE = -4
+PLK_ERR_TIMEOUT = -5
+PLK_ERR_NUMERIC = -6
+PLK_ERR_TIP = -7
+PLK_ERR_NODEV = -8
+PLK_ERR_UNSUPPORTED = -9
+
+PLK_FP64 = 0
+PLK_FP32S = 1
+PLK_P_TAYLOR20 = 0
+PLK_P_EXACT = 1
+PLK_NODES_COND = 0
+PLK_NODES_MARGINAL = 1
+
+# Every symbol include/plk.h declares (checked by the tests).
+EXPORTS = [
+    "plk_create", "plk_destroy", "plk_last_error", "plk_status_string", "plk_api_version",
+    "plk_set_alignment", "plk_set_tree", "plk_set_rate_model", "plk_set_model",
+    "plk_loglik", "plk_site_loglik", "plk_node_states", "plk_n_internal",
+    "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
+    "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
+]
+
+_lib = None
+
+
+class PlkError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"plk status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libplk.so not built at {LIB_PATH}: run `python -m phylommand_gb300.build`")
+    L = ctypes.CDLL(LIB_PATH)
+    c_int, c_double, c_void_p = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    fp = ctypes.POINTER(ctypes.c_float)
+    up = ctypes.POINTER(ctypes.c_uint)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    hp = ctypes.c_void_p
+    L.plk_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int]
+    L.plk_destroy.argtypes = [hp]
+    L.plk_destroy.restype = None
+    L.plk_last_error.argtypes = [hp]
+    L.plk_last_error.restype = ctypes.c_char_p
+    L.plk_status_string.argtypes = [c_int]
+    L.plk_status_string.restype = ctypes.c_char_p
+    L.plk_api_version.argtypes = []
+    L.plk_set_alignment.argtypes = [hp, c_int, c_int, c_int, u32p]
+    L.plk_set_tree.argtypes = [hp, c_int, ip, ip, dp]
+    L.plk_set_rate_model.argtypes = [hp, c_int, c_int, fp, fp, ip, c_int, fp]
+    L.plk_set_model.argtypes = [hp, c_int, dp, dp, c_int, c_int, dp, dp, c_int]
+    L.plk_loglik.argtypes = [hp, c_int, dp]
+    L.plk_site_loglik.argtypes = [hp, dp]
+    L.plk_node_states.argtypes = [hp, c_int, c_int, dp]
+    L.plk_n_internal.argtypes = [hp]
+    L.plk_q_matrix.argtypes = [c_int, c_int, up, dp, dp, dp]
+    L.plk_pmat_host.argtypes = [c_int, dp, dp, c_int, c_double, c_int, dp]
+    L.plk_discrete_gamma.argtypes = [c_double, c_int, dp]
+    L.plk_effective_lengths.argtypes = [c_int, ip, ip, dp, c_int, c_int, fp, fp, ip, c_int, fp, dp]
+    L.plk_loglik_async.argtypes = [hp, c_int]
+    L.plk_loglik_result.argtypes = [hp, dp]
+    L.plk_set_stream.argtypes = [hp, c_void_p]
+    L.plk_set_profiling.argtypes = [hp, c_int]
+    L.plk_kernel_times.argtypes = [hp, dp, ip, c_int]
+    for name in EXPORTS:
+        if name not in ("plk_destroy", "plk_last_error", "plk_status_string"):
+            getattr(L, name).restype = c_int
+    _lib = L
+    return L
+
+
+def _p(a, ct):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def _check(status: int, handle=None) -> None:
+    if status != PLK_OK:
+        msg = lib().plk_last_error(handle)
+        raise PlkError(status, msg.decode() if msg else "")
+
+
+# ---------------------------------------------------------------- host helpers
+def q_matrix(n_states: int, reversible: bool, rate_spec, rates, freqs=None) -> np.ndarray:
+    spec = np.ascontiguousarray(rate_spec, dtype=np.uint32)
+    r = np.ascontiguousarray(rates, dtype=np.float64)
+    f = None if freqs is None else np.ascontiguousarray(freqs, dtype=np.float64)
+    Q = np.zeros((n_states, n_states))
+    _check(lib().plk_q_matrix(n_states, int(reversible), _p(spec, ctypes.c_uint), _p(r, ctypes.c_double),
+                              _p(f, ctypes.c_double), _p(Q, ctypes.c_double)))
+    return Q
+
+
+def pmat_host(Q, t: float, p_mode: int = PLK_P_EXACT, root_weights=None, reversible: bool = True) -> np.ndarray:
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    w = None if root_weights is None else np.ascontiguousarray(root_weights, dtype=np.float64)
+    P = np.zeros_like(Q)
+    _check(lib().plk_pmat_host(Q.shape[0], _p(Q, ctypes.c_double), _p(w, ctypes.c_double), int(reversible),
+                               float(t), int(p_mode), _p(P, ctypes.c_double)))
+    return P
+
+
+def discrete_gamma(alpha: float, K: int) -> np.ndarray:
+    out = np.zeros(K)
+    _check(lib().plk_discrete_gamma(float(alpha), int(K), _p(out, ctypes.c_double)))
+    return out
+
+
+def effective_lengths(left, right, branch_length, root_quirk: bool = True, cut_off=(), cut_rate=(),
+                      clade_of_node=None, clade_rate=()) -> np.ndarray:
+    l = np.ascontiguousarray(left, dtype=np.int32)
+    r = np.ascontiguousarray(right, dtype=np.int32)
+    b = np.ascontiguousarray(branch_length, dtype=np.float64)
+    co = np.ascontiguousarray(cut_off, dtype=np.float32)
+    cr = np.ascontiguousarray(cut_rate, dtype=np.float32)
+    crt = np.ascontiguousarray(clade_rate, dtype=np.float32)
+    con = None if clade_of_node is None else np.ascontiguousarray(clade_of_node, dtype=np.int32)
+    out = np.zeros(l.shape[0])
+    _check(lib().plk_effective_lengths(l.shape[0], _p(l, ctypes.c_int), _p(r, ctypes.c_int), _p(b, ctypes.c_double),
+                                       int(root_quirk), len(co), _p(co, ctypes.c_float) if len(co) else None,
+                                       _p(cr, ctypes.c_float) if len(cr) else None, _p(con, ctypes.c_int),
+                                       len(crt), _p(crt, ctypes.c_float) if len(crt) else None,
+                                       _p(out, ctypes.c_double)))
+    return out
+
+
+# ---------------------------------------------------------------------- handle
+class Handle:
+    """One alignment + tree + model resident on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        _check(lib().plk_create(ctypes.byref(self._h), int(device)), None)
+        self.n_states = 0
+        self.n_sites = 0
+
+    def close(self) -> None:
+        if self._h:
+            lib().plk_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def raw(self):
+        return self._h
+
+    def set_alignment(self, masks: np.ndarray, n_states: int) -> None:
+        m = np.ascontiguousarray(masks, dtype=np.uint32)
+        _check(lib().plk_set_alignment(self._h, m.shape[0], m.shape[1], int(n_states), _p(m, ctypes.c_uint32)), self._h)
+        self.n_states = int(n_states)
+        self.n_sites = int(m.shape[1])
+
+    def set_tree(self, left, right, branch_length) -> None:
+        l = np.ascontiguousarray(left, dtype=np.int32)
+        r = np.ascontiguousarray(right, dtype=np.int32)
+        b = np.ascontiguousarray(branch_length, dtype=np.float64)
+        _check(lib().plk_set_tree(self._h, l.shape[0], _p(l, ctypes.c_int), _p(r, ctypes.c_int), _p(b, ctypes.c_double)), self._h)
+
+    def set_rate_model(self, root_quirk: bool = True, cut_off=(), cut_rate=(), clade_of_node=None, clade_rate=()) -> None:
+        co = np.ascontiguousarray(cut_off, dtype=np.float32)
+        cr = np.ascontiguousarray(cut_rate, dtype=np.float32)
+        crt = np.ascontiguousarray(clade_rate, dtype=np.float32)
+        con = None if clade_of_node is None else np.ascontiguousarray(clade_of_node, dtype=np.int32)
+        _check(lib().plk_set_rate_model(self._h, int(root_quirk), len(co), _p(co, ctypes.c_float) if len(co) else None,
+                                        _p(cr, ctypes.c_float) if len(cr) else None,
+                                        _p(con, ctypes.c_int), len(crt), _p(crt, ctypes.c_float) if len(crt) else None), self._h)
+
+    def set_model(self, Q, root_weights, reversible: bool = True, cat_rates=(1.0,), cat_weights=(1.0,),
+                  p_mode: int = PLK_P_TAYLOR20) -> None:
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        w = np.ascontiguousarray(root_weights, dtype=np.float64)
+        cr = np.ascontiguousarray(cat_rates, dtype=np.float64)
+        cw = np.ascontiguousarray(cat_weights, dtype=np.float64)
+        _check(lib().plk_set_model(self._h, Q.shape[0], _p(Q, ctypes.c_double), _p(w, ctypes.c_double), int(reversible),
+                                   cr.shape[0], _p(cr, ctypes.c_double), _p(cw, ctypes.c_double), int(p_mode)), self._h)
+
+    def loglik(self, precision: int = PLK_FP64) -> float:
+        out = ctypes.c_double(0.0)
+        _check(lib().plk_loglik(self._h, int(precision), ctypes.byref(out)), self._h)
+        return out.value
+
+    def loglik_status(self, precision: int = PLK_FP64) -> tuple[int, float]:
+        out = ctypes.c_double(0.0)
+        st = lib().plk_loglik(self._h, int(precision), ctypes.byref(out))
+        return st, out.value
+
+    def loglik_async(self, precision: int = PLK_FP32S) -> None:
+        _check(lib().plk_loglik_async(self._h, int(precision)), self._h)
+
+    def loglik_result(self) -> float:
+        out = ctypes.c_double(0.0)
+        _check(lib().plk_loglik_result(self._h, ctypes.byref(out)), self._h)
+        return out.value
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        """Run on an existing CUDA stream (e.g. torch.cuda.Stream().cuda_stream)."""
+        _check(lib().plk_set_stream(self._h, ctypes.c_void_p(cuda_stream or 0)), self._h)
+
+    def set_profiling(self, on: bool) -> None:
+        _check(lib().plk_set_profiling(self._h, int(on)), self._h)
+
+    def kernel_times(self, reset: bool = True) -> tuple[np.ndarray, int]:
+        """Summed ms of (P(t), post-order, reduction) and the evaluation count."""
+        ms = np.zeros(3)
+        n = ctypes.c_int(0)
+        _check(lib().plk_kernel_times(self._h, _p(ms, ctypes.c_double), ctypes.byref(n), int(reset)), self._h)
+        return ms, n.value
+
+    def site_loglik(self) -> np.ndarray:
+        out = np.zeros(self.n_sites)
+        _check(lib().plk_site_loglik(self._h, _p(out, ctypes.c_double)), self._h)
+        return out
+
+    def n_internal(self) -> int:
+        return int(lib().plk_n_internal(self._h))
+
+    def node_states(self, mode: int = PLK_NODES_COND, precision: int = PLK_FP64) -> np.ndarray:
+        out = np.zeros((self.n_internal(), self.n_sites, self.n_states))
+        _check(lib().plk_node_states(self._h, int(mode), int(precision), _p(out, ctypes.c_double)), self._h)
+        return out
+

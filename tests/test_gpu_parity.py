@@ -1,0 +1,203 @@
+"""GPU parity: the engine (through the C ABI) against the reference's golden
+fixtures and against the FP64 oracle.
+
+Tolerances: FP64 plain form 1e-12 relative on lnL (the reference order is kept,
+so it is equal up to the order of the final site sum); FP32 scaled form 1e-6
+relative on lnL and 1e-5 absolute on normalised node probabilities."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from phylommand_gb300 import plk, synth
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+FP64_REL = 1e-12
+FP32_REL = 1e-6
+FP32_PROB = 1e-5
+
+
+@pytest.mark.parametrize("name", H.fixture_names())
+def test_fp64_matches_reference_fixture(name):
+    fx = H.load_fixture(name)
+    with H.engine_for_fixture(fx) as h:
+        lnl = h.loglik(plk.PLK_FP64)
+        assert lnl == pytest.approx(float(fx["lnl"]), rel=FP64_REL)
+        site = h.site_loglik()
+        # per site, the same operations in the same order as the reference
+        np.testing.assert_allclose(site, fx["site_lnl"], rtol=1e-14, atol=1e-14)
+        nodes = h.node_states(plk.PLK_NODES_COND, plk.PLK_FP64)
+        k = fx["node_cond"].shape[1]
+        ref = H.normalise_cond(fx["node_cond"], fx["cat_weights"])
+        np.testing.assert_allclose(nodes[:, :k], ref, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", H.fixture_names())
+def test_fp32_scaled_matches_reference_fixture(name):
+    fx = H.load_fixture(name)
+    with H.engine_for_fixture(fx) as h:
+        lnl = h.loglik(plk.PLK_FP32S)
+        assert lnl == pytest.approx(float(fx["lnl"]), rel=FP32_REL)
+        nodes = h.node_states(plk.PLK_NODES_COND, plk.PLK_FP32S)
+        k = fx["node_cond"].shape[1]
+        ref = H.normalise_cond(fx["node_cond"], fx["cat_weights"])
+        np.testing.assert_allclose(nodes[:, :k], ref, rtol=0, atol=FP32_PROB)
+
+
+@pytest.mark.parametrize("name", H.fixture_names())
+def test_marginals_match_oracle(name):
+    fx = H.load_fixture(name)
+    orc = H.oracle_for_fixture(fx, want_marginal=True)
+    with H.engine_for_fixture(fx) as h:
+        m64 = h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64)
+        np.testing.assert_allclose(m64, orc.marginal, rtol=0, atol=1e-12)
+        m32 = h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP32S)
+        np.testing.assert_allclose(m32, orc.marginal, rtol=0, atol=FP32_PROB)
+
+
+@pytest.mark.parametrize("name", ["ex_gtr_gamma_noquirk", "syn_gtr_gamma_ambig", "syn_protein20", "syn_nontr"])
+def test_exact_pmat_mode_matches_oracle(name):
+    fx = H.load_fixture(name)
+    orc = H.oracle_for_fixture(fx, p_mode=O.P_EXACT)
+    with H.engine_for_fixture(fx, p_mode=plk.PLK_P_EXACT) as h:
+        assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-11)
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+
+
+def _random_case(rng, n_tips, n_sites, S=4, C=1, missing=0.02, shape="yule"):
+    if shape == "yule":
+        left, right, bl = synth.yule_tree(n_tips, 0.1, rng)
+    else:  # caterpillar: ((((t0,t1),t2),t3)...)
+        n_nodes = 2 * n_tips - 1
+        left = np.full(n_nodes, -1, dtype=np.int32)
+        right = np.full(n_nodes, -1, dtype=np.int32)
+        prev = 0
+        for i in range(1, n_tips):
+            u = n_tips + i - 1
+            left[u], right[u] = prev, i
+            prev = u
+        bl = rng.exponential(0.1, n_nodes)
+    f = rng.dirichlet(np.ones(S) * 5)
+    npos = S * (S - 1) // 2
+    Q = synth.reversible_q(S, rng.uniform(0.5, 3, npos), f)
+    masks = (np.uint32(1) << rng.integers(0, S, size=(n_tips, n_sites)).astype(np.uint32)).astype(np.uint32)
+    masks[rng.random(masks.shape) < missing] = np.uint32((1 << S) - 1)
+    cr = plk.discrete_gamma(0.6, C) if C > 1 else np.ones(1)
+    cw = np.full(C, 1.0 / C)
+    return left, right, bl, masks, Q, f, cr, cw
+
+
+def _engine(left, right, bl, masks, S, Q, f, cr, cw, p_mode=plk.PLK_P_EXACT, quirk=False):
+    h = plk.Handle()
+    h.set_alignment(masks, S)
+    h.set_tree(left, right, bl)
+    h.set_rate_model(quirk)
+    h.set_model(Q, f, True, cr, cw, p_mode)
+    return h
+
+
+@pytest.mark.parametrize("n_sites", [1, 31, 127, 128, 129, 1000, 4099])
+def test_ragged_site_counts(n_sites):
+    rng = np.random.default_rng(n_sites)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 13, n_sites, C=4)
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
+    with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
+        assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-11)
+        np.testing.assert_allclose(h.site_loglik(), orc.site_lnl, rtol=1e-11)
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+
+
+@pytest.mark.parametrize("S,C", [(2, 1), (3, 2), (4, 8), (4, 12), (5, 4), (20, 4), (24, 2)])
+def test_state_and_category_counts(S, C):
+    """Fused 4-state kernel for C <= 8, generic kernel otherwise."""
+    rng = np.random.default_rng(S * 100 + C)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 17, 300, S=S, C=C)
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT, want_marginal=True)
+    with _engine(left, right, bl, masks, S, Q, f, cr, cw) as h:
+        assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-11)
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+        np.testing.assert_allclose(h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64), orc.marginal, atol=1e-11)
+
+
+@pytest.mark.parametrize("shape,n_tips", [("yule", 600), ("caterpillar", 400)])
+def test_deep_and_wide_trees(shape, n_tips):
+    rng = np.random.default_rng(n_tips)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, 333, C=4, shape=shape)
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
+    with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
+        assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-11)
+        # a caterpillar of 400 tips underflows FP32 without the per-site scaling
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+
+
+def test_unary_nodes():
+    """A node with one child passes its child's transported vector up."""
+    # root(6) has one child 5; 5 = (4, t2); 4 = (t0, t1); node 3 = unary above t3? keep tips 0..3
+    left = np.array([-1, -1, -1, -1, 0, 4, 5, 3], dtype=np.int32)
+    right = np.array([-1, -1, -1, -1, 1, 2, -1, 6], dtype=np.int32)
+    bl = np.array([0.1, 0.2, 0.3, 0.15, 0.05, 0.07, 0.2, 0.0])
+    rng = np.random.default_rng(3)
+    masks = (1 << rng.integers(0, 4, size=(4, 50))).astype(np.uint32)
+    f = np.full(4, 0.25)
+    Q = synth.reversible_q(4, np.ones(6), f)
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, p_mode=O.P_EXACT, want_marginal=True)
+    with _engine(left, right, bl, masks, 4, Q, f, np.ones(1), np.ones(1)) as h:
+        assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-12)
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+        np.testing.assert_allclose(h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64), orc.marginal, atol=1e-12)
+
+
+def test_tip_without_state_returns_zero_like_the_reference():
+    """simpleML::check_nodes fails -> calculate_log_likelihood returns 0.0."""
+    fx = H.load_fixture("quirk_a")
+    masks = fx["masks"].copy()
+    masks[2, 3] = 0
+    with plk.Handle() as h:
+        h.set_alignment(masks, 4)
+        h.set_tree(fx["left"], fx["right"], fx["bl"])
+        h.set_model(fx["Q"], fx["root_w"], True)
+        st, v = h.loglik_status(plk.PLK_FP64)
+        assert st == plk.PLK_ERR_TIP and v == 0.0
+
+
+def test_call_order_and_argument_errors():
+    with plk.Handle() as h:
+        st, _ = h.loglik_status()
+        assert st == plk.PLK_ERR_STATE
+        with pytest.raises(plk.PlkError) as e:
+            h.set_alignment(np.zeros((3, 0), dtype=np.uint32), 4)
+        assert e.value.status == plk.PLK_ERR_ARG
+        with pytest.raises(plk.PlkError):
+            h.set_tree([-1, -1, 0], [-1, -1, 1], [0.1, np.nan, 0.0])
+        h.set_alignment(np.full((2, 5), 15, dtype=np.uint32), 4)
+        h.set_tree([-1, -1, -1, 0], [-1, -1, -1, 1], [0.1, 0.1, 0.1, 0.0])  # 3 leaves vs 2 rows
+        h.set_model(np.full((4, 4), 1 / 3) - np.eye(4) * (4 / 3), np.full(4, 0.25), True)
+        st, _ = h.loglik_status()
+        assert st == plk.PLK_ERR_ARG
+
+
+def test_repeat_calls_are_deterministic():
+    fx = H.load_fixture("syn_gtr_gamma_ambig")
+    with H.engine_for_fixture(fx, p_mode=plk.PLK_P_EXACT) as h:
+        a = [h.loglik(plk.PLK_FP32S) for _ in range(3)]
+        b = [h.loglik(plk.PLK_FP64) for _ in range(3)]
+        assert a[0] == a[1] == a[2] and b[0] == b[1] == b[2]
+
+
+def test_full_size_dna_gtr_gamma_fp32_against_fp64():
+    """128 taxa x 100,000 sites, GTR+Gamma4, 2% missing: FP32-scaled vs FP64
+    engine vs FP64 oracle (a size-independent relative bound)."""
+    w = synth.make("cfg2", seed=2)
+    teff = plk.effective_lengths(w.left, w.right, w.bl, False)
+    orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights,
+                   p_mode=O.P_EXACT, threads=8)
+    with _engine(w.left, w.right, w.bl, w.masks, 4, w.Q, w.freqs, w.cat_rates, w.cat_weights) as h:
+        l64 = h.loglik(plk.PLK_FP64)
+        l32 = h.loglik(plk.PLK_FP32S)
+    assert l64 == pytest.approx(orc.lnl, rel=1e-11)
+    assert l32 == pytest.approx(orc.lnl, rel=FP32_REL)
