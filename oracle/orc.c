@@ -318,6 +318,7 @@ static void* run_sites(void* arg) {
     double* xbuf = (double*)malloc(sizeof(double) * (size_t)S);
     double* Dtmp = (double*)malloc(sizeof(double) * (size_t)S);
     for (int site = J->site_lo; site < J->site_hi; ++site) {
+        long site_exp = 0;
         /* check_nodes: a tip cell with no allowed state fails the whole call */
         for (int t = 0; t < J->n_tips; ++t)
             if ((J->tips[(size_t)t * J->n_sites + site] & ((S >= 32) ? 0xffffffffu : ((1u << S) - 1u))) == 0)
@@ -346,6 +347,16 @@ static void* run_sites(void* arg) {
                     }
                 }
             }
+            /* power-of-two rescaling below 2^-256 (exact; absent in the
+             * reference, whose trees never get there) */
+            double mx = 0.0;
+            for (int q = 0; q < C * S; ++q) if (cs[(size_t)r * C * S + q] > mx) mx = cs[(size_t)r * C * S + q];
+            if (mx > 0.0 && mx < 0x1p-256) {
+                int e;
+                frexp(mx, &e);
+                for (int q = 0; q < C * S; ++q) cs[(size_t)r * C * S + q] = ldexp(cs[(size_t)r * C * S + q], -e);
+                site_exp += e;
+            }
         }
         /* root: sum_k w_k sum_s L[s] * (tr ? pi_s : 1)  (src/simpleML.h:123-141) */
         int rroot = n_int - 1;
@@ -356,7 +367,7 @@ static void* run_sites(void* arg) {
             for (int s = 0; s < S; ++s) lk += R[s] * J->root_w[s];
             lsum += J->cat_weight[k] * lk;
         }
-        if (J->site_lnl) J->site_lnl[site] = log(lsum);
+        if (J->site_lnl) J->site_lnl[site] = site_exp ? log(lsum) + (double)site_exp * 0.69314718055994530942 : log(lsum);
         if (J->cond_out)
             for (int r = 0; r < n_int; ++r)
                 memcpy(J->cond_out + (((size_t)r * J->n_sites + site) * C) * S,
@@ -396,6 +407,14 @@ static void* run_sites(void* arg) {
                             for (int a = 0; a < S; ++a) acc += Dtmp[a] * Pv[a * S + b];
                             Ov[b] = acc;
                         }
+                    }
+                    double* Ov0 = out + (size_t)J->rank[v] * C * S;
+                    double mo = 0.0;
+                    for (int q = 0; q < C * S; ++q) if (Ov0[q] > mo) mo = Ov0[q];
+                    if (mo > 0.0 && mo < 0x1p-256) {
+                        int e;
+                        frexp(mo, &e);
+                        for (int q = 0; q < C * S; ++q) Ov0[q] = ldexp(Ov0[q], -e);
                     }
                 }
             }
