@@ -55,9 +55,20 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 template <typename T>
 __device__ __forceinline__ T scale_threshold();
 template <>
-__device__ __forceinline__ float scale_threshold<float>() { return 5.421010862427522e-20f; }  // 2^-64
+__device__ __forceinline__ float scale_threshold<float>() { return 2.3283064365386963e-10f; }  // 2^-32
 template <>
 __device__ __forceinline__ double scale_threshold<double>() { return 8.636168555094445e-78; }  // 2^-256
+
+// Rescale a vector whose maximum mx lies below the threshold so that the
+// maximum lands in [0.5, 1): multiply by 2^-e (mx = f 2^e) in two exact
+// power-of-two steps, each finite in T even when mx is subnormal.
+template <typename T>
+__device__ __forceinline__ void pow2_factors(T mx, int* e, T* f1, T* f2) {
+    frexp(mx, e);
+    const int k = -*e, half = k / 2;
+    *f1 = ldexp(T(1), half);
+    *f2 = ldexp(T(1), k - half);
+}
 
 }  // namespace
 
@@ -302,12 +313,12 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
                 for (int i = 0; i < 4; ++i) mx = fmax(mx, acc[k][i]);
         if (mx < scale_threshold<T>() && mx > T(0)) {
             int e;
-            frexp(mx, &e);
-            const T f = ldexp(T(1), -e);
+            T f1, f2;
+            pow2_factors(mx, &e, &f1, &f2);
 #pragma unroll
             for (int k = 0; k < CM; ++k)
 #pragma unroll
-                for (int i = 0; i < 4; ++i) acc[k][i] *= f;
+                for (int i = 0; i < 4; ++i) acc[k][i] = (acc[k][i] * f1) * f2;
             scale_e += e;
         }
         if (STORE) {
@@ -460,11 +471,11 @@ __global__ void __launch_bounds__(kPruneThreads) prune_generic_kernel(GenericArg
         }
         if (mx < scale_threshold<T>() && mx > T(0)) {
             int e;
-            frexp(mx, &e);
-            const T f = ldexp(T(1), -e);
+            T f1, f2;
+            pow2_factors(mx, &e, &f1, &f2);
             for (int k = 0; k < C; ++k) {
                 T* dst = work + (((size_t)r * C + k) * a.n_sites + cs) * S;
-                for (int i = 0; i < S; ++i) dst[i] *= f;
+                for (int i = 0; i < S; ++i) dst[i] = (dst[i] * f1) * f2;
             }
             scale_e += e;
         }
@@ -750,11 +761,11 @@ __global__ void __launch_bounds__(128) preorder_kernel(PreorderArgs a) {
             }
             if (mx < scale_threshold<T>() && mx > T(0)) {
                 int e;
-                frexp(mx, &e);
-                const T f = ldexp(T(1), -e);
+                T f1, f2;
+                pow2_factors(mx, &e, &f1, &f2);
                 for (int k = 0; k < C; ++k) {
                     T* ov = outside + (((size_t)rv * C + k) * a.n_sites + site) * S;
-                    for (int b = 0; b < S; ++b) ov[b] *= f;
+                    for (int b = 0; b < S; ++b) ov[b] = (ov[b] * f1) * f2;
                 }
             }
         }

@@ -175,7 +175,7 @@ def test_call_order_and_argument_errors():
         with pytest.raises(plk.PlkError):
             h.set_tree([-1, -1, 0], [-1, -1, 1], [0.1, np.nan, 0.0])
         h.set_alignment(np.full((2, 5), 15, dtype=np.uint32), 4)
-        h.set_tree([-1, -1, -1, 0], [-1, -1, -1, 1], [0.1, 0.1, 0.1, 0.0])  # 3 leaves vs 2 rows
+        h.set_tree([-1, -1, -1, 0, 3], [-1, -1, -1, 1, 2], [0.1, 0.1, 0.1, 0.1, 0.0])  # 3 leaves vs 2 rows
         h.set_model(np.full((4, 4), 1 / 3) - np.eye(4) * (4 / 3), np.full(4, 0.25), True)
         st, _ = h.loglik_status()
         assert st == plk.PLK_ERR_ARG
