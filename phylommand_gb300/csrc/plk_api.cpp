@@ -47,6 +47,11 @@ struct DevBuf {
 
 }  // namespace
 
+plk_status plk::report_error(plk_status s, const std::string& msg) {
+    g_create_error = msg;
+    return s;
+}
+
 struct plk_handle {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -84,6 +89,9 @@ struct plk_handle {
     DevBuf d_mask_raw, d_flag;
     bool have_lnl = false;
     bool lnl_pending = false;
+    // autotuned 4-state FP32 kernel (-1: not tuned for the current inputs)
+    int variant = -1;
+    float tune_ms[3] = {0.f, 0.f, 0.f};
     // streams: own_stream is created with the handle; stream is the active one
     cudaStream_t own_stream = nullptr;
     // kernel timing (plk_set_profiling)
@@ -176,7 +184,7 @@ PruneArgs prune_args(plk_handle* h, int precision) {
     a.n_ops = (int)h->prog.ops.size();
     a.max_depth = h->prog.max_depth;
     a.codes = h->d_codes.as<uint8_t>();
-    a.site_stride = h->n_sites;
+    a.site_stride = code_stride(h->n_sites);
     a.n_sites = h->n_sites;
     a.n_codes = h->n_codes;
     a.C = h->C;
@@ -203,6 +211,47 @@ bool fused_kernel_applies(const plk_handle* h, int precision) {
     return ops_bytes + stack <= 227 * 1024;
 }
 
+// Autotuner of the 4-state FP32 post-order kernel: times every candidate
+// (prune4_kernel; prune4s_kernel with 1 and 2 sites per thread) on this
+// handle's tree and sites -- one warm-up and three timed launches each, CUDA
+// events on the handle's stream -- and keeps the fastest until the tree,
+// alignment or model changes.  PLK_PRUNE_VARIANT=0|1|2 forces a choice.
+plk_status autotune_prune(plk_handle* h, PruneArgs a) {
+    if (const char* f = getenv("PLK_PRUNE_VARIANT")) {
+        const int v = atoi(f);
+        if (v >= 0 && v <= 2 && (v == 0 || prune4s_fits(a, v))) {
+            h->variant = v;
+            return PLK_OK;
+        }
+    }
+    cudaEvent_t e0, e1;
+    PLK_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
+    PLK_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
+    float best = 1e30f;
+    int best_v = 0;
+    cudaError_t err = cudaSuccess;
+    for (int v = 0; v <= 2 && err == cudaSuccess; ++v) {
+        if (v > 0 && !prune4s_fits(a, v)) continue;
+        a.variant = v;
+        int nb = 0;
+        err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
+        if (err != cudaSuccess) break;
+        err = cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 3 && err == cudaSuccess; ++r) err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
+        if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        h->tune_ms[v] = ms / 3.0f;
+        if (err == cudaSuccess && ms < best) { best = ms; best_v = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return cuda_fail(h, err, "autotune post-order kernel");
+    h->variant = best_v;
+    return PLK_OK;
+}
+
 // Runs the post-order pass (P(t) already built); store != null asks for the
 // conditional vectors of every internal node in *store.
 plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* after_prune = nullptr) {
@@ -221,6 +270,13 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     } else if (store) {
         PLK_CUDA(h, h->d_cond.ensure(vec_bytes), "allocate node vectors");
         a.cond = h->d_cond.p;
+    }
+    if (fused && !store && precision == PLK_FP32S) {
+        if (h->variant < 0) {
+            plk_status s = autotune_prune(h, a);
+            if (s != PLK_OK) return s;
+        }
+        a.variant = h->variant;
     }
     int nb = 0;
     PLK_CUDA(h, launch_prune(a, h->S, precision, store != nullptr, &nb, h->stream), "post-order kernel launch");
@@ -306,13 +362,13 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
         // device straight from the caller's masks
         for (uint32_t c = 0; c < (1u << n_states); ++c) table.push_back(c);
         PLK_CUDA(h, h->d_mask_raw.ensure(n_cells * sizeof(uint32_t)), "allocate mask staging");
-        PLK_CUDA(h, h->d_codes.ensure(n_cells), "allocate tip codes");
+        PLK_CUDA(h, h->d_codes.ensure((size_t)n_tips * code_stride(n_sites)), "allocate tip codes");
         PLK_CUDA(h, h->d_flag.ensure(sizeof(int)), "allocate flag");
         PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks, n_cells * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream),
                  "upload masks");
         PLK_CUDA(h, cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "clear flag");
-        PLK_CUDA(h, launch_encode_small(h->d_mask_raw.as<uint32_t>(), n_cells, all, h->d_codes.as<uint8_t>(),
-                                        h->d_flag.as<int>(), h->stream),
+        PLK_CUDA(h, launch_encode_small(h->d_mask_raw.as<uint32_t>(), n_tips, n_sites, code_stride(n_sites), all,
+                                        h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->stream),
                  "encode kernel launch");
         int flag = 0;
         PLK_CUDA(h, cudaMemcpyAsync(&flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
@@ -320,9 +376,10 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
         PLK_CUDA(h, cudaStreamSynchronize(h->stream), "encode tip codes");
         bad = flag != 0;
     } else {
-        std::vector<uint8_t> codes(n_cells);
+        const size_t stride = (size_t)code_stride(n_sites);
+        std::vector<uint8_t> codes((size_t)n_tips * stride, 0);
         std::map<uint32_t, int> index;
-        for (size_t i = 0; i < codes.size(); ++i) {
+        for (size_t i = 0; i < n_cells; ++i) {
             const uint32_t m = masks[i] & all;
             if (m == 0) bad = true;
             auto it = index.find(m);
@@ -333,7 +390,7 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
                 index.emplace(m, c);
                 table.push_back(m);
             } else c = it->second;
-            codes[i] = (uint8_t)c;
+            codes[(i / n_sites) * stride + (i % n_sites)] = (uint8_t)c;
         }
         PLK_CUDA(h, upload(h->d_codes, codes, h->stream), "upload tip codes");
         PLK_CUDA(h, upload(h->d_code_mask, table, h->stream), "upload code table");
@@ -346,6 +403,7 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
     h->code_mask = table;
     h->bad_tip = bad;
     h->have_aln = true;
+    h->variant = -1;
     h->have_lnl = false;
     return PLK_OK;
 }
@@ -386,6 +444,7 @@ plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* 
     h->clade_rate.clear();
     h->teff_dirty = true;
     h->have_tree = true;
+    h->variant = -1;
     h->have_lnl = false;
     return PLK_OK;
 }
@@ -430,6 +489,7 @@ plk_status plk_set_model(plk_handle* h, int S, const double* Q, const double* ro
     h->root_w.assign(root_w, root_w + S);
     h->cat_rate.assign(cat_rates, cat_rates + n_cats);
     h->cat_w.assign(cat_weights, cat_weights + n_cats);
+    if (h->C != n_cats) h->variant = -1;
     h->C = n_cats;
     h->reversible = reversible;
     h->lam.assign(S, 0.0);
@@ -571,7 +631,7 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
         p.order = h->d_order.as<int>(); p.left = h->d_left.as<int>(); p.right = h->d_right.as<int>();
         p.rank = h->d_rank.as<int>(); p.n_int = n_int; p.n_tips = h->n_tips; p.n_sites = h->n_sites;
         p.n_codes = h->n_codes; p.S = h->S; p.C = h->C; p.codes = h->d_codes.as<uint8_t>();
-        p.site_stride = h->n_sites;
+        p.site_stride = code_stride(h->n_sites);
         p.P = fp64 ? (const void*)h->d_P64.p : (const void*)h->d_P32.p;
         p.tipT = fp64 ? (const void*)h->d_tip64.p : (const void*)h->d_tip32.p;
         p.root_w = h->d_rootw.as<double>(); p.cat_w = h->d_catw.as<double>();

@@ -1,0 +1,100 @@
+// Device helpers shared by the kernels of libplk.
+#pragma once
+
+#include <cstdint>
+
+#include "plk_internal.h"
+
+namespace plk {
+namespace dev {
+
+constexpr int kPruneThreads = 128;
+
+template <typename T>
+struct alignas(4 * sizeof(T)) V4 {
+    T v[4];
+};
+
+// EXACT arithmetic keeps every multiply and add separately rounded in the
+// reference's order; the fast forms use FMA chains.
+template <typename T>
+__device__ __forceinline__ T mul_rn(T a, T b);
+template <>
+__device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+template <>
+__device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b);
+template <>
+__device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
+template <>
+__device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+    s = __dadd_rn(a, b);
+    const double bb = __dsub_rn(s, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+
+template <typename T>
+__device__ __forceinline__ T scale_threshold();
+template <>
+__device__ __forceinline__ float scale_threshold<float>() { return 2.3283064365386963e-10f; }  // 2^-32
+template <>
+__device__ __forceinline__ double scale_threshold<double>() { return 8.636168555094445e-78; }  // 2^-256
+
+// Rescale a vector whose maximum mx lies below the threshold so that the
+// maximum lands in [0.5, 1): multiply by 2^-e (mx = f 2^e) in two exact
+// power-of-two steps, each finite in T even when mx is subnormal.
+template <typename T>
+__device__ __forceinline__ void pow2_factors(T mx, int* e, T* f1, T* f2) {
+    frexp(mx, e);
+    const int k = -*e, half = k / 2;
+    *f1 = ldexp(T(1), half);
+    *f2 = ldexp(T(1), k - half);
+}
+
+// Compensated (TwoSum) reduction of (s, c) over the block; thread 0 of the
+// block ends with the block's pair.  All threads of the block must call it.
+__device__ __forceinline__ void block_sum_pair(double& s, double& c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double os = __shfl_down_sync(0xffffffffu, s, off);
+        const double oc = __shfl_down_sync(0xffffffffu, c, off);
+        double ns, e;
+        two_sum(s, os, ns, e);
+        s = ns;
+        c = c + oc + e;
+    }
+    __shared__ double red_s[32], red_c[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        s = lane < nw ? red_s[lane] : 0.0;
+        c = lane < nw ? red_c[lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double os = __shfl_down_sync(0xffffffffu, s, off);
+            const double oc = __shfl_down_sync(0xffffffffu, c, off);
+            double ns, e;
+            two_sum(s, os, ns, e);
+            s = ns;
+            c = c + oc + e;
+        }
+    }
+}
+
+// 16-byte asynchronous global-to-shared copies (sm_80+ cp.async).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+}  // namespace dev
+}  // namespace plk

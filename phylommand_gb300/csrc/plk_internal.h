@@ -40,6 +40,9 @@ struct Program {
     int max_depth = 0;
 };
 
+// Records msg as the handle-less error (plk_last_error(NULL)) and returns s.
+plk_status report_error(plk_status s, const std::string& msg);
+
 // ---- host model math (plk_host.cpp) --------------------------------------
 unsigned rate_pos(unsigned n, bool tr, unsigned row, unsigned col);
 void q_matrix(int n, bool tr, const unsigned* spec, const double* rates, const double* freqs,
@@ -107,15 +110,24 @@ struct PruneArgs {
     const int* rank;           // [n_nodes], -1 for tips
     int n_int;
     int n_tips;
+    // 4-state FP32 kernel choice: 0 = prune4_kernel, 1/2 = prune4s_kernel
+    // with 1/2 sites per thread (picked by the autotuner)
+    int variant;
 };
+// Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
+bool prune4s_fits(const PruneArgs& a, int spt);
+cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);
 // Chooses the kernel for (S, C, precision); returns the number of blocks used
 // for the partial sums in *n_blocks.
 cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, int* n_blocks,
                          cudaStream_t st);
 cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cudaStream_t st);
-// codes[i] = masks[i] & all (alphabets of <= 4 states); *bad |= 1 if a cell is empty.
-cudaError_t launch_encode_small(const uint32_t* masks, size_t n, uint32_t all, uint8_t* codes, int* bad,
-                                cudaStream_t st);
+// codes[t * stride + s] = masks[t * n_sites + s] & all (alphabets of <= 4
+// states), padding bytes 0; *bad |= 1 if a cell allows no state.
+cudaError_t launch_encode_small(const uint32_t* masks, int n_tips, int n_sites, int stride, uint32_t all,
+                                uint8_t* codes, int* bad, cudaStream_t st);
+// Row stride of the tip-code matrix: n_sites rounded up to 16 bytes.
+inline int code_stride(int n_sites) { return (n_sites + 15) & ~15; }
 
 struct PreorderArgs {
     const int* order;   // internal nodes in post-order [n_int]

@@ -18,59 +18,12 @@
 //  reduce_kernel    compensated (TwoSum) sum of the block partial sums.
 #include <cstdio>
 
+#include "plk_device.cuh"
 #include "plk_internal.h"
 
 namespace plk {
 
-namespace {
-
-constexpr int kPruneThreads = 128;
-
-template <typename T>
-struct alignas(4 * sizeof(T)) V4 {
-    T v[4];
-};
-
-// ---- arithmetic helpers: EXACT keeps every multiply and add separately
-// rounded in the reference's order; otherwise FMA chains.
-template <typename T>
-__device__ __forceinline__ T mul_rn(T a, T b);
-template <>
-__device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
-template <>
-__device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
-template <typename T>
-__device__ __forceinline__ T add_rn(T a, T b);
-template <>
-__device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
-template <>
-__device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
-
-__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
-    s = __dadd_rn(a, b);
-    const double bb = __dsub_rn(s, a);
-    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
-}
-
-template <typename T>
-__device__ __forceinline__ T scale_threshold();
-template <>
-__device__ __forceinline__ float scale_threshold<float>() { return 2.3283064365386963e-10f; }  // 2^-32
-template <>
-__device__ __forceinline__ double scale_threshold<double>() { return 8.636168555094445e-78; }  // 2^-256
-
-// Rescale a vector whose maximum mx lies below the threshold so that the
-// maximum lands in [0.5, 1): multiply by 2^-e (mx = f 2^e) in two exact
-// power-of-two steps, each finite in T even when mx is subnormal.
-template <typename T>
-__device__ __forceinline__ void pow2_factors(T mx, int* e, T* f1, T* f2) {
-    frexp(mx, e);
-    const int k = -*e, half = k / 2;
-    *f1 = ldexp(T(1), half);
-    *f2 = ldexp(T(1), k - half);
-}
-
-}  // namespace
+using namespace dev;
 
 // =========================================================================
 // P(t)
@@ -560,6 +513,8 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
     const int blocks = (a.n_sites + kPruneThreads - 1) / kPruneThreads;
     *n_blocks = blocks;
     const bool fp64 = precision == PLK_FP64;
+    if (!fp64 && !store && S == 4 && a.C <= 8 && a.variant > 0 && prune4s_fits(a, a.variant))
+        return launch_prune4s(a, a.variant, n_blocks, st);
     if (S == 4 && a.C <= 8) {
         const size_t ops_bytes = ((size_t)a.n_ops * sizeof(Op) + 31) & ~(size_t)31;
         const int cm = a.C == 1 ? 1 : (a.C <= 4 ? 4 : 8);
@@ -587,32 +542,42 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
 // Tip encoding for alphabets of <= 4 states: the code is the state set
 // itself; a cell with no allowed state raises the flag (check_nodes).
 // =========================================================================
-__global__ void encode_small_kernel(const uint32_t* __restrict__ masks, size_t n, uint32_t all,
-                                    uint8_t* __restrict__ codes, int* __restrict__ bad) {
-    const size_t n4 = n / 4;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
+__global__ void encode_small_kernel(const uint32_t* __restrict__ masks, int n_tips, int n_sites, int stride,
+                                    uint32_t all, uint8_t* __restrict__ codes, int* __restrict__ bad) {
+    // one thread per 4 consecutive sites of a row; rows of `codes` are padded
+    // to `stride` (a multiple of 16) and the padding is written as 0
+    const int chunks = stride / 4;
+    const size_t total = (size_t)n_tips * chunks;
+    const size_t step = (size_t)gridDim.x * blockDim.x;
     int any_bad = 0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-        const uint4 m = reinterpret_cast<const uint4*>(masks)[i];
-        const uint32_t a = m.x & all, b = m.y & all, c = m.z & all, d = m.w & all;
-        any_bad |= (a == 0) | (b == 0) | (c == 0) | (d == 0);
-        reinterpret_cast<uchar4*>(codes)[i] = make_uchar4((uint8_t)a, (uint8_t)b, (uint8_t)c, (uint8_t)d);
-    }
-    for (size_t i = n4 * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t a = masks[i] & all;
-        any_bad |= (a == 0);
-        codes[i] = (uint8_t)a;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += step) {
+        const int t = (int)(i / chunks), s0 = (int)(i % chunks) * 4;
+        const uint32_t* row = masks + (size_t)t * n_sites;
+        uint8_t c[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int s = s0 + j;
+            if (s < n_sites) {
+                const uint32_t m = row[s] & all;
+                any_bad |= (m == 0);
+                c[j] = (uint8_t)m;
+            } else {
+                c[j] = 0;
+            }
+        }
+        reinterpret_cast<uchar4*>(codes + (size_t)t * stride)[s0 / 4] = make_uchar4(c[0], c[1], c[2], c[3]);
     }
     if (__any_sync(0xffffffffu, any_bad) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
 }
 
-cudaError_t launch_encode_small(const uint32_t* masks, size_t n, uint32_t all, uint8_t* codes, int* bad,
-                                cudaStream_t st) {
+cudaError_t launch_encode_small(const uint32_t* masks, int n_tips, int n_sites, int stride, uint32_t all,
+                                uint8_t* codes, int* bad, cudaStream_t st) {
     const int threads = 256;
-    size_t blocks = (n / 4 + threads - 1) / threads;
+    const size_t total = (size_t)n_tips * (stride / 4);
+    size_t blocks = (total + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    encode_small_kernel<<<(unsigned)blocks, threads, 0, st>>>(masks, n, all, codes, bad);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    encode_small_kernel<<<(unsigned)blocks, threads, 0, st>>>(masks, n_tips, n_sites, stride, all, codes, bad);
     return cudaGetLastError();
 }
 

@@ -256,4 +256,3 @@ class Handle:
         out = np.zeros((self.n_internal(), self.n_sites, self.n_states))
         _check(lib().plk_node_states(self._h, int(mode), int(precision), _p(out, ctypes.c_double)), self._h)
         return out
-

@@ -189,6 +189,25 @@ def test_repeat_calls_are_deterministic():
         assert a[0] == a[1] == a[2] and b[0] == b[1] == b[2]
 
 
+@pytest.mark.parametrize("n_tips,n_sites,C", [(128, 1000, 4), (40, 257, 1), (1300, 300, 4), (60, 129, 8)])
+def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
+    """Every candidate of the autotuner (prune4_kernel, prune4s_kernel with 1
+    and 2 sites per thread; tip codes in shared memory or read from global for
+    the 1300-tip tree) gives the same per-site values."""
+    rng = np.random.default_rng(n_tips + n_sites)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, C=C)
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
+    sites = []
+    for v in ("0", "1", "2"):
+        monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
+        with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
+            assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+            sites.append(h.site_loglik())
+    np.testing.assert_allclose(sites[1], sites[0], rtol=1e-12)
+    np.testing.assert_allclose(sites[2], sites[0], rtol=1e-12)
+
+
 def test_full_size_dna_gtr_gamma_fp32_against_fp64():
     """128 taxa x 100,000 sites, GTR+Gamma4, 2% missing: FP32-scaled vs FP64
     engine vs FP64 oracle (a size-independent relative bound)."""
