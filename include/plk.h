@@ -179,6 +179,26 @@ plk_status plk_effective_lengths(int n_nodes, const int* left, const int* right,
                                  const int* clade_of_node, int n_clades, const float* clade_rate,
                                  double* t_eff_out);
 
+/* ---- allocation-free entry point ----------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need the result -- work recorded into a CUDA stream
+ * capture (cudaMalloc cannot be captured), programs whose device memory is
+ * owned by another allocator, or callers that cannot afford cudaMalloc /
+ * cudaFree synchronising the device.
+ *
+ * Compensated (TwoSum) sum of n_sites per-site log-likelihoods in device
+ * memory (d_site_lnl), written to one double in device memory (d_lnl_out), on
+ * cuda_stream (a cudaStream_t as void*, NULL = default stream), asynchronously.
+ * Allocates nothing: its block partial sums live in a 64 KiB file-scope device
+ * array that every GPU loading the library keeps until exit.
+ *  - 1 <= n_sites <= 1,048,576; anything else returns PLK_ERR_ARG with a
+ *    message in plk_last_error(NULL).
+ *  - The first call on a device (that device current) resolves the array's
+ *    device address; make that first call before any stream capture.
+ *  - All calls share the array: calls that overlap on the GPU race. */
+plk_status plk_sum_sites_noalloc(const double* d_site_lnl, int n_sites, double* d_lnl_out,
+                                 void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,7 @@ EXPORTS = [
     "plk_loglik", "plk_site_loglik", "plk_node_states", "plk_n_internal",
     "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
+    "plk_sum_sites_noalloc",
 ]
 
 _lib = None
@@ -90,6 +91,7 @@ def lib() -> ctypes.CDLL:
     L.plk_set_stream.argtypes = [hp, c_void_p]
     L.plk_set_profiling.argtypes = [hp, c_int]
     L.plk_kernel_times.argtypes = [hp, dp, ip, c_int]
+    L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
     for name in EXPORTS:
         if name not in ("plk_destroy", "plk_last_error", "plk_status_string"):
             getattr(L, name).restype = c_int
@@ -256,3 +258,11 @@ class Handle:
         out = np.zeros((self.n_internal(), self.n_sites, self.n_states))
         _check(lib().plk_node_states(self._h, int(mode), int(precision), _p(out, ctypes.c_double)), self._h)
         return out
+
+
+
+def sum_sites_noalloc(d_site_lnl: int, n_sites: int, d_lnl_out: int, cuda_stream: int | None = None) -> None:
+    """Compensated sum of per-site log-likelihoods in device memory into one
+    device double, allocating nothing (device addresses as integers)."""
+    _check(lib().plk_sum_sites_noalloc(ctypes.c_void_p(d_site_lnl), int(n_sites), ctypes.c_void_p(d_lnl_out),
+                                       ctypes.c_void_p(cuda_stream or 0)))
