@@ -156,6 +156,26 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out);
 /* Number of internal nodes of the current tree (rows of plk_node_states). */
 int plk_n_internal(const plk_handle* h);
 
+/* ---- maximum-likelihood fit ----------------------------------------------------
+ * The likelihood calls of treeator's NLopt optimisation (opt_function,
+ * src/treeator.cpp:1122-1129, maximised by LN_NELDERMEAD at
+ * src/treeator.cpp:791-805), run inside the engine with its own Nelder-Mead
+ * (Nelder & Mead 1965).  Fits a reversible GTR(+Gamma) model on the handle's
+ * alignment and tree over
+ *   x = (log exchangeabilities relative to the last one,
+ *        log Gamma shape alpha  (only when n_cats > 1),
+ *        log tree-length scale  (multiplies every branch length))
+ * with fixed frequencies freqs[n_states] and Q normalised to mean rate 1.
+ * x0 = NULL starts at x = 0 (all exchangeabilities 1, alpha 1, scale 1).  The
+ * simplex starts at x0 + step * e_i; the fit stops when the spread of -lnL
+ * over the simplex is <= ftol and every coordinate's extent is <= xtol, or
+ * after max_evals evaluations.  x_out receives plk_fit_n_params values; the
+ * handle keeps the fitted model. */
+plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_cats, const double* x0,
+                       double step, double ftol, double xtol, int max_evals, double* x_out,
+                       double* lnl_out, int* n_evals_out);
+int plk_fit_n_params(int n_states, int n_cats);
+
 /* ---- host helpers (FP64, no device work) ---------------------------------- */
 /* Q as sub_model::calc_Q_matrix (src/sub_model.cpp:99-114): off-diagonal
  * Q[i][j] = rates[rate_spec[pos(i,j)]] * (reversible ? freq_j : 1), diagonal =

@@ -2,6 +2,7 @@
 // device buffers and kernel sequencing.  Host code only; kernels live in
 // plk_kernels.cu.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -92,6 +93,7 @@ struct plk_handle {
     // autotuned 4-state FP32 kernel (-1: not tuned for the current inputs)
     int variant = -1;
     float tune_ms[3] = {0.f, 0.f, 0.f};
+    std::map<std::array<int, 5>, int> tune_cache;  // (sites, tips, ops, depth, cats) -> variant
     // streams: own_stream is created with the handle; stream is the active one
     cudaStream_t own_stream = nullptr;
     // kernel timing (plk_set_profiling)
@@ -224,6 +226,13 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a) {
             return PLK_OK;
         }
     }
+    // same sizes as an earlier tuning on this handle: reuse its choice
+    const std::array<int, 5> key = {a.n_sites, a.n_tips, a.n_ops, a.max_depth, a.C};
+    auto hit = h->tune_cache.find(key);
+    if (hit != h->tune_cache.end()) {
+        h->variant = hit->second;
+        return PLK_OK;
+    }
     cudaEvent_t e0, e1;
     PLK_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
     PLK_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
@@ -249,6 +258,7 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a) {
     cudaEventDestroy(e1);
     if (err != cudaSuccess) return cuda_fail(h, err, "autotune post-order kernel");
     h->variant = best_v;
+    h->tune_cache[key] = best_v;
     return PLK_OK;
 }
 
@@ -641,6 +651,56 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
     PLK_CUDA(h, cudaMemcpyAsync(out, h->d_nodes_out.p, out_n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy node states");
     PLK_CUDA(h, cudaStreamSynchronize(h->stream), "node-state kernels");
     h->have_lnl = true;
+    return PLK_OK;
+}
+
+int plk_fit_n_params(int n_states, int n_cats) {
+    if (n_states < 2 || n_states > kMaxStates || n_cats < 1 || n_cats > kMaxCats) return 0;
+    return gtr_n_params(n_states, n_cats);
+}
+
+plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_cats, const double* x0,
+                       double step, double ftol, double xtol, int max_evals, double* x_out, double* lnl_out,
+                       int* n_evals_out) {
+    if (!h) return PLK_ERR_ARG;
+    if (!h->have_aln || !h->have_tree) return fail(h, PLK_ERR_STATE, "set the alignment and tree before fitting");
+    const int S = h->S;
+    if (S < 2 || !freqs || n_cats < 1 || n_cats > kMaxCats || !(step > 0.0) || max_evals < 1 || !x_out || !lnl_out)
+        return fail(h, PLK_ERR_ARG, "bad arguments to plk_fit_gtr");
+    for (int i = 0; i < S; ++i)
+        if (!(freqs[i] > 0.0)) return fail(h, PLK_ERR_ARG, "frequencies must be positive");
+    const int n = gtr_n_params(S, n_cats);
+    std::vector<double> start(n, 0.0);
+    if (x0) std::copy(x0, x0 + n, start.begin());
+    NelderMead nm(n, start.data(), step, ftol, xtol, max_evals);
+    std::vector<double> Q((size_t)S * S), cr(n_cats), cw(n_cats);
+    auto set_x = [&](const double* x, bool* ok) -> plk_status {
+        double scale = 1.0;
+        *ok = gtr_model_from_x(S, x, n_cats, freqs, Q.data(), cr.data(), cw.data(), &scale);
+        if (!*ok) return PLK_OK;
+        for (int c = 0; c < n_cats; ++c) cr[c] *= scale;
+        return plk_set_model(h, S, Q.data(), freqs, 1, n_cats, cr.data(), cw.data(), PLK_P_EXACT);
+    };
+    while (!nm.done()) {
+        bool ok = false;
+        plk_status s = set_x(nm.point().data(), &ok);
+        if (s != PLK_OK) return s;
+        double f = HUGE_VAL;
+        if (ok) {
+            double l = 0.0;
+            s = plk_loglik(h, precision, &l);
+            if (s == PLK_OK) f = -l;
+            else if (s != PLK_ERR_NUMERIC) return s;
+        }
+        nm.tell(f);
+    }
+    const std::vector<double>& bx = nm.best_x();
+    std::copy(bx.begin(), bx.end(), x_out);
+    bool ok = false;
+    plk_status s = set_x(bx.data(), &ok);
+    if (s != PLK_OK) return s;
+    *lnl_out = -nm.best_f();
+    if (n_evals_out) *n_evals_out = nm.evals();
     return PLK_OK;
 }
 

@@ -68,6 +68,42 @@ bool check_tree(int n_tips, int n_nodes, const int* left, const int* right, int*
 Program build_program(int n_tips, int n_nodes, const int* left, const int* right, int root,
                       const std::vector<int>& rank);
 
+// ---- fitting (plk_fit.cpp) ---------------------------------------------------
+// Nelder-Mead minimiser as a state machine: evaluate point(), report the
+// objective with tell(), repeat until done().
+class NelderMead {
+  public:
+    NelderMead(int n, const double* x0, double step, double ftol_abs, double xtol, int max_evals);
+    bool done() const { return state_ == State::Done; }
+    bool converged_ok() const { return converged_; }
+    const std::vector<double>& point() const { return point_; }
+    void tell(double f);
+    const std::vector<double>& best_x() const;
+    double best_f() const;
+    int evals() const { return evals_; }
+
+  private:
+    enum class State { Init, Reflect, Expand, ContractOut, ContractIn, Shrink, Done };
+    void order();
+    bool converged() const;
+    void begin_iteration();
+    void start_shrink();
+    int n_;
+    double ftol_, xtol_;
+    int max_evals_;
+    int evals_ = 0;
+    bool converged_ = false;
+    State state_;
+    int init_i_ = 0, shrink_i_ = 0;
+    std::vector<std::vector<double>> simplex_;
+    std::vector<double> fvals_, point_, centroid_, xr_;
+    double fr_ = 0.0;
+};
+// GTR(+Gamma) parameters of the fits (see plk_fit.cpp); false outside the domain.
+bool gtr_model_from_x(int S, const double* x, int n_cats, const double* freqs, double* Q, double* cat_rates,
+                      double* cat_weights, double* scale);
+int gtr_n_params(int S, int n_cats);
+
 // ---- device launches (plk_kernels.cu) -------------------------------------
 struct DeviceModel {
     int S, C, n_nodes, n_tips, n_codes;

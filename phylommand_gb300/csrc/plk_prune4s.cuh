@@ -1,0 +1,258 @@
+// Per-tile body of the staged 4-state FP32 post-order pass (see
+// plk_prune4s.cu), shared by the single-tree and the batch kernels.
+#pragma once
+
+#include "plk_device.cuh"
+#include "plk_internal.h"
+
+namespace plk {
+namespace dev {
+
+constexpr int kCodes = 16;                      // state sets of a <= 4-state alphabet
+constexpr size_t kMaxSmem = 227 * 1024;         // dynamic shared memory per CTA
+constexpr size_t kCodesSmemBudget = 160 * 1024; // stage tip codes only below this
+
+template <int CM>
+struct alignas(16) Stage {
+    float4 p[2][CM][4];          // [child][category][row] of P(t), internal children
+    float4 tip[2][CM][kCodes];   // [child][category][code] of the tip table, tip children
+};
+
+__host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// One site tile of one tree.
+struct TileJob {
+    const Op* ops;
+    int n_ops;
+    const uint8_t* codes;   // [n_tips][site_stride]
+    int site_stride;
+    int n_sites;
+    int n_tips;
+    const float* P;         // [n_nodes][C][16]
+    const float* tipT;      // [n_tips][C][16][4]
+    const double* root_w;   // [4]
+    const double* cat_w;    // [C]
+    int C;
+    int tile_base;          // first site of the tile
+    double* site_lnl;       // [n_sites] or null
+};
+
+// Shared memory: three stage slots | ops | tip codes (optional) | spill stack.
+template <int CM, int SPT, bool CODES_SMEM>
+__host__ __device__ inline size_t tile_smem_bytes(int n_ops, int n_tips, int max_depth) {
+    constexpr int TILE = kPruneThreads * SPT;
+    size_t s = 3 * sizeof(Stage<CM>) + align16((size_t)n_ops * sizeof(Op));
+    if (CODES_SMEM) s += align16((size_t)n_tips * TILE);
+    s += (size_t)(max_depth > 0 ? max_depth : 1) * SPT * CM * 16 * kPruneThreads;
+    return s;
+}
+
+inline size_t tile_smem_min(int C, int spt, int n_ops, int n_tips, int max_depth) {
+    const int cm = C == 1 ? 1 : (C <= 4 ? 4 : 8);
+    if (cm == 1) return spt == 1 ? tile_smem_bytes<1, 1, false>(n_ops, n_tips, max_depth)
+                                 : tile_smem_bytes<1, 2, false>(n_ops, n_tips, max_depth);
+    if (cm == 4) return spt == 1 ? tile_smem_bytes<4, 1, false>(n_ops, n_tips, max_depth)
+                                 : tile_smem_bytes<4, 2, false>(n_ops, n_tips, max_depth);
+    return spt == 1 ? tile_smem_bytes<8, 1, false>(n_ops, n_tips, max_depth)
+                    : tile_smem_bytes<8, 2, false>(n_ops, n_tips, max_depth);
+}
+
+template <int CM>
+__device__ __forceinline__ void stage_op(Stage<CM>* st, const Op& op, int C, const float* __restrict__ P,
+                                         const float* __restrict__ tipT) {
+    const int n0 = (op.s0 >= 0) ? C * kCodes : C * 4;
+    const int n1 = (op.s1 == kSrcNone) ? 0 : ((op.s1 >= 0) ? C * kCodes : C * 4);
+    for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
+        const int c = i < n0 ? 0 : 1;
+        const int j = c ? i - n0 : i;
+        const int src = c ? op.s1 : op.s0;
+        const int e = c ? op.e1 : op.e0;
+        if (src >= 0) {
+            const int k = j / kCodes, code = j % kCodes;
+            cp_async16(&st->tip[c][k][code], tipT + (((size_t)src * C + k) * kCodes + code) * 4);
+        } else {
+            const int k = j >> 2, row = j & 3;
+            cp_async16(&st->p[c][k][row], P + ((size_t)e * C + k) * 16 + row * 4);
+        }
+    }
+}
+
+__device__ __forceinline__ void mv4(const float4* rows, const float x[4], float out[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float4 r = rows[i];
+        float acc = x[0] * r.x;
+        acc = fmaf(x[1], r.y, acc);
+        acc = fmaf(x[2], r.z, acc);
+        acc = fmaf(x[3], r.w, acc);
+        out[i] = acc;
+    }
+}
+
+// Runs one tile; every thread of the CTA must call it.  Adds this thread's
+// site log-likelihoods (TwoSum-compensated) to (tsum, tcomp) and writes them
+// to j.site_lnl when it is not null.  Ends with no cp.async in flight; the
+// caller must __syncthreads() before reusing the shared memory.
+template <int CM, int SPT, bool CODES_SMEM>
+__device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp) {
+    constexpr int TILE = kPruneThreads * SPT;
+    Stage<CM>* stages = reinterpret_cast<Stage<CM>*>(sm);
+    size_t off = 3 * sizeof(Stage<CM>);
+    Op* s_ops = reinterpret_cast<Op*>(sm + off);
+    off += align16((size_t)j.n_ops * sizeof(Op));
+    uint8_t* s_codes = sm + off;
+    if (CODES_SMEM) off += align16((size_t)j.n_tips * TILE);
+    float4* s_stack = reinterpret_cast<float4*>(sm + off);
+
+    const int C = j.C;
+    const int tid = threadIdx.x;
+    const float* __restrict__ P = j.P;
+    const float* __restrict__ tipT = j.tipT;
+
+    for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
+    if (CODES_SMEM) {
+        constexpr int chunks = TILE / 16;
+        for (int i = tid; i < j.n_tips * chunks; i += kPruneThreads) {
+            const int t = i / chunks, q = i % chunks, col = j.tile_base + 16 * q;
+            uint8_t* dst = s_codes + (size_t)t * TILE + 16 * q;
+            if (col < j.site_stride) cp_async16(dst, j.codes + (size_t)t * j.site_stride + col);
+            else *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    __syncthreads();
+    stage_op<CM>(&stages[0], s_ops[0], C, P, tipT);
+    cp_async_commit();
+    if (j.n_ops > 1) stage_op<CM>(&stages[1], s_ops[1], C, P, tipT);
+    cp_async_commit();
+
+    float acc[SPT][CM][4];
+    int scale_e[SPT];
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+        scale_e[s] = 0;
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[s][k][i] = 1.0f;
+    }
+    int sp = 0;
+
+    for (int o = 0; o < j.n_ops; ++o) {
+        cp_async_wait<1>();
+        __syncthreads();
+        if (o + 2 < j.n_ops) stage_op<CM>(&stages[(o + 2) % 3], s_ops[o + 2], C, P, tipT);
+        cp_async_commit();
+        const Op op = s_ops[o];
+        const Stage<CM>& stg = stages[o % 3];
+        if (op.s0 == kSrcPop) --sp;
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) {
+            const int lsite = tid + s * kPruneThreads;
+            float d0[CM][4], d1[CM][4];
+            if (op.s0 >= 0) {
+                int code;
+                if (CODES_SMEM) code = s_codes[(size_t)op.s0 * TILE + lsite];
+                else code = j.codes[(size_t)op.s0 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+                code &= kCodes - 1;
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+                    if (k < C) {
+                        const float4 t = stg.tip[0][k][code];
+                        d0[k][0] = t.x; d0[k][1] = t.y; d0[k][2] = t.z; d0[k][3] = t.w;
+                    }
+            } else {
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+                    if (k < C) {
+                        float x[4];
+                        if (op.s0 == kSrcPop) {
+                            const float4 v = s_stack[((size_t)(sp * SPT + s) * CM + k) * kPruneThreads + tid];
+                            x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) x[i] = acc[s][k][i];
+                        }
+                        mv4(stg.p[0][k], x, d0[k]);
+                    }
+            }
+            if (op.s1 >= 0) {
+                int code;
+                if (CODES_SMEM) code = s_codes[(size_t)op.s1 * TILE + lsite];
+                else code = j.codes[(size_t)op.s1 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+                code &= kCodes - 1;
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+                    if (k < C) {
+                        const float4 t = stg.tip[1][k][code];
+                        d1[k][0] = t.x; d1[k][1] = t.y; d1[k][2] = t.z; d1[k][3] = t.w;
+                    }
+            } else if (op.s1 == kSrcAcc) {
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+                    if (k < C) mv4(stg.p[1][k], acc[s][k], d1[k]);
+            }
+            if (op.s1 == kSrcNone) {
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[s][k][i] = d0[k][i];
+            } else {
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[s][k][i] = d0[k][i] * d1[k][i];
+            }
+            float mx = 0.0f;
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) mx = fmaxf(mx, acc[s][k][i]);
+            if (mx < scale_threshold<float>() && mx > 0.0f) {
+                int e;
+                float f1, f2;
+                pow2_factors(mx, &e, &f1, &f2);
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[s][k][i] = (acc[s][k][i] * f1) * f2;
+                scale_e[s] += e;
+            }
+            if (op.push) {
+#pragma unroll
+                for (int k = 0; k < CM; ++k)
+                    if (k < C)
+                        s_stack[((size_t)(sp * SPT + s) * CM + k) * kPruneThreads + tid] =
+                            make_float4(acc[s][k][0], acc[s][k][1], acc[s][k][2], acc[s][k][3]);
+            }
+        }
+        if (op.push) ++sp;
+    }
+    cp_async_wait<0>();
+
+    // root: sum_k w_k sum_s L[s] * root_w[s] in FP64, log, scaler exponents
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+        const int site = j.tile_base + tid + s * kPruneThreads;
+        double lsum = 0.0;
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                double lk = (double)acc[s][k][0] * j.root_w[0];
+#pragma unroll
+                for (int i = 1; i < 4; ++i) lk = fma((double)acc[s][k][i], j.root_w[i], lk);
+                lsum = fma(j.cat_w[k], lk, lsum);
+            }
+        if (site < j.n_sites) {
+            const double lnl = log(lsum) + (double)scale_e[s] * 0.69314718055994530942;
+            if (j.site_lnl) j.site_lnl[site] = lnl;
+            double ns, e;
+            two_sum(tsum, lnl, ns, e);
+            tsum = ns;
+            tcomp += e;
+        }
+    }
+}
+
+}  // namespace dev
+}  // namespace plk

@@ -40,6 +40,7 @@ EXPORTS = [
     "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
     "plk_sum_sites_noalloc",
+    "plk_fit_gtr", "plk_fit_n_params",
 ]
 
 _lib = None
@@ -92,6 +93,8 @@ def lib() -> ctypes.CDLL:
     L.plk_set_profiling.argtypes = [hp, c_int]
     L.plk_kernel_times.argtypes = [hp, dp, ip, c_int]
     L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
+    L.plk_fit_gtr.argtypes = [hp, c_int, dp, c_int, dp, c_double, c_double, c_double, c_int, dp, dp, ip]
+    L.plk_fit_n_params.argtypes = [c_int, c_int]
     for name in EXPORTS:
         if name not in ("plk_destroy", "plk_last_error", "plk_status_string"):
             getattr(L, name).restype = c_int
@@ -250,6 +253,21 @@ class Handle:
         out = np.zeros(self.n_sites)
         _check(lib().plk_site_loglik(self._h, _p(out, ctypes.c_double)), self._h)
         return out
+
+    def fit_gtr(self, freqs, n_cats: int = 4, x0=None, precision: int = PLK_FP32S, step: float = 0.5,
+                ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 2000):
+        """Nelder-Mead ML fit of GTR(+Gamma) exchangeabilities, Gamma shape and
+        tree-length scale; returns (x, lnL, evaluations)."""
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        n = int(lib().plk_fit_n_params(self.n_states, int(n_cats)))
+        x = np.zeros(n)
+        x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+        lnl = ctypes.c_double(0.0)
+        ne = ctypes.c_int(0)
+        _check(lib().plk_fit_gtr(self._h, int(precision), _p(f, ctypes.c_double), int(n_cats), _p(x0a, ctypes.c_double),
+                                 float(step), float(ftol), float(xtol), int(max_evals), _p(x, ctypes.c_double),
+                                 ctypes.byref(lnl), ctypes.byref(ne)), self._h)
+        return x, lnl.value, ne.value
 
     def n_internal(self) -> int:
         return int(lib().plk_n_internal(self._h))
