@@ -176,6 +176,53 @@ plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_
                        double* lnl_out, int* n_evals_out);
 int plk_fit_n_params(int n_states, int n_cats);
 
+/* ---- batches: many alignments, trees and models in one launch -------------------
+ * The reference scores one tree per simpleML object in treeator's loop over
+ * the tree file (src/treeator.cpp:705-990), and maps sites to models through
+ * partition_models (src/partition_models.h:30-165).  A batch holds many
+ * 4-state alignments, each with its own tree and reversible model, and scores
+ * all of them in one persistent launch (work units = site tiles of a tree,
+ * largest trees first) replayed from a captured CUDA graph; an autotuner picks
+ * the sites per thread and CTAs per SM on the batch itself.  FP32 partials
+ * with per-site scaling, FP64 P(t) and sums; effective lengths are the raw
+ * branch lengths (no root quirk); n_cats is fixed per batch (1..8). */
+typedef struct plk_batch plk_batch;
+plk_status plk_batch_create(plk_batch** out, int device, int n_cats);
+void plk_batch_destroy(plk_batch* b);
+const char* plk_batch_last_error(const plk_batch* b);
+int plk_batch_n_items(const plk_batch* b);
+/* Append an item: masks[n_tips * n_sites] (bits 0..3), tree as in plk_set_tree. */
+plk_status plk_batch_add(plk_batch* b, int n_tips, int n_sites, const uint32_t* masks, int n_nodes,
+                         const int* left, const int* right, const double* branch_length, int* item_out);
+/* Model of one item: reversible Q (4 x 4) with frequencies freqs (the root
+ * weights), category rates and weights (n_cats each; rates may carry a tree
+ * scale).  Cheap: call it per optimiser step, then plk_batch_loglik. */
+plk_status plk_batch_set_model(plk_batch* b, int item, const double* Q, const double* freqs,
+                               const double* cat_rates, const double* cat_weights);
+/* lnL of every item (n_items doubles), one graph replay. */
+plk_status plk_batch_loglik(plk_batch* b, double* lnl_out);
+/* The autotuner's choice: sites per thread, persistent grid size, ms of one
+ * post-order launch, and whether evaluations replay a CUDA graph. */
+plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid, double* ms,
+                            int* uses_graph);
+
+/* NNI neighbours of every item: the trees one nearest-neighbour interchange
+ * away, with branch lengths kept on their edges -- what `treebender --nni`
+ * writes out for treeator to re-score tree by tree (src/tree.cpp:2482-2548,
+ * src/treebender.cpp:897-915), scored here without building the trees:
+ * post-order messages, pre-order outside vectors, then each interchange from
+ * the vectors around its edge.  A binary tree with n tips has 2(n - 3) moves.
+ * plk_batch_nni_moves describes move m of an item as moves[2m] = node v (the
+ * caller's id) and moves[2m+1] = which:
+ *   0  swap right(v) with v's sibling          (parent of v not the root)
+ *   1  swap left(v)  with v's sibling          (parent of v not the root)
+ *   2  swap right(v) with left(c)              (v, c the root's children)
+ *   3  swap right(v) with right(c)
+ * plk_batch_nni_loglik writes, item after item, the lnL of every move. */
+int plk_batch_nni_count(const plk_batch* b, int item);
+plk_status plk_batch_nni_moves(const plk_batch* b, int item, int* moves);
+plk_status plk_batch_nni_loglik(plk_batch* b, double* lnl_out);
+
 /* ---- host helpers (FP64, no device work) ---------------------------------- */
 /* Q as sub_model::calc_Q_matrix (src/sub_model.cpp:99-114): off-diagonal
  * Q[i][j] = rates[rate_spec[pos(i,j)]] * (reversible ? freq_j : 1), diagonal =

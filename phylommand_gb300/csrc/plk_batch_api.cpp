@@ -1,0 +1,664 @@
+// C ABI of the batch engine (include/plk.h, "batches").
+//
+// A batch holds many 4-state alignments, each with its own tree and model --
+// the many trees treeator scores one simpleML at a time
+// (src/treeator.cpp:705-990) and the per-partition models of partition_models
+// (src/partition_models.h:30-165) -- and scores them all in one persistent
+// launch.  The launch sequence (clear the work-queue head, upload the models
+// from pinned host memory, P(t) for every node, the post-order pass, the
+// per-item reduction, download the lnLs) is captured once into a CUDA graph
+// and replayed for every evaluation.  An autotuner picks the sites per thread
+// and the CTAs per SM of the persistent kernel on the batch itself.  NNI
+// scoring (plk_nni.cu) reuses the same table.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "plk_batch.h"
+#include "plk_internal.h"
+
+using namespace plk;
+
+namespace {
+
+struct BBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    BBuf() = default;
+    BBuf(const BBuf&) = delete;
+    BBuf& operator=(const BBuf&) = delete;
+    ~BBuf() { if (p) cudaFree(p); }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+struct ItemHost {
+    int n_tips = 0, n_sites = 0, n_nodes = 0, n_int = 0;
+    Program prog;
+    std::vector<double> t_eff;     // by internal id
+    std::vector<int2> child;       // by internal id
+    std::vector<uint8_t> codes;    // [n_tips][stride]
+    std::vector<double> model;     // lam L R root_w cat_rate cat_w
+    std::vector<NniMoveDev> moves; // internal ids
+    std::vector<int> move_report;  // (caller's node id, which) per move
+    bool has_model = false;
+};
+
+// Work units of one tile size plus their per-item index.
+struct UnitSet {
+    BBuf units, ptr, idx, sums, move_off;
+    int n_units = 0;
+    int spt = 0;
+    std::vector<int2> host_units;
+};
+
+constexpr int kThreads = 128;
+
+}  // namespace
+
+struct plk_batch {
+    int device = 0;
+    int C = 1;
+    int n_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<ItemHost> items;
+    bool layout_dirty = true;
+    // device layout
+    BBuf d_items, d_codes, d_ops, d_teff, d_node_item, d_child, d_model, d_P32, d_tip32, d_lnl, d_counter;
+    BBuf d_moves, d_move_item, d_nni_out, d_unit_move_sums, d_scr_D, d_scr_ED, d_scr_O, d_scr_EO;
+    double* h_model = nullptr;  // pinned staging of the models
+    double* h_lnl = nullptr;    // pinned lnL download
+    size_t h_model_n = 0, h_lnl_n = 0;
+    int n_nodes_total = 0, max_ops = 0, max_tips = 0, max_depth = 0, max_int = 0, total_moves = 0;
+    UnitSet lnl_units, nni_units;
+    // tuning of the lnL kernel
+    int spt = 1, grid = 0;
+    bool codes_smem = false;
+    size_t smem = 0;
+    double tuned_ms = 0.0;
+    bool tuned = false;
+    // graph
+    cudaGraphExec_t exec = nullptr;
+    bool use_graph = true;
+    ~plk_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (h_model) cudaFreeHost(h_model);
+        if (h_lnl) cudaFreeHost(h_lnl);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+plk_status bfail(plk_batch* b, plk_status s, const std::string& m) {
+    if (b) b->err = m;
+    else report_error(s, m);
+    return s;
+}
+
+#define PLK_BCUDA(b, expr, what)                                                                    \
+    do {                                                                                            \
+        cudaError_t _e = (expr);                                                                    \
+        if (_e != cudaSuccess)                                                                      \
+            return bfail(b, _e == cudaErrorMemoryAllocation ? PLK_ERR_ALLOC : PLK_ERR_CUDA,          \
+                         std::string(what) + ": " + cudaGetErrorString(_e));                        \
+    } while (0)
+
+BatchDev device_view(plk_batch* b, const UnitSet& us) {
+    BatchDev d{};
+    d.n_items = (int)b->items.size();
+    d.n_units = us.n_units;
+    d.n_nodes_total = b->n_nodes_total;
+    d.C = b->C;
+    d.max_depth = b->max_depth;
+    d.items = b->d_items.as<BatchItemDev>();
+    d.codes = b->d_codes.as<uint8_t>();
+    d.ops = b->d_ops.as<Op>();
+    d.t_eff = b->d_teff.as<double>();
+    d.node_item = b->d_node_item.as<int2>();
+    d.child = b->d_child.as<int2>();
+    d.model = b->d_model.as<double>();
+    d.P32 = b->d_P32.as<float>();
+    d.tip32 = b->d_tip32.as<float>();
+    d.units = us.units.as<int2>();
+    d.unit_sums = us.sums.as<double>();
+    d.item_unit_ptr = us.ptr.as<int>();
+    d.item_units = us.idx.as<int>();
+    d.lnl = b->d_lnl.as<double>();
+    d.counter = b->d_counter.as<int>();
+    d.moves = b->d_moves.as<NniMoveDev>();
+    d.unit_move_off = us.move_off.as<long long>();
+    d.unit_move_sums = b->d_unit_move_sums.as<double>();
+    d.nni_out = b->d_nni_out.as<double>();
+    d.move_item = b->d_move_item.as<int>();
+    d.total_moves = b->total_moves;
+    d.scratch_int = b->max_int;
+    d.scr_D = b->d_scr_D.as<float4>();
+    d.scr_ED = b->d_scr_ED.as<int>();
+    d.scr_O = b->d_scr_O.as<float4>();
+    d.scr_EO = b->d_scr_EO.as<int>();
+    return d;
+}
+
+// Work units for tiles of 128 * spt sites: items with the longest op lists
+// first, so the persistent grid ends on the cheapest units.
+plk_status build_units(plk_batch* b, UnitSet& us, int spt, bool with_moves) {
+    const int tile = kThreads * spt;
+    std::vector<int> order(b->items.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return b->items[x].prog.ops.size() > b->items[y].prog.ops.size();
+    });
+    std::vector<int2> units;
+    std::vector<std::vector<int>> per_item(b->items.size());
+    for (int i : order) {
+        const int tiles = (b->items[i].n_sites + tile - 1) / tile;
+        for (int t = 0; t < tiles; ++t) {
+            per_item[i].push_back((int)units.size());
+            units.push_back(make_int2(i, t));
+        }
+    }
+    std::vector<int> ptr(b->items.size() + 1, 0), idx;
+    for (size_t i = 0; i < b->items.size(); ++i) {
+        ptr[i + 1] = ptr[i] + (int)per_item[i].size();
+        idx.insert(idx.end(), per_item[i].begin(), per_item[i].end());
+    }
+    us.n_units = (int)units.size();
+    PLK_BCUDA(b, us.units.ensure(units.size() * sizeof(int2)), "allocate units");
+    PLK_BCUDA(b, us.sums.ensure(units.size() * 2 * sizeof(double)), "allocate unit sums");
+    PLK_BCUDA(b, us.ptr.ensure(ptr.size() * sizeof(int)), "allocate unit index");
+    PLK_BCUDA(b, us.idx.ensure(std::max<size_t>(idx.size(), 1) * sizeof(int)), "allocate unit index");
+    PLK_BCUDA(b, cudaMemcpy(us.units.p, units.data(), units.size() * sizeof(int2), cudaMemcpyHostToDevice), "upload units");
+    PLK_BCUDA(b, cudaMemcpy(us.ptr.p, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice), "upload units");
+    if (!idx.empty())
+        PLK_BCUDA(b, cudaMemcpy(us.idx.p, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice), "upload units");
+    if (with_moves) {
+        std::vector<long long> off(units.size());
+        long long tot = 0;
+        for (size_t u = 0; u < units.size(); ++u) {
+            off[u] = tot;
+            tot += (long long)b->items[units[u].x].moves.size();
+        }
+        PLK_BCUDA(b, us.move_off.ensure(std::max<size_t>(off.size(), 1) * sizeof(long long)), "allocate move offsets");
+        PLK_BCUDA(b, cudaMemcpy(us.move_off.p, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice),
+                  "upload move offsets");
+        PLK_BCUDA(b, b->d_unit_move_sums.ensure((size_t)std::max<long long>(tot, 1) * 2 * sizeof(double)),
+                  "allocate move partial sums");
+    }
+    us.spt = spt;
+    us.host_units = units;
+    return PLK_OK;
+}
+
+plk_status build_layout(plk_batch* b) {
+    const int C = b->C;
+    std::vector<BatchItemDev> it(b->items.size());
+    std::vector<Op> ops;
+    std::vector<double> teff;
+    std::vector<int2> node_item, child;
+    std::vector<NniMoveDev> moves;
+    std::vector<int> move_item;
+    size_t codes_bytes = 0;
+    int tips_total = 0;
+    b->max_ops = b->max_tips = b->max_depth = b->max_int = 0;
+    for (size_t i = 0; i < b->items.size(); ++i) {
+        const ItemHost& h = b->items[i];
+        BatchItemDev& d = it[i];
+        std::memset(&d, 0, sizeof(d));
+        d.codes_off = (long long)codes_bytes;
+        d.ops_off = (int)ops.size();
+        d.n_ops = (int)h.prog.ops.size();
+        d.node_off = (int)teff.size();
+        d.tip_off = tips_total;
+        d.n_tips = h.n_tips;
+        d.n_sites = h.n_sites;
+        d.site_stride = code_stride(h.n_sites);
+        d.model_off = (int)i * batch_model_stride(C);
+        d.moves_off = (int)moves.size();
+        d.n_moves = (int)h.moves.size();
+        d.move_out_off = (int)moves.size();
+        d.n_int = h.n_int;
+        codes_bytes += h.codes.size();
+        ops.insert(ops.end(), h.prog.ops.begin(), h.prog.ops.end());
+        teff.insert(teff.end(), h.t_eff.begin(), h.t_eff.end());
+        child.insert(child.end(), h.child.begin(), h.child.end());
+        for (int v = 0; v < h.n_nodes; ++v) node_item.push_back(make_int2((int)i, v));
+        moves.insert(moves.end(), h.moves.begin(), h.moves.end());
+        for (size_t m = 0; m < h.moves.size(); ++m) move_item.push_back((int)i);
+        tips_total += h.n_tips;
+        b->max_ops = std::max(b->max_ops, d.n_ops);
+        b->max_tips = std::max(b->max_tips, h.n_tips);
+        b->max_depth = std::max(b->max_depth, h.prog.max_depth);
+        b->max_int = std::max(b->max_int, h.n_int);
+    }
+    b->n_nodes_total = (int)teff.size();
+    b->total_moves = (int)moves.size();
+    PLK_BCUDA(b, b->d_items.ensure(it.size() * sizeof(BatchItemDev)), "allocate batch table");
+    PLK_BCUDA(b, b->d_codes.ensure(codes_bytes), "allocate tip codes");
+    PLK_BCUDA(b, b->d_ops.ensure(ops.size() * sizeof(Op)), "allocate programs");
+    PLK_BCUDA(b, b->d_teff.ensure(teff.size() * sizeof(double)), "allocate lengths");
+    PLK_BCUDA(b, b->d_node_item.ensure(node_item.size() * sizeof(int2)), "allocate node map");
+    PLK_BCUDA(b, b->d_child.ensure(child.size() * sizeof(int2)), "allocate child table");
+    PLK_BCUDA(b, b->d_model.ensure(it.size() * batch_model_stride(C) * sizeof(double)), "allocate models");
+    PLK_BCUDA(b, b->d_P32.ensure((size_t)b->n_nodes_total * C * 16 * sizeof(float)), "allocate P");
+    PLK_BCUDA(b, b->d_tip32.ensure((size_t)tips_total * C * 16 * 4 * sizeof(float)), "allocate tip tables");
+    PLK_BCUDA(b, b->d_lnl.ensure(it.size() * sizeof(double)), "allocate lnL");
+    PLK_BCUDA(b, b->d_counter.ensure(sizeof(int)), "allocate counter");
+    PLK_BCUDA(b, b->d_moves.ensure(std::max<size_t>(moves.size(), 1) * sizeof(NniMoveDev)), "allocate moves");
+    PLK_BCUDA(b, b->d_move_item.ensure(std::max<size_t>(move_item.size(), 1) * sizeof(int)), "allocate moves");
+    PLK_BCUDA(b, b->d_nni_out.ensure(std::max<size_t>(moves.size(), 1) * sizeof(double)), "allocate NNI output");
+    PLK_BCUDA(b, cudaMemcpy(b->d_items.p, it.data(), it.size() * sizeof(BatchItemDev), cudaMemcpyHostToDevice), "upload table");
+    size_t off = 0;
+    for (const ItemHost& h : b->items) {
+        PLK_BCUDA(b, cudaMemcpy(b->d_codes.as<uint8_t>() + off, h.codes.data(), h.codes.size(), cudaMemcpyHostToDevice),
+                  "upload tip codes");
+        off += h.codes.size();
+    }
+    PLK_BCUDA(b, cudaMemcpy(b->d_ops.p, ops.data(), ops.size() * sizeof(Op), cudaMemcpyHostToDevice), "upload programs");
+    PLK_BCUDA(b, cudaMemcpy(b->d_teff.p, teff.data(), teff.size() * sizeof(double), cudaMemcpyHostToDevice), "upload lengths");
+    PLK_BCUDA(b, cudaMemcpy(b->d_node_item.p, node_item.data(), node_item.size() * sizeof(int2), cudaMemcpyHostToDevice),
+              "upload node map");
+    PLK_BCUDA(b, cudaMemcpy(b->d_child.p, child.data(), child.size() * sizeof(int2), cudaMemcpyHostToDevice),
+              "upload child table");
+    if (!moves.empty()) {
+        PLK_BCUDA(b, cudaMemcpy(b->d_moves.p, moves.data(), moves.size() * sizeof(NniMoveDev), cudaMemcpyHostToDevice),
+                  "upload moves");
+        PLK_BCUDA(b, cudaMemcpy(b->d_move_item.p, move_item.data(), move_item.size() * sizeof(int), cudaMemcpyHostToDevice),
+                  "upload moves");
+    }
+    const size_t mn = it.size() * batch_model_stride(C);
+    if (mn > b->h_model_n) {
+        if (b->h_model) cudaFreeHost(b->h_model);
+        b->h_model = nullptr;
+        PLK_BCUDA(b, cudaMallocHost(&b->h_model, mn * sizeof(double)), "allocate pinned models");
+        b->h_model_n = mn;
+    }
+    const size_t ln = std::max(it.size(), moves.size());
+    if (ln > b->h_lnl_n) {
+        if (b->h_lnl) cudaFreeHost(b->h_lnl);
+        b->h_lnl = nullptr;
+        PLK_BCUDA(b, cudaMallocHost(&b->h_lnl, ln * sizeof(double)), "allocate pinned lnL");
+        b->h_lnl_n = ln;
+    }
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    b->lnl_units.spt = 0;
+    b->nni_units.spt = 0;
+    b->tuned = false;
+    b->layout_dirty = false;
+    return PLK_OK;
+}
+
+// The evaluation sequence (graph body).
+plk_status enqueue_eval(plk_batch* b) {
+    const BatchDev d = device_view(b, b->lnl_units);
+    const size_t mn = b->items.size() * batch_model_stride(b->C);
+    PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, mn * sizeof(double), cudaMemcpyHostToDevice, b->stream),
+              "upload models");
+    PLK_BCUDA(b, launch_batch_pmat(d, b->stream), "batch P(t) launch");
+    PLK_BCUDA(b, launch_batch_prune(d, b->spt, b->codes_smem, b->grid, b->smem, b->stream), "batch post-order launch");
+    PLK_BCUDA(b, launch_batch_reduce(d, b->stream), "batch reduce launch");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->h_lnl, b->d_lnl.p, b->items.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                 b->stream),
+              "download lnL");
+    return PLK_OK;
+}
+
+// Autotuner: sites per thread (1, 2) x CTAs per SM (1 .. occupancy), each
+// timed over two launches of the persistent kernel after a warm-up.
+plk_status tune(plk_batch* b) {
+    cudaEvent_t e0, e1;
+    PLK_BCUDA(b, cudaEventCreate(&e0), "cudaEventCreate");
+    PLK_BCUDA(b, cudaEventCreate(&e1), "cudaEventCreate");
+    double best = 1e30;
+    int best_spt = 1, best_grid = 0;
+    bool best_codes = false;
+    size_t best_smem = 0;
+    const char* force_spt = getenv("PLK_BATCH_SPT");
+    for (int spt = 1; spt <= 2; ++spt) {
+        if (force_spt && atoi(force_spt) != spt) continue;
+        size_t smem = batch_smem_bytes(b->C, spt, true, b->max_ops, b->max_tips, b->max_depth);
+        bool codes_smem = smem <= 160 * 1024;
+        if (!codes_smem) smem = batch_smem_bytes(b->C, spt, false, b->max_ops, b->max_tips, b->max_depth);
+        if (smem > 227 * 1024) continue;
+        const int occ = batch_occupancy(b->C, spt, codes_smem, smem);
+        if (occ < 1) continue;
+        plk_status s = build_units(b, b->lnl_units, spt, false);
+        if (s != PLK_OK) return s;
+        const BatchDev d = device_view(b, b->lnl_units);
+        for (int per_sm = 1; per_sm <= occ; ++per_sm) {
+            const int grid = std::min(b->lnl_units.n_units, per_sm * b->n_sms);
+            if (grid < 1) continue;
+            float ms = 0.f;
+            for (int rep = 0; rep < 3; ++rep) {  // warm-up, then two timed launches
+                PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
+                if (rep == 1) PLK_BCUDA(b, cudaEventRecord(e0, b->stream), "cudaEventRecord");
+                PLK_BCUDA(b, launch_batch_prune(d, spt, codes_smem, grid, smem, b->stream), "batch post-order launch");
+            }
+            PLK_BCUDA(b, cudaEventRecord(e1, b->stream), "cudaEventRecord");
+            PLK_BCUDA(b, cudaEventSynchronize(e1), "tune");
+            PLK_BCUDA(b, cudaEventElapsedTime(&ms, e0, e1), "tune");
+            if (ms < best) {
+                best = ms;
+                best_spt = spt;
+                best_grid = grid;
+                best_codes = codes_smem;
+                best_smem = smem;
+            }
+            if (grid == b->lnl_units.n_units) break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_grid == 0) return bfail(b, PLK_ERR_UNSUPPORTED, "no batch kernel configuration fits these trees");
+    b->spt = best_spt;
+    b->grid = best_grid;
+    b->codes_smem = best_codes;
+    b->smem = best_smem;
+    b->tuned_ms = best / 2.0;
+    if (b->lnl_units.spt != best_spt) {
+        plk_status s = build_units(b, b->lnl_units, best_spt, false);
+        if (s != PLK_OK) return s;
+    }
+    b->tuned = true;
+    return PLK_OK;
+}
+
+plk_status prepare_layout(plk_batch* b) {
+    PLK_BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    if (b->items.empty()) return bfail(b, PLK_ERR_STATE, "batch is empty");
+    for (size_t i = 0; i < b->items.size(); ++i)
+        if (!b->items[i].has_model) return bfail(b, PLK_ERR_STATE, "item " + std::to_string(i) + " has no model");
+    if (b->layout_dirty) {
+        plk_status s = build_layout(b);
+        if (s != PLK_OK) return s;
+    }
+    const int stride = batch_model_stride(b->C);
+    for (size_t i = 0; i < b->items.size(); ++i)
+        std::memcpy(b->h_model + i * stride, b->items[i].model.data(), stride * sizeof(double));
+    return PLK_OK;
+}
+
+plk_status prepare(plk_batch* b) {
+    plk_status s = prepare_layout(b);
+    if (s != PLK_OK) return s;
+    const int stride = batch_model_stride(b->C);
+    if (!b->tuned) {
+        // models must be on the device before timing the kernels
+        PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, b->items.size() * stride * sizeof(double),
+                                     cudaMemcpyHostToDevice, b->stream),
+                  "upload models");
+        PLK_BCUDA(b, launch_batch_pmat(device_view(b, b->lnl_units), b->stream), "batch P(t) launch");
+        s = tune(b);
+        if (s != PLK_OK) return s;
+    }
+    if (b->use_graph && !b->exec) {
+        cudaGraph_t g = nullptr;
+        PLK_BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        s = enqueue_eval(b);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (s != PLK_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            b->use_graph = false;  // run the same sequence without a graph
+        } else {
+            e = cudaGraphInstantiate(&b->exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                b->exec = nullptr;
+                cudaGetLastError();
+                b->use_graph = false;
+            }
+        }
+    }
+    return PLK_OK;
+}
+
+// Relabel internal nodes n_tips + post-order rank, then enumerate the NNI
+// rearrangements of the rooted tree: for an internal node v whose parent u
+// is not the root, swap one of v's children with v's sibling (two moves);
+// across the root edge between two internal root children v (left) and c,
+// swap v's right child with either child of c (two moves).  A binary tree
+// with n tips gets 2(n - 3) moves: every internal edge of the unrooted tree
+// and both of its interchanges once.
+void relabel_and_enumerate(int n_tips, int n_nodes, const int* left, const int* right, const double* bl,
+                           const std::vector<int>& rank, int root, ItemHost* h, std::vector<int>* L2,
+                           std::vector<int>* R2, std::vector<double>* B2) {
+    std::vector<int> nid(n_nodes), oid(n_nodes);
+    for (int v = 0; v < n_nodes; ++v) {
+        nid[v] = v < n_tips ? v : n_tips + rank[v];
+        oid[nid[v]] = v;
+    }
+    L2->assign(n_nodes, -1);
+    R2->assign(n_nodes, -1);
+    B2->assign(n_nodes, 0.0);
+    for (int v = 0; v < n_nodes; ++v) {
+        (*L2)[nid[v]] = left[v] >= 0 ? nid[left[v]] : -1;
+        (*R2)[nid[v]] = right[v] >= 0 ? nid[right[v]] : -1;
+        (*B2)[nid[v]] = bl[v];
+    }
+    const int r2 = nid[root];
+    std::vector<int> parent(n_nodes, -1);
+    for (int v = 0; v < n_nodes; ++v) {
+        if ((*L2)[v] >= 0) parent[(*L2)[v]] = v;
+        if ((*R2)[v] >= 0) parent[(*R2)[v]] = v;
+    }
+    auto binary = [&](int v) { return v >= n_tips && (*L2)[v] >= 0 && (*R2)[v] >= 0; };
+    h->moves.clear();
+    h->move_report.clear();
+    auto add = [&](int kind, int which, int v, int u, int c, int x, int y, int z, int p, int q) {
+        NniMoveDev m{};
+        m.kind = kind; m.v = v; m.u = u; m.c = c; m.x = x; m.y = y; m.z = z; m.p = p; m.q = q;
+        h->moves.push_back(m);
+        h->move_report.push_back(oid[v]);
+        h->move_report.push_back(which);
+    };
+    for (int v = n_tips; v < n_nodes; ++v) {
+        if (v == r2 || !binary(v)) continue;
+        const int u = parent[v];
+        if (!binary(u)) continue;
+        const int c = (*L2)[u] == v ? (*R2)[u] : (*L2)[u];
+        const int a = (*L2)[v], bb = (*R2)[v];
+        if (u != r2) {
+            add(0, 0, v, u, -1, a, c, bb, -1, -1);   // v' = (a, c), u' = (v', b)
+            add(0, 1, v, u, -1, c, bb, a, -1, -1);   // v' = (c, b), u' = (v', a)
+        } else if ((*L2)[u] == v && binary(c)) {
+            const int d = (*L2)[c], e = (*R2)[c];
+            add(1, 2, v, u, c, a, d, -1, bb, e);     // v' = (a, d), c' = (b, e)
+            add(1, 3, v, u, c, a, e, -1, d, bb);     // v' = (a, e), c' = (d, b)
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+plk_status plk_batch_create(plk_batch** out, int device, int n_cats) {
+    if (!out) return report_error(PLK_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (n_cats < 1 || n_cats > 8) return report_error(PLK_ERR_ARG, "batches support 1..8 rate categories");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return report_error(PLK_ERR_NODEV, "no CUDA device");
+    if (device < 0 || device >= n) return report_error(PLK_ERR_ARG, "device index out of range");
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return report_error(PLK_ERR_CUDA, cudaGetErrorString(e));
+    plk_batch* b = new (std::nothrow) plk_batch();
+    if (!b) return report_error(PLK_ERR_ALLOC, "host allocation failed");
+    b->device = device;
+    b->C = n_cats;
+    cudaDeviceGetAttribute(&b->n_sms, cudaDevAttrMultiProcessorCount, device);
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete b;
+        return report_error(PLK_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (const char* g = getenv("PLK_BATCH_NOGRAPH")) b->use_graph = atoi(g) == 0;
+    *out = b;
+    return PLK_OK;
+}
+
+void plk_batch_destroy(plk_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    delete b;
+}
+
+const char* plk_batch_last_error(const plk_batch* b) { return b ? b->err.c_str() : plk_last_error(nullptr); }
+
+int plk_batch_n_items(const plk_batch* b) { return b ? (int)b->items.size() : 0; }
+
+plk_status plk_batch_add(plk_batch* b, int n_tips, int n_sites, const uint32_t* masks, int n_nodes, const int* left,
+                         const int* right, const double* bl, int* item_out) {
+    if (!b) return PLK_ERR_ARG;
+    if (n_tips < 2 || n_sites < 1 || !masks || n_nodes < 3 || !left || !right || !bl)
+        return bfail(b, PLK_ERR_ARG, "batch item needs >= 2 tips, >= 1 site and a tree");
+    ItemHost h;
+    std::vector<int> post, rank;
+    int root = -1;
+    std::string err;
+    int n_leaves = 0;
+    for (int v = 0; v < n_nodes; ++v)
+        if (left[v] < 0 && right[v] < 0) ++n_leaves;
+    if (n_leaves != n_tips) return bfail(b, PLK_ERR_ARG, "tree tips and alignment rows differ");
+    if (!check_tree(n_tips, n_nodes, left, right, &root, &post, &rank, &err)) return bfail(b, PLK_ERR_ARG, err);
+    for (int v = 0; v < n_nodes; ++v)
+        if (!std::isfinite(bl[v])) return bfail(b, PLK_ERR_ARG, "non-finite branch length");
+    std::vector<int> L2, R2;
+    std::vector<double> B2;
+    relabel_and_enumerate(n_tips, n_nodes, left, right, bl, rank, root, &h, &L2, &R2, &B2);
+    std::vector<int> post2, rank2;
+    int root2 = -1;
+    if (!check_tree(n_tips, n_nodes, L2.data(), R2.data(), &root2, &post2, &rank2, &err))
+        return bfail(b, PLK_ERR_ARG, err);
+    h.n_tips = n_tips;
+    h.n_sites = n_sites;
+    h.n_nodes = n_nodes;
+    h.n_int = (int)post2.size();
+    h.prog = build_program(n_tips, n_nodes, L2.data(), R2.data(), root2, rank2);
+    h.t_eff.assign(n_nodes, 0.0);
+    effective_lengths(n_nodes, L2.data(), R2.data(), root2, B2.data(), false, {}, {}, {}, {}, h.t_eff.data());
+    h.child.resize(n_nodes);
+    for (int v = 0; v < n_nodes; ++v) h.child[v] = make_int2(L2[v], R2[v]);
+    const int stride = code_stride(n_sites);
+    h.codes.assign((size_t)n_tips * stride, 0);
+    for (int t = 0; t < n_tips; ++t)
+        for (int s = 0; s < n_sites; ++s) {
+            const uint32_t m = masks[(size_t)t * n_sites + s] & 0xFu;
+            if (m == 0) return bfail(b, PLK_ERR_TIP, "a tip cell allows no state");
+            h.codes[(size_t)t * stride + s] = (uint8_t)m;
+        }
+    h.model.assign(batch_model_stride(b->C), 0.0);
+    b->items.push_back(std::move(h));
+    b->layout_dirty = true;
+    if (item_out) *item_out = (int)b->items.size() - 1;
+    return PLK_OK;
+}
+
+plk_status plk_batch_set_model(plk_batch* b, int item, const double* Q, const double* freqs, const double* cat_rates,
+                               const double* cat_weights) {
+    if (!b) return PLK_ERR_ARG;
+    if (item < 0 || item >= (int)b->items.size() || !Q || !freqs || !cat_rates || !cat_weights)
+        return bfail(b, PLK_ERR_ARG, "bad arguments to plk_batch_set_model");
+    std::vector<double>& m = b->items[item].model;
+    if (!reversible_eigen(4, Q, freqs, m.data(), m.data() + 4, m.data() + 20))
+        return bfail(b, PLK_ERR_ARG, "reversible model needs positive frequencies");
+    for (int s = 0; s < 4; ++s) m[36 + s] = freqs[s];
+    for (int k = 0; k < b->C; ++k) {
+        if (!(cat_rates[k] >= 0.0) || !std::isfinite(cat_weights[k]))
+            return bfail(b, PLK_ERR_ARG, "bad category rate or weight");
+        m[40 + k] = cat_rates[k];
+        m[40 + b->C + k] = cat_weights[k];
+    }
+    b->items[item].has_model = true;
+    return PLK_OK;
+}
+
+plk_status plk_batch_loglik(plk_batch* b, double* lnl_out) {
+    if (!b || !lnl_out) return b ? bfail(b, PLK_ERR_ARG, "lnl_out is NULL") : PLK_ERR_ARG;
+    plk_status s = prepare(b);
+    if (s != PLK_OK) return s;
+    if (b->exec) PLK_BCUDA(b, cudaGraphLaunch(b->exec, b->stream), "graph launch");
+    else if ((s = enqueue_eval(b)) != PLK_OK) return s;
+    PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "batch evaluation");
+    std::memcpy(lnl_out, b->h_lnl, b->items.size() * sizeof(double));
+    for (size_t i = 0; i < b->items.size(); ++i)
+        if (!std::isfinite(lnl_out[i])) return bfail(b, PLK_ERR_NUMERIC, "a log-likelihood is not finite");
+    return PLK_OK;
+}
+
+plk_status plk_batch_tuning(const plk_batch* b, int* spt, int* grid, double* ms, int* uses_graph) {
+    if (!b) return PLK_ERR_ARG;
+    if (spt) *spt = b->spt;
+    if (grid) *grid = b->grid;
+    if (ms) *ms = b->tuned_ms;
+    if (uses_graph) *uses_graph = b->exec != nullptr;
+    return PLK_OK;
+}
+
+int plk_batch_nni_count(const plk_batch* b, int item) {
+    if (!b || item < 0 || item >= (int)b->items.size()) return 0;
+    return (int)b->items[item].moves.size();
+}
+
+plk_status plk_batch_nni_moves(const plk_batch* b, int item, int* moves) {
+    if (!b || !moves || item < 0 || item >= (int)b->items.size()) return PLK_ERR_ARG;
+    const std::vector<int>& r = b->items[item].move_report;
+    std::copy(r.begin(), r.end(), moves);
+    return PLK_OK;
+}
+
+plk_status plk_batch_nni_loglik(plk_batch* b, double* out) {
+    if (!b || !out) return b ? bfail(b, PLK_ERR_ARG, "out is NULL") : PLK_ERR_ARG;
+    plk_status s = prepare_layout(b);
+    if (s != PLK_OK) return s;
+    if (b->total_moves == 0) return PLK_OK;
+    if (b->nni_units.spt != 1) {
+        s = build_units(b, b->nni_units, 1, true);
+        if (s != PLK_OK) return s;
+    }
+    size_t smem = nni_smem_bytes(b->C, true, b->max_ops, b->max_tips, b->max_depth);
+    bool codes_smem = smem <= 160 * 1024;
+    if (!codes_smem) smem = nni_smem_bytes(b->C, false, b->max_ops, b->max_tips, b->max_depth);
+    if (smem > 227 * 1024) return bfail(b, PLK_ERR_UNSUPPORTED, "trees too large for NNI scoring");
+    const int grid = std::max(1, std::min(b->nni_units.n_units, 2 * b->n_sms));
+    const size_t slice = (size_t)b->max_int * kThreads;
+    PLK_BCUDA(b, b->d_scr_D.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate NNI scratch");
+    PLK_BCUDA(b, b->d_scr_O.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate NNI scratch");
+    PLK_BCUDA(b, b->d_scr_ED.ensure((size_t)grid * slice * sizeof(int)), "allocate NNI scratch");
+    PLK_BCUDA(b, b->d_scr_EO.ensure((size_t)grid * slice * sizeof(int)), "allocate NNI scratch");
+    const BatchDev d = device_view(b, b->nni_units);
+    const size_t mn = b->items.size() * batch_model_stride(b->C);
+    PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, mn * sizeof(double), cudaMemcpyHostToDevice, b->stream),
+              "upload models");
+    PLK_BCUDA(b, launch_batch_pmat(d, b->stream), "batch P(t) launch");
+    PLK_BCUDA(b, launch_batch_nni(d, codes_smem, grid, smem, b->stream), "NNI kernel launch");
+    PLK_BCUDA(b, launch_batch_nni_reduce(d, b->stream), "NNI reduce launch");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->h_lnl, b->d_nni_out.p, (size_t)b->total_moves * sizeof(double),
+                                 cudaMemcpyDeviceToHost, b->stream),
+              "download NNI lnL");
+    PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "NNI scoring");
+    std::memcpy(out, b->h_lnl, (size_t)b->total_moves * sizeof(double));
+    return PLK_OK;
+}
+
+}  // extern "C"

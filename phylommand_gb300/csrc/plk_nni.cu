@@ -1,0 +1,348 @@
+// NNI-neighbour scoring of a batch: the likelihood of every tree one nearest
+// neighbour interchange away from each batch tree (the rearrangements
+// treebender --nni writes out, src/tree.cpp:2482-2548, which treeator then
+// re-parses and scores from scratch, src/treeator.cpp:705-990), with branch
+// lengths kept on their edges.
+//
+// Per work unit (one site tile of one tree) a CTA runs three phases:
+//  A  the staged post-order pass (plk_prune4s.cuh, STORE_D): every internal
+//     non-root node's message to its parent, D = P(t) x conditional vector,
+//     goes to the CTA's scratch slice with its power-of-two exponent;
+//  B  pre-order: outside vectors Out(v) = P_v^T (Out(u) x D_sibling),
+//     Out(root) = frequencies, into the scratch slice;
+//  C  every move of the tree: for an interchange across edge (u, v) the new
+//     pair v' = (x, y) and u' = (v', z) give
+//       L = sum_k w_k sum_s Out_u[s] D_z[s] (P_v (D_x x D_y))[s],
+//     and across the root edge (v, c): v' = (x, y), c' = (p, q),
+//       L = sum_k w_k sum_s pi_s (P_v (D_x x D_y))[s] (P_c (D_p x D_q))[s];
+//     log site likelihoods summed per warp, then per CTA in warp order.
+// A last kernel sums each (tree, move) over its tiles in site order.
+#include "plk_batch.h"
+#include "plk_device.cuh"
+#include "plk_prune4s.cuh"
+
+namespace plk {
+using namespace dev;
+
+namespace {
+
+constexpr int TILE = kPruneThreads;  // one site per thread
+
+struct ItemView {
+    const BatchItemDev* it;
+    const float* P;        // item's P32
+    const float* tipT;     // item's tip32
+    const uint8_t* codes;  // item's codes
+    const int2* child;     // item's child table
+    const double* root_w;
+    const double* cat_w;
+};
+
+// Message of node `node` to its parent at this thread's site, category k,
+// and its exponent: tip -> tip-table row of the site's code, internal ->
+// scratch written by phase A.
+__device__ __forceinline__ float4 message(const ItemView& iv, const BatchDev& b, int node, int k, int site_c, int tid,
+                                          const float4* sD, const int* sED, int* e) {
+    const BatchItemDev& it = *iv.it;
+    if (node < it.n_tips) {
+        const int code = iv.codes[(size_t)node * it.site_stride + site_c] & (kCodes - 1);
+        *e = 0;
+        return *reinterpret_cast<const float4*>(iv.tipT + (((size_t)node * b.C + k) * kCodes + code) * 4);
+    }
+    const int r = node - it.n_tips;
+    *e = sED[(size_t)r * TILE + tid];
+    return sD[((size_t)r * b.C + k) * TILE + tid];
+}
+
+__device__ __forceinline__ float4 mul4(float4 a, float4 c) { return make_float4(a.x * c.x, a.y * c.y, a.z * c.z, a.w * c.w); }
+
+__device__ __forceinline__ float4 pmv(const float* Pk, float4 x) {
+    const float4 r0 = *reinterpret_cast<const float4*>(Pk);
+    const float4 r1 = *reinterpret_cast<const float4*>(Pk + 4);
+    const float4 r2 = *reinterpret_cast<const float4*>(Pk + 8);
+    const float4 r3 = *reinterpret_cast<const float4*>(Pk + 12);
+    float4 o;
+    o.x = fmaf(x.w, r0.w, fmaf(x.z, r0.z, fmaf(x.y, r0.y, x.x * r0.x)));
+    o.y = fmaf(x.w, r1.w, fmaf(x.z, r1.z, fmaf(x.y, r1.y, x.x * r1.x)));
+    o.z = fmaf(x.w, r2.w, fmaf(x.z, r2.z, fmaf(x.y, r2.y, x.x * r2.x)));
+    o.w = fmaf(x.w, r3.w, fmaf(x.z, r3.z, fmaf(x.y, r3.y, x.x * r3.x)));
+    return o;
+}
+
+// y = P^T x (outside propagation): y[b] = sum_a x[a] P[a][b]
+__device__ __forceinline__ float4 pmv_t(const float* Pk, float4 x) {
+    const float4 r0 = *reinterpret_cast<const float4*>(Pk);
+    const float4 r1 = *reinterpret_cast<const float4*>(Pk + 4);
+    const float4 r2 = *reinterpret_cast<const float4*>(Pk + 8);
+    const float4 r3 = *reinterpret_cast<const float4*>(Pk + 12);
+    float4 o;
+    o.x = fmaf(x.w, r3.x, fmaf(x.z, r2.x, fmaf(x.y, r1.x, x.x * r0.x)));
+    o.y = fmaf(x.w, r3.y, fmaf(x.z, r2.y, fmaf(x.y, r1.y, x.x * r0.y)));
+    o.z = fmaf(x.w, r3.z, fmaf(x.z, r2.z, fmaf(x.y, r1.z, x.x * r0.z)));
+    o.w = fmaf(x.w, r3.w, fmaf(x.z, r2.w, fmaf(x.y, r1.w, x.x * r0.w)));
+    return o;
+}
+
+__device__ __forceinline__ float max4(float4 a) { return fmaxf(fmaxf(a.x, a.y), fmaxf(a.z, a.w)); }
+
+__device__ __forceinline__ float4 scale4(float4 a, float f1, float f2) {
+    return make_float4((a.x * f1) * f2, (a.y * f1) * f2, (a.z * f1) * f2, (a.w * f1) * f2);
+}
+
+template <int CM>
+__device__ void phase_b(const ItemView& iv, const BatchDev& b, int site_c, int tid, const float4* sD, const int* sED,
+                        float4* sO, int* sEO) {
+    const BatchItemDev& it = *iv.it;
+    const int C = b.C;
+    for (int r = it.n_int - 1; r >= 0; --r) {
+        const int u = it.n_tips + r;
+        const bool is_root = r == it.n_int - 1;
+        float4 ou[CM];
+        int eu = 0;
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                if (is_root) ou[k] = make_float4((float)iv.root_w[0], (float)iv.root_w[1], (float)iv.root_w[2], (float)iv.root_w[3]);
+                else ou[k] = sO[((size_t)r * C + k) * TILE + tid];
+            }
+        if (!is_root) eu = sEO[(size_t)r * TILE + tid];
+        const int2 ch = iv.child[u];
+        const int kids[2] = {ch.x, ch.y};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int v = kids[c], w = kids[1 - c];
+            if (v < it.n_tips) continue;  // tips (and absent children) need no outside vector
+            float4 ov[CM];
+            int ew = 0;
+            float mx = 0.0f;
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) {
+                    float4 t = ou[k];
+                    if (w >= 0) t = mul4(t, message(iv, b, w, k, site_c, tid, sD, sED, &ew));
+                    ov[k] = pmv_t(iv.P + ((size_t)v * C + k) * 16, t);
+                    mx = fmaxf(mx, max4(ov[k]));
+                }
+            int e = 0;
+            if (mx < scale_threshold<float>() && mx > 0.0f) {
+                float f1, f2;
+                pow2_factors(mx, &e, &f1, &f2);
+#pragma unroll
+                for (int k = 0; k < CM; ++k) ov[k] = scale4(ov[k], f1, f2);
+            }
+            const int rv = v - it.n_tips;
+#pragma unroll
+            for (int k = 0; k < CM; ++k)
+                if (k < C) sO[((size_t)rv * C + k) * TILE + tid] = ov[k];
+            sEO[(size_t)rv * TILE + tid] = eu + ew + e;
+        }
+    }
+}
+
+// log-likelihood of one move at this thread's site
+template <int CM>
+__device__ double move_site_lnl(const ItemView& iv, const BatchDev& b, const NniMoveDev& mv, int site_c, int tid,
+                                const float4* sD, const int* sED, const float4* sO, const int* sEO) {
+    const BatchItemDev& it = *iv.it;
+    const int C = b.C;
+    float4 t1[CM];
+    int ex = 0, ey = 0, ez = 0, ep = 0, eq = 0;
+    float mx = 0.0f;
+#pragma unroll
+    for (int k = 0; k < CM; ++k)
+        if (k < C) {
+            t1[k] = mul4(message(iv, b, mv.x, k, site_c, tid, sD, sED, &ex),
+                         message(iv, b, mv.y, k, site_c, tid, sD, sED, &ey));
+            mx = fmaxf(mx, max4(t1[k]));
+        }
+    int e1 = 0;
+    if (mx < scale_threshold<float>() && mx > 0.0f) {
+        float f1, f2;
+        pow2_factors(mx, &e1, &f1, &f2);
+#pragma unroll
+        for (int k = 0; k < CM; ++k) t1[k] = scale4(t1[k], f1, f2);
+    }
+    double lsum = 0.0;
+    int etot = ex + ey + e1;
+    if (mv.kind == 0) {
+        const int ru = mv.u - it.n_tips;
+        const bool u_root = ru == it.n_int - 1;
+        etot += u_root ? 0 : sEO[(size_t)ru * TILE + tid];
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                const float4 a = pmv(iv.P + ((size_t)mv.v * C + k) * 16, t1[k]);
+                const float4 z = message(iv, b, mv.z, k, site_c, tid, sD, sED, &ez);
+                const float4 o = u_root ? make_float4((float)iv.root_w[0], (float)iv.root_w[1], (float)iv.root_w[2],
+                                                      (float)iv.root_w[3])
+                                        : sO[((size_t)ru * C + k) * TILE + tid];
+                double lk = (double)o.x * ((double)a.x * (double)z.x);
+                lk = fma((double)o.y, (double)a.y * (double)z.y, lk);
+                lk = fma((double)o.z, (double)a.z * (double)z.z, lk);
+                lk = fma((double)o.w, (double)a.w * (double)z.w, lk);
+                lsum = fma(iv.cat_w[k], lk, lsum);
+            }
+        etot += ez;
+    } else {
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                const float4 a = pmv(iv.P + ((size_t)mv.v * C + k) * 16, t1[k]);
+                const float4 t4 = mul4(message(iv, b, mv.p, k, site_c, tid, sD, sED, &ep),
+                                       message(iv, b, mv.q, k, site_c, tid, sD, sED, &eq));
+                const float4 c = pmv(iv.P + ((size_t)mv.c * C + k) * 16, t4);
+                double lk = iv.root_w[0] * ((double)a.x * (double)c.x);
+                lk = fma(iv.root_w[1], (double)a.y * (double)c.y, lk);
+                lk = fma(iv.root_w[2], (double)a.z * (double)c.z, lk);
+                lk = fma(iv.root_w[3], (double)a.w * (double)c.w, lk);
+                lsum = fma(iv.cat_w[k], lk, lsum);
+            }
+        etot += ep + eq;
+    }
+    return log(lsum) + (double)etot * 0.69314718055994530942;
+}
+
+template <int CM, bool CODES_SMEM>
+__global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ int s_unit;
+    __shared__ double s_red[kPruneThreads / 32][32][2];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const size_t vec_slice = (size_t)b.scratch_int * b.C * TILE;
+    const size_t int_slice = (size_t)b.scratch_int * TILE;
+    float4* sD = b.scr_D + blockIdx.x * vec_slice;
+    int* sED = b.scr_ED + blockIdx.x * int_slice;
+    float4* sO = b.scr_O + blockIdx.x * vec_slice;
+    int* sEO = b.scr_EO + blockIdx.x * int_slice;
+    for (;;) {
+        if (tid == 0) s_unit = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= b.n_units) break;
+        const int2 unit = b.units[u];
+        const BatchItemDev* itp = b.items + unit.x;
+        const BatchItemDev it = *itp;
+        ItemView iv;
+        iv.it = &it;
+        iv.P = b.P32 + (size_t)it.node_off * b.C * 16;
+        iv.tipT = b.tip32 + (size_t)it.tip_off * b.C * kCodes * 4;
+        iv.codes = b.codes + it.codes_off;
+        iv.child = b.child + it.node_off;
+        iv.root_w = b.model + it.model_off + 36;
+        iv.cat_w = b.model + it.model_off + 40 + b.C;
+        // phase A
+        TileJob j;
+        j.ops = b.ops + it.ops_off;
+        j.n_ops = it.n_ops;
+        j.codes = iv.codes;
+        j.site_stride = it.site_stride;
+        j.n_sites = it.n_sites;
+        j.n_tips = it.n_tips;
+        j.P = iv.P;
+        j.tipT = iv.tipT;
+        j.root_w = iv.root_w;
+        j.cat_w = iv.cat_w;
+        j.C = b.C;
+        j.tile_base = unit.y * TILE;
+        j.site_lnl = nullptr;
+        j.max_depth = b.max_depth;
+        DStore ds{sD, sED};
+        double ts = 0.0, tc = 0.0;
+        run_tile<CM, 1, CODES_SMEM, true>(j, sm, ts, tc, &ds);
+        // phases B and C touch only this thread's site column of the scratch
+        const int site = j.tile_base + tid;
+        const bool valid = site < it.n_sites;
+        const int site_c = min(site, it.site_stride - 1);
+        phase_b<CM>(iv, b, site_c, tid, sD, sED, sO, sEO);
+        const long long out_off = b.unit_move_off[u];
+        for (int m0 = 0; m0 < it.n_moves; m0 += 32) {
+            const int mcount = min(32, it.n_moves - m0);
+            for (int mi = 0; mi < mcount; ++mi) {
+                const NniMoveDev mv = b.moves[it.moves_off + m0 + mi];
+                double s = valid ? move_site_lnl<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO) : 0.0, c = 0.0;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const double os = __shfl_down_sync(0xffffffffu, s, off);
+                    const double oc = __shfl_down_sync(0xffffffffu, c, off);
+                    double ns, e;
+                    two_sum(s, os, ns, e);
+                    s = ns;
+                    c = c + oc + e;
+                }
+                if (lane == 0) {
+                    s_red[warp][mi][0] = s;
+                    s_red[warp][mi][1] = c;
+                }
+            }
+            __syncthreads();
+            if (tid < mcount) {
+                double s = 0.0, c = 0.0;
+                for (int w = 0; w < kPruneThreads / 32; ++w) {
+                    double ns, e;
+                    two_sum(s, s_red[w][tid][0], ns, e);
+                    s = ns;
+                    c += s_red[w][tid][1] + e;
+                }
+                b.unit_move_sums[2 * (out_off + m0 + tid)] = s;
+                b.unit_move_sums[2 * (out_off + m0 + tid) + 1] = c;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// one thread per (item, move): sum its tiles in site order
+__global__ void batch_nni_reduce_kernel(BatchDev b) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.total_moves) return;
+    const int item = b.move_item[g];
+    const BatchItemDev it = b.items[item];
+    const int m = g - it.move_out_off;
+    double s = 0.0, c = 0.0;
+    for (int q = b.item_unit_ptr[item]; q < b.item_unit_ptr[item + 1]; ++q) {
+        const int u = b.item_units[q];
+        const double* p = b.unit_move_sums + 2 * (b.unit_move_off[u] + m);
+        double ns, e;
+        two_sum(s, p[0], ns, e);
+        s = ns;
+        c += p[1] + e;
+    }
+    b.nni_out[g] = s + c;
+}
+
+template <int CM, bool CODES_SMEM>
+cudaError_t launch_nni_t(const BatchDev& b, int grid, size_t smem, cudaStream_t st) {
+    auto kern = batch_nni_kernel<CM, CODES_SMEM>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kPruneThreads, smem, st>>>(b);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t nni_smem_bytes(int C, bool codes_smem, int max_ops, int max_tips, int max_depth) {
+    const int cm = C == 1 ? 1 : (C <= 4 ? 4 : 8);
+    if (cm == 1) return codes_smem ? tile_smem_bytes<1, 1, true, true>(max_ops, max_tips, max_depth)
+                                   : tile_smem_bytes<1, 1, false, true>(max_ops, max_tips, max_depth);
+    if (cm == 4) return codes_smem ? tile_smem_bytes<4, 1, true, true>(max_ops, max_tips, max_depth)
+                                   : tile_smem_bytes<4, 1, false, true>(max_ops, max_tips, max_depth);
+    return codes_smem ? tile_smem_bytes<8, 1, true, true>(max_ops, max_tips, max_depth)
+                      : tile_smem_bytes<8, 1, false, true>(max_ops, max_tips, max_depth);
+}
+
+cudaError_t launch_batch_nni(const BatchDev& b, bool codes_smem, int grid, size_t smem, cudaStream_t st) {
+    const int cm = b.C == 1 ? 1 : (b.C <= 4 ? 4 : 8);
+    if (cm == 1) return codes_smem ? launch_nni_t<1, true>(b, grid, smem, st) : launch_nni_t<1, false>(b, grid, smem, st);
+    if (cm == 4) return codes_smem ? launch_nni_t<4, true>(b, grid, smem, st) : launch_nni_t<4, false>(b, grid, smem, st);
+    return codes_smem ? launch_nni_t<8, true>(b, grid, smem, st) : launch_nni_t<8, false>(b, grid, smem, st);
+}
+
+cudaError_t launch_batch_nni_reduce(const BatchDev& b, cudaStream_t st) {
+    if (b.total_moves == 0) return cudaSuccess;
+    const int threads = 128;
+    batch_nni_reduce_kernel<<<(b.total_moves + threads - 1) / threads, threads, 0, st>>>(b);
+    return cudaGetLastError();
+}
+
+}  // namespace plk

@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4s_kernel(PruneArgs a) {
     j.C = a.C;
     j.tile_base = blockIdx.x * kPruneThreads * SPT;
     j.site_lnl = a.site_lnl;
+    j.max_depth = a.max_depth;
     double tsum = 0.0, tcomp = 0.0;
     run_tile<CM, SPT, CODES_SMEM>(j, sm, tsum, tcomp);
     block_sum_pair(tsum, tcomp);

@@ -35,15 +35,28 @@ struct TileJob {
     int C;
     int tile_base;          // first site of the tile
     double* site_lnl;       // [n_sites] or null
+    int max_depth;          // spill-stack depth (read only with STORE_D)
 };
 
-// Shared memory: three stage slots | ops | tip codes (optional) | spill stack.
-template <int CM, int SPT, bool CODES_SMEM>
+// Where a STORE_D tile leaves the message each internal non-root node sends
+// to its parent (D = P(t) x conditional vector, FP32, scaled) and its
+// power-of-two exponent: D[(rank * C + k) * TILE + site], ED[rank * TILE + site].
+// Requires internal nodes numbered n_tips + post-order rank.
+struct DStore {
+    float4* D;
+    int* ED;
+};
+
+// Shared memory: three stage slots | ops | tip codes (optional) | spill stack
+// | spill-stack exponents (STORE_D only).
+template <int CM, int SPT, bool CODES_SMEM, bool STORE_D = false>
 __host__ __device__ inline size_t tile_smem_bytes(int n_ops, int n_tips, int max_depth) {
     constexpr int TILE = kPruneThreads * SPT;
+    const size_t depth = (size_t)(max_depth > 0 ? max_depth : 1);
     size_t s = 3 * sizeof(Stage<CM>) + align16((size_t)n_ops * sizeof(Op));
     if (CODES_SMEM) s += align16((size_t)n_tips * TILE);
-    s += (size_t)(max_depth > 0 ? max_depth : 1) * SPT * CM * 16 * kPruneThreads;
+    s += depth * SPT * CM * 16 * kPruneThreads;
+    if (STORE_D) s += depth * SPT * sizeof(int) * kPruneThreads;
     return s;
 }
 
@@ -92,9 +105,12 @@ __device__ __forceinline__ void mv4(const float4* rows, const float x[4], float 
 // Runs one tile; every thread of the CTA must call it.  Adds this thread's
 // site log-likelihoods (TwoSum-compensated) to (tsum, tcomp) and writes them
 // to j.site_lnl when it is not null.  Ends with no cp.async in flight; the
-// caller must __syncthreads() before reusing the shared memory.
-template <int CM, int SPT, bool CODES_SMEM>
-__device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp) {
+// caller must __syncthreads() before reusing the shared memory.  With
+// STORE_D, also writes the message every internal child sends to its parent
+// (and its exponent) to *ds; the per-node exponents are tracked for that.
+template <int CM, int SPT, bool CODES_SMEM, bool STORE_D = false>
+__device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp,
+                         const DStore* ds = nullptr) {
     constexpr int TILE = kPruneThreads * SPT;
     Stage<CM>* stages = reinterpret_cast<Stage<CM>*>(sm);
     size_t off = 3 * sizeof(Stage<CM>);
@@ -103,6 +119,13 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
     uint8_t* s_codes = sm + off;
     if (CODES_SMEM) off += align16((size_t)j.n_tips * TILE);
     float4* s_stack = reinterpret_cast<float4*>(sm + off);
+    int* s_stack_e = nullptr;
+    if (STORE_D)
+        s_stack_e = reinterpret_cast<int*>(sm + off + (size_t)(j.max_depth > 0 ? j.max_depth : 1) * SPT * CM * 16 *
+                                                          kPruneThreads);
+    int acc_e[SPT];
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) acc_e[s] = 0;
 
     const int C = j.C;
     const int tid = threadIdx.x;
@@ -149,6 +172,12 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
         for (int s = 0; s < SPT; ++s) {
             const int lsite = tid + s * kPruneThreads;
             float d0[CM][4], d1[CM][4];
+            int e_ch0 = 0, e_ch1 = 0;  // exponents of the two child vectors (STORE_D)
+            if constexpr (STORE_D) {
+                if (op.s0 == kSrcPop) e_ch0 = s_stack_e[(sp * SPT + s) * kPruneThreads + tid];
+                else if (op.s0 == kSrcAcc) e_ch0 = acc_e[s];
+                if (op.s1 == kSrcAcc) e_ch1 = acc_e[s];
+            }
             if (op.s0 >= 0) {
                 int code;
                 if (CODES_SMEM) code = s_codes[(size_t)op.s0 * TILE + lsite];
@@ -191,6 +220,24 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
                 for (int k = 0; k < CM; ++k)
                     if (k < C) mv4(stg.p[1][k], acc[s][k], d1[k]);
             }
+            if constexpr (STORE_D) {
+                // messages of internal children to this node, for the pre-order
+                // and NNI phases
+                if (op.s0 < 0) {
+                    const int r = op.e0 - j.n_tips;
+#pragma unroll
+                    for (int k = 0; k < CM; ++k)
+                        if (k < C) ds->D[((size_t)r * C + k) * TILE + lsite] = make_float4(d0[k][0], d0[k][1], d0[k][2], d0[k][3]);
+                    ds->ED[(size_t)r * TILE + lsite] = e_ch0;
+                }
+                if (op.s1 == kSrcAcc) {
+                    const int r = op.e1 - j.n_tips;
+#pragma unroll
+                    for (int k = 0; k < CM; ++k)
+                        if (k < C) ds->D[((size_t)r * C + k) * TILE + lsite] = make_float4(d1[k][0], d1[k][1], d1[k][2], d1[k][3]);
+                    ds->ED[(size_t)r * TILE + lsite] = e_ch1;
+                }
+            }
             if (op.s1 == kSrcNone) {
 #pragma unroll
                 for (int k = 0; k < CM; ++k)
@@ -208,6 +255,7 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
                 if (k < C)
 #pragma unroll
                     for (int i = 0; i < 4; ++i) mx = fmaxf(mx, acc[s][k][i]);
+            int e_node = 0;
             if (mx < scale_threshold<float>() && mx > 0.0f) {
                 int e;
                 float f1, f2;
@@ -217,13 +265,16 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
 #pragma unroll
                     for (int i = 0; i < 4; ++i) acc[s][k][i] = (acc[s][k][i] * f1) * f2;
                 scale_e[s] += e;
+                e_node = e;
             }
+            if constexpr (STORE_D) acc_e[s] = e_ch0 + e_ch1 + e_node;
             if (op.push) {
 #pragma unroll
                 for (int k = 0; k < CM; ++k)
                     if (k < C)
                         s_stack[((size_t)(sp * SPT + s) * CM + k) * kPruneThreads + tid] =
                             make_float4(acc[s][k][0], acc[s][k][1], acc[s][k][2], acc[s][k][3]);
+                if constexpr (STORE_D) s_stack_e[(sp * SPT + s) * kPruneThreads + tid] = acc_e[s];
             }
         }
         if (op.push) ++sp;

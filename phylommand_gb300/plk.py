@@ -41,6 +41,9 @@ EXPORTS = [
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
     "plk_sum_sites_noalloc",
     "plk_fit_gtr", "plk_fit_n_params",
+    "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
+    "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
+    "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik",
 ]
 
 _lib = None
@@ -95,8 +98,22 @@ def lib() -> ctypes.CDLL:
     L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
     L.plk_fit_gtr.argtypes = [hp, c_int, dp, c_int, dp, c_double, c_double, c_double, c_int, dp, dp, ip]
     L.plk_fit_n_params.argtypes = [c_int, c_int]
+    L.plk_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int]
+    L.plk_batch_destroy.argtypes = [hp]
+    L.plk_batch_destroy.restype = None
+    L.plk_batch_last_error.argtypes = [hp]
+    L.plk_batch_last_error.restype = ctypes.c_char_p
+    L.plk_batch_n_items.argtypes = [hp]
+    L.plk_batch_add.argtypes = [hp, c_int, c_int, u32p, c_int, ip, ip, dp, ip]
+    L.plk_batch_set_model.argtypes = [hp, c_int, dp, dp, dp, dp]
+    L.plk_batch_loglik.argtypes = [hp, dp]
+    L.plk_batch_tuning.argtypes = [hp, ip, ip, dp, ip]
+    L.plk_batch_nni_count.argtypes = [hp, c_int]
+    L.plk_batch_nni_moves.argtypes = [hp, c_int, ip]
+    L.plk_batch_nni_loglik.argtypes = [hp, dp]
+    no_status = ("plk_destroy", "plk_last_error", "plk_status_string", "plk_batch_destroy", "plk_batch_last_error")
     for name in EXPORTS:
-        if name not in ("plk_destroy", "plk_last_error", "plk_status_string"):
+        if name not in no_status:
             getattr(L, name).restype = c_int
     _lib = L
     return L
@@ -284,3 +301,87 @@ def sum_sites_noalloc(d_site_lnl: int, n_sites: int, d_lnl_out: int, cuda_stream
     device double, allocating nothing (device addresses as integers)."""
     _check(lib().plk_sum_sites_noalloc(ctypes.c_void_p(d_site_lnl), int(n_sites), ctypes.c_void_p(d_lnl_out),
                                        ctypes.c_void_p(cuda_stream or 0)))
+
+
+class Batch:
+    """Many 4-state alignments, trees and models scored in one launch."""
+
+    def __init__(self, n_cats: int = 4, device: int = 0):
+        self._b = ctypes.c_void_p()
+        _check(lib().plk_batch_create(ctypes.byref(self._b), int(device), int(n_cats)), None)
+        self.n_cats = int(n_cats)
+
+    def _check(self, status: int) -> None:
+        if status != PLK_OK:
+            msg = lib().plk_batch_last_error(self._b)
+            raise PlkError(status, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if self._b:
+            lib().plk_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self) -> int:
+        return int(lib().plk_batch_n_items(self._b))
+
+    def add(self, masks, left, right, branch_length) -> int:
+        m = np.ascontiguousarray(masks, dtype=np.uint32)
+        l = np.ascontiguousarray(left, dtype=np.int32)
+        r = np.ascontiguousarray(right, dtype=np.int32)
+        b = np.ascontiguousarray(branch_length, dtype=np.float64)
+        item = ctypes.c_int(-1)
+        self._check(lib().plk_batch_add(self._b, m.shape[0], m.shape[1], _p(m, ctypes.c_uint32), l.shape[0],
+                                        _p(l, ctypes.c_int), _p(r, ctypes.c_int), _p(b, ctypes.c_double),
+                                        ctypes.byref(item)))
+        return item.value
+
+    def set_model(self, item: int, Q, freqs, cat_rates, cat_weights) -> None:
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        cr = np.ascontiguousarray(cat_rates, dtype=np.float64)
+        cw = np.ascontiguousarray(cat_weights, dtype=np.float64)
+        self._check(lib().plk_batch_set_model(self._b, int(item), _p(Q, ctypes.c_double), _p(f, ctypes.c_double),
+                                              _p(cr, ctypes.c_double), _p(cw, ctypes.c_double)))
+
+    def loglik(self) -> np.ndarray:
+        out = np.zeros(len(self))
+        self._check(lib().plk_batch_loglik(self._b, _p(out, ctypes.c_double)))
+        return out
+
+    def nni_moves(self, item: int) -> np.ndarray:
+        """[n_moves, 2]: (node v, which) of every NNI move of an item."""
+        n = int(lib().plk_batch_nni_count(self._b, int(item)))
+        out = np.zeros((n, 2), dtype=np.int32)
+        if n:
+            self._check(lib().plk_batch_nni_moves(self._b, int(item), _p(out, ctypes.c_int)))
+        return out
+
+    def nni_loglik(self) -> list:
+        """lnL of every NNI neighbour, one array per item."""
+        counts = [int(lib().plk_batch_nni_count(self._b, i)) for i in range(len(self))]
+        out = np.zeros(max(sum(counts), 1))
+        self._check(lib().plk_batch_nni_loglik(self._b, _p(out, ctypes.c_double)))
+        res, o = [], 0
+        for c in counts:
+            res.append(out[o:o + c].copy())
+            o += c
+        return res
+
+    def tuning(self) -> dict:
+        spt, grid, graph = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        ms = ctypes.c_double(0.0)
+        self._check(lib().plk_batch_tuning(self._b, ctypes.byref(spt), ctypes.byref(grid), ctypes.byref(ms),
+                                           ctypes.byref(graph)))
+        return {"sites_per_thread": spt.value, "grid": grid.value, "postorder_ms": ms.value, "graph": bool(graph.value)}
