@@ -223,6 +223,19 @@ int plk_batch_nni_count(const plk_batch* b, int item);
 plk_status plk_batch_nni_moves(const plk_batch* b, int item, int* moves);
 plk_status plk_batch_nni_loglik(plk_batch* b, double* lnl_out);
 
+/* ---- simulation -------------------------------------------------------------
+ * Seeded simulation of n_sites sites down a tree (the engine's counterpart of
+ * simpleML::simulate_chars, src/simpleML.cpp:233-292, which draws from the
+ * clock-seeded rand()): root state from freqs, then each edge from the row of
+ * exp(Q * branch_length * r_k) of the parent's state, one of the n_cats rate
+ * categories drawn uniformly per site.  Q must be reversible with freqs.
+ * masks_out[tip * n_sites + site] = 1 << state.  Counter-based random numbers
+ * keyed by (seed, site, node): the result does not depend on n_threads. */
+plk_status plk_simulate(int n_nodes, const int* left, const int* right, const double* branch_length,
+                        int n_states, const double* Q, const double* freqs, int n_cats,
+                        const double* cat_rates, int n_sites, uint64_t seed, int n_threads,
+                        uint32_t* masks_out);
+
 /* ---- host helpers (FP64, no device work) ---------------------------------- */
 /* Q as sub_model::calc_Q_matrix (src/sub_model.cpp:99-114): off-diagonal
  * Q[i][j] = rates[rate_spec[pos(i,j)]] * (reversible ? freq_j : 1), diagonal =

@@ -20,7 +20,7 @@ ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["plk_kernels.cu", "plk_prune4s.cu", "plk_batch.cu", "plk_nni.cu", "plk_noalloc.cu"]
-CPP_SOURCES = ["plk_api.cpp", "plk_host.cpp", "plk_fit.cpp", "plk_batch_api.cpp"]
+CPP_SOURCES = ["plk_api.cpp", "plk_host.cpp", "plk_fit.cpp", "plk_batch_api.cpp", "plk_sim.cpp"]
 
 
 def _cuda_home() -> str:

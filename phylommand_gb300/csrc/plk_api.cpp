@@ -654,6 +654,25 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
     return PLK_OK;
 }
 
+plk_status plk_simulate(int n_nodes, const int* left, const int* right, const double* bl, int n_states,
+                        const double* Q, const double* freqs, int n_cats, const double* cat_rates, int n_sites,
+                        uint64_t seed, int n_threads, uint32_t* masks_out) {
+    if (n_nodes < 2 || !left || !right || !bl || n_states < 2 || n_states > kMaxStates || !Q || !freqs ||
+        n_cats < 1 || n_cats > kMaxCats || !cat_rates || n_sites < 1 || !masks_out)
+        return fail(nullptr, PLK_ERR_ARG, "bad arguments to plk_simulate");
+    int n_leaves = 0;
+    for (int v = 0; v < n_nodes; ++v)
+        if (left[v] < 0 && right[v] < 0) ++n_leaves;
+    std::vector<int> post, rank;
+    int root = -1;
+    std::string err;
+    if (!check_tree(n_leaves, n_nodes, left, right, &root, &post, &rank, &err)) return fail(nullptr, PLK_ERR_ARG, err);
+    if (!simulate_sites(n_leaves, n_nodes, left, right, root, bl, n_states, Q, freqs, n_cats, cat_rates, n_sites, seed,
+                        n_threads, masks_out))
+        return fail(nullptr, PLK_ERR_ARG, "simulation needs a reversible Q with positive frequencies");
+    return PLK_OK;
+}
+
 int plk_fit_n_params(int n_states, int n_cats) {
     if (n_states < 2 || n_states > kMaxStates || n_cats < 1 || n_cats > kMaxCats) return 0;
     return gtr_n_params(n_states, n_cats);

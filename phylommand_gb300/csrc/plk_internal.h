@@ -68,6 +68,11 @@ bool check_tree(int n_tips, int n_nodes, const int* left, const int* right, int*
 Program build_program(int n_tips, int n_nodes, const int* left, const int* right, int root,
                       const std::vector<int>& rank);
 
+// ---- simulation (plk_sim.cpp) -------------------------------------------------
+bool simulate_sites(int n_tips, int n_nodes, const int* left, const int* right, int root, const double* bl,
+                    int S, const double* Q, const double* freqs, int n_cats, const double* cat_rates,
+                    int n_sites, uint64_t seed, int n_threads, uint32_t* masks);
+
 // ---- fitting (plk_fit.cpp) ---------------------------------------------------
 // Nelder-Mead minimiser as a state machine: evaluate point(), report the
 // objective with tell(), repeat until done().

@@ -43,7 +43,7 @@ EXPORTS = [
     "plk_fit_gtr", "plk_fit_n_params",
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
-    "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik",
+    "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate",
 ]
 
 _lib = None
@@ -111,6 +111,7 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_nni_count.argtypes = [hp, c_int]
     L.plk_batch_nni_moves.argtypes = [hp, c_int, ip]
     L.plk_batch_nni_loglik.argtypes = [hp, dp]
+    L.plk_simulate.argtypes = [c_int, ip, ip, dp, c_int, dp, dp, c_int, dp, c_int, ctypes.c_uint64, c_int, u32p]
     no_status = ("plk_destroy", "plk_last_error", "plk_status_string", "plk_batch_destroy", "plk_batch_last_error")
     for name in EXPORTS:
         if name not in no_status:
@@ -147,6 +148,23 @@ def pmat_host(Q, t: float, p_mode: int = PLK_P_EXACT, root_weights=None, reversi
     _check(lib().plk_pmat_host(Q.shape[0], _p(Q, ctypes.c_double), _p(w, ctypes.c_double), int(reversible),
                                float(t), int(p_mode), _p(P, ctypes.c_double)))
     return P
+
+
+def simulate(left, right, branch_length, Q, freqs, cat_rates, n_sites: int, seed: int, threads: int = 0) -> np.ndarray:
+    """Seeded simulation down a tree; returns state-set masks [n_tips, n_sites]."""
+    l = np.ascontiguousarray(left, dtype=np.int32)
+    r = np.ascontiguousarray(right, dtype=np.int32)
+    b = np.ascontiguousarray(branch_length, dtype=np.float64)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    f = np.ascontiguousarray(freqs, dtype=np.float64)
+    cr = np.ascontiguousarray(cat_rates, dtype=np.float64)
+    n_tips = int(np.sum((l < 0) & (r < 0)))
+    out = np.zeros((n_tips, int(n_sites)), dtype=np.uint32)
+    _check(lib().plk_simulate(l.shape[0], _p(l, ctypes.c_int), _p(r, ctypes.c_int), _p(b, ctypes.c_double), Q.shape[0],
+                              _p(Q, ctypes.c_double), _p(f, ctypes.c_double), cr.shape[0], _p(cr, ctypes.c_double),
+                              int(n_sites), ctypes.c_uint64(seed), int(threads or os.cpu_count() or 1),
+                              _p(out, ctypes.c_uint32)))
+    return out
 
 
 def discrete_gamma(alpha: float, K: int) -> np.ndarray:

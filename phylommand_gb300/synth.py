@@ -163,8 +163,7 @@ def make(name: str, seed: int = 1, n_sites: int | None = None, n_tips: int | Non
     if n_tips is not None:
         n = int(n_tips)
     left, right, bl = yule_tree(n, mean, rng)
-    states = simulate(left, right, bl, Q, freqs, cr, N, rng)
-    masks = to_masks(states)
+    masks = plk.simulate(left, right, bl, Q, freqs, cr, N, seed=int(rng.integers(1 << 62)))
     if missing > 0:
         hole = rng.random(masks.shape) < missing
         masks[hole] = np.uint32((1 << S) - 1)

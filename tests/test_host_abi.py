@@ -131,3 +131,25 @@ def test_discrete_gamma_rejects_bad_alpha():
         plk.discrete_gamma(0.0, 4)
     with pytest.raises(plk.PlkError):
         plk.discrete_gamma(1.0, 0)
+
+
+def test_simulator_is_seeded_and_follows_the_model():
+    from phylommand_gb300 import synth
+    rng = np.random.default_rng(3)
+    left, right, bl = synth.yule_tree(20, 0.1, rng)
+    f = rng.dirichlet(np.full(4, 5.0))
+    Q = synth.reversible_q(4, rng.uniform(0.5, 4, 6), f)
+    cr = plk.discrete_gamma(0.7, 4)
+    a = plk.simulate(left, right, bl, Q, f, cr, 20000, seed=11, threads=1)
+    b = plk.simulate(left, right, bl, Q, f, cr, 20000, seed=11, threads=7)
+    c = plk.simulate(left, right, bl, Q, f, cr, 20000, seed=12, threads=7)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    freq = np.bincount(np.log2(a.ravel()).astype(int), minlength=4) / a.size
+    np.testing.assert_allclose(freq, f, atol=0.01)
+    # two tips joined by a path of length t: P(same state) = sum_i pi_i P_ii(t)
+    L2 = np.array([-1, -1, 0]); R2 = np.array([-1, -1, 1]); B2 = np.array([0.15, 0.25, 0.0])
+    m = plk.simulate(L2, R2, B2, Q, f, np.ones(1), 200000, seed=5)
+    same = np.mean(m[0] == m[1])
+    P = plk.pmat_host(Q, 0.4, plk.PLK_P_EXACT, f, True)
+    expect = float(np.dot(f, np.diag(P)))
+    assert abs(same - expect) < 4 * np.sqrt(expect * (1 - expect) / 200000)
