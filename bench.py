@@ -319,12 +319,113 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def nni_batch_workload(n_items: int, seed: int):
+    """Uneven batch: taxa U{8..256}, sites log-uniform 200-50,000, each with
+    its own Yule tree (Exp(mean 0.05)) and GTR+Gamma4 model (exchangeabilities
+    U(0.5, 5), frequencies Dir(10^4), alpha 0.5)."""
+    from phylommand_gb300 import plk, synth
+    rng = np.random.default_rng(seed)
+    cr = plk.discrete_gamma(0.5, 4)
+    for i in range(n_items):
+        n = int(rng.integers(8, 257))
+        N = int(np.exp(rng.uniform(np.log(200), np.log(50000))))
+        left, right, bl = synth.yule_tree(n, 0.05, rng)
+        f = rng.dirichlet(np.full(4, 10.0))
+        Q = synth.reversible_q(4, rng.uniform(0.5, 5.0, 6), f)
+        masks = plk.simulate(left, right, bl, Q, f, cr, N, seed=int(rng.integers(1 << 62)))
+        yield masks, left, right, bl, Q, f, cr
+
+
+def run_nni(args):
+    """Trees scored per second: every batch tree and all its NNI neighbours,
+    batched (one persistent launch for the base trees, one for all the
+    neighbours) against one plain launch per tree (set the tree, evaluate),
+    the latter timed on a sample of the items and scaled by site-node work."""
+    from phylommand_gb300 import plk
+    from phylommand_gb300.nni import neighbour_tree
+    n_items = args.nni_items
+    b = plk.Batch(4)
+    sample, work = [], []
+    t0 = time.perf_counter()
+    for i, (masks, left, right, bl, Q, f, cr) in enumerate(nni_batch_workload(n_items, SEED)):
+        b.add(masks, left, right, bl)
+        b.set_model(i, Q, f, cr, np.full(4, 0.25))
+        work.append((masks.shape[0] - 1) * masks.shape[1])
+        if i < args.nni_sample:
+            sample.append((masks, left, right, bl, Q, f, cr))
+    build_s = time.perf_counter() - t0
+    counts = [len(b.nni_moves(i)) for i in range(n_items)]
+    trees = n_items + sum(counts)
+    for _ in range(max(1, args.warmup)):
+        b.loglik()
+        b.nni_loglik()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        base = b.loglik()
+        nni = b.nni_loglik()
+    batched_s = (time.perf_counter() - t0) / args.steps
+    plain_s, sample_work, err = 0.0, 0.0, 0.0
+    w4 = np.full(4, 0.25)
+    with plk.Handle() as h:
+        for i, (masks, left, right, bl, Q, f, cr) in enumerate(sample):
+            moves = b.nni_moves(i)
+            topologies = [(left, right)] + [neighbour_tree(left, right, int(v), int(w)) for v, w in moves]
+            batched = [base[i]] + list(nni[i])
+            h.set_alignment(masks, 4)
+            h.set_tree(left, right, bl)
+            h.set_rate_model(False)
+            h.set_model(Q, f, True, cr, w4, plk.PLK_P_EXACT)
+            h.loglik(plk.PLK_FP32S)  # tuning for this shape
+            t0 = time.perf_counter()
+            for L, R in topologies:
+                h.set_tree(L, R, bl)
+                h.set_rate_model(False)
+                h.loglik(plk.PLK_FP32S)
+            plain_s += time.perf_counter() - t0
+            sample_work += work[i] * len(topologies)
+            for (L, R), got in list(zip(topologies, batched))[:8]:
+                h.set_tree(L, R, bl)
+                h.set_rate_model(False)
+                ref = h.loglik(plk.PLK_FP64)
+                err = max(err, abs(got - ref) / abs(ref))
+    total_work = float(sum(w * (1 + c) for w, c in zip(work, counts)))
+    plain_total_s = plain_s * total_work / sample_work
+    line = {"metric": "trees scored/s (512 uneven alignments + all NNI neighbours)", "value": trees / batched_s,
+            "unit": "trees/s", "n_items": n_items, "trees": trees, "batched_s_per_pass": batched_s,
+            "plain_s_per_pass_estimated": plain_total_s, "plain_trees_per_s": trees / plain_total_s,
+            "plain_sample_items": len(sample), "speedup_vs_plain_per_tree": plain_total_s / batched_s,
+            "max_rel_err_fp32_batched_vs_fp64_per_tree": err, "build_s": build_s, "tuning": b.tuning(),
+            "steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "uneven batch: taxa U{8..256}, sites log-uniform 200-50,000, GTR+Gamma4 each",
+                       "seed": SEED}}
+    b.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dna", choices=["dna", "nni"],
+                    help="dna: the headline workload; nni: the uneven batch with NNI neighbours")
+    ap.add_argument("--nni-items", type=int, default=512)
+    ap.add_argument("--nni-sample", type=int, default=24)
+    args = ap.parse_args()
+    if args.workload == "nni":
+        run_nni(args)
+        return
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dna", choices=["dna", "nni"],
+                    help="dna: the headline workload; nni: the uneven batch with NNI neighbours")
     args = ap.parse_args()
     world, rank, local = (1, 0, 0) if args.impl == "reference" else dist_setup(args.gpus)
     if args.impl == "reference":

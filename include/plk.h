@@ -220,6 +220,10 @@ plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid
  *   3  swap right(v) with right(c)
  * plk_batch_nni_loglik writes, item after item, the lnL of every move. */
 int plk_batch_nni_count(const plk_batch* b, int item);
+/* The same moves of one tree on the host (no device): *n_moves_out moves,
+ * 2 ints each in moves_out (may be NULL to query the count). */
+plk_status plk_nni_moves_host(int n_nodes, const int* left, const int* right, int* moves_out,
+                              int* n_moves_out);
 plk_status plk_batch_nni_moves(const plk_batch* b, int item, int* moves);
 plk_status plk_batch_nni_loglik(plk_batch* b, double* lnl_out);
 

@@ -614,6 +614,24 @@ plk_status plk_batch_tuning(const plk_batch* b, int* spt, int* grid, double* ms,
     return PLK_OK;
 }
 
+plk_status plk_nni_moves_host(int n_nodes, const int* left, const int* right, int* moves_out, int* n_moves_out) {
+    if (n_nodes < 3 || !left || !right || !n_moves_out) return report_error(PLK_ERR_ARG, "bad arguments to plk_nni_moves_host");
+    int n_leaves = 0;
+    for (int v = 0; v < n_nodes; ++v)
+        if (left[v] < 0 && right[v] < 0) ++n_leaves;
+    std::vector<int> post, rank;
+    int root = -1;
+    std::string err;
+    if (!check_tree(n_leaves, n_nodes, left, right, &root, &post, &rank, &err)) return report_error(PLK_ERR_ARG, err);
+    std::vector<double> bl(n_nodes, 0.0), B2;
+    std::vector<int> L2, R2;
+    ItemHost h;
+    relabel_and_enumerate(n_leaves, n_nodes, left, right, bl.data(), rank, root, &h, &L2, &R2, &B2);
+    *n_moves_out = (int)h.moves.size();
+    if (moves_out) std::copy(h.move_report.begin(), h.move_report.end(), moves_out);
+    return PLK_OK;
+}
+
 int plk_batch_nni_count(const plk_batch* b, int item) {
     if (!b || item < 0 || item >= (int)b->items.size()) return 0;
     return (int)b->items[item].moves.size();

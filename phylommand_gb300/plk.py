@@ -43,7 +43,7 @@ EXPORTS = [
     "plk_fit_gtr", "plk_fit_n_params",
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
-    "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate",
+    "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate", "plk_nni_moves_host",
 ]
 
 _lib = None
@@ -112,6 +112,7 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_nni_moves.argtypes = [hp, c_int, ip]
     L.plk_batch_nni_loglik.argtypes = [hp, dp]
     L.plk_simulate.argtypes = [c_int, ip, ip, dp, c_int, dp, dp, c_int, dp, c_int, ctypes.c_uint64, c_int, u32p]
+    L.plk_nni_moves_host.argtypes = [c_int, ip, ip, ip, ip]
     no_status = ("plk_destroy", "plk_last_error", "plk_status_string", "plk_batch_destroy", "plk_batch_last_error")
     for name in EXPORTS:
         if name not in no_status:
@@ -164,6 +165,19 @@ def simulate(left, right, branch_length, Q, freqs, cat_rates, n_sites: int, seed
                               _p(Q, ctypes.c_double), _p(f, ctypes.c_double), cr.shape[0], _p(cr, ctypes.c_double),
                               int(n_sites), ctypes.c_uint64(seed), int(threads or os.cpu_count() or 1),
                               _p(out, ctypes.c_uint32)))
+    return out
+
+
+def nni_moves(left, right) -> np.ndarray:
+    """[n_moves, 2]: (node v, which) of every NNI move of a tree (host only)."""
+    l = np.ascontiguousarray(left, dtype=np.int32)
+    r = np.ascontiguousarray(right, dtype=np.int32)
+    n = ctypes.c_int(0)
+    _check(lib().plk_nni_moves_host(l.shape[0], _p(l, ctypes.c_int), _p(r, ctypes.c_int), None, ctypes.byref(n)))
+    out = np.zeros((n.value, 2), dtype=np.int32)
+    if n.value:
+        _check(lib().plk_nni_moves_host(l.shape[0], _p(l, ctypes.c_int), _p(r, ctypes.c_int), _p(out, ctypes.c_int),
+                                        ctypes.byref(n)))
     return out
 
 

@@ -5,6 +5,7 @@ import pytest
 
 from oracle import oracle as O
 from phylommand_gb300 import plk, synth
+from phylommand_gb300.nni import neighbour_tree
 
 pytestmark = pytest.mark.gpu
 
@@ -81,31 +82,6 @@ def test_batch_paths_agree(monkeypatch, env):
         if "PLK_BATCH_NOGRAPH" in env:
             assert not b.tuning()["graph"]
     np.testing.assert_allclose(got, ref, rtol=1e-12)
-
-
-def neighbour_tree(left, right, v, which):
-    """The tree of one NNI move, built explicitly (branch lengths stay with
-    their nodes)."""
-    L, R = np.array(left).copy(), np.array(right).copy()
-    parent = {int(c): p for p in range(len(L)) for c in (L[p], R[p]) if c >= 0}
-    u = parent[v]
-    if which in (0, 1):
-        c = R[u] if L[u] == v else L[u]
-        if which == 0:
-            moved, R[v] = R[v], c
-        else:
-            moved, L[v] = L[v], c
-        if L[u] == c:
-            L[u] = moved
-        else:
-            R[u] = moved
-    else:
-        c = R[u]
-        if which == 2:
-            R[v], L[c] = L[c], R[v]
-        else:
-            R[v], R[c] = R[c], R[v]
-    return L, R
 
 
 @pytest.mark.parametrize("C", [4, 1])
