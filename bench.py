@@ -416,17 +416,6 @@ def main():
     if args.workload == "nni":
         run_nni(args)
         return
-
-
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dna", choices=["dna", "nni"],
-                    help="dna: the headline workload; nni: the uneven batch with NNI neighbours")
-    args = ap.parse_args()
     world, rank, local = (1, 0, 0) if args.impl == "reference" else dist_setup(args.gpus)
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))

@@ -219,6 +219,54 @@ plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid
  *   2  swap right(v) with left(c)              (v, c the root's children)
  *   3  swap right(v) with right(c)
  * plk_batch_nni_loglik writes, item after item, the lnL of every move. */
+/* Summary statistics of every item (the warm-start network's inputs), 43
+ * floats per item: base frequencies (4), mean pairwise proportions of the
+ * substitution types A<->G, A<->C, A<->T, G<->C, G<->T, C<->T (6), histogram of
+ * per-site entropy in 32 bins over [0, ln 4] (32), mean p-distance (1). */
+plk_status plk_batch_features(plk_batch* b, float* out);
+/* Maximum-likelihood fits of every item at once: one Nelder-Mead per item
+ * (the parameterisation of plk_fit_gtr: log exchangeabilities relative to the
+ * last, log alpha, log tree-length scale; n_params = plk_fit_n_params(4,
+ * n_cats)), advanced in lockstep so that each round evaluates every
+ * unfinished fit's next point in one batch launch.  freqs[n_items][4] fixed;
+ * x0[n_items][n_params] or NULL (all zero); step[n_items] initial simplex
+ * sizes or NULL (0.5).  Outputs per item: x_out, lnl_out, evals_out (may be
+ * NULL); rounds_out = batch evaluations used. */
+plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0, const double* step,
+                             double ftol, double xtol, int max_evals, double* x_out, double* lnl_out,
+                             int* evals_out, int* rounds_out);
+/* lnL of every item at the GTR parameter vector x[n_items][n_params] (the
+ * parameterisation of plk_batch_fit_gtr) in one batch evaluation; the items
+ * keep these models.  -HUGE_VAL where a vector gives no valid model. */
+plk_status plk_batch_eval_gtr(plk_batch* b, const double* freqs, const double* x, double* lnl_out);
+
+/* ---- warm-start network --------------------------------------------------------
+ * No counterpart in the reference (its optimiser starts from fixed values,
+ * src/treeator.cpp:612-615).  A fully connected network n_in -> n_hidden
+ * (x n_hidden_layers, ReLU) -> n_out that maps plk_batch_features rows to a
+ * starting point of plk_batch_fit_gtr.  BF16 weights and activations in the
+ * tensor-core GEMMs, FP32 accumulation, FP32 master weights; trained with
+ * Adam on the mean squared error.  Parameters are one flat FP32 vector: per
+ * layer W[out][in] then b[out].  Weights start He-normal from `seed`. */
+typedef struct plk_mlp plk_mlp;
+plk_status plk_mlp_create(plk_mlp** out, int device, int n_in, int n_hidden, int n_hidden_layers,
+                          int n_out, uint64_t seed);
+void plk_mlp_destroy(plk_mlp* m);
+const char* plk_mlp_last_error(const plk_mlp* m);
+int plk_mlp_n_params(const plk_mlp* m);
+plk_status plk_mlp_get_params(const plk_mlp* m, float* out);
+plk_status plk_mlp_set_params(plk_mlp* m, const float* in);
+/* y[batch][n_out] = network(x[batch][n_in]); host buffers. */
+plk_status plk_mlp_forward(plk_mlp* m, int batch, const float* x, float* y);
+/* Gradient of the loss (mean over batch x n_out of squared error against
+ * t[batch][n_out]) into grad[n_params] (may be NULL); loss may be NULL. */
+plk_status plk_mlp_gradients(plk_mlp* m, int batch, const float* x, const float* t, float* grad,
+                             float* loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) at learning rate lr; loss before
+ * the step into *loss (may be NULL). */
+plk_status plk_mlp_train_step(plk_mlp* m, int batch, const float* x, const float* t, float lr,
+                              float* loss);
+
 int plk_batch_nni_count(const plk_batch* b, int item);
 /* The same moves of one tree on the host (no device): *n_moves_out moves,
  * 2 ints each in moves_out (may be NULL to query the count). */

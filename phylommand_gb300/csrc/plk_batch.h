@@ -81,4 +81,8 @@ size_t nni_smem_bytes(int C, bool codes_smem, int max_ops, int max_tips, int max
 cudaError_t launch_batch_nni(const BatchDev& b, bool codes_smem, int grid, size_t smem, cudaStream_t st);
 cudaError_t launch_batch_nni_reduce(const BatchDev& b, cudaStream_t st);
 
+// Summary statistics of every item (plk_features.cu): out[n_items][43].
+constexpr int kNumFeatures = 43;
+cudaError_t launch_features(const BatchDev& b, float* out, cudaStream_t st);
+
 }  // namespace plk

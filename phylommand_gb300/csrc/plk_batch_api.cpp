@@ -16,6 +16,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "plk_batch.h"
@@ -611,6 +612,138 @@ plk_status plk_batch_tuning(const plk_batch* b, int* spt, int* grid, double* ms,
     if (grid) *grid = b->grid;
     if (ms) *ms = b->tuned_ms;
     if (uses_graph) *uses_graph = b->exec != nullptr;
+    return PLK_OK;
+}
+
+plk_status plk_batch_features(plk_batch* b, float* out) {
+    if (!b || !out) return b ? bfail(b, PLK_ERR_ARG, "out is NULL") : PLK_ERR_ARG;
+    PLK_BCUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    if (b->items.empty()) return bfail(b, PLK_ERR_STATE, "batch is empty");
+    if (b->layout_dirty) {
+        plk_status s = build_layout(b);
+        if (s != PLK_OK) return s;
+    }
+    BBuf feat;
+    const size_t n = b->items.size() * kNumFeatures;
+    PLK_BCUDA(b, feat.ensure(n * sizeof(float)), "allocate features");
+    PLK_BCUDA(b, launch_features(device_view(b, b->lnl_units), feat.as<float>(), b->stream), "features launch");
+    PLK_BCUDA(b, cudaMemcpyAsync(out, feat.p, n * sizeof(float), cudaMemcpyDeviceToHost, b->stream), "download features");
+    PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "features");
+    return PLK_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Sets the model of every item whose point(i) is not null from that GTR
+// parameter vector (the plk_fit_gtr parameterisation, tree-length scale folded
+// into the category rates), in parallel over items; in_domain[i] = 0 where the
+// vector gives no valid model (that item's model is left unchanged).
+template <class PointFn>
+plk_status set_gtr_models(plk_batch* b, const double* freqs, PointFn point, std::vector<char>& in_domain) {
+    const int n_items = (int)b->items.size();
+    const int C = b->C;
+    const int n_threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<plk_status> st(n_threads, PLK_OK);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < n_threads; ++t)
+        pool.emplace_back([&, t]() {
+            std::vector<double> Q(16), cr(C), cw(C);
+            for (int i = t; i < n_items; i += n_threads) {
+                const double* x = point(i);
+                if (!x) continue;
+                double scale = 1.0;
+                in_domain[i] = gtr_model_from_x(4, x, C, freqs + (size_t)i * 4, Q.data(), cr.data(), cw.data(), &scale);
+                if (!in_domain[i]) continue;
+                for (int k = 0; k < C; ++k) cr[k] *= scale;
+                const plk_status s = plk_batch_set_model(b, i, Q.data(), freqs + (size_t)i * 4, cr.data(), cw.data());
+                if (s != PLK_OK) st[t] = s;
+            }
+        });
+    for (auto& th : pool) th.join();
+    for (plk_status s : st)
+        if (s != PLK_OK) return s;
+    return PLK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+plk_status plk_batch_eval_gtr(plk_batch* b, const double* freqs, const double* x, double* lnl_out) {
+    if (!b || !freqs || !x || !lnl_out) return b ? bfail(b, PLK_ERR_ARG, "bad arguments to plk_batch_eval_gtr") : PLK_ERR_ARG;
+    const int n_items = (int)b->items.size();
+    if (n_items == 0) return bfail(b, PLK_ERR_STATE, "batch is empty");
+    const int np = gtr_n_params(4, b->C);
+    std::vector<char> in_domain(n_items, 1);
+    plk_status s = set_gtr_models(b, freqs, [&](int i) { return x + (size_t)i * np; }, in_domain);
+    if (s != PLK_OK) return s;
+    for (int i = 0; i < n_items; ++i)
+        if (!in_domain[i] && !b->items[i].has_model)
+            return bfail(b, PLK_ERR_ARG, "parameter vector of item " + std::to_string(i) + " gives no valid model");
+    s = plk_batch_loglik(b, lnl_out);
+    if (s != PLK_OK && s != PLK_ERR_NUMERIC) return s;
+    for (int i = 0; i < n_items; ++i)
+        if (!in_domain[i]) lnl_out[i] = -HUGE_VAL;
+    return PLK_OK;
+}
+
+plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0, const double* step, double ftol,
+                             double xtol, int max_evals, double* x_out, double* lnl_out, int* evals_out,
+                             int* rounds_out) {
+    if (!b || !freqs || !x_out || !lnl_out || max_evals < 1)
+        return b ? bfail(b, PLK_ERR_ARG, "bad arguments to plk_batch_fit_gtr") : PLK_ERR_ARG;
+    const int n_items = (int)b->items.size();
+    if (n_items == 0) return bfail(b, PLK_ERR_STATE, "batch is empty");
+    const int C = b->C;
+    const int np = gtr_n_params(4, C);
+    std::vector<NelderMead> nms;
+    nms.reserve(n_items);
+    for (int i = 0; i < n_items; ++i) {
+        std::vector<double> start(np, 0.0);
+        if (x0) std::copy(x0 + (size_t)i * np, x0 + (size_t)(i + 1) * np, start.begin());
+        nms.emplace_back(np, start.data(), step ? step[i] : 0.5, ftol, xtol, max_evals);
+    }
+    std::vector<char> in_domain(n_items, 1);
+    std::vector<double> lnl(n_items);
+    // the models of the points every unfinished fit asks for
+    auto set_points = [&]() -> plk_status {
+        return set_gtr_models(
+            b, freqs, [&](int i) { return nms[i].done() ? nullptr : nms[i].point().data(); }, in_domain);
+    };
+    // every item needs a model before the first evaluation
+    for (int i = 0; i < n_items; ++i)
+        if (!b->items[i].has_model) {
+            std::vector<double> Q(16), cr(C), cw(C);
+            double scale = 1.0;
+            std::vector<double> zero(np, 0.0);
+            gtr_model_from_x(4, zero.data(), C, freqs + (size_t)i * 4, Q.data(), cr.data(), cw.data(), &scale);
+            plk_status s = plk_batch_set_model(b, i, Q.data(), freqs + (size_t)i * 4, cr.data(), cw.data());
+            if (s != PLK_OK) return s;
+        }
+    int rounds = 0;
+    for (;;) {
+        bool any = false;
+        for (const auto& nm : nms) any = any || !nm.done();
+        if (!any) break;
+        plk_status s = set_points();
+        if (s != PLK_OK) return s;
+        s = plk_batch_loglik(b, lnl.data());
+        if (s != PLK_OK && s != PLK_ERR_NUMERIC) return s;
+        ++rounds;
+        for (int i = 0; i < n_items; ++i) {
+            if (nms[i].done()) continue;
+            nms[i].tell(in_domain[i] && std::isfinite(lnl[i]) ? -lnl[i] : HUGE_VAL);
+        }
+    }
+    for (int i = 0; i < n_items; ++i) {
+        const std::vector<double>& bx = nms[i].best_x();
+        std::copy(bx.begin(), bx.end(), x_out + (size_t)i * np);
+        lnl_out[i] = -nms[i].best_f();
+        if (evals_out) evals_out[i] = nms[i].evals();
+    }
+    if (rounds_out) *rounds_out = rounds;
     return PLK_OK;
 }
 

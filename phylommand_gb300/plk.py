@@ -44,6 +44,9 @@ EXPORTS = [
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
     "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate", "plk_nni_moves_host",
+    "plk_batch_features", "plk_batch_fit_gtr", "plk_batch_eval_gtr",
+    "plk_mlp_create", "plk_mlp_destroy", "plk_mlp_last_error", "plk_mlp_n_params", "plk_mlp_get_params",
+    "plk_mlp_set_params", "plk_mlp_forward", "plk_mlp_gradients", "plk_mlp_train_step",
 ]
 
 _lib = None
@@ -113,7 +116,22 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_nni_loglik.argtypes = [hp, dp]
     L.plk_simulate.argtypes = [c_int, ip, ip, dp, c_int, dp, dp, c_int, dp, c_int, ctypes.c_uint64, c_int, u32p]
     L.plk_nni_moves_host.argtypes = [c_int, ip, ip, ip, ip]
-    no_status = ("plk_destroy", "plk_last_error", "plk_status_string", "plk_batch_destroy", "plk_batch_last_error")
+    L.plk_batch_features.argtypes = [hp, fp]
+    L.plk_batch_fit_gtr.argtypes = [hp, dp, dp, dp, c_double, c_double, c_int, dp, dp, ip, ip]
+    L.plk_batch_eval_gtr.argtypes = [hp, dp, dp, dp]
+    L.plk_mlp_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64]
+    L.plk_mlp_destroy.argtypes = [hp]
+    L.plk_mlp_destroy.restype = None
+    L.plk_mlp_last_error.argtypes = [hp]
+    L.plk_mlp_last_error.restype = ctypes.c_char_p
+    L.plk_mlp_n_params.argtypes = [hp]
+    L.plk_mlp_get_params.argtypes = [hp, fp]
+    L.plk_mlp_set_params.argtypes = [hp, fp]
+    L.plk_mlp_forward.argtypes = [hp, c_int, fp, fp]
+    L.plk_mlp_gradients.argtypes = [hp, c_int, fp, fp, fp, fp]
+    L.plk_mlp_train_step.argtypes = [hp, c_int, fp, fp, ctypes.c_float, fp]
+    no_status = ("plk_destroy", "plk_last_error", "plk_status_string", "plk_batch_destroy", "plk_batch_last_error",
+                 "plk_mlp_destroy", "plk_mlp_last_error")
     for name in EXPORTS:
         if name not in no_status:
             getattr(L, name).restype = c_int
@@ -392,6 +410,40 @@ class Batch:
         self._check(lib().plk_batch_loglik(self._b, _p(out, ctypes.c_double)))
         return out
 
+    def features(self) -> np.ndarray:
+        """[n_items, 43] summary statistics (see plk_batch_features)."""
+        out = np.zeros((len(self), 43), dtype=np.float32)
+        self._check(lib().plk_batch_features(self._b, _p(out, ctypes.c_float)))
+        return out
+
+    def fit_gtr(self, freqs, x0=None, step=None, ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 3000):
+        """Lockstep Nelder-Mead ML fits of every item; returns (x, lnL, evals, rounds)."""
+        n = len(self)
+        np_ = int(lib().plk_fit_n_params(4, self.n_cats))
+        f = np.ascontiguousarray(freqs, dtype=np.float64).reshape(n, 4)
+        x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64).reshape(n, np_)
+        st = None if step is None else np.ascontiguousarray(np.broadcast_to(step, (n,)), dtype=np.float64)
+        x = np.zeros((n, np_))
+        lnl = np.zeros(n)
+        ev = np.zeros(n, dtype=np.int32)
+        rounds = ctypes.c_int(0)
+        self._check(lib().plk_batch_fit_gtr(self._b, _p(f, ctypes.c_double), _p(x0a, ctypes.c_double),
+                                            _p(st, ctypes.c_double), float(ftol), float(xtol), int(max_evals),
+                                            _p(x, ctypes.c_double), _p(lnl, ctypes.c_double), _p(ev, ctypes.c_int),
+                                            ctypes.byref(rounds)))
+        return x, lnl, ev, rounds.value
+
+    def eval_gtr(self, freqs, x) -> np.ndarray:
+        """lnL of every item at its GTR parameter vector x[n_items, n_params]."""
+        n = len(self)
+        np_ = int(lib().plk_fit_n_params(4, self.n_cats))
+        f = np.ascontiguousarray(freqs, dtype=np.float64).reshape(n, 4)
+        xa = np.ascontiguousarray(x, dtype=np.float64).reshape(n, np_)
+        out = np.zeros(n)
+        self._check(lib().plk_batch_eval_gtr(self._b, _p(f, ctypes.c_double), _p(xa, ctypes.c_double),
+                                             _p(out, ctypes.c_double)))
+        return out
+
     def nni_moves(self, item: int) -> np.ndarray:
         """[n_moves, 2]: (node v, which) of every NNI move of an item."""
         n = int(lib().plk_batch_nni_count(self._b, int(item)))
@@ -417,3 +469,80 @@ class Batch:
         self._check(lib().plk_batch_tuning(self._b, ctypes.byref(spt), ctypes.byref(grid), ctypes.byref(ms),
                                            ctypes.byref(graph)))
         return {"sites_per_thread": spt.value, "grid": grid.value, "postorder_ms": ms.value, "graph": bool(graph.value)}
+
+
+class MLP:
+    """The warm-start network (see plk_mlp_create): n_in -> n_hidden x layers
+    (ReLU) -> n_out, BF16 tensor-core GEMMs, FP32 master weights, Adam."""
+
+    def __init__(self, n_in: int, n_out: int, n_hidden: int = 256, n_hidden_layers: int = 3, seed: int = 0,
+                 device: int = 0):
+        self._m = ctypes.c_void_p()
+        _check(lib().plk_mlp_create(ctypes.byref(self._m), int(device), int(n_in), int(n_hidden),
+                                    int(n_hidden_layers), int(n_out), int(seed)), None)
+        self.n_in, self.n_out = int(n_in), int(n_out)
+        self.n_hidden, self.n_hidden_layers = int(n_hidden), int(n_hidden_layers)
+
+    def _check(self, status: int) -> None:
+        if status != PLK_OK:
+            msg = lib().plk_mlp_last_error(self._m)
+            raise PlkError(status, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if self._m:
+            lib().plk_mlp_destroy(self._m)
+            self._m = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_params(self) -> int:
+        return int(lib().plk_mlp_n_params(self._m))
+
+    def layer_shapes(self) -> list:
+        dims = [self.n_in] + [self.n_hidden] * self.n_hidden_layers + [self.n_out]
+        return [(dims[i + 1], dims[i]) for i in range(len(dims) - 1)]
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        self._check(lib().plk_mlp_get_params(self._m, _p(out, ctypes.c_float)))
+        return out
+
+    def set_params(self, p) -> None:
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        if a.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {a.size}")
+        self._check(lib().plk_mlp_set_params(self._m, _p(a, ctypes.c_float)))
+
+    def forward(self, x) -> np.ndarray:
+        xa = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        y = np.zeros((xa.shape[0], self.n_out), dtype=np.float32)
+        self._check(lib().plk_mlp_forward(self._m, xa.shape[0], _p(xa, ctypes.c_float), _p(y, ctypes.c_float)))
+        return y
+
+    def gradients(self, x, t):
+        xa = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        ta = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, self.n_out)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = ctypes.c_float(0.0)
+        self._check(lib().plk_mlp_gradients(self._m, xa.shape[0], _p(xa, ctypes.c_float), _p(ta, ctypes.c_float),
+                                            _p(g, ctypes.c_float), ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def train_step(self, x, t, lr: float) -> float:
+        xa = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        ta = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, self.n_out)
+        loss = ctypes.c_float(0.0)
+        self._check(lib().plk_mlp_train_step(self._m, xa.shape[0], _p(xa, ctypes.c_float), _p(ta, ctypes.c_float),
+                                             float(lr), ctypes.byref(loss)))
+        return float(loss.value)

@@ -1,0 +1,277 @@
+"""Learned warm start for the GTR+Gamma maximum-likelihood fit.
+
+The reference maximises lnL with NLopt's Nelder-Mead from fixed starting
+values -- every free rate 1.0 (src/treeator.cpp:612-615, the optimiser at
+:791-805).  Here a small network maps summary statistics of an alignment
+(``plk_batch_features``: base frequencies, substitution-type proportions,
+site-entropy histogram, mean p-distance) to a starting point of the same fit
+(``plk_batch_fit_gtr``: 5 log exchangeabilities relative to C<->T, log Gamma
+shape, log tree-length scale).
+
+Pipeline, every step on the GPU through libplk:
+  1. simulate alignments on Yule trees under GTR+Gamma parameters drawn from
+     the priors below (``plk_simulate``);
+  2. label them with the plain fit from the default start (all
+     exchangeabilities 1, alpha 1, scale 1) -- the network learns the ML
+     point the GPU likelihood itself finds;
+  3. train the network (``plk_mlp_*``: BF16 tensor-core GEMMs, FP32
+     accumulation, Adam) on standardised features and labels;
+  4. fit new alignments from the predicted start.  The default start stays
+     the fallback: both starts are scored first and the better one is used.
+
+The tree handed to the fit carries the simulated topology with branch lengths
+rescaled to mean ``INPUT_MEAN_BL``, so the tree-length scale is a real unknown.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import plk, synth
+
+N_CATS = 4
+N_PARAMS = 7          # 5 log exchangeabilities, log alpha, log tree-length scale
+N_FEATURES = 43
+INPUT_MEAN_BL = 0.1
+DEFAULT_STEP = 0.5
+
+# priors of the simulated training and evaluation alignments
+EXCH_RANGE = (0.5, 5.0)        # each of AG, AC, AT, GC, GT, CT ~ U
+FREQ_DIRICHLET = 10.0          # base frequencies ~ Dir(10, 10, 10, 10)
+ALPHA_RANGE = (0.2, 5.0)       # Gamma shape ~ log-uniform
+MEAN_BL_RANGE = (0.02, 0.2)    # mean branch length ~ log-uniform
+
+
+def _loguniform(rng, lo, hi):
+    return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+
+def simulate_batch(n_items: int, n_taxa: int, n_sites: int, seed: int):
+    """A plk.Batch of ``n_items`` simulated alignments and the generating
+    parameters of each in the fit's parameterisation, shape [n_items, 7]."""
+    rng = np.random.default_rng(seed)
+    b = plk.Batch(N_CATS)
+    truth = np.zeros((n_items, N_PARAMS))
+    for i in range(n_items):
+        exch = rng.uniform(*EXCH_RANGE, size=6)
+        freqs = rng.dirichlet(np.full(4, FREQ_DIRICHLET))
+        alpha = _loguniform(rng, *ALPHA_RANGE)
+        mean_bl = _loguniform(rng, *MEAN_BL_RANGE)
+        left, right, bl = synth.yule_tree(n_taxa, mean_bl, rng)
+        Q = synth.reversible_q(4, exch, freqs)
+        cr = plk.discrete_gamma(alpha, N_CATS)
+        masks = plk.simulate(left, right, bl, Q, freqs, cr, n_sites, seed=int(rng.integers(1 << 62)))
+        edges = bl[:-1]  # the last node is the root
+        real_mean = float(edges.mean())
+        b.add(masks, left, right, bl * (INPUT_MEAN_BL / real_mean))
+        truth[i, :5] = np.log(exch[:5] / exch[5])
+        truth[i, 5] = np.log(alpha)
+        truth[i, 6] = np.log(real_mean / INPUT_MEAN_BL)
+    return b, truth
+
+
+def empirical_freqs(features: np.ndarray) -> np.ndarray:
+    """The fixed base frequencies of the fits: the observed ones, floored."""
+    f = np.maximum(features[:, :4].astype(np.float64), 1e-6)
+    return f / f.sum(axis=1, keepdims=True)
+
+
+@dataclass
+class LabelledSet:
+    features: np.ndarray   # [n, 43] float32
+    freqs: np.ndarray      # [n, 4]
+    truth: np.ndarray      # [n, 7] generating parameters
+    labels: np.ndarray     # [n, 7] ML fit from the default start
+    lnl: np.ndarray        # [n]
+    evals: np.ndarray      # [n]
+    fit_s: float
+
+    def save(self, path: str) -> None:
+        np.savez(path, features=self.features, freqs=self.freqs, truth=self.truth, labels=self.labels,
+                 lnl=self.lnl, evals=self.evals, fit_s=self.fit_s)
+
+    @staticmethod
+    def load(path: str) -> "LabelledSet":
+        z = np.load(path)
+        return LabelledSet(z["features"], z["freqs"], z["truth"], z["labels"], z["lnl"], z["evals"],
+                           float(z["fit_s"]))
+
+
+def make_labelled(n_items: int, n_taxa: int, n_sites: int, seed: int, ftol: float = 1e-4, xtol: float = 1e-3,
+                  max_evals: int = 4000) -> LabelledSet:
+    """Simulate, extract features and label with the plain GPU ML fit."""
+    b, truth = simulate_batch(n_items, n_taxa, n_sites, seed)
+    try:
+        feats = b.features()
+        freqs = empirical_freqs(feats)
+        t0 = time.perf_counter()
+        x, lnl, ev, _ = b.fit_gtr(freqs, None, DEFAULT_STEP, ftol, xtol, max_evals)
+        fit_s = time.perf_counter() - t0
+    finally:
+        b.close()
+    return LabelledSet(feats, freqs, truth, x, lnl, ev, fit_s)
+
+
+class WarmStart:
+    """The trained network with its input/output standardisation and the
+    initial simplex size used from its predictions."""
+
+    def __init__(self, net: plk.MLP, x_mean, x_std, y_mean, y_std, step: float):
+        self.net = net
+        self.x_mean, self.x_std = np.asarray(x_mean, np.float32), np.asarray(x_std, np.float32)
+        self.y_mean, self.y_std = np.asarray(y_mean, np.float32), np.asarray(y_std, np.float32)
+        self.step = float(step)
+
+    def predict(self, features) -> np.ndarray:
+        z = (np.asarray(features, np.float32) - self.x_mean) / self.x_std
+        return (self.net.forward(z) * self.y_std + self.y_mean).astype(np.float64)
+
+    def save(self, path: str) -> None:
+        np.savez(path, params=self.net.get_params(), x_mean=self.x_mean, x_std=self.x_std, y_mean=self.y_mean,
+                 y_std=self.y_std, step=self.step,
+                 shape=np.array([self.net.n_in, self.net.n_out, self.net.n_hidden, self.net.n_hidden_layers]))
+
+    @staticmethod
+    def load(path: str, device: int = 0) -> "WarmStart":
+        z = np.load(path)
+        n_in, n_out, n_hidden, layers = (int(v) for v in z["shape"])
+        net = plk.MLP(n_in, n_out, n_hidden, layers, device=device)
+        net.set_params(z["params"])
+        return WarmStart(net, z["x_mean"], z["x_std"], z["y_mean"], z["y_std"], float(z["step"]))
+
+
+def train(data: LabelledSet, epochs: int = 200, batch: int = 256, lr: float = 1e-3, seed: int = 0,
+          val_frac: float = 0.1, n_hidden: int = 256, n_hidden_layers: int = 3):
+    """Adam on the mean squared error of standardised labels; returns the
+    WarmStart and a history dict (losses, validation RMSE per parameter)."""
+    rng = np.random.default_rng(seed)
+    n = data.features.shape[0]
+    perm = rng.permutation(n)
+    n_val = max(1, int(round(val_frac * n)))
+    val, tr = perm[:n_val], perm[n_val:]
+    X = data.features.astype(np.float32)
+    Y = data.labels.astype(np.float32)
+    x_mean, x_std = X[tr].mean(0), X[tr].std(0)
+    x_std = np.where(x_std > 1e-6, x_std, 1.0).astype(np.float32)
+    y_mean, y_std = Y[tr].mean(0), Y[tr].std(0)
+    y_std = np.where(y_std > 1e-6, y_std, 1.0).astype(np.float32)
+    Xs = (X - x_mean) / x_std
+    Ys = (Y - y_mean) / y_std
+    net = plk.MLP(N_FEATURES, N_PARAMS, n_hidden, n_hidden_layers, seed=seed)
+    losses = []
+    steps_per_epoch = max(1, len(tr) // batch)
+    total = epochs * steps_per_epoch
+    step = 0
+    t0 = time.perf_counter()
+    for ep in range(epochs):
+        order = rng.permutation(tr)
+        ep_loss = 0.0
+        for s in range(steps_per_epoch):
+            idx = order[s * batch:(s + 1) * batch]
+            # cosine decay to a tenth of the initial rate
+            rate = lr * (0.1 + 0.9 * 0.5 * (1.0 + np.cos(np.pi * step / total)))
+            ep_loss += net.train_step(Xs[idx], Ys[idx], rate)
+            step += 1
+        losses.append(ep_loss / steps_per_epoch)
+    train_s = time.perf_counter() - t0
+    ws = WarmStart(net, x_mean, x_std, y_mean, y_std, DEFAULT_STEP)
+    resid = ws.predict(X[val]) - data.labels[val]
+    rmse = np.sqrt(np.mean(resid ** 2, axis=0))
+    # start simplex: about twice the typical prediction error, within [0.05, 0.5]
+    ws.step = float(np.clip(2.0 * np.sqrt(np.mean(rmse ** 2)), 0.05, DEFAULT_STEP))
+    base = np.sqrt(np.mean((data.labels[val] - y_mean) ** 2, axis=0))
+    hist = {"train_loss": losses, "val_rmse": rmse.tolist(), "val_rmse_mean_predictor": base.tolist(),
+            "train_s": train_s, "steps": step, "start_step": ws.step}
+    return ws, hist
+
+
+def fit_warm(b: plk.Batch, freqs, features, ws: WarmStart, ftol: float = 1e-4, xtol: float = 1e-3,
+             max_evals: int = 4000):
+    """The fit from the network's start where that start scores at least as
+    well as the default one, else from the default start.  Returns (x, lnL,
+    evals incl. the two start evaluations, rounds, used_network)."""
+    n = len(b)
+    x_net = ws.predict(features)
+    x_def = np.zeros((n, N_PARAMS))
+    l_net = b.eval_gtr(freqs, x_net)
+    l_def = b.eval_gtr(freqs, x_def)
+    use = l_net >= l_def
+    x0 = np.where(use[:, None], x_net, x_def)
+    step = np.where(use, ws.step, DEFAULT_STEP)
+    x, lnl, ev, rounds = b.fit_gtr(freqs, x0, step, ftol, xtol, max_evals)
+    return x, lnl, ev + 2, rounds + 2, use
+
+
+def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int = 5000, seed: int = 7,
+             ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 4000) -> dict:
+    """Held-out comparison of the plain default-start fit and the warm fit on
+    the same simulated alignments: evaluations, wall time and final lnL."""
+    b, truth = simulate_batch(n_items, n_taxa, n_sites, seed)
+    try:
+        feats = b.features()
+        freqs = empirical_freqs(feats)
+        b.eval_gtr(freqs, np.zeros((n_items, N_PARAMS)))  # tuning and graph capture outside the timings
+        t0 = time.perf_counter()
+        xp, lp, ep, rp = b.fit_gtr(freqs, None, DEFAULT_STEP, ftol, xtol, max_evals)
+        plain_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        xw, lw, ew, rw, used = fit_warm(b, freqs, feats, ws, ftol, xtol, max_evals)
+        warm_s = time.perf_counter() - t0
+    finally:
+        b.close()
+    deficit = lp - lw   # > 0 where the warm fit ends below the plain optimum
+    return {
+        "n_items": n_items, "n_taxa": n_taxa, "n_sites": n_sites, "seed": seed,
+        "plain_evals_mean": float(ep.mean()), "warm_evals_mean": float(ew.mean()),
+        "evals_ratio_warm_over_plain": float(ew.mean() / ep.mean()),
+        "plain_evals_median": float(np.median(ep)), "warm_evals_median": float(np.median(ew)),
+        "plain_rounds": int(rp), "warm_rounds": int(rw),
+        "plain_wall_s": plain_s, "warm_wall_s": warm_s, "wall_ratio_warm_over_plain": warm_s / plain_s,
+        "frac_within_1e-3_of_plain": float(np.mean(deficit <= 1e-3)),
+        "max_lnl_deficit": float(deficit.max()), "mean_lnl_gain": float((-deficit).mean()),
+        "frac_network_start_used": float(used.mean()),
+        "x_rmse_vs_plain_fit": np.sqrt(np.mean((xw - xp) ** 2, axis=0)).tolist(),
+        "prediction_rmse_vs_plain_fit": np.sqrt(np.mean((ws.predict(feats) - xp) ** 2, axis=0)).tolist(),
+        "prediction_rmse_vs_truth": np.sqrt(np.mean((ws.predict(feats) - truth) ** 2, axis=0)).tolist(),
+    }
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="train and evaluate the learned warm start")
+    ap.add_argument("--cache", default="warmstart_cache", help="directory of the labelled set and the weights")
+    ap.add_argument("--train-items", type=int, default=10000)
+    ap.add_argument("--train-taxa", type=int, default=32)
+    ap.add_argument("--train-sites", type=int, default=2000)
+    ap.add_argument("--eval-items", type=int, default=1000)
+    ap.add_argument("--eval-taxa", type=int, default=64)
+    ap.add_argument("--eval-sites", type=int, default=5000)
+    ap.add_argument("--epochs", type=int, default=200)
+    ap.add_argument("--seed", type=int, default=1)
+    args = ap.parse_args(argv)
+    os.makedirs(args.cache, exist_ok=True)
+    data_path = os.path.join(args.cache, "labelled.npz")
+    net_path = os.path.join(args.cache, "warmstart.npz")
+    if os.path.exists(data_path):
+        data = LabelledSet.load(data_path)
+    else:
+        data = make_labelled(args.train_items, args.train_taxa, args.train_sites, args.seed)
+        data.save(data_path)
+    if os.path.exists(net_path):
+        ws, hist = WarmStart.load(net_path), {}
+    else:
+        ws, hist = train(data, epochs=args.epochs, seed=args.seed)
+        ws.save(net_path)
+    res = evaluate(ws, args.eval_items, args.eval_taxa, args.eval_sites, seed=args.seed + 1000)
+    res["label_fit_s"] = data.fit_s
+    res["label_evals_mean"] = float(data.evals.mean())
+    res["training"] = {k: v for k, v in hist.items() if k != "train_loss"}
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
