@@ -63,7 +63,7 @@ def load_peaks():
 def load_traffic():
     """DRAM bytes per launch of the post-order kernel from the committed ncu
     summary of this workload (None when no capture has been summarised)."""
-    p = os.path.join(ROOT, "profiles", "prune4_dna_gtr_g4_128x100k.json")
+    p = os.path.join(ROOT, "profiles", "prune4s_kernel_dna_gtr_g4_128x100k.json")
     if os.path.exists(p):
         d = json.load(open(p))
         return d.get("dram_bytes_per_launch")
@@ -237,6 +237,7 @@ def run_ours(args, world, rank, local):
     kern_ms, n_evals = h.kernel_times(reset=True)
     h.set_profiling(False)
     lnl_timed = h.loglik_result()
+    h_variant = h.prune_kernel()
     max_ms = reduce_max(world, dev_ms, dev)
     value = world * args.steps / (max_ms / 1e3)
 
@@ -297,7 +298,7 @@ def run_ours(args, world, rank, local):
                                "reduce": kern_ms[2] / max(n_evals, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": load_traffic(),
-                     "kernel": "prune4_kernel (post-order pass)",
+                     "kernel": f"{h_variant} (post-order pass)",
                      "algorithmic_bytes_per_launch": bytes_per_launch, "peak_source": peak_src,
                      "note": "algorithmic bytes of a level-by-level pass; this kernel keeps partials on chip"},
         "roofline_fp32": {"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -316,6 +317,76 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
     }
     del lnl32
+    print(json.dumps(line), flush=True)
+
+
+def run_protein(args):
+    """lnL evals/s of the 20-state workload (64 taxa, 20,000 sites, Gamma4):
+    each 20-state kernel forced in turn, then the autotuner's choice; the
+    post-order kernel time per evaluation against the roofline, and the error
+    against the FP64 oracle."""
+    import torch
+    from phylommand_gb300 import plk, synth
+    from oracle import oracle as O
+    w = synth.make("cfg3", seed=3)
+    teff = plk.effective_lengths(w.left, w.right, w.bl, False)
+    orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights, p_mode=O.P_EXACT,
+                   threads=os.cpu_count() or 1)
+    n_int = w.n_tips - 1
+    S, C = 20, len(w.cat_rates)
+    bytes_per_eval = algorithmic_bytes_per_site(w.n_tips, S, C, 4) * w.n_sites
+    flops_per_eval = algorithmic_flops_per_site(w.n_tips, S, C) * w.n_sites
+    hbm_peak, _, peak_src = load_peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    res = {}
+    names = {"1": "prune20_kernel, CUDA cores", "2": "prune20_kernel, tensor cores (split TF32)", "auto": "autotuned"}
+    for v in ("1", "2", "auto"):
+        if v == "auto":
+            os.environ.pop("PLK_PRUNE_VARIANT", None)
+        else:
+            os.environ["PLK_PRUNE_VARIANT"] = v
+        with plk.Handle() as h:
+            h.set_alignment(w.masks, S)
+            h.set_tree(w.left, w.right, w.bl)
+            h.set_rate_model(False)
+            h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
+            h.set_stream(stream.cuda_stream)
+            for _ in range(max(args.warmup, 3)):
+                h.loglik_async(plk.PLK_FP32S)
+            h.loglik_result()
+            h.set_profiling(True)
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+            torch.cuda.synchronize()
+            for k in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                starts[k].record(stream)
+                h.loglik_async(plk.PLK_FP32S)
+                ends[k].record(stream)
+            torch.cuda.synchronize()
+            ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+            kern, n = h.kernel_times(reset=True)
+            h.set_profiling(False)
+            lnl = h.loglik_result()
+            post_ms = kern[1] / max(n, 1)
+            res[v] = {"kernel": names[v], "evals_per_s": 1e3 / ms, "ms_per_eval": ms, "postorder_ms": post_ms,
+                      "gsite_node_updates_per_s": n_int * w.n_sites / (ms / 1e3) / 1e9,
+                      "achieved_tflops": flops_per_eval / (post_ms / 1e3) / 1e12,
+                      "achieved_gbs_algorithmic": bytes_per_eval / (post_ms / 1e3) / 1e9,
+                      "rel_err_vs_fp64_oracle": abs(lnl - orc.lnl) / abs(orc.lnl)}
+    os.environ.pop("PLK_PRUNE_VARIANT", None)
+    best = res["auto"]
+    line = {"metric": "lnL evals/s (20 states)", "value": best["evals_per_s"], "unit": "evals/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_eval"], "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "20-state, 64-taxon Yule tree, 20,000 sites, exchangeabilities LogNormal(0,1), "
+                                   "Gamma4 alpha 1", "l2": "flushed before every step"},
+            "roofline": {"bound": "hbm", "achieved": best["achieved_gbs_algorithmic"], "peak": hbm_peak,
+                         "unit": "GB/s", "frac": best["achieved_gbs_algorithmic"] / hbm_peak, "traffic": None,
+                         "algorithmic_bytes_per_launch": bytes_per_eval, "peak_source": peak_src},
+            "algorithmic_flops_per_eval": flops_per_eval, "variants": res}
     print(json.dumps(line), flush=True)
 
 
@@ -408,13 +479,16 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dna", choices=["dna", "nni"],
+    ap.add_argument("--workload", default="dna", choices=["dna", "nni", "protein"],
                     help="dna: the headline workload; nni: the uneven batch with NNI neighbours")
     ap.add_argument("--nni-items", type=int, default=512)
     ap.add_argument("--nni-sample", type=int, default=24)
     args = ap.parse_args()
     if args.workload == "nni":
         run_nni(args)
+        return
+    if args.workload == "protein":
+        run_protein(args)
         return
     world, rank, local = (1, 0, 0) if args.impl == "reference" else dist_setup(args.gpus)
     if args.impl == "reference":

@@ -147,6 +147,12 @@ plk_status plk_set_stream(plk_handle* h, void* cuda_stream);
  * reset, and their number. */
 plk_status plk_set_profiling(plk_handle* h, int on);
 plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int reset);
+/* The 4-state FP32 post-order kernel the autotuner chose for the current
+ * tree and alignment: 0 = prune4_kernel (partials in registers, P(t) from
+ * global memory), 1 / 2 = prune4s_kernel with 1 / 2 sites per thread (P(t)
+ * rows and tip tables staged in shared memory); -1 = not tuned yet or another
+ * kernel applies (FP64, S != 4, more than 8 categories). */
+int plk_prune_variant(const plk_handle* h);
 /* Per-site log-likelihoods of the last plk_loglik (n_sites doubles). */
 plk_status plk_site_loglik(plk_handle* h, double* out);
 /* Node-state output for every internal node: out[(rank * n_sites + site) *
@@ -222,7 +228,10 @@ plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid
 /* Summary statistics of every item (the warm-start network's inputs), 43
  * floats per item: base frequencies (4), mean pairwise proportions of the
  * substitution types A<->G, A<->C, A<->T, G<->C, G<->T, C<->T (6), histogram of
- * per-site entropy in 32 bins over [0, ln 4] (32), mean p-distance (1). */
+ * per-site collision entropy -ln(sum_s c_s (c_s - 1) / (m (m - 1))) (c_s the
+ * counts of m unambiguous taxa) in 32 bins over [0, ln 4] (32), mean
+ * p-distance (1).  Every statistic is a pairwise one, so none drifts with the
+ * number of taxa. */
 plk_status plk_batch_features(plk_batch* b, float* out);
 /* Maximum-likelihood fits of every item at once: one Nelder-Mead per item
  * (the parameterisation of plk_fit_gtr: log exchangeabilities relative to the
@@ -231,10 +240,15 @@ plk_status plk_batch_features(plk_batch* b, float* out);
  * unfinished fit's next point in one batch launch.  freqs[n_items][4] fixed;
  * x0[n_items][n_params] or NULL (all zero); step[n_items] initial simplex
  * sizes or NULL (0.5).  Outputs per item: x_out, lnl_out, evals_out (may be
- * NULL); rounds_out = batch evaluations used. */
+ * NULL); rounds_out = batch evaluations used.  Stopping rule of every fit:
+ * the simplex's lnL spread <= ftol and its extent <= xtol in every
+ * coordinate, or max_evals.  Optional: with target_lnl[n_items],
+ * hit_evals_out[i] = the number of evaluations after which item i first
+ * reached lnL >= target_lnl[i] - target_tol (-1 if never). */
 plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0, const double* step,
                              double ftol, double xtol, int max_evals, double* x_out, double* lnl_out,
-                             int* evals_out, int* rounds_out);
+                             int* evals_out, int* rounds_out, const double* target_lnl,
+                             double target_tol, int* hit_evals_out);
 /* lnL of every item at the GTR parameter vector x[n_items][n_params] (the
  * parameterisation of plk_batch_fit_gtr) in one batch evaluation; the items
  * keep these models.  -HUGE_VAL where a vector gives no valid model. */

@@ -93,7 +93,7 @@ struct plk_handle {
     // autotuned 4-state FP32 kernel (-1: not tuned for the current inputs)
     int variant = -1;
     float tune_ms[3] = {0.f, 0.f, 0.f};
-    std::map<std::array<int, 5>, int> tune_cache;  // (sites, tips, ops, depth, cats) -> variant
+    std::map<std::array<int, 6>, int> tune_cache;  // (sites, tips, ops, depth, cats, states) -> variant
     // streams: own_stream is created with the handle; stream is the active one
     cudaStream_t own_stream = nullptr;
     // kernel timing (plk_set_profiling)
@@ -202,6 +202,7 @@ PruneArgs prune_args(plk_handle* h, int precision) {
     a.rank = h->d_rank.as<int>();
     a.n_int = (int)h->post.size();
     a.n_tips = h->n_tips;
+    a.n_nodes = h->n_nodes;
     return a;
 }
 
@@ -213,34 +214,41 @@ bool fused_kernel_applies(const plk_handle* h, int precision) {
     return ops_bytes + stack <= 227 * 1024;
 }
 
-// Autotuner of the 4-state FP32 post-order kernel: times every candidate
-// (prune4_kernel; prune4s_kernel with 1 and 2 sites per thread) on this
+// Autotuner of the FP32 post-order kernels: times every candidate on this
 // handle's tree and sites -- one warm-up and three timed launches each, CUDA
 // events on the handle's stream -- and keeps the fastest until the tree,
-// alignment or model changes.  PLK_PRUNE_VARIANT=0|1|2 forces a choice.
-plk_status autotune_prune(plk_handle* h, PruneArgs a) {
+// alignment or model changes.  4 states: prune4_kernel and prune4s_kernel
+// with 1 and 2 sites per thread; 20 states: prune20_kernel on CUDA cores and
+// on tensor cores.  PLK_PRUNE_VARIANT=<n> forces candidate n where it applies.
+plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& cands) {
+    if (cands.empty()) return fail(h, PLK_ERR_STATE, "no post-order kernel applies");
     if (const char* f = getenv("PLK_PRUNE_VARIANT")) {
         const int v = atoi(f);
-        if (v >= 0 && v <= 2 && (v == 0 || prune4s_fits(a, v))) {
+        if (std::find(cands.begin(), cands.end(), v) != cands.end()) {
             h->variant = v;
             return PLK_OK;
         }
     }
     // same sizes as an earlier tuning on this handle: reuse its choice
-    const std::array<int, 5> key = {a.n_sites, a.n_tips, a.n_ops, a.max_depth, a.C};
+    const std::array<int, 6> key = {a.n_sites, a.n_tips, a.n_ops, a.max_depth, a.C, h->S};
     auto hit = h->tune_cache.find(key);
     if (hit != h->tune_cache.end()) {
         h->variant = hit->second;
+        return PLK_OK;
+    }
+    if (cands.size() == 1) {
+        h->variant = cands[0];
+        h->tune_cache[key] = cands[0];
         return PLK_OK;
     }
     cudaEvent_t e0, e1;
     PLK_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
     PLK_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
     float best = 1e30f;
-    int best_v = 0;
+    int best_v = cands[0];
     cudaError_t err = cudaSuccess;
-    for (int v = 0; v <= 2 && err == cudaSuccess; ++v) {
-        if (v > 0 && !prune4s_fits(a, v)) continue;
+    for (int v : cands) {
+        if (err != cudaSuccess) break;
         a.variant = v;
         int nb = 0;
         err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
@@ -251,7 +259,7 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a) {
         if (err == cudaSuccess) err = cudaEventSynchronize(e1);
         float ms = 0.f;
         if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-        h->tune_ms[v] = ms / 3.0f;
+        if (v >= 0 && v < 3) h->tune_ms[v] = ms / 3.0f;
         if (err == cudaSuccess && ms < best) { best = ms; best_v = v; }
     }
     cudaEventDestroy(e0);
@@ -273,7 +281,19 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     PLK_CUDA(h, h->d_lnl.ensure(sizeof(double)), "allocate lnL");
     PruneArgs a = prune_args(h, precision);
     const bool fused = fused_kernel_applies(h, precision);
-    if (!fused) {
+    std::vector<int> cands20;
+    if (!store && precision == PLK_FP32S && h->S == 20)
+        for (int v = 1; v <= 2; ++v)
+            if (prune20_fits(a, v)) cands20.push_back(v);
+    if (!cands20.empty()) {
+        PLK_CUDA(h, h->d_work.ensure(prune20_scratch_bytes(a, h->n_nodes)), "allocate scratch");
+        a.scratch = h->d_work.p;
+        if (h->variant < 0) {
+            plk_status s = autotune_prune(h, a, cands20);
+            if (s != PLK_OK) return s;
+        }
+        a.variant = h->variant;
+    } else if (!fused) {
         PLK_CUDA(h, h->d_work.ensure(vec_bytes), "allocate work vectors");
         a.work = h->d_work.p;
         a.cond = h->d_work.p;
@@ -283,7 +303,10 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     }
     if (fused && !store && precision == PLK_FP32S) {
         if (h->variant < 0) {
-            plk_status s = autotune_prune(h, a);
+            std::vector<int> cands = {0};
+            for (int v = 1; v <= 2; ++v)
+                if (prune4s_fits(a, v)) cands.push_back(v);
+            plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }
         a.variant = h->variant;
@@ -603,6 +626,8 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
     if (reset) h->ev_used = 0;
     return PLK_OK;
 }
+
+int plk_prune_variant(const plk_handle* h) { return h ? h->variant : -1; }
 
 plk_status plk_site_loglik(plk_handle* h, double* out) {
     if (!h) return PLK_ERR_ARG;

@@ -691,7 +691,7 @@ plk_status plk_batch_eval_gtr(plk_batch* b, const double* freqs, const double* x
 
 plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0, const double* step, double ftol,
                              double xtol, int max_evals, double* x_out, double* lnl_out, int* evals_out,
-                             int* rounds_out) {
+                             int* rounds_out, const double* target_lnl, double target_tol, int* hit_evals_out) {
     if (!b || !freqs || !x_out || !lnl_out || max_evals < 1)
         return b ? bfail(b, PLK_ERR_ARG, "bad arguments to plk_batch_fit_gtr") : PLK_ERR_ARG;
     const int n_items = (int)b->items.size();
@@ -723,6 +723,7 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
             if (s != PLK_OK) return s;
         }
     int rounds = 0;
+    std::vector<int> hit(n_items, -1);
     for (;;) {
         bool any = false;
         for (const auto& nm : nms) any = any || !nm.done();
@@ -734,9 +735,13 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
         ++rounds;
         for (int i = 0; i < n_items; ++i) {
             if (nms[i].done()) continue;
-            nms[i].tell(in_domain[i] && std::isfinite(lnl[i]) ? -lnl[i] : HUGE_VAL);
+            const bool ok = in_domain[i] && std::isfinite(lnl[i]);
+            nms[i].tell(ok ? -lnl[i] : HUGE_VAL);
+            // first evaluation that comes within target_tol of the target
+            if (target_lnl && hit[i] < 0 && ok && lnl[i] >= target_lnl[i] - target_tol) hit[i] = nms[i].evals();
         }
     }
+    if (hit_evals_out) std::copy(hit.begin(), hit.end(), hit_evals_out);
     for (int i = 0; i < n_items; ++i) {
         const std::vector<double>& bx = nms[i].best_x();
         std::copy(bx.begin(), bx.end(), x_out + (size_t)i * np);

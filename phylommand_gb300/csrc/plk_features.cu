@@ -4,7 +4,8 @@
 //   [4, 10)   mean pairwise proportions of the six substitution types
 //             A<->G, A<->C, A<->T, G<->C, G<->T, C<->T among all tip pairs
 //             that carry unambiguous states at a site
-//   [10, 42)  histogram of per-site Shannon entropy in 32 bins over [0, ln 4]
+//   [10, 42)  histogram of per-site collision (order-2 Renyi) entropy in 32
+//             bins over [0, ln 4]
 //   42        mean pairwise p-distance
 // Per site only the four state counts c_s of the unambiguous tips matter:
 // pairs of type (a, b) number c_a c_b and identical pairs c_a (c_a - 1) / 2,
@@ -49,17 +50,17 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(BatchDev b, floa
         for (int s = 0; s < 4; ++s) same += 0.5 * c[s] * (c[s] - 1);
         acc[10] += same;
         acc[11] += 0.5 * (double)m * (m - 1);
-        double h = 0.0;
-        if (m > 0)
-            for (int s = 0; s < 4; ++s)
-                if (c[s] > 0) {
-                    const double p = (double)c[s] / m;
-                    h -= p * log(p);
-                }
-        // entropies exactly on a bin edge (e.g. two equal counts: half of
-        // ln 4) go up whatever the last bit of log(); 1e-9 is far below the
-        // spacing of the entropies integer counts can give
-        int bin = (int)(h / 1.3862943611198906 * 32.0 + 1e-9);
+        // collision entropy -ln(sum_s c_s (c_s - 1) / (m (m - 1))): the pair
+        // estimate is unbiased for any number of observed taxa m, so the
+        // histogram does not drift with the taxon count; sites with fewer
+        // than two observed taxa or no identical pair go to the last bin
+        int bin = 31;
+        if (m >= 2 && same > 0.0) {
+            const double h = -log(same / (0.5 * (double)m * (m - 1)));
+            // entropies exactly on a bin edge go up whatever the last bit of
+            // log(); 1e-9 is far below the spacing integer counts can give
+            bin = (int)(h / 1.3862943611198906 * 32.0 + 1e-9);
+        }
         bin = bin < 0 ? 0 : (bin > 31 ? 31 : bin);
         acc[12 + bin] += 1.0;
     }

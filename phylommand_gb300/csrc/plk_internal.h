@@ -151,10 +151,21 @@ struct PruneArgs {
     const int* rank;           // [n_nodes], -1 for tips
     int n_int;
     int n_tips;
-    // 4-state FP32 kernel choice: 0 = prune4_kernel, 1/2 = prune4s_kernel
-    // with 1/2 sites per thread (picked by the autotuner)
+    // FP32 kernel choice (picked by the autotuner).  4 states: 0 =
+    // prune4_kernel, 1/2 = prune4s_kernel with 1/2 sites per thread.
+    // 20 states: 0 = prune_generic_kernel, 1 = prune20_kernel on CUDA cores,
+    // 2 = prune20_kernel on tensor cores (TF32, three-product split).
     int variant;
+    int n_nodes;
+    void* scratch;             // kernel-specific scratch (prune20_scratch_bytes)
 };
+// Fused 20-state FP32 kernels (plk_prune20.cu): mode 1 = CUDA cores, 2 =
+// tensor cores.  Launches the relayout, the pass and the per-site combine;
+// *n_blocks = the block sums left for launch_reduce.
+bool prune20_fits(const PruneArgs& a, int mode);
+size_t prune20_scratch_bytes(const PruneArgs& a, int n_nodes);
+cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scratch, int* n_blocks,
+                           cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
 bool prune4s_fits(const PruneArgs& a, int spt);
 cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);

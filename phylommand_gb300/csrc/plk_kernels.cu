@@ -515,6 +515,8 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
     const bool fp64 = precision == PLK_FP64;
     if (!fp64 && !store && S == 4 && a.C <= 8 && a.variant > 0 && prune4s_fits(a, a.variant))
         return launch_prune4s(a, a.variant, n_blocks, st);
+    if (!fp64 && !store && S == 20 && a.variant > 0 && prune20_fits(a, a.variant))
+        return launch_prune20(a, a.n_nodes, a.variant, a.scratch, n_blocks, st);
     if (S == 4 && a.C <= 8) {
         const size_t ops_bytes = ((size_t)a.n_ops * sizeof(Op) + 31) & ~(size_t)31;
         const int cm = a.C == 1 ? 1 : (a.C <= 4 ? 4 : 8);

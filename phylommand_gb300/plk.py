@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -39,7 +40,7 @@ EXPORTS = [
     "plk_loglik", "plk_site_loglik", "plk_node_states", "plk_n_internal",
     "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
-    "plk_sum_sites_noalloc",
+    "plk_sum_sites_noalloc", "plk_prune_variant",
     "plk_fit_gtr", "plk_fit_n_params",
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
@@ -98,6 +99,7 @@ def lib() -> ctypes.CDLL:
     L.plk_set_stream.argtypes = [hp, c_void_p]
     L.plk_set_profiling.argtypes = [hp, c_int]
     L.plk_kernel_times.argtypes = [hp, dp, ip, c_int]
+    L.plk_prune_variant.argtypes = [hp]
     L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
     L.plk_fit_gtr.argtypes = [hp, c_int, dp, c_int, dp, c_double, c_double, c_double, c_int, dp, dp, ip]
     L.plk_fit_n_params.argtypes = [c_int, c_int]
@@ -117,7 +119,7 @@ def lib() -> ctypes.CDLL:
     L.plk_simulate.argtypes = [c_int, ip, ip, dp, c_int, dp, dp, c_int, dp, c_int, ctypes.c_uint64, c_int, u32p]
     L.plk_nni_moves_host.argtypes = [c_int, ip, ip, ip, ip]
     L.plk_batch_features.argtypes = [hp, fp]
-    L.plk_batch_fit_gtr.argtypes = [hp, dp, dp, dp, c_double, c_double, c_int, dp, dp, ip, ip]
+    L.plk_batch_fit_gtr.argtypes = [hp, dp, dp, dp, c_double, c_double, c_int, dp, dp, ip, ip, dp, c_double, ip]
     L.plk_batch_eval_gtr.argtypes = [hp, dp, dp, dp]
     L.plk_mlp_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64]
     L.plk_mlp_destroy.argtypes = [hp]
@@ -316,6 +318,12 @@ class Handle:
         _check(lib().plk_kernel_times(self._h, _p(ms, ctypes.c_double), ctypes.byref(n), int(reset)), self._h)
         return ms, n.value
 
+    PRUNE_KERNELS = {0: "prune4_kernel", 1: "prune4s_kernel (1 site/thread)", 2: "prune4s_kernel (2 sites/thread)"}
+
+    def prune_kernel(self) -> str:
+        """Name of the autotuned 4-state FP32 post-order kernel (or 'other')."""
+        return self.PRUNE_KERNELS.get(int(lib().plk_prune_variant(self._h)), "other")
+
     def site_loglik(self) -> np.ndarray:
         out = np.zeros(self.n_sites)
         _check(lib().plk_site_loglik(self._h, _p(out, ctypes.c_double)), self._h)
@@ -351,6 +359,18 @@ def sum_sites_noalloc(d_site_lnl: int, n_sites: int, d_lnl_out: int, cuda_stream
     device double, allocating nothing (device addresses as integers)."""
     _check(lib().plk_sum_sites_noalloc(ctypes.c_void_p(d_site_lnl), int(n_sites), ctypes.c_void_p(d_lnl_out),
                                        ctypes.c_void_p(cuda_stream or 0)))
+
+
+@dataclass
+class BatchFit:
+    """Result of Batch.fit_gtr: per item the parameter vector, lnL and
+    evaluation count; the batch evaluations (rounds) used; with a target, the
+    evaluations each item needed to come within the tolerance of it."""
+    x: np.ndarray
+    lnl: np.ndarray
+    evals: np.ndarray
+    rounds: int
+    hit_evals: np.ndarray | None = None
 
 
 class Batch:
@@ -416,22 +436,26 @@ class Batch:
         self._check(lib().plk_batch_features(self._b, _p(out, ctypes.c_float)))
         return out
 
-    def fit_gtr(self, freqs, x0=None, step=None, ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 3000):
-        """Lockstep Nelder-Mead ML fits of every item; returns (x, lnL, evals, rounds)."""
+    def fit_gtr(self, freqs, x0=None, step=None, ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 3000,
+                target=None, target_tol: float = 1e-3) -> "BatchFit":
+        """Lockstep Nelder-Mead ML fits of every item (see plk_batch_fit_gtr)."""
         n = len(self)
         np_ = int(lib().plk_fit_n_params(4, self.n_cats))
         f = np.ascontiguousarray(freqs, dtype=np.float64).reshape(n, 4)
         x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64).reshape(n, np_)
         st = None if step is None else np.ascontiguousarray(np.broadcast_to(step, (n,)), dtype=np.float64)
+        tg = None if target is None else np.ascontiguousarray(target, dtype=np.float64).reshape(n)
         x = np.zeros((n, np_))
         lnl = np.zeros(n)
         ev = np.zeros(n, dtype=np.int32)
+        hits = np.full(n, -1, dtype=np.int32)
         rounds = ctypes.c_int(0)
         self._check(lib().plk_batch_fit_gtr(self._b, _p(f, ctypes.c_double), _p(x0a, ctypes.c_double),
                                             _p(st, ctypes.c_double), float(ftol), float(xtol), int(max_evals),
                                             _p(x, ctypes.c_double), _p(lnl, ctypes.c_double), _p(ev, ctypes.c_int),
-                                            ctypes.byref(rounds)))
-        return x, lnl, ev, rounds.value
+                                            ctypes.byref(rounds), _p(tg, ctypes.c_double), float(target_tol),
+                                            _p(hits, ctypes.c_int)))
+        return BatchFit(x, lnl, ev, rounds.value, hits if tg is not None else None)
 
     def eval_gtr(self, freqs, x) -> np.ndarray:
         """lnL of every item at its GTR parameter vector x[n_items, n_params]."""

@@ -126,10 +126,10 @@ def _features_ref(masks):
     types = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
     for q, (a, b) in enumerate(types):
         out[4 + q] = (c[a] * c[b]).sum() / pairs
-    with np.errstate(divide="ignore", invalid="ignore"):
-        p = np.where(m > 0, c / np.maximum(m, 1), 0.0)
-        h = -np.where(p > 0, p * np.log(np.where(p > 0, p, 1.0)), 0.0).sum(axis=0)
-    bins = np.clip((h / np.log(4.0) * 32.0 + 1e-9).astype(int), 0, 31)
+    same = (0.5 * c * (c - 1)).sum(axis=0)
+    ok = (m >= 2) & (same > 0)
+    h = -np.log(np.where(ok, same, 1.0) / np.where(ok, 0.5 * m * (m - 1), 1.0))
+    bins = np.where(ok, np.clip((h / np.log(4.0) * 32.0 + 1e-9).astype(int), 0, 31), 31)
     out[10:42] = np.bincount(bins, minlength=32) / masks.shape[1]
     out[42] = 1.0 - (0.5 * c * (c - 1)).sum() / pairs
     return out
@@ -188,6 +188,7 @@ def test_warm_start_end_to_end_small():
     assert hist["train_loss"][-1] < 0.5 * hist["train_loss"][0]
     # the network beats predicting the label mean on held-out labels
     assert np.mean(hist["val_rmse"]) < np.mean(hist["val_rmse_mean_predictor"])
-    res = warmstart.evaluate(ws, n_items=120, n_taxa=16, n_sites=1000, seed=99)
-    assert res["frac_within_1e-3_of_plain"] >= 0.95, res
-    assert res["warm_evals_mean"] < res["plain_evals_mean"], res
+    # held out, and with twice the taxa of the training alignments
+    res = warmstart.evaluate(ws, n_items=120, n_taxa=32, n_sites=1000, seed=99)
+    assert res["frac_final_within_tol_of_plain"] >= 0.9, res
+    assert res["evals_to_optimum_ratio_warm_over_plain"] < 0.8, res

@@ -220,3 +220,38 @@ def test_full_size_dna_gtr_gamma_fp32_against_fp64():
         l32 = h.loglik(plk.PLK_FP32S)
     assert l64 == pytest.approx(orc.lnl, rel=1e-11)
     assert l32 == pytest.approx(orc.lnl, rel=FP32_REL)
+
+
+@pytest.mark.parametrize("n_tips,n_sites,C,shape", [(64, 2000, 4, "yule"), (7, 1, 1, "yule"), (33, 129, 8, "yule"),
+                                                    (200, 300, 4, "caterpillar"), (16, 4099, 2, "yule")])
+def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
+    """20 states: prune20_kernel on CUDA cores (1) and on tensor cores with
+    the split-TF32 products (2) against the FP64 oracle, per site; the
+    caterpillar tree forces repeated rescaling, ambiguity codes the table
+    look-ups."""
+    rng = np.random.default_rng(n_tips * 7 + n_sites)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, S=20, C=C, missing=0.03, shape=shape)
+    amb = rng.random(masks.shape) < 0.02
+    masks[amb] |= np.uint32(1 << 3)                          # two-state ambiguity
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
+    for v in ("1", "2"):
+        monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
+        with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
+            got = h.loglik(plk.PLK_FP32S)
+            assert h.prune_kernel() == "other"                 # names only the 4-state kernels
+            assert got == pytest.approx(orc.lnl, rel=FP32_REL), v
+            np.testing.assert_allclose(h.site_loglik(), orc.site_lnl, rtol=2e-6, atol=1e-9)
+            # the plain FP64 form stays bit-compatible with the oracle
+            assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-11)
+
+
+def test_protein_autotuned_full_size():
+    """64 taxa x 20,000 sites, 20 states, Gamma4: the autotuned 20-state
+    kernel within 1e-6 relative of the FP64 oracle."""
+    w = synth.make("cfg3", seed=3)
+    teff = plk.effective_lengths(w.left, w.right, w.bl, False)
+    orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights,
+                   p_mode=O.P_EXACT, threads=8)
+    with _engine(w.left, w.right, w.bl, w.masks, 20, w.Q, w.freqs, w.cat_rates, w.cat_weights) as h:
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
