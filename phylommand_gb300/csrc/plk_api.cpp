@@ -302,10 +302,18 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
         a.cond = h->d_cond.p;
     }
     if (fused && !store && precision == PLK_FP32S) {
+        // the paired kernels read P(t) and tip tables re-laid out in scratch
+        const bool paired = prune4p_fits(a, 1) || prune4p_fits(a, 2);
+        if (paired) {
+            PLK_CUDA(h, h->d_work.ensure(prune4p_scratch_bytes(a)), "allocate scratch");
+            a.scratch = h->d_work.p;
+        }
         if (h->variant < 0) {
             std::vector<int> cands = {0};
             for (int v = 1; v <= 2; ++v)
                 if (prune4s_fits(a, v)) cands.push_back(v);
+            for (int v = 3; v <= 4; ++v)
+                if (prune4p_fits(a, v - 2)) cands.push_back(v);
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }

@@ -318,11 +318,18 @@ class Handle:
         _check(lib().plk_kernel_times(self._h, _p(ms, ctypes.c_double), ctypes.byref(n), int(reset)), self._h)
         return ms, n.value
 
-    PRUNE_KERNELS = {0: "prune4_kernel", 1: "prune4s_kernel (1 site/thread)", 2: "prune4s_kernel (2 sites/thread)"}
+    PRUNE_KERNELS = {
+        4: {0: "prune4_kernel", 1: "prune4s_kernel (1 site/thread)", 2: "prune4s_kernel (2 sites/thread)",
+            3: "prune4p_kernel (category pairs on FP32x2, 1 site/thread)",
+            4: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread)"},
+        20: {1: "prune20_kernel (CUDA cores)", 2: "prune20_kernel (tensor cores, split TF32)"},
+    }
 
     def prune_kernel(self) -> str:
-        """Name of the autotuned 4-state FP32 post-order kernel (or 'other')."""
-        return self.PRUNE_KERNELS.get(int(lib().plk_prune_variant(self._h)), "other")
+        """Name of the autotuned FP32 post-order kernel, or 'other' where no
+        tuned choice applies (FP64, other state counts, untuned)."""
+        v = int(lib().plk_prune_variant(self._h))
+        return self.PRUNE_KERNELS.get(getattr(self, "n_states", 0), {}).get(v, "other")
 
     def site_loglik(self) -> np.ndarray:
         out = np.zeros(self.n_sites)

@@ -192,20 +192,25 @@ def test_repeat_calls_are_deterministic():
 @pytest.mark.parametrize("n_tips,n_sites,C", [(128, 1000, 4), (40, 257, 1), (1300, 300, 4), (60, 129, 8)])
 def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
     """Every candidate of the autotuner (prune4_kernel, prune4s_kernel with 1
-    and 2 sites per thread; tip codes in shared memory or read from global for
-    the 1300-tip tree) gives the same per-site values."""
+    and 2 sites per thread, prune4p_kernel with category pairs on FP32x2 where
+    C is 2, 4 or 8; tip codes in shared memory or read from global for the
+    1300-tip tree) gives the same per-site values."""
     rng = np.random.default_rng(n_tips + n_sites)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, C=C)
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
     sites = []
-    for v in ("0", "1", "2"):
+    variants = ("0", "1", "2", "3", "4") if C in (2, 4, 8) else ("0", "1", "2")
+    for v in variants:
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
             assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+            assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[4][int(v)]
             sites.append(h.site_loglik())
     np.testing.assert_allclose(sites[1], sites[0], rtol=1e-12)
-    np.testing.assert_allclose(sites[2], sites[0], rtol=1e-12)
+    for s in sites[2:]:
+        # the staged kernels do the same operations in the same order: the same bits
+        np.testing.assert_array_equal(s, sites[1])
 
 
 def test_full_size_dna_gtr_gamma_fp32_against_fp64():
@@ -239,7 +244,7 @@ def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
             got = h.loglik(plk.PLK_FP32S)
-            assert h.prune_kernel() == "other"                 # names only the 4-state kernels
+            assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[20][int(v)]
             assert got == pytest.approx(orc.lnl, rel=FP32_REL), v
             np.testing.assert_allclose(h.site_loglik(), orc.site_lnl, rtol=2e-6, atol=1e-9)
             # the plain FP64 form stays bit-compatible with the oracle
