@@ -238,8 +238,9 @@ plk_status plk_batch_features(plk_batch* b, float* out);
  * last, log alpha, log tree-length scale; n_params = plk_fit_n_params(4,
  * n_cats)), advanced in lockstep so that each round evaluates every
  * unfinished fit's next point in one batch launch.  freqs[n_items][4] fixed;
- * x0[n_items][n_params] or NULL (all zero); step[n_items] initial simplex
- * sizes or NULL (0.5).  Outputs per item: x_out, lnl_out, evals_out (may be
+ * x0[n_items][n_params] or NULL (all zero); step[n_items][n_params] initial
+ * simplex steps (vertex i = x0 + step_i e_i) or NULL (all 0.5).  Outputs
+ * per item: x_out, lnl_out, evals_out (may be
  * NULL); rounds_out = batch evaluations used.  Stopping rule of every fit:
  * the simplex's lnL spread <= ftol and its extent <= xtol in every
  * coordinate, or max_evals.  Optional: with target_lnl[n_items],

@@ -703,7 +703,9 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
     for (int i = 0; i < n_items; ++i) {
         std::vector<double> start(np, 0.0);
         if (x0) std::copy(x0 + (size_t)i * np, x0 + (size_t)(i + 1) * np, start.begin());
-        nms.emplace_back(np, start.data(), step ? step[i] : 0.5, ftol, xtol, max_evals);
+        std::vector<double> steps(np, 0.5);
+        if (step) std::copy(step + (size_t)i * np, step + (size_t)(i + 1) * np, steps.begin());
+        nms.emplace_back(np, start.data(), steps.data(), ftol, xtol, max_evals);
     }
     std::vector<char> in_domain(n_items, 1);
     std::vector<double> lnl(n_items);

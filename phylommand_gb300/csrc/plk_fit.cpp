@@ -26,6 +26,12 @@ NelderMead::NelderMead(int n, const double* x0, double step, double ftol_abs, do
     init_i_ = 0;
 }
 
+NelderMead::NelderMead(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals)
+    : NelderMead(n, x0, 0.0, ftol_abs, xtol, max_evals) {
+    for (int i = 0; i < n; ++i) simplex_[i + 1][i] = x0[i] + steps[i];
+    point_ = simplex_[0];
+}
+
 void NelderMead::order() {
     std::vector<int> idx(n_ + 1);
     std::iota(idx.begin(), idx.end(), 0);

@@ -79,6 +79,8 @@ bool simulate_sites(int n_tips, int n_nodes, const int* left, const int* right, 
 class NelderMead {
   public:
     NelderMead(int n, const double* x0, double step, double ftol_abs, double xtol, int max_evals);
+    // initial simplex x0 + steps[i] e_i (one step per coordinate)
+    NelderMead(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals);
     bool done() const { return state_ == State::Done; }
     bool converged_ok() const { return converged_; }
     const std::vector<double>& point() const { return point_; }

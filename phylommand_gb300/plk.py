@@ -450,7 +450,13 @@ class Batch:
         np_ = int(lib().plk_fit_n_params(4, self.n_cats))
         f = np.ascontiguousarray(freqs, dtype=np.float64).reshape(n, 4)
         x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64).reshape(n, np_)
-        st = None if step is None else np.ascontiguousarray(np.broadcast_to(step, (n,)), dtype=np.float64)
+        st = None
+        if step is not None:
+            # a scalar, one step per item, one per parameter, or [n_items, n_params]
+            s = np.asarray(step, dtype=np.float64)
+            if s.ndim == 1 and s.shape[0] == n and n != np_:
+                s = s[:, None]
+            st = np.ascontiguousarray(np.broadcast_to(s, (n, np_)), dtype=np.float64)
         tg = None if target is None else np.ascontiguousarray(target, dtype=np.float64).reshape(n)
         x = np.zeros((n, np_))
         lnl = np.zeros(n)

@@ -151,13 +151,13 @@ def make_labelled(n_items: int, n_taxa: int, n_sites: int, seed: int, ftol: floa
 
 class WarmStart:
     """The trained network with its input/output standardisation and the
-    initial simplex size used from its predictions."""
+    initial simplex steps (one per parameter) used from its predictions."""
 
-    def __init__(self, net: plk.MLP, x_mean, x_std, y_mean, y_std, step: float):
+    def __init__(self, net: plk.MLP, x_mean, x_std, y_mean, y_std, step):
         self.net = net
         self.x_mean, self.x_std = np.asarray(x_mean, np.float32), np.asarray(x_std, np.float32)
         self.y_mean, self.y_std = np.asarray(y_mean, np.float32), np.asarray(y_std, np.float32)
-        self.step = float(step)
+        self.step = np.broadcast_to(np.asarray(step, np.float64), (N_PARAMS,)).copy()
 
     def predict(self, features) -> np.ndarray:
         z = (np.asarray(features, np.float32) - self.x_mean) / self.x_std
@@ -174,13 +174,15 @@ class WarmStart:
         n_in, n_out, n_hidden, layers = (int(v) for v in z["shape"])
         net = plk.MLP(n_in, n_out, n_hidden, layers, device=device)
         net.set_params(z["params"])
-        return WarmStart(net, z["x_mean"], z["x_std"], z["y_mean"], z["y_std"], float(z["step"]))
+        return WarmStart(net, z["x_mean"], z["x_std"], z["y_mean"], z["y_std"], z["step"])
 
 
 def train(data: LabelledSet, epochs: int = 200, batch: int = 256, lr: float = 1e-3, seed: int = 0,
-          val_frac: float = 0.1, n_hidden: int = 256, n_hidden_layers: int = 3):
+          val_frac: float = 0.1, n_hidden: int = 256, n_hidden_layers: int = 3, step_scale: float = 1.0):
     """Adam on the mean squared error of standardised labels; returns the
-    WarmStart and a history dict (losses, validation RMSE per parameter)."""
+    WarmStart and a history dict (losses, validation RMSE per parameter).
+    The initial simplex step of each parameter is step_scale times its
+    validation RMSE, within [0.02, 0.5]."""
     rng = np.random.default_rng(seed)
     n = data.features.shape[0]
     perm = rng.permutation(n)
@@ -214,11 +216,10 @@ def train(data: LabelledSet, epochs: int = 200, batch: int = 256, lr: float = 1e
     ws = WarmStart(net, x_mean, x_std, y_mean, y_std, DEFAULT_STEP)
     resid = ws.predict(X[val]) - data.labels[val]
     rmse = np.sqrt(np.mean(resid ** 2, axis=0))
-    # start simplex: about twice the typical prediction error, within [0.05, 0.5]
-    ws.step = float(np.clip(2.0 * np.sqrt(np.mean(rmse ** 2)), 0.05, DEFAULT_STEP))
+    ws.step = np.clip(step_scale * rmse, 0.02, DEFAULT_STEP)
     base = np.sqrt(np.mean((data.labels[val] - y_mean) ** 2, axis=0))
     hist = {"train_loss": losses, "val_rmse": rmse.tolist(), "val_rmse_mean_predictor": base.tolist(),
-            "train_s": train_s, "steps": step, "start_step": ws.step}
+            "train_s": train_s, "steps": step, "start_step": ws.step.tolist()}
     return ws, hist
 
 
@@ -235,7 +236,7 @@ def fit_warm(b: plk.Batch, freqs, features, ws: WarmStart, ftol: float = 1e-4, x
     l_def = b.eval_gtr(freqs, x_def)
     use = l_net >= l_def
     x0 = np.where(use[:, None], x_net, x_def)
-    step = np.where(use, ws.step, DEFAULT_STEP)
+    step = np.where(use[:, None], ws.step[None, :], DEFAULT_STEP)
     fit = b.fit_gtr(freqs, x0, step, ftol, xtol, max_evals, target=target, target_tol=target_tol)
     fit.evals = fit.evals + 2
     fit.rounds += 2
