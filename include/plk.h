@@ -97,6 +97,17 @@ int plk_api_version(void);
 plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states,
                              const uint32_t* masks);
 
+/* Site patterns (off by default, as the reference evaluates every site; its
+ * unfinished MLtree.h declares n_patterns / char_per_pattern for this).  On:
+ * the next plk_set_alignment keeps one column per distinct site pattern and
+ * its count; the kernels evaluate patterns, plk_loglik sums pattern lnL x
+ * count (compensated), plk_site_loglik and plk_node_states still return every
+ * input site.  Changing the setting drops the current alignment. */
+plk_status plk_set_patterns(plk_handle* h, int on);
+/* Columns the kernels evaluate: the distinct patterns, or n_sites when off;
+ * 0 before an alignment. */
+int plk_n_patterns(const plk_handle* h);
+
 /* Tree topology and raw branch lengths (see the conventions above). */
 plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* right,
                         const double* branch_length);
@@ -230,8 +241,9 @@ plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid
  * substitution types A<->G, A<->C, A<->T, G<->C, G<->T, C<->T (6), histogram of
  * per-site collision entropy -ln(sum_s c_s (c_s - 1) / (m (m - 1))) (c_s the
  * counts of m unambiguous taxa) in 32 bins over [0, ln 4] (32), mean
- * p-distance (1).  Every statistic is a pairwise one, so none drifts with the
- * number of taxa. */
+ * p-distance (1).  Every statistic is a pairwise one, taken over at most 32
+ * taxa (rows floor(q n / 32), q < 32), so none drifts with the number of
+ * taxa. */
 plk_status plk_batch_features(plk_batch* b, float* out);
 /* Maximum-likelihood fits of every item at once: one Nelder-Mead per item
  * (the parameterisation of plk_fit_gtr: log exchangeabilities relative to the

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "plk_internal.h"
@@ -64,6 +65,13 @@ struct plk_handle {
     int n_codes = 0;
     std::vector<uint32_t> code_mask;
     DevBuf d_codes, d_code_mask;
+    // site patterns (plk_set_patterns): the kernels see n_sites = the number
+    // of distinct columns; site_pattern maps every input site to its column
+    bool patterns = false;
+    int n_sites_full = 0;
+    std::vector<int> site_pattern;
+    std::vector<double> pattern_w;
+    DevBuf d_pattern_w;
     // tree
     bool have_tree = false;
     int n_nodes = 0, tree_tips = 0, root = -1;
@@ -389,11 +397,64 @@ void plk_destroy(plk_handle* h) {
     delete h;
 }
 
+plk_status plk_set_patterns(plk_handle* h, int on) {
+    if (!h) return PLK_ERR_ARG;
+    if ((on != 0) != h->patterns) {
+        h->patterns = on != 0;
+        h->have_aln = false;  // the next plk_set_alignment applies the choice
+        h->have_lnl = false;
+    }
+    return PLK_OK;
+}
+
+int plk_n_patterns(const plk_handle* h) { return h && h->have_aln ? h->n_sites : 0; }
+
 plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states, const uint32_t* masks) {
     if (!h) return PLK_ERR_ARG;
     if (n_tips < 1 || n_sites < 1 || n_states < 1 || n_states > kMaxStates || !masks)
         return fail(h, PLK_ERR_ARG, "alignment needs n_tips >= 1, n_sites >= 1, 1 <= n_states <= 24");
     PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    h->n_sites_full = n_sites;
+    h->site_pattern.clear();
+    h->pattern_w.clear();
+    std::vector<uint32_t> pmasks;
+    if (h->patterns) {
+        // distinct columns in order of first appearance, with their counts
+        const uint32_t keep = (n_states >= 32) ? 0xffffffffu : ((1u << n_states) - 1u);
+        std::unordered_map<uint64_t, std::vector<int>> buckets;
+        std::vector<int> first;  // first site of every pattern
+        h->site_pattern.resize(n_sites);
+        for (int s = 0; s < n_sites; ++s) {
+            uint64_t hash = 1469598103934665603ull;  // FNV-1a over the column
+            for (int t = 0; t < n_tips; ++t) {
+                hash ^= (uint64_t)(masks[(size_t)t * n_sites + s] & keep);
+                hash *= 1099511628211ull;
+            }
+            std::vector<int>& cand = buckets[hash];
+            int found = -1;
+            for (int p : cand) {
+                const int f = first[p];
+                int t = 0;
+                while (t < n_tips && (masks[(size_t)t * n_sites + f] & keep) == (masks[(size_t)t * n_sites + s] & keep)) ++t;
+                if (t == n_tips) { found = p; break; }
+            }
+            if (found < 0) {
+                found = (int)first.size();
+                first.push_back(s);
+                cand.push_back(found);
+                h->pattern_w.push_back(0.0);
+            }
+            h->site_pattern[s] = found;
+            h->pattern_w[found] += 1.0;
+        }
+        const int n_pat = (int)first.size();
+        pmasks.resize((size_t)n_tips * n_pat);
+        for (int t = 0; t < n_tips; ++t)
+            for (int p = 0; p < n_pat; ++p) pmasks[(size_t)t * n_pat + p] = masks[(size_t)t * n_sites + first[p]];
+        PLK_CUDA(h, upload(h->d_pattern_w, h->pattern_w, h->stream), "upload pattern weights");
+        masks = pmasks.data();
+        n_sites = n_pat;
+    }
     const uint32_t all = (n_states >= 32) ? 0xffffffffu : ((1u << n_states) - 1u);
     const size_t n_cells = (size_t)n_tips * n_sites;
     std::vector<uint32_t> table;
@@ -574,6 +635,10 @@ plk_status plk_loglik_async(plk_handle* h, int precision) {
     if ((s = build_pmats(h)) != PLK_OK) return s;
     if (ev) PLK_CUDA(h, cudaEventRecord(ev->e[1], h->stream), "cudaEventRecord");
     if ((s = run_prune(h, precision, nullptr, ev ? &ev->e[2] : nullptr)) != PLK_OK) return s;
+    if (h->patterns)  // every pattern's lnL counts once per site showing it
+        PLK_CUDA(h, launch_weighted_sum(h->d_site_lnl.as<double>(), h->d_pattern_w.as<double>(), h->n_sites,
+                                        h->d_lnl.as<double>(), h->stream),
+                 "weighted sum kernel launch");
     if (ev) PLK_CUDA(h, cudaEventRecord(ev->e[3], h->stream), "cudaEventRecord");
     h->lnl_pending = true;
     return PLK_OK;
@@ -642,8 +707,17 @@ plk_status plk_site_loglik(plk_handle* h, double* out) {
     if (!out) return fail(h, PLK_ERR_ARG, "out is NULL");
     if (!h->have_lnl) return fail(h, PLK_ERR_STATE, "no likelihood computed yet (plk_loglik)");
     PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    PLK_CUDA(h, cudaMemcpyAsync(out, h->d_site_lnl.p, sizeof(double) * h->n_sites, cudaMemcpyDeviceToHost, h->stream), "copy site lnL");
+    if (!h->patterns) {
+        PLK_CUDA(h, cudaMemcpyAsync(out, h->d_site_lnl.p, sizeof(double) * h->n_sites, cudaMemcpyDeviceToHost, h->stream),
+                 "copy site lnL");
+        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "copy site lnL");
+        return PLK_OK;
+    }
+    std::vector<double> per_pattern(h->n_sites);
+    PLK_CUDA(h, cudaMemcpyAsync(per_pattern.data(), h->d_site_lnl.p, sizeof(double) * h->n_sites,
+                                cudaMemcpyDeviceToHost, h->stream), "copy site lnL");
     PLK_CUDA(h, cudaStreamSynchronize(h->stream), "copy site lnL");
+    for (int s = 0; s < h->n_sites_full; ++s) out[s] = per_pattern[h->site_pattern[s]];
     return PLK_OK;
 }
 
@@ -681,8 +755,22 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
         p.cond = cond; p.outside = h->d_outside.p; p.out = h->d_nodes_out.as<double>();
         PLK_CUDA(h, launch_preorder(p, precision, h->stream), "pre-order kernel launch");
     }
-    PLK_CUDA(h, cudaMemcpyAsync(out, h->d_nodes_out.p, out_n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy node states");
-    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "node-state kernels");
+    if (!h->patterns) {
+        PLK_CUDA(h, cudaMemcpyAsync(out, h->d_nodes_out.p, out_n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+                 "copy node states");
+        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "node-state kernels");
+    } else {
+        // [rank][pattern][S] on the device -> [rank][site][S] for the caller
+        std::vector<double> per_pattern(out_n);
+        PLK_CUDA(h, cudaMemcpyAsync(per_pattern.data(), h->d_nodes_out.p, out_n * sizeof(double),
+                                    cudaMemcpyDeviceToHost, h->stream), "copy node states");
+        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "node-state kernels");
+        const size_t S = (size_t)h->S;
+        for (int r = 0; r < n_int; ++r)
+            for (int s = 0; s < h->n_sites_full; ++s)
+                std::copy_n(&per_pattern[((size_t)r * h->n_sites + h->site_pattern[s]) * S], S,
+                            out + ((size_t)r * h->n_sites_full + s) * S);
+    }
     h->have_lnl = true;
     return PLK_OK;
 }

@@ -7,6 +7,9 @@
 //   [10, 42)  histogram of per-site collision (order-2 Renyi) entropy in 32
 //             bins over [0, ln 4]
 //   42        mean pairwise p-distance
+// Statistics are taken over at most 32 taxa, rows floor(q n / 32) for
+// q < 32, so that a network trained on 32-taxon alignments sees the same
+// sampling spread on larger ones.
 // Per site only the four state counts c_s of the unambiguous tips matter:
 // pairs of type (a, b) number c_a c_b and identical pairs c_a (c_a - 1) / 2,
 // so no pair loop is needed.  One CTA per item, sums in FP64.  No counterpart
@@ -20,6 +23,7 @@ using namespace dev;
 namespace {
 
 constexpr int kFeatThreads = 256;
+constexpr int kFeatureTaxa = 32;  // taxa the statistics are taken over
 
 __global__ void __launch_bounds__(kFeatThreads) features_kernel(BatchDev b, float* out) {
     const int item = blockIdx.x;
@@ -28,9 +32,13 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(BatchDev b, floa
     // per thread: base counts (4), type pairs (6), same pairs, all pairs, hist (32), sites
     double acc[4 + 6 + 2 + 32];
     for (int q = 0; q < 44; ++q) acc[q] = 0.0;
+    // a fixed number of taxa, evenly spread over the rows, so that alignments
+    // of any size present statistics with the same sampling spread
+    const int m_taxa = it.n_tips < kFeatureTaxa ? it.n_tips : kFeatureTaxa;
     for (int site = threadIdx.x; site < it.n_sites; site += blockDim.x) {
         int c[4] = {0, 0, 0, 0};
-        for (int t = 0; t < it.n_tips; ++t) {
+        for (int q = 0; q < m_taxa; ++q) {
+            const int t = (int)(((long long)q * it.n_tips) / m_taxa);
             const int code = codes[(size_t)t * it.site_stride + site];
             // unambiguous: exactly one of the four bits
             if (code == 1) ++c[0];

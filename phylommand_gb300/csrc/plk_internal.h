@@ -183,6 +183,8 @@ cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStrea
 cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, int* n_blocks,
                          cudaStream_t st);
 cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cudaStream_t st);
+// *out = compensated sum_i w[i] x[i] (one CTA)
+cudaError_t launch_weighted_sum(const double* x, const double* w, int n, double* out, cudaStream_t st);
 // codes[t * stride + s] = masks[t * n_sites + s] & all (alphabets of <= 4
 // states), padding bytes 0; *bad |= 1 if a cell allows no state.
 cudaError_t launch_encode_small(const uint32_t* masks, int n_tips, int n_sites, int stride, uint32_t all,

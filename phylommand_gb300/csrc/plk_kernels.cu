@@ -629,6 +629,28 @@ cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cu
     return cudaGetLastError();
 }
 
+// sum_i w_i x_i with TwoSum compensation in one CTA (site patterns: x = the
+// pattern lnL, w = its number of sites)
+__global__ void __launch_bounds__(1024) weighted_sum_kernel(const double* __restrict__ x,
+                                                            const double* __restrict__ w, int n, double* out) {
+    double s = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double p = w[i] * x[i];
+        const double pe = fma(w[i], x[i], -p);  // exact rounding error of the product
+        double ns, e;
+        two_sum(s, p, ns, e);
+        s = ns;
+        c = c + e + pe;
+    }
+    block_sum_pair(s, c);
+    if (threadIdx.x == 0) *out = s + c;
+}
+
+cudaError_t launch_weighted_sum(const double* x, const double* w, int n, double* out, cudaStream_t st) {
+    weighted_sum_kernel<<<1, 1024, 0, st>>>(x, w, n, out);
+    return cudaGetLastError();
+}
+
 // =========================================================================
 // Node-state outputs
 // =========================================================================

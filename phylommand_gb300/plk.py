@@ -40,7 +40,7 @@ EXPORTS = [
     "plk_loglik", "plk_site_loglik", "plk_node_states", "plk_n_internal",
     "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
-    "plk_sum_sites_noalloc", "plk_prune_variant",
+    "plk_sum_sites_noalloc", "plk_prune_variant", "plk_set_patterns", "plk_n_patterns",
     "plk_fit_gtr", "plk_fit_n_params",
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
@@ -100,6 +100,8 @@ def lib() -> ctypes.CDLL:
     L.plk_set_profiling.argtypes = [hp, c_int]
     L.plk_kernel_times.argtypes = [hp, dp, ip, c_int]
     L.plk_prune_variant.argtypes = [hp]
+    L.plk_set_patterns.argtypes = [hp, c_int]
+    L.plk_n_patterns.argtypes = [hp]
     L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
     L.plk_fit_gtr.argtypes = [hp, c_int, dp, c_int, dp, c_double, c_double, c_double, c_int, dp, dp, ip]
     L.plk_fit_n_params.argtypes = [c_int, c_int]
@@ -255,6 +257,15 @@ class Handle:
     @property
     def raw(self):
         return self._h
+
+    def set_patterns(self, on: bool) -> None:
+        """Evaluate distinct site patterns once, weighted by their counts
+        (takes effect at the next set_alignment)."""
+        _check(lib().plk_set_patterns(self._h, int(bool(on))), self._h)
+
+    @property
+    def n_patterns(self) -> int:
+        return int(lib().plk_n_patterns(self._h))
 
     def set_alignment(self, masks: np.ndarray, n_states: int) -> None:
         m = np.ascontiguousarray(masks, dtype=np.uint32)

@@ -260,3 +260,35 @@ def test_protein_autotuned_full_size():
                    p_mode=O.P_EXACT, threads=8)
     with _engine(w.left, w.right, w.bl, w.masks, 20, w.Q, w.freqs, w.cat_rates, w.cat_weights) as h:
         assert h.loglik(plk.PLK_FP32S) == pytest.approx(orc.lnl, rel=FP32_REL)
+
+
+@pytest.mark.parametrize("S,n_tips,n_sites,C", [(4, 24, 3000, 4), (20, 12, 700, 2), (4, 5, 1, 1)])
+def test_site_patterns(S, n_tips, n_sites, C):
+    """Pattern mode against plain mode on an alignment with many repeated
+    columns: the same total (compensated weighted sum), the same per-site
+    values and node states for every input site, fewer evaluated columns."""
+    rng = np.random.default_rng(S * 100 + n_tips)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, S=S, C=C)
+    # few distinct columns: draw every column from a small pool
+    pool = masks[:, : max(1, n_sites // 30)]
+    masks = np.ascontiguousarray(pool[:, rng.integers(0, pool.shape[1], n_sites)])
+    teff = plk.effective_lengths(left, right, bl, False)
+    orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
+    res = {}
+    for on in (False, True):
+        h = plk.Handle()
+        h.set_patterns(on)
+        h.set_alignment(masks, S)
+        h.set_tree(left, right, bl)
+        h.set_rate_model(False)
+        h.set_model(Q, f, True, cr, cw, plk.PLK_P_EXACT)
+        res[on] = (h.loglik(plk.PLK_FP64), h.site_loglik(), h.loglik(plk.PLK_FP32S), h.site_loglik(),
+                   h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64), h.n_patterns)
+        h.close()
+    assert res[False][5] == n_sites
+    assert res[True][5] == len({tuple(c) for c in masks.T})
+    assert res[True][0] == pytest.approx(orc.lnl, rel=1e-12)
+    assert res[True][0] == pytest.approx(res[False][0], rel=1e-13)
+    assert res[True][2] == pytest.approx(orc.lnl, rel=FP32_REL)
+    for i in (1, 3, 4):
+        np.testing.assert_array_equal(res[True][i], res[False][i])
