@@ -290,5 +290,8 @@ def test_site_patterns(S, n_tips, n_sites, C):
     assert res[True][0] == pytest.approx(orc.lnl, rel=1e-12)
     assert res[True][0] == pytest.approx(res[False][0], rel=1e-13)
     assert res[True][2] == pytest.approx(orc.lnl, rel=FP32_REL)
-    for i in (1, 3, 4):
-        np.testing.assert_array_equal(res[True][i], res[False][i])
+    # FP64: the same operations per column, so the same bits
+    np.testing.assert_array_equal(res[True][1], res[False][1])
+    np.testing.assert_array_equal(res[True][4], res[False][4])
+    # FP32: the autotuner may pick another 20-state form for the other column count
+    np.testing.assert_allclose(res[True][3], res[False][3], rtol=1e-6)
