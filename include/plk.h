@@ -192,6 +192,9 @@ plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_
                        double step, double ftol, double xtol, int max_evals, double* x_out,
                        double* lnl_out, int* n_evals_out);
 int plk_fit_n_params(int n_states, int n_cats);
+/* Optimiser of plk_fit_gtr on this handle: PLK_FIT_NELDER_MEAD (default) or
+ * PLK_FIT_QUASI_NEWTON (defined with the batch fit below). */
+plk_status plk_set_fit_method(plk_handle* h, int method);
 
 /* ---- batches: many alignments, trees and models in one launch -------------------
  * The reference scores one tree per simpleML object in treeator's loop over
@@ -262,6 +265,15 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
                              double ftol, double xtol, int max_evals, double* x_out, double* lnl_out,
                              int* evals_out, int* rounds_out, const double* target_lnl,
                              double target_tol, int* hit_evals_out);
+/* Optimiser of plk_batch_fit_gtr (and, with plk_set_fit_method, of
+ * plk_fit_gtr).  PLK_FIT_NELDER_MEAD (default) is the counterpart of the
+ * reference's NLopt LN_NELDERMEAD; PLK_FIT_QUASI_NEWTON is BFGS on
+ * central-difference gradients (2 n evaluations per gradient, the first
+ * inverse Hessian from their diagonal curvature), same stopping tolerances
+ * (or three iterations in a row improving lnL by at most ftol). */
+#define PLK_FIT_NELDER_MEAD 0
+#define PLK_FIT_QUASI_NEWTON 1
+plk_status plk_batch_set_fit_method(plk_batch* b, int method);
 /* lnL of every item at the GTR parameter vector x[n_items][n_params] (the
  * parameterisation of plk_batch_fit_gtr) in one batch evaluation; the items
  * keep these models.  -HUGE_VAL where a vector gives no valid model. */

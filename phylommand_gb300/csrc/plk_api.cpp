@@ -98,6 +98,7 @@ struct plk_handle {
     DevBuf d_mask_raw, d_flag;
     bool have_lnl = false;
     bool lnl_pending = false;
+    int fit_method = PLK_FIT_NELDER_MEAD;
     // autotuned 4-state FP32 kernel (-1: not tuned for the current inputs)
     int variant = -1;
     float tune_ms[3] = {0.f, 0.f, 0.f};
@@ -810,9 +811,8 @@ plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_
     for (int i = 0; i < S; ++i)
         if (!(freqs[i] > 0.0)) return fail(h, PLK_ERR_ARG, "frequencies must be positive");
     const int n = gtr_n_params(S, n_cats);
-    std::vector<double> start(n, 0.0);
+    std::vector<double> start(n, 0.0), steps(n, step);
     if (x0) std::copy(x0, x0 + n, start.begin());
-    NelderMead nm(n, start.data(), step, ftol, xtol, max_evals);
     std::vector<double> Q((size_t)S * S), cr(n_cats), cw(n_cats);
     auto set_x = [&](const double* x, bool* ok) -> plk_status {
         double scale = 1.0;
@@ -821,26 +821,41 @@ plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_
         for (int c = 0; c < n_cats; ++c) cr[c] *= scale;
         return plk_set_model(h, S, Q.data(), freqs, 1, n_cats, cr.data(), cw.data(), PLK_P_EXACT);
     };
-    while (!nm.done()) {
-        bool ok = false;
-        plk_status s = set_x(nm.point().data(), &ok);
-        if (s != PLK_OK) return s;
-        double f = HUGE_VAL;
-        if (ok) {
-            double l = 0.0;
-            s = plk_loglik(h, precision, &l);
-            if (s == PLK_OK) f = -l;
-            else if (s != PLK_ERR_NUMERIC) return s;
+    auto run = [&](auto& opt) -> plk_status {
+        while (!opt.done()) {
+            bool ok = false;
+            plk_status s = set_x(opt.point().data(), &ok);
+            if (s != PLK_OK) return s;
+            double f = HUGE_VAL;
+            if (ok) {
+                double l = 0.0;
+                s = plk_loglik(h, precision, &l);
+                if (s == PLK_OK) f = -l;
+                else if (s != PLK_ERR_NUMERIC) return s;
+            }
+            opt.tell(f);
         }
-        nm.tell(f);
+        const std::vector<double>& bx = opt.best_x();
+        std::copy(bx.begin(), bx.end(), x_out);
+        bool ok = false;
+        plk_status s = set_x(bx.data(), &ok);
+        if (s != PLK_OK) return s;
+        *lnl_out = -opt.best_f();
+        if (n_evals_out) *n_evals_out = opt.evals();
+        return PLK_OK;
+    };
+    if (h->fit_method == PLK_FIT_QUASI_NEWTON) {
+        QuasiNewton qn(n, start.data(), steps.data(), ftol, xtol, max_evals);
+        return run(qn);
     }
-    const std::vector<double>& bx = nm.best_x();
-    std::copy(bx.begin(), bx.end(), x_out);
-    bool ok = false;
-    plk_status s = set_x(bx.data(), &ok);
-    if (s != PLK_OK) return s;
-    *lnl_out = -nm.best_f();
-    if (n_evals_out) *n_evals_out = nm.evals();
+    NelderMead nm(n, start.data(), steps.data(), ftol, xtol, max_evals);
+    return run(nm);
+}
+
+plk_status plk_set_fit_method(plk_handle* h, int method) {
+    if (!h) return PLK_ERR_ARG;
+    if (method != PLK_FIT_NELDER_MEAD && method != PLK_FIT_QUASI_NEWTON) return fail(h, PLK_ERR_ARG, "unknown fit method");
+    h->fit_method = method;
     return PLK_OK;
 }
 

@@ -93,6 +93,8 @@ struct plk_batch {
     size_t smem = 0;
     double tuned_ms = 0.0;
     bool tuned = false;
+    // optimiser of plk_batch_fit_gtr
+    int fit_method = PLK_FIT_NELDER_MEAD;
     // graph
     cudaGraphExec_t exec = nullptr;
     bool use_graph = true;
@@ -667,6 +669,67 @@ plk_status set_gtr_models(plk_batch* b, const double* freqs, PointFn point, std:
     return PLK_OK;
 }
 
+struct FitOut {
+    double* x;
+    double* lnl;
+    int* evals;
+    int* rounds;
+    const double* target;
+    double target_tol;
+    int* hits;
+};
+
+// Advances every item's optimiser (NelderMead or QuasiNewton) in lockstep:
+// each round sets the model of the point every unfinished fit asks for and
+// evaluates the whole batch once.
+template <class Opt>
+plk_status run_fits(plk_batch* b, const double* freqs, std::vector<Opt>& opts, const FitOut& out) {
+    const int n_items = (int)b->items.size();
+    const int C = b->C;
+    const int np = gtr_n_params(4, C);
+    std::vector<char> in_domain(n_items, 1);
+    std::vector<double> lnl(n_items);
+    // every item needs a model before the first evaluation
+    for (int i = 0; i < n_items; ++i)
+        if (!b->items[i].has_model) {
+            std::vector<double> Q(16), cr(C), cw(C);
+            double scale = 1.0;
+            std::vector<double> zero(np, 0.0);
+            gtr_model_from_x(4, zero.data(), C, freqs + (size_t)i * 4, Q.data(), cr.data(), cw.data(), &scale);
+            plk_status s = plk_batch_set_model(b, i, Q.data(), freqs + (size_t)i * 4, cr.data(), cw.data());
+            if (s != PLK_OK) return s;
+        }
+    int rounds = 0;
+    std::vector<int> hit(n_items, -1);
+    for (;;) {
+        bool any = false;
+        for (const auto& o : opts) any = any || !o.done();
+        if (!any) break;
+        plk_status s = set_gtr_models(
+            b, freqs, [&](int i) { return opts[i].done() ? nullptr : opts[i].point().data(); }, in_domain);
+        if (s != PLK_OK) return s;
+        s = plk_batch_loglik(b, lnl.data());
+        if (s != PLK_OK && s != PLK_ERR_NUMERIC) return s;
+        ++rounds;
+        for (int i = 0; i < n_items; ++i) {
+            if (opts[i].done()) continue;
+            const bool ok = in_domain[i] && std::isfinite(lnl[i]);
+            opts[i].tell(ok ? -lnl[i] : HUGE_VAL);
+            // first evaluation that comes within target_tol of the target
+            if (out.target && hit[i] < 0 && ok && lnl[i] >= out.target[i] - out.target_tol) hit[i] = opts[i].evals();
+        }
+    }
+    if (out.hits) std::copy(hit.begin(), hit.end(), out.hits);
+    for (int i = 0; i < n_items; ++i) {
+        const std::vector<double>& bx = opts[i].best_x();
+        std::copy(bx.begin(), bx.end(), out.x + (size_t)i * np);
+        out.lnl[i] = -opts[i].best_f();
+        if (out.evals) out.evals[i] = opts[i].evals();
+    }
+    if (out.rounds) *out.rounds = rounds;
+    return PLK_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -696,61 +759,30 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
         return b ? bfail(b, PLK_ERR_ARG, "bad arguments to plk_batch_fit_gtr") : PLK_ERR_ARG;
     const int n_items = (int)b->items.size();
     if (n_items == 0) return bfail(b, PLK_ERR_STATE, "batch is empty");
-    const int C = b->C;
-    const int np = gtr_n_params(4, C);
-    std::vector<NelderMead> nms;
-    nms.reserve(n_items);
-    for (int i = 0; i < n_items; ++i) {
-        std::vector<double> start(np, 0.0);
-        if (x0) std::copy(x0 + (size_t)i * np, x0 + (size_t)(i + 1) * np, start.begin());
-        std::vector<double> steps(np, 0.5);
-        if (step) std::copy(step + (size_t)i * np, step + (size_t)(i + 1) * np, steps.begin());
-        nms.emplace_back(np, start.data(), steps.data(), ftol, xtol, max_evals);
+    const int np = gtr_n_params(4, b->C);
+    std::vector<double> starts((size_t)n_items * np, 0.0), steps((size_t)n_items * np, 0.5);
+    if (x0) std::copy(x0, x0 + (size_t)n_items * np, starts.begin());
+    if (step) std::copy(step, step + (size_t)n_items * np, steps.begin());
+    FitOut out{x_out, lnl_out, evals_out, rounds_out, target_lnl, target_tol, hit_evals_out};
+    if (b->fit_method == PLK_FIT_QUASI_NEWTON) {
+        std::vector<QuasiNewton> opts;
+        opts.reserve(n_items);
+        for (int i = 0; i < n_items; ++i)
+            opts.emplace_back(np, &starts[(size_t)i * np], &steps[(size_t)i * np], ftol, xtol, max_evals);
+        return run_fits(b, freqs, opts, out);
     }
-    std::vector<char> in_domain(n_items, 1);
-    std::vector<double> lnl(n_items);
-    // the models of the points every unfinished fit asks for
-    auto set_points = [&]() -> plk_status {
-        return set_gtr_models(
-            b, freqs, [&](int i) { return nms[i].done() ? nullptr : nms[i].point().data(); }, in_domain);
-    };
-    // every item needs a model before the first evaluation
+    std::vector<NelderMead> opts;
+    opts.reserve(n_items);
     for (int i = 0; i < n_items; ++i)
-        if (!b->items[i].has_model) {
-            std::vector<double> Q(16), cr(C), cw(C);
-            double scale = 1.0;
-            std::vector<double> zero(np, 0.0);
-            gtr_model_from_x(4, zero.data(), C, freqs + (size_t)i * 4, Q.data(), cr.data(), cw.data(), &scale);
-            plk_status s = plk_batch_set_model(b, i, Q.data(), freqs + (size_t)i * 4, cr.data(), cw.data());
-            if (s != PLK_OK) return s;
-        }
-    int rounds = 0;
-    std::vector<int> hit(n_items, -1);
-    for (;;) {
-        bool any = false;
-        for (const auto& nm : nms) any = any || !nm.done();
-        if (!any) break;
-        plk_status s = set_points();
-        if (s != PLK_OK) return s;
-        s = plk_batch_loglik(b, lnl.data());
-        if (s != PLK_OK && s != PLK_ERR_NUMERIC) return s;
-        ++rounds;
-        for (int i = 0; i < n_items; ++i) {
-            if (nms[i].done()) continue;
-            const bool ok = in_domain[i] && std::isfinite(lnl[i]);
-            nms[i].tell(ok ? -lnl[i] : HUGE_VAL);
-            // first evaluation that comes within target_tol of the target
-            if (target_lnl && hit[i] < 0 && ok && lnl[i] >= target_lnl[i] - target_tol) hit[i] = nms[i].evals();
-        }
-    }
-    if (hit_evals_out) std::copy(hit.begin(), hit.end(), hit_evals_out);
-    for (int i = 0; i < n_items; ++i) {
-        const std::vector<double>& bx = nms[i].best_x();
-        std::copy(bx.begin(), bx.end(), x_out + (size_t)i * np);
-        lnl_out[i] = -nms[i].best_f();
-        if (evals_out) evals_out[i] = nms[i].evals();
-    }
-    if (rounds_out) *rounds_out = rounds;
+        opts.emplace_back(np, &starts[(size_t)i * np], &steps[(size_t)i * np], ftol, xtol, max_evals);
+    return run_fits(b, freqs, opts, out);
+}
+
+plk_status plk_batch_set_fit_method(plk_batch* b, int method) {
+    if (!b) return PLK_ERR_ARG;
+    if (method != PLK_FIT_NELDER_MEAD && method != PLK_FIT_QUASI_NEWTON)
+        return bfail(b, PLK_ERR_ARG, "unknown fit method");
+    b->fit_method = method;
     return PLK_OK;
 }
 

@@ -135,6 +135,170 @@ const std::vector<double>& NelderMead::best_x() const {
 
 double NelderMead::best_f() const { return *std::min_element(fvals_.begin(), fvals_.end()); }
 
+// ---------------------------------------------------------------------------
+// Quasi-Newton (BFGS, Nocedal & Wright 2006, ch. 6) on central-difference
+// gradients.  The first inverse Hessian is the inverse of the diagonal
+// curvature the central differences give for free, so the first step is a
+// diagonal Newton step; later ones use the BFGS update of the inverse
+// Hessian.  Steps are capped at 1 in the max norm; the line search halves the
+// step (quadratic interpolation, within [0.1, 0.5] of the last trial) until
+// the Armijo condition holds.
+// ---------------------------------------------------------------------------
+QuasiNewton::QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals)
+    : n_(n), ftol_(ftol_abs), xtol_(xtol), h_(1e-3), max_evals_(max_evals) {
+    x_.assign(x0, x0 + n);
+    max_step_.assign(steps, steps + n);
+    point_ = x_;
+    g_.assign(n, 0.0);
+    fplus_.assign(n, 0.0);
+    dir_.assign(n, 0.0);
+    H_.assign((size_t)n * n, 0.0);
+}
+
+void QuasiNewton::start_gradient() {
+    gi_ = 0;
+    next_grad_point();
+    state_ = State::Grad;
+}
+
+// evaluation k of a gradient: coordinate k / 2, +h for even k, -h for odd k
+void QuasiNewton::next_grad_point() {
+    point_ = x_;
+    point_[gi_ / 2] += (gi_ % 2 == 0) ? h_ : -h_;
+}
+
+void QuasiNewton::finish_gradient() {
+    if (have_prev_) {
+        std::vector<double> s(n_), y(n_), Hy(n_, 0.0);
+        double sy = 0.0, ss = 0.0, yy = 0.0;
+        for (int i = 0; i < n_; ++i) {
+            s[i] = x_[i] - x_prev_[i];
+            y[i] = g_[i] - g_prev_[i];
+            sy += s[i] * y[i];
+            ss += s[i] * s[i];
+            yy += y[i] * y[i];
+        }
+        if (sy > 1e-12 * std::sqrt(ss * yy)) {
+            const double rho = 1.0 / sy;
+            double yHy = 0.0;
+            for (int i = 0; i < n_; ++i) {
+                for (int j = 0; j < n_; ++j) Hy[i] += H_[(size_t)i * n_ + j] * y[j];
+                yHy += y[i] * Hy[i];
+            }
+            for (int i = 0; i < n_; ++i)
+                for (int j = 0; j < n_; ++j)
+                    H_[(size_t)i * n_ + j] += -rho * (s[i] * Hy[j] + Hy[i] * s[j]) + (rho * rho * yHy + rho) * s[i] * s[j];
+        }
+    }
+    start_line();
+}
+
+void QuasiNewton::start_line() {
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        double m = 0.0;
+        slope_ = 0.0;
+        for (int i = 0; i < n_; ++i) {
+            double d = 0.0;
+            for (int j = 0; j < n_; ++j) d -= H_[(size_t)i * n_ + j] * g_[j];
+            dir_[i] = d;
+            m = std::max(m, std::fabs(d));
+        }
+        if (m > 1.0)
+            for (double& d : dir_) d /= m;
+        for (int i = 0; i < n_; ++i) slope_ += g_[i] * dir_[i];
+        if (slope_ < 0.0) break;
+        // not a descent direction: fall back to the steepest descent scaled by
+        // the initial steps
+        std::fill(H_.begin(), H_.end(), 0.0);
+        const double gn = std::sqrt(std::inner_product(g_.begin(), g_.end(), g_.begin(), 0.0));
+        for (int i = 0; i < n_; ++i) H_[(size_t)i * n_ + i] = max_step_[i] / std::max(gn, 1e-300);
+    }
+    if (!(slope_ < 0.0)) {
+        state_ = State::Done;
+        return;
+    }
+    t_ = 1.0;
+    backtracks_ = 0;
+    for (int i = 0; i < n_; ++i) point_[i] = x_[i] + t_ * dir_[i];
+    state_ = State::Line;
+}
+
+void QuasiNewton::tell(double f) {
+    if (state_ == State::Done) return;
+    if (!std::isfinite(f)) f = HUGE_VAL;
+    ++evals_;
+    switch (state_) {
+        case State::Start:
+            f_ = f;
+            if (!std::isfinite(f_)) { state_ = State::Done; return; }
+            start_gradient();
+            break;
+        case State::Grad: {
+            const int k = gi_ / 2;
+            if (gi_ % 2 == 0) {
+                fplus_[k] = f;
+            } else {
+                const double fp = fplus_[k], fm = f;
+                double curv = 0.0;
+                if (std::isfinite(fp) && std::isfinite(fm)) {
+                    g_[k] = (fp - fm) / (2.0 * h_);
+                    curv = (fp - 2.0 * f_ + fm) / (h_ * h_);
+                } else if (std::isfinite(fp)) {
+                    g_[k] = (fp - f_) / h_;
+                } else if (std::isfinite(fm)) {
+                    g_[k] = (f_ - fm) / h_;
+                } else {
+                    g_[k] = 0.0;
+                }
+                if (!have_prev_) {
+                    // first inverse Hessian: diagonal Newton where the curvature is positive
+                    H_[(size_t)k * n_ + k] = curv > 1e-12 ? 1.0 / curv : max_step_[k] / std::max(std::fabs(g_[k]), 1e-12);
+                }
+            }
+            if (++gi_ < 2 * n_) next_grad_point();
+            else finish_gradient();
+            break;
+        }
+        case State::Line:
+            if (f <= f_ + 1e-4 * t_ * slope_) {
+                double moved = 0.0;
+                for (int i = 0; i < n_; ++i) moved = std::max(moved, std::fabs(point_[i] - x_[i]));
+                x_prev_ = x_;
+                g_prev_ = g_;
+                f_prev_ = f_;
+                x_ = point_;
+                f_ = f;
+                have_prev_ = true;
+                ++iter_;
+                // converged: a small decrease with a small step, or three
+                // small decreases in a row (a flat direction)
+                flat_ = (f_prev_ - f_ <= ftol_) ? flat_ + 1 : 0;
+                if ((f_prev_ - f_ <= ftol_ && moved <= xtol_) || flat_ >= 3) {
+                    state_ = State::Done;
+                    return;
+                }
+                start_gradient();
+            } else {
+                if (++backtracks_ > 30) {
+                    state_ = State::Done;  // no decrease along a descent direction: at the noise floor
+                    return;
+                }
+                // minimiser of the quadratic through f_, slope_ and this trial
+                double tn = 0.5 * t_;
+                if (std::isfinite(f)) {
+                    const double denom = 2.0 * (f - f_ - slope_ * t_);
+                    if (denom > 0.0) tn = -slope_ * t_ * t_ / denom;
+                }
+                t_ = std::min(std::max(tn, 0.1 * t_), 0.5 * t_);
+                for (int i = 0; i < n_; ++i) point_[i] = x_[i] + t_ * dir_[i];
+            }
+            break;
+        case State::Done:
+            return;
+    }
+    if (evals_ >= max_evals_) state_ = State::Done;
+}
+
 // GTR(+Gamma) parameter vector of the fits:
 //   x[0 .. npos-2]   log exchangeabilities relative to the last one (fixed 1)
 //   x[npos-1]        log Gamma shape alpha (absent when n_cats == 1)

@@ -106,6 +106,38 @@ class NelderMead {
     std::vector<double> fvals_, point_, centroid_, xr_;
     double fr_ = 0.0;
 };
+// Quasi-Newton minimiser with central-difference gradients (BFGS update of
+// the inverse Hessian, first scaled by the central differences' diagonal
+// curvature; backtracking Armijo line search).  Same ask/tell interface as
+// NelderMead.  Stops when an iteration lowers f by at most ftol_abs and moves
+// every coordinate by at most xtol, after three iterations in a row that
+// lower f by at most ftol_abs, when the line search fails, or at max_evals.
+class QuasiNewton {
+  public:
+    QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals);
+    bool done() const { return state_ == State::Done; }
+    const std::vector<double>& point() const { return point_; }
+    void tell(double f);
+    const std::vector<double>& best_x() const { return x_; }
+    double best_f() const { return f_; }
+    int evals() const { return evals_; }
+
+  private:
+    enum class State { Start, Grad, Line, Done };
+    void start_gradient();
+    void next_grad_point();
+    void finish_gradient();
+    void start_line();
+    int n_;
+    double ftol_, xtol_, h_;
+    int max_evals_, evals_ = 0;
+    State state_ = State::Start;
+    std::vector<double> x_, g_, point_, fplus_, dir_, x_prev_, g_prev_, max_step_;
+    std::vector<double> H_;  // inverse Hessian, row-major
+    double f_ = HUGE_VAL, f_prev_ = HUGE_VAL, t_ = 1.0, slope_ = 0.0;
+    int gi_ = 0, backtracks_ = 0, iter_ = 0, flat_ = 0;
+    bool have_prev_ = false;
+};
 // GTR(+Gamma) parameters of the fits (see plk_fit.cpp); false outside the domain.
 bool gtr_model_from_x(int S, const double* x, int n_cats, const double* freqs, double* Q, double* cat_rates,
                       double* cat_weights, double* scale);

@@ -73,20 +73,19 @@ inline size_t tile_smem_min(int C, int spt, int n_ops, int n_tips, int max_depth
 template <int CM>
 __device__ __forceinline__ void stage_op(Stage<CM>* st, const Op& op, int C, const float* __restrict__ P,
                                          const float* __restrict__ tipT) {
+    // every child's tip table ([category][code]) or P rows ([category][row])
+    // is one contiguous run of 16-byte chunks in global and in the stage slot
     const int n0 = (op.s0 >= 0) ? C * kCodes : C * 4;
     const int n1 = (op.s1 == kSrcNone) ? 0 : ((op.s1 >= 0) ? C * kCodes : C * 4);
-    for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
-        const int c = i < n0 ? 0 : 1;
-        const int j = c ? i - n0 : i;
-        const int src = c ? op.s1 : op.s0;
-        const int e = c ? op.e1 : op.e0;
-        if (src >= 0) {
-            const int k = j / kCodes, code = j % kCodes;
-            cp_async16(&st->tip[c][k][code], tipT + (((size_t)src * C + k) * kCodes + code) * 4);
-        } else {
-            const int k = j >> 2, row = j & 3;
-            cp_async16(&st->p[c][k][row], P + ((size_t)e * C + k) * 16 + row * 4);
-        }
+    const float4* src0 = reinterpret_cast<const float4*>(op.s0 >= 0 ? tipT + (size_t)op.s0 * C * kCodes * 4
+                                                                    : P + (size_t)op.e0 * C * 16);
+    float4* dst0 = op.s0 >= 0 ? &st->tip[0][0][0] : &st->p[0][0][0];
+    for (int i = threadIdx.x; i < n0; i += blockDim.x) cp_async16(dst0 + i, src0 + i);
+    if (n1) {
+        const float4* src1 = reinterpret_cast<const float4*>(op.s1 >= 0 ? tipT + (size_t)op.s1 * C * kCodes * 4
+                                                                        : P + (size_t)op.e1 * C * 16);
+        float4* dst1 = op.s1 >= 0 ? &st->tip[1][0][0] : &st->p[1][0][0];
+        for (int i = threadIdx.x; i < n1; i += blockDim.x) cp_async16(dst1 + i, src1 + i);
     }
 }
 

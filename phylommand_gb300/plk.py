@@ -32,6 +32,8 @@ PLK_P_TAYLOR20 = 0
 PLK_P_EXACT = 1
 PLK_NODES_COND = 0
 PLK_NODES_MARGINAL = 1
+PLK_FIT_NELDER_MEAD = 0
+PLK_FIT_QUASI_NEWTON = 1
 
 # Every symbol include/plk.h declares (checked by the tests).
 EXPORTS = [
@@ -45,7 +47,8 @@ EXPORTS = [
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
     "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate", "plk_nni_moves_host",
-    "plk_batch_features", "plk_batch_fit_gtr", "plk_batch_eval_gtr",
+    "plk_batch_features", "plk_batch_fit_gtr", "plk_batch_eval_gtr", "plk_batch_set_fit_method",
+    "plk_set_fit_method",
     "plk_mlp_create", "plk_mlp_destroy", "plk_mlp_last_error", "plk_mlp_n_params", "plk_mlp_get_params",
     "plk_mlp_set_params", "plk_mlp_forward", "plk_mlp_gradients", "plk_mlp_train_step",
 ]
@@ -123,6 +126,8 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_features.argtypes = [hp, fp]
     L.plk_batch_fit_gtr.argtypes = [hp, dp, dp, dp, c_double, c_double, c_int, dp, dp, ip, ip, dp, c_double, ip]
     L.plk_batch_eval_gtr.argtypes = [hp, dp, dp, dp]
+    L.plk_batch_set_fit_method.argtypes = [hp, c_int]
+    L.plk_set_fit_method.argtypes = [hp, c_int]
     L.plk_mlp_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64]
     L.plk_mlp_destroy.argtypes = [hp]
     L.plk_mlp_destroy.restype = None
@@ -347,6 +352,10 @@ class Handle:
         _check(lib().plk_site_loglik(self._h, _p(out, ctypes.c_double)), self._h)
         return out
 
+    def set_fit_method(self, method: int) -> None:
+        """PLK_FIT_NELDER_MEAD (default) or PLK_FIT_QUASI_NEWTON for fit_gtr."""
+        _check(lib().plk_set_fit_method(self._h, int(method)), self._h)
+
     def fit_gtr(self, freqs, n_cats: int = 4, x0=None, precision: int = PLK_FP32S, step: float = 0.5,
                 ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 2000):
         """Nelder-Mead ML fit of GTR(+Gamma) exchangeabilities, Gamma shape and
@@ -480,6 +489,10 @@ class Batch:
                                             ctypes.byref(rounds), _p(tg, ctypes.c_double), float(target_tol),
                                             _p(hits, ctypes.c_int)))
         return BatchFit(x, lnl, ev, rounds.value, hits if tg is not None else None)
+
+    def set_fit_method(self, method: int) -> None:
+        """PLK_FIT_NELDER_MEAD (default) or PLK_FIT_QUASI_NEWTON for fit_gtr."""
+        self._check(lib().plk_batch_set_fit_method(self._b, int(method)))
 
     def eval_gtr(self, freqs, x) -> np.ndarray:
         """lnL of every item at its GTR parameter vector x[n_items, n_params]."""

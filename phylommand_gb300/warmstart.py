@@ -246,14 +246,17 @@ def fit_warm(b: plk.Batch, freqs, features, ws: WarmStart, ftol: float = 1e-4, x
 
 
 def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int = 5000, seed: int = 7,
-             ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 4000, tol: float = 1e-3) -> dict:
+             ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 4000, tol: float = 1e-3,
+             method: int = plk.PLK_FIT_NELDER_MEAD) -> dict:
     """Held-out comparison of the plain default-start fit and the warm fit on
-    the same simulated alignments.  Two evaluation counts per item: until
-    the stopping rule ends the fit, and until the fit first comes within
-    ``tol`` of the plain fit's final lnL (the plain fit's own count for the
-    latter is taken on a second identical run with that target)."""
+    the same simulated alignments, both with the optimiser ``method``.  Two
+    evaluation counts per item: until the stopping rule ends the fit, and
+    until the fit first comes within ``tol`` of the plain fit's final lnL (the
+    plain fit's own count for the latter is taken on a second identical run
+    with that target)."""
     b, truth = simulate_batch(n_items, n_taxa, n_sites, seed)
     try:
+        b.set_fit_method(method)
         feats = b.features()
         freqs = empirical_freqs(feats)
         b.eval_gtr(freqs, np.zeros((n_items, N_PARAMS)))  # tuning and graph capture outside the timings
@@ -273,6 +276,7 @@ def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int 
     pred = ws.predict(feats)
     return {
         "n_items": n_items, "n_taxa": n_taxa, "n_sites": n_sites, "seed": seed, "tol": tol,
+        "method": "quasi-newton" if method == plk.PLK_FIT_QUASI_NEWTON else "nelder-mead",
         "plain_evals_mean": float(plain.evals.mean()), "warm_evals_mean": float(warm.evals.mean()),
         "evals_ratio_warm_over_plain": float(warm.evals.mean() / plain.evals.mean()),
         "plain_evals_to_optimum_mean": float(plain_hit.mean()),
