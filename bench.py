@@ -60,10 +60,10 @@ def load_peaks():
     return FALLBACK_HBM_GBS, FALLBACK_BF16_TFLOPS, "fallback"
 
 
-def load_traffic():
-    """DRAM bytes per launch of the post-order kernel from the committed ncu
-    summary of this workload (None when no capture has been summarised)."""
-    p = os.path.join(ROOT, "profiles", "prune4s_kernel_dna_gtr_g4_128x100k.json")
+def load_traffic(kernel: str):
+    """DRAM bytes per launch of the named post-order kernel on this workload
+    from its committed ncu summary (None when none has been summarised)."""
+    p = os.path.join(ROOT, "profiles", f"{kernel.split()[0]}_dna_gtr_g4_128x100k.json")
     if os.path.exists(p):
         d = json.load(open(p))
         return d.get("dram_bytes_per_launch")
@@ -297,7 +297,7 @@ def run_ours(args, world, rank, local):
         "kernel_ms_per_eval": {"pmat": kern_ms[0] / max(n_evals, 1), "postorder": prune_ms,
                                "reduce": kern_ms[2] / max(n_evals, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": load_traffic(),
+                     "frac": achieved / hbm_peak, "traffic": load_traffic(h_variant),
                      "kernel": f"{h_variant} (post-order pass)",
                      "algorithmic_bytes_per_launch": bytes_per_launch, "peak_source": peak_src,
                      "note": "algorithmic bytes of a level-by-level pass; this kernel keeps partials on chip"},

@@ -268,9 +268,10 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
 /* Optimiser of plk_batch_fit_gtr (and, with plk_set_fit_method, of
  * plk_fit_gtr).  PLK_FIT_NELDER_MEAD (default) is the counterpart of the
  * reference's NLopt LN_NELDERMEAD; PLK_FIT_QUASI_NEWTON is BFGS on
- * central-difference gradients (2 n evaluations per gradient, the first
- * inverse Hessian from their diagonal curvature), same stopping tolerances
- * (or three iterations in a row improving lnL by at most ftol). */
+ * central-difference gradients (2 n evaluations per gradient; at the start a
+ * full finite-difference Hessian, n (n - 1) / 2 more, so the first step is a
+ * Newton step), same stopping tolerances (or three iterations in a row
+ * improving lnL by at most ftol). */
 #define PLK_FIT_NELDER_MEAD 0
 #define PLK_FIT_QUASI_NEWTON 1
 plk_status plk_batch_set_fit_method(plk_batch* b, int method);

@@ -137,12 +137,14 @@ double NelderMead::best_f() const { return *std::min_element(fvals_.begin(), fva
 
 // ---------------------------------------------------------------------------
 // Quasi-Newton (BFGS, Nocedal & Wright 2006, ch. 6) on central-difference
-// gradients.  The first inverse Hessian is the inverse of the diagonal
-// curvature the central differences give for free, so the first step is a
-// diagonal Newton step; later ones use the BFGS update of the inverse
-// Hessian.  Steps are capped at 1 in the max norm; the line search halves the
-// step (quadratic interpolation, within [0.1, 0.5] of the last trial) until
-// the Armijo condition holds.
+// gradients.  At the start point the full Hessian is taken by finite
+// differences (the diagonal comes free with the central differences, the
+// n (n - 1) / 2 off-diagonal terms from forward mixed differences), shifted
+// by a multiple of the identity until Cholesky succeeds, and inverted: the
+// first step is a Newton step.  Later iterations use the BFGS update of the
+// inverse Hessian.  Steps are capped at 1 in the max norm; the line search
+// shortens the step (quadratic interpolation, within [0.1, 0.5] of the last
+// trial) until the Armijo condition holds.
 // ---------------------------------------------------------------------------
 QuasiNewton::QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals)
     : n_(n), ftol_(ftol_abs), xtol_(xtol), h_(1e-3), max_evals_(max_evals) {
@@ -152,6 +154,7 @@ QuasiNewton::QuasiNewton(int n, const double* x0, const double* steps, double ft
     g_.assign(n, 0.0);
     fplus_.assign(n, 0.0);
     dir_.assign(n, 0.0);
+    curv_.assign(n, 0.0);
     H_.assign((size_t)n * n, 0.0);
 }
 
@@ -167,7 +170,83 @@ void QuasiNewton::next_grad_point() {
     point_[gi_ / 2] += (gi_ % 2 == 0) ? h_ : -h_;
 }
 
+void QuasiNewton::next_hess_point() {
+    point_ = x_;
+    point_[pairs_[hi_].first] += h_;
+    point_[pairs_[hi_].second] += h_;
+}
+
+// H = finite-difference Hessian at the start, made positive definite by a
+// growing multiple of the identity (Cholesky as the test), inverted into H_
+void QuasiNewton::finish_hessian() {
+    const int n = n_;
+    std::vector<double> A((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        const double c = curv_[i];
+        // no usable curvature: a step of about max_step_ along the gradient
+        A[(size_t)i * n + i] = (std::isfinite(c) && c > 1e-12) ? c : std::max(std::fabs(g_[i]), 1e-12) / max_step_[i];
+    }
+    for (size_t p = 0; p < pairs_.size(); ++p) {
+        const int i = pairs_[p].first, j = pairs_[p].second;
+        const double v = (hmix_[p] - fplus_[i] - fplus_[j] + f_) / (h_ * h_);
+        if (std::isfinite(v) && curv_[i] > 1e-12 && curv_[j] > 1e-12) A[(size_t)i * n + j] = A[(size_t)j * n + i] = v;
+    }
+    double dmax = 0.0;
+    for (int i = 0; i < n; ++i) dmax = std::max(dmax, A[(size_t)i * n + i]);
+    std::vector<double> Lc((size_t)n * n);
+    double mu = 0.0;
+    bool ok = false;
+    for (int attempt = 0; attempt < 30 && !ok; ++attempt) {
+        ok = true;
+        for (int i = 0; i < n && ok; ++i)
+            for (int j = 0; j <= i; ++j) {
+                double s = A[(size_t)i * n + j] + (i == j ? mu : 0.0);
+                for (int k = 0; k < j; ++k) s -= Lc[(size_t)i * n + k] * Lc[(size_t)j * n + k];
+                if (i == j) {
+                    if (!(s > 0.0)) { ok = false; break; }
+                    Lc[(size_t)i * n + i] = std::sqrt(s);
+                } else {
+                    Lc[(size_t)i * n + j] = s / Lc[(size_t)j * n + j];
+                }
+            }
+        if (!ok) mu = (mu == 0.0) ? 1e-6 * dmax : 10.0 * mu;
+    }
+    if (!ok) {
+        for (int i = 0; i < n; ++i) H_[(size_t)i * n + i] = 1.0 / A[(size_t)i * n + i];
+    } else {
+        // columns of the inverse: solve L L^T x = e_c
+        std::vector<double> y(n), x(n);
+        for (int c = 0; c < n; ++c) {
+            for (int i = 0; i < n; ++i) {
+                double s = (i == c) ? 1.0 : 0.0;
+                for (int k = 0; k < i; ++k) s -= Lc[(size_t)i * n + k] * y[k];
+                y[i] = s / Lc[(size_t)i * n + i];
+            }
+            for (int i = n - 1; i >= 0; --i) {
+                double s = y[i];
+                for (int k = i + 1; k < n; ++k) s -= Lc[(size_t)k * n + i] * x[k];
+                x[i] = s / Lc[(size_t)i * n + i];
+            }
+            for (int i = 0; i < n; ++i) H_[(size_t)i * n + c] = x[i];
+        }
+    }
+    start_line();
+}
+
 void QuasiNewton::finish_gradient() {
+    if (!have_prev_ && hmix_.empty() && n_ > 1) {
+        // first iterate: the mixed differences of the full Hessian
+        for (int i = 0; i < n_; ++i)
+            for (int j = i + 1; j < n_; ++j) pairs_.emplace_back(i, j);
+        hmix_.assign(pairs_.size(), HUGE_VAL);
+        hi_ = 0;
+        next_hess_point();
+        state_ = State::Hess;
+        return;
+    }
+    if (!have_prev_ && n_ == 1) {
+        H_[0] = curv_[0] > 1e-12 ? 1.0 / curv_[0] : max_step_[0] / std::max(std::fabs(g_[0]), 1e-12);
+    }
     if (have_prev_) {
         std::vector<double> s(n_), y(n_), Hy(n_, 0.0);
         double sy = 0.0, ss = 0.0, yy = 0.0;
@@ -250,15 +329,17 @@ void QuasiNewton::tell(double f) {
                 } else {
                     g_[k] = 0.0;
                 }
-                if (!have_prev_) {
-                    // first inverse Hessian: diagonal Newton where the curvature is positive
-                    H_[(size_t)k * n_ + k] = curv > 1e-12 ? 1.0 / curv : max_step_[k] / std::max(std::fabs(g_[k]), 1e-12);
-                }
+                if (!have_prev_) curv_[k] = curv;
             }
             if (++gi_ < 2 * n_) next_grad_point();
             else finish_gradient();
             break;
         }
+        case State::Hess:
+            hmix_[hi_] = f;
+            if (++hi_ < (int)pairs_.size()) next_hess_point();
+            else finish_hessian();
+            break;
         case State::Line:
             if (f <= f_ + 1e-4 * t_ * slope_) {
                 double moved = 0.0;

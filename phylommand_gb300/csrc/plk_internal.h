@@ -106,10 +106,11 @@ class NelderMead {
     std::vector<double> fvals_, point_, centroid_, xr_;
     double fr_ = 0.0;
 };
-// Quasi-Newton minimiser with central-difference gradients (BFGS update of
-// the inverse Hessian, first scaled by the central differences' diagonal
-// curvature; backtracking Armijo line search).  Same ask/tell interface as
-// NelderMead.  Stops when an iteration lowers f by at most ftol_abs and moves
+// Quasi-Newton minimiser with central-difference gradients: the first
+// inverse Hessian is the inverse of a finite-difference Hessian at the start
+// (diagonal from the central differences, off-diagonal from n (n - 1) / 2
+// mixed differences; made positive definite), later ones BFGS updates;
+// backtracking Armijo line search.  Same ask/tell interface as NelderMead.  Stops when an iteration lowers f by at most ftol_abs and moves
 // every coordinate by at most xtol, after three iterations in a row that
 // lower f by at most ftol_abs, when the line search fails, or at max_evals.
 class QuasiNewton {
@@ -123,11 +124,17 @@ class QuasiNewton {
     int evals() const { return evals_; }
 
   private:
-    enum class State { Start, Grad, Line, Done };
+    enum class State { Start, Grad, Hess, Line, Done };
     void start_gradient();
     void next_grad_point();
     void finish_gradient();
+    void next_hess_point();
+    void finish_hessian();
     void start_line();
+    std::vector<double> hmix_;  // forward mixed differences f(x + h e_i + h e_j), i < j
+    std::vector<std::pair<int, int>> pairs_;
+    std::vector<double> curv_;  // central-difference curvature of the first gradient
+    int hi_ = 0;
     int n_;
     double ftol_, xtol_, h_;
     int max_evals_, evals_ = 0;
