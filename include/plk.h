@@ -268,12 +268,14 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
 /* Optimiser of plk_batch_fit_gtr (and, with plk_set_fit_method, of
  * plk_fit_gtr).  PLK_FIT_NELDER_MEAD (default) is the counterpart of the
  * reference's NLopt LN_NELDERMEAD; PLK_FIT_QUASI_NEWTON is BFGS on
- * central-difference gradients (2 n evaluations per gradient; at the start a
- * full finite-difference Hessian, n (n - 1) / 2 more, so the first step is a
- * Newton step), same stopping tolerances (or three iterations in a row
- * improving lnL by at most ftol). */
+ * central-difference gradients (step 1e-2, 2 n evaluations per gradient; the
+ * first inverse Hessian from their diagonal curvature); PLK_FIT_NEWTON_START
+ * is the same with a full finite-difference Hessian at the start (n (n - 1)
+ * / 2 more evaluations, so the first step is a Newton step).  Same stopping
+ * tolerances (or three iterations in a row improving lnL by at most ftol). */
 #define PLK_FIT_NELDER_MEAD 0
 #define PLK_FIT_QUASI_NEWTON 1
+#define PLK_FIT_NEWTON_START 2
 plk_status plk_batch_set_fit_method(plk_batch* b, int method);
 /* lnL of every item at the GTR parameter vector x[n_items][n_params] (the
  * parameterisation of plk_batch_fit_gtr) in one batch evaluation; the items
@@ -306,6 +308,25 @@ plk_status plk_mlp_gradients(plk_mlp* m, int batch, const float* x, const float*
  * the step into *loss (may be NULL). */
 plk_status plk_mlp_train_step(plk_mlp* m, int batch, const float* x, const float* t, float lr,
                               float* loss);
+
+/* ---- branch lengths (no counterpart in the reference: its branch lengths
+ * are fixed inputs, src/tree.cpp:136, 176) ------------------------------------
+ * First and second derivatives of every item's lnL with respect to the length
+ * of the edge above every node, from one post-order and one pre-order pass
+ * (P(t) = L diag(exp(lambda t)) R: the derivatives weight the same eigen
+ * terms by lambda r and (lambda r)^2).  out: item after item, [n_nodes][2] in
+ * the caller's node ids (d1, d2); the root's pair is 0. */
+plk_status plk_batch_edge_derivatives(plk_batch* b, double* out);
+/* Maximum-likelihood branch lengths of every item under its current model:
+ * each iteration takes one Newton step on every edge of an item at once (a
+ * step along the slope where the curvature is not negative; lengths within
+ * [1e-8, 20], at most x10 per step; of the two root edges only the first
+ * moves, their sum being what counts), halving the item's steps until its lnL
+ * does not drop.  An item stops when an iteration gains less than tol.
+ * lnl_out[n_items] (may be NULL), iters_out = iterations run. */
+plk_status plk_batch_optimize_branches(plk_batch* b, int max_iter, double tol, double* lnl_out, int* iters_out);
+/* An item's current branch lengths in the caller's node ids. */
+plk_status plk_batch_branch_lengths(const plk_batch* b, int item, double* bl_out);
 
 int plk_batch_nni_count(const plk_batch* b, int item);
 /* The same moves of one tree on the host (no device): *n_moves_out moves,

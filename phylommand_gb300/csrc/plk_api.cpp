@@ -844,8 +844,8 @@ plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_
         if (n_evals_out) *n_evals_out = opt.evals();
         return PLK_OK;
     };
-    if (h->fit_method == PLK_FIT_QUASI_NEWTON) {
-        QuasiNewton qn(n, start.data(), steps.data(), ftol, xtol, max_evals);
+    if (h->fit_method == PLK_FIT_QUASI_NEWTON || h->fit_method == PLK_FIT_NEWTON_START) {
+        QuasiNewton qn(n, start.data(), steps.data(), ftol, xtol, max_evals, h->fit_method == PLK_FIT_NEWTON_START);
         return run(qn);
     }
     NelderMead nm(n, start.data(), steps.data(), ftol, xtol, max_evals);
@@ -854,7 +854,8 @@ plk_status plk_fit_gtr(plk_handle* h, int precision, const double* freqs, int n_
 
 plk_status plk_set_fit_method(plk_handle* h, int method) {
     if (!h) return PLK_ERR_ARG;
-    if (method != PLK_FIT_NELDER_MEAD && method != PLK_FIT_QUASI_NEWTON) return fail(h, PLK_ERR_ARG, "unknown fit method");
+    if (method != PLK_FIT_NELDER_MEAD && method != PLK_FIT_QUASI_NEWTON && method != PLK_FIT_NEWTON_START)
+        return fail(h, PLK_ERR_ARG, "unknown fit method");
     h->fit_method = method;
     return PLK_OK;
 }

@@ -81,6 +81,23 @@ size_t nni_smem_bytes(int C, bool codes_smem, int max_ops, int max_tips, int max
 cudaError_t launch_batch_nni(const BatchDev& b, bool codes_smem, int grid, size_t smem, cudaStream_t st);
 cudaError_t launch_batch_nni_reduce(const BatchDev& b, cudaStream_t st);
 
+// Branch-length derivatives of every edge of every item (plk_nni.cu): per
+// work unit the sums over its sites of d lnL / dt and d2 lnL / dt2 for each
+// edge slot (slot i = child i % 2 of internal node n_tips + i / 2), then per
+// item over its units in site order.  Same units, scratch and shared memory
+// as the NNI kernel.
+struct BlenDev {
+    const long long* unit_edge_off;  // [n_units] first slot of each unit in unit_edge_sums
+    double* unit_edge_sums;          // [slots][2]
+    const int* item_edge_off;        // [n_items] first global slot of each item
+    const int* edge_item;            // [total_slots]
+    int total_slots;
+    double* edge_out;                // [total_slots][2] (d1, d2)
+};
+cudaError_t launch_batch_blen(const BatchDev& b, const BlenDev& bd, bool codes_smem, int grid, size_t smem,
+                              cudaStream_t st);
+cudaError_t launch_batch_blen_reduce(const BatchDev& b, const BlenDev& bd, cudaStream_t st);
+
 // Summary statistics of every item (plk_features.cu): out[n_items][43].
 constexpr int kNumFeatures = 43;
 cudaError_t launch_features(const BatchDev& b, float* out, cudaStream_t st);

@@ -56,6 +56,7 @@ struct ItemHost {
     std::vector<double> model;     // lam L R root_w cat_rate cat_w
     std::vector<NniMoveDev> moves; // internal ids
     std::vector<int> move_report;  // (caller's node id, which) per move
+    std::vector<int> caller_id;    // caller's node id of every internal id
     bool has_model = false;
 };
 
@@ -82,6 +83,7 @@ struct plk_batch {
     // device layout
     BBuf d_items, d_codes, d_ops, d_teff, d_node_item, d_child, d_model, d_P32, d_tip32, d_lnl, d_counter;
     BBuf d_moves, d_move_item, d_nni_out, d_unit_move_sums, d_scr_D, d_scr_ED, d_scr_O, d_scr_EO;
+    BBuf d_blen_ueo, d_blen_ues, d_blen_ieo, d_blen_ei, d_blen_out;  // branch-length derivative slots
     double* h_model = nullptr;  // pinned staging of the models
     double* h_lnl = nullptr;    // pinned lnL download
     size_t h_model_n = 0, h_lnl_n = 0;
@@ -464,6 +466,7 @@ void relabel_and_enumerate(int n_tips, int n_nodes, const int* left, const int* 
         if ((*L2)[v] >= 0) parent[(*L2)[v]] = v;
         if ((*R2)[v] >= 0) parent[(*R2)[v]] = v;
     }
+    h->caller_id = oid;
     auto binary = [&](int v) { return v >= n_tips && (*L2)[v] >= 0 && (*R2)[v] >= 0; };
     h->moves.clear();
     h->move_report.clear();
@@ -764,11 +767,12 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
     if (x0) std::copy(x0, x0 + (size_t)n_items * np, starts.begin());
     if (step) std::copy(step, step + (size_t)n_items * np, steps.begin());
     FitOut out{x_out, lnl_out, evals_out, rounds_out, target_lnl, target_tol, hit_evals_out};
-    if (b->fit_method == PLK_FIT_QUASI_NEWTON) {
+    if (b->fit_method == PLK_FIT_QUASI_NEWTON || b->fit_method == PLK_FIT_NEWTON_START) {
         std::vector<QuasiNewton> opts;
         opts.reserve(n_items);
         for (int i = 0; i < n_items; ++i)
-            opts.emplace_back(np, &starts[(size_t)i * np], &steps[(size_t)i * np], ftol, xtol, max_evals);
+            opts.emplace_back(np, &starts[(size_t)i * np], &steps[(size_t)i * np], ftol, xtol, max_evals,
+                              b->fit_method == PLK_FIT_NEWTON_START);
         return run_fits(b, freqs, opts, out);
     }
     std::vector<NelderMead> opts;
@@ -780,7 +784,7 @@ plk_status plk_batch_fit_gtr(plk_batch* b, const double* freqs, const double* x0
 
 plk_status plk_batch_set_fit_method(plk_batch* b, int method) {
     if (!b) return PLK_ERR_ARG;
-    if (method != PLK_FIT_NELDER_MEAD && method != PLK_FIT_QUASI_NEWTON)
+    if (method != PLK_FIT_NELDER_MEAD && method != PLK_FIT_QUASI_NEWTON && method != PLK_FIT_NEWTON_START)
         return bfail(b, PLK_ERR_ARG, "unknown fit method");
     b->fit_method = method;
     return PLK_OK;
@@ -848,6 +852,196 @@ plk_status plk_batch_nni_loglik(plk_batch* b, double* out) {
               "download NNI lnL");
     PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "NNI scoring");
     std::memcpy(out, b->h_lnl, (size_t)b->total_moves * sizeof(double));
+    return PLK_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// d lnL / dt and d2 lnL / dt2 of every edge slot of every item into deriv
+// ([slot][2], item after item; item i's slots start at item_edge_off[i]).
+plk_status blen_pass(plk_batch* b, std::vector<double>& deriv, std::vector<int>& item_edge_off) {
+    const int n_items = (int)b->items.size();
+    if (n_items == 0) return bfail(b, PLK_ERR_STATE, "batch is empty");
+    for (const auto& it : b->items)
+        if (!it.has_model) return bfail(b, PLK_ERR_STATE, "every item needs a model (plk_batch_set_model)");
+    plk_status s = prepare_layout(b);
+    if (s != PLK_OK) return s;
+    if (b->nni_units.spt != 1) {
+        s = build_units(b, b->nni_units, 1, true);
+        if (s != PLK_OK) return s;
+    }
+    size_t smem = nni_smem_bytes(b->C, true, b->max_ops, b->max_tips, b->max_depth);
+    bool codes_smem = smem <= 160 * 1024;
+    if (!codes_smem) smem = nni_smem_bytes(b->C, false, b->max_ops, b->max_tips, b->max_depth);
+    if (smem > 227 * 1024) return bfail(b, PLK_ERR_UNSUPPORTED, "trees too large for branch-length derivatives");
+    const int grid = std::max(1, std::min(b->nni_units.n_units, 2 * b->n_sms));
+    const size_t slice = (size_t)b->max_int * kThreads;
+    PLK_BCUDA(b, b->d_scr_D.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate scratch");
+    PLK_BCUDA(b, b->d_scr_O.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate scratch");
+    PLK_BCUDA(b, b->d_scr_ED.ensure((size_t)grid * slice * sizeof(int)), "allocate scratch");
+    PLK_BCUDA(b, b->d_scr_EO.ensure((size_t)grid * slice * sizeof(int)), "allocate scratch");
+    // edge slots: 2 per internal node of every item, per unit and per item
+    item_edge_off.assign(n_items, 0);
+    std::vector<int> edge_item;
+    int total_slots = 0;
+    for (int i = 0; i < n_items; ++i) {
+        item_edge_off[i] = total_slots;
+        total_slots += 2 * b->items[i].n_int;
+        edge_item.insert(edge_item.end(), 2 * b->items[i].n_int, i);
+    }
+    const std::vector<int2>& units = b->nni_units.host_units;
+    std::vector<long long> unit_edge_off(units.size());
+    long long unit_slots = 0;
+    for (size_t u = 0; u < units.size(); ++u) {
+        unit_edge_off[u] = unit_slots;
+        unit_slots += 2 * b->items[units[u].x].n_int;
+    }
+    PLK_BCUDA(b, b->d_blen_ueo.ensure(unit_edge_off.size() * sizeof(long long)), "allocate edge slots");
+    PLK_BCUDA(b, b->d_blen_ues.ensure((size_t)unit_slots * 2 * sizeof(double)), "allocate edge slots");
+    PLK_BCUDA(b, b->d_blen_ieo.ensure(item_edge_off.size() * sizeof(int)), "allocate edge slots");
+    PLK_BCUDA(b, b->d_blen_ei.ensure(edge_item.size() * sizeof(int)), "allocate edge slots");
+    PLK_BCUDA(b, b->d_blen_out.ensure((size_t)total_slots * 2 * sizeof(double)), "allocate edge slots");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_blen_ueo.p, unit_edge_off.data(), unit_edge_off.size() * sizeof(long long),
+                                 cudaMemcpyHostToDevice, b->stream), "upload edge slots");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_blen_ieo.p, item_edge_off.data(), item_edge_off.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, b->stream), "upload edge slots");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_blen_ei.p, edge_item.data(), edge_item.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, b->stream), "upload edge slots");
+    BlenDev bd{b->d_blen_ueo.as<long long>(), b->d_blen_ues.as<double>(), b->d_blen_ieo.as<int>(),
+               b->d_blen_ei.as<int>(), total_slots, b->d_blen_out.as<double>()};
+    deriv.assign((size_t)total_slots * 2, 0.0);
+    const BatchDev d = device_view(b, b->nni_units);
+    const size_t mn = (size_t)n_items * batch_model_stride(b->C);
+    PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, mn * sizeof(double), cudaMemcpyHostToDevice, b->stream),
+              "upload models");
+    PLK_BCUDA(b, launch_batch_pmat(d, b->stream), "batch P(t) launch");
+    PLK_BCUDA(b, launch_batch_blen(d, bd, codes_smem, grid, smem, b->stream), "branch-length kernel launch");
+    PLK_BCUDA(b, launch_batch_blen_reduce(d, bd, b->stream), "branch-length reduce launch");
+    PLK_BCUDA(b, cudaMemcpyAsync(deriv.data(), b->d_blen_out.p, deriv.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                 b->stream), "download derivatives");
+    PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "branch-length derivatives");
+    return PLK_OK;
+}
+
+// the lengths as the kernels see them, packed in layout order
+plk_status upload_lengths(plk_batch* b) {
+    std::vector<double> teff;
+    teff.reserve(b->n_nodes_total);
+    for (const auto& it : b->items) teff.insert(teff.end(), it.t_eff.begin(), it.t_eff.end());
+    PLK_BCUDA(b, cudaMemcpyAsync(b->d_teff.p, teff.data(), teff.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                 b->stream), "upload lengths");
+    PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "upload lengths");
+    return PLK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+plk_status plk_batch_edge_derivatives(plk_batch* b, double* out) {
+    if (!b || !out) return b ? bfail(b, PLK_ERR_ARG, "out is NULL") : PLK_ERR_ARG;
+    std::vector<double> deriv;
+    std::vector<int> ieo;
+    plk_status s = blen_pass(b, deriv, ieo);
+    if (s != PLK_OK) return s;
+    size_t off = 0;
+    for (size_t i = 0; i < b->items.size(); ++i) {
+        const ItemHost& h = b->items[i];
+        for (int v = 0; v < 2 * h.n_nodes; ++v) out[off + v] = 0.0;
+        for (int slot = 0; slot < 2 * h.n_int; ++slot) {
+            const int2 ch = h.child[h.n_tips + slot / 2];
+            const int v = (slot % 2 == 0) ? ch.x : ch.y;
+            if (v < 0) continue;
+            out[off + 2 * h.caller_id[v]] = deriv[2 * (ieo[i] + slot)];
+            out[off + 2 * h.caller_id[v] + 1] = deriv[2 * (ieo[i] + slot) + 1];
+        }
+        off += 2 * (size_t)h.n_nodes;
+    }
+    return PLK_OK;
+}
+
+plk_status plk_batch_optimize_branches(plk_batch* b, int max_iter, double tol, double* lnl_out, int* iters_out) {
+    if (!b || max_iter < 1 || !(tol > 0.0)) return b ? bfail(b, PLK_ERR_ARG, "bad arguments to plk_batch_optimize_branches") : PLK_ERR_ARG;
+    const int n_items = (int)b->items.size();
+    if (n_items == 0) return bfail(b, PLK_ERR_STATE, "batch is empty");
+    std::vector<double> cur(n_items), trial(n_items), deriv;
+    std::vector<int> item_edge_off;
+    plk_status s = plk_batch_loglik(b, cur.data());
+    if (s != PLK_OK) return s;
+    std::vector<char> done(n_items, 0);
+    int it_n = 0;
+    const double t_min = 1e-8, t_max = 20.0;
+    for (; it_n < max_iter; ++it_n) {
+        bool any = false;
+        for (char d : done) any = any || !d;
+        if (!any) break;
+        if ((s = blen_pass(b, deriv, item_edge_off)) != PLK_OK) return s;
+        // one Newton step per edge (all edges of an item at once), halved
+        // until the item's lnL does not drop
+        std::vector<std::vector<double>> old(n_items), step(n_items);
+        for (int i = 0; i < n_items; ++i) {
+            ItemHost& h = b->items[i];
+            old[i] = h.t_eff;
+            step[i].assign(h.n_nodes, 0.0);
+            if (done[i]) continue;
+            for (int slot = 0; slot < 2 * h.n_int; ++slot) {
+                const int2 ch = h.child[h.n_tips + slot / 2];
+                const int v = (slot % 2 == 0) ? ch.x : ch.y;
+                if (v < 0) continue;
+                // the two root edges act through their sum (reversible model,
+                // root weights = frequencies): only the first one moves
+                if (slot / 2 == h.n_int - 1 && slot % 2 == 1) continue;
+                const double g = deriv[2 * (item_edge_off[i] + slot)], c = deriv[2 * (item_edge_off[i] + slot) + 1];
+                const double t = h.t_eff[v];
+                double tn;
+                if (c < 0.0) tn = t - g / c;                 // Newton on a concave direction
+                else tn = g > 0.0 ? 2.0 * t + 1e-3 : 0.5 * t;  // otherwise move along the slope
+                tn = std::min(std::max(tn, std::max(t_min, 0.1 * t)), std::min(t_max, 10.0 * t + 0.05));
+                step[i][v] = tn - t;
+            }
+        }
+        std::vector<char> accepted(n_items, 0);
+        for (int half = 0; half < 6; ++half) {
+            for (int i = 0; i < n_items; ++i) {
+                if (done[i] || accepted[i]) continue;
+                const double f = std::ldexp(1.0, -half);
+                for (int v = 0; v < b->items[i].n_nodes; ++v) b->items[i].t_eff[v] = old[i][v] + f * step[i][v];
+            }
+            if ((s = upload_lengths(b)) != PLK_OK) return s;
+            s = plk_batch_loglik(b, trial.data());
+            if (s != PLK_OK && s != PLK_ERR_NUMERIC) return s;
+            bool pending = false;
+            for (int i = 0; i < n_items; ++i) {
+                if (done[i] || accepted[i]) continue;
+                if (std::isfinite(trial[i]) && trial[i] >= cur[i] - 1e-12 * std::fabs(cur[i])) accepted[i] = 1;
+                else pending = true;
+            }
+            if (!pending) break;
+        }
+        for (int i = 0; i < n_items; ++i) {
+            if (done[i]) continue;
+            if (!accepted[i]) {  // no step helps: keep the old lengths, the item has converged
+                b->items[i].t_eff = old[i];
+                done[i] = 1;
+                continue;
+            }
+            if (trial[i] - cur[i] < tol) done[i] = 1;
+            cur[i] = trial[i];
+        }
+        if ((s = upload_lengths(b)) != PLK_OK) return s;
+    }
+    if (lnl_out) std::copy(cur.begin(), cur.end(), lnl_out);
+    if (iters_out) *iters_out = it_n;
+    return PLK_OK;
+}
+
+plk_status plk_batch_branch_lengths(const plk_batch* b, int item, double* bl_out) {
+    if (!b || !bl_out || item < 0 || item >= (int)b->items.size()) return PLK_ERR_ARG;
+    const ItemHost& h = b->items[item];
+    for (int v = 0; v < h.n_nodes; ++v) bl_out[h.caller_id[v]] = h.t_eff[v];
     return PLK_OK;
 }
 

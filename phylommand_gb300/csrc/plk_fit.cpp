@@ -146,8 +146,9 @@ double NelderMead::best_f() const { return *std::min_element(fvals_.begin(), fva
 // shortens the step (quadratic interpolation, within [0.1, 0.5] of the last
 // trial) until the Armijo condition holds.
 // ---------------------------------------------------------------------------
-QuasiNewton::QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals)
-    : n_(n), ftol_(ftol_abs), xtol_(xtol), h_(1e-3), max_evals_(max_evals) {
+QuasiNewton::QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals,
+                         bool full_hessian)
+    : n_(n), ftol_(ftol_abs), xtol_(xtol), h_(1e-2), max_evals_(max_evals), full_hessian_(full_hessian) {
     x_.assign(x0, x0 + n);
     max_step_.assign(steps, steps + n);
     point_ = x_;
@@ -234,6 +235,14 @@ void QuasiNewton::finish_hessian() {
 }
 
 void QuasiNewton::finish_gradient() {
+    if (!have_prev_ && !full_hessian_) {
+        // first inverse Hessian: diagonal Newton where the curvature is positive
+        for (int k = 0; k < n_; ++k)
+            H_[(size_t)k * n_ + k] =
+                curv_[k] > 1e-12 ? 1.0 / curv_[k] : max_step_[k] / std::max(std::fabs(g_[k]), 1e-12);
+        start_line();
+        return;
+    }
     if (!have_prev_ && hmix_.empty() && n_ > 1) {
         // first iterate: the mixed differences of the full Hessian
         for (int i = 0; i < n_; ++i)

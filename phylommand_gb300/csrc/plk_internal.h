@@ -106,16 +106,18 @@ class NelderMead {
     std::vector<double> fvals_, point_, centroid_, xr_;
     double fr_ = 0.0;
 };
-// Quasi-Newton minimiser with central-difference gradients: the first
-// inverse Hessian is the inverse of a finite-difference Hessian at the start
-// (diagonal from the central differences, off-diagonal from n (n - 1) / 2
-// mixed differences; made positive definite), later ones BFGS updates;
-// backtracking Armijo line search.  Same ask/tell interface as NelderMead.  Stops when an iteration lowers f by at most ftol_abs and moves
+// Quasi-Newton minimiser with central-difference gradients (step 1e-2): the
+// first inverse Hessian is the inverse of the central differences' diagonal
+// curvature, or with full_hessian of a finite-difference Hessian at the start
+// (off-diagonal terms from n (n - 1) / 2 mixed differences; made positive
+// definite); later ones BFGS updates; backtracking Armijo line search.  Same
+// ask/tell interface as NelderMead.  Stops when an iteration lowers f by at most ftol_abs and moves
 // every coordinate by at most xtol, after three iterations in a row that
 // lower f by at most ftol_abs, when the line search fails, or at max_evals.
 class QuasiNewton {
   public:
-    QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals);
+    QuasiNewton(int n, const double* x0, const double* steps, double ftol_abs, double xtol, int max_evals,
+                bool full_hessian);
     bool done() const { return state_ == State::Done; }
     const std::vector<double>& point() const { return point_; }
     void tell(double f);
@@ -144,6 +146,7 @@ class QuasiNewton {
     double f_ = HUGE_VAL, f_prev_ = HUGE_VAL, t_ = 1.0, slope_ = 0.0;
     int gi_ = 0, backtracks_ = 0, iter_ = 0, flat_ = 0;
     bool have_prev_ = false;
+    bool full_hessian_ = false;
 };
 // GTR(+Gamma) parameters of the fits (see plk_fit.cpp); false outside the domain.
 bool gtr_model_from_x(int S, const double* x, int n_cats, const double* freqs, double* Q, double* cat_rates,

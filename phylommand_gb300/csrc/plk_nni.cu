@@ -310,6 +310,196 @@ __global__ void batch_nni_reduce_kernel(BatchDev b) {
     b.nni_out[g] = s + c;
 }
 
+// ---------------------------------------------------------------------------
+// Branch-length derivatives (no counterpart in the reference, whose branch
+// lengths are fixed inputs, src/tree.cpp:136, 176).  For the edge above v
+// (parent u, sibling w) the site likelihood as a function of its length t is
+//   L(t) = sum_k w_k A_k^T P(r_k t) c_k,   A_k = Out(u) x D_w,  c_k = cond(v),
+// and with P(t) = L diag(exp(lambda t)) R (the model's eigen form)
+//   L(t) = sum_k w_k sum_m a_km b_km exp(rho_km t),  rho_km = lambda_m r_k,
+//   a_k = L^T A_k,  b_k = R c_k,
+// so L' and L'' only weight the same terms by rho and rho^2.  Every site adds
+// d1 = L'/L and d2 = L''/L - (L'/L)^2 (the first and second derivatives of its
+// log likelihood; the power-of-two exponents cancel in the ratios).  Edge
+// slot i of an item is child i % 2 of internal node n_tips + i / 2.
+// ---------------------------------------------------------------------------
+template <int CM>
+__device__ void edge_site_derivs(const ItemView& iv, const BatchDev& b, int u, int v, int w, int site_c, int tid,
+                                 const float4* sD, const int* sED, const float4* sO, double* d1, double* d2) {
+    const BatchItemDev& it = *iv.it;
+    const int C = b.C;
+    const double* mdl = b.model + it.model_off;
+    const double* lam = mdl;
+    const double* Lm = mdl + 4;
+    const double* Rm = mdl + 20;
+    const double* cat_rate = mdl + 40;
+    const bool u_root = (u - it.n_tips) == it.n_int - 1;
+    const double t = b.t_eff[it.node_off + v];
+    // cond(v): a tip's state set, or the product of v's children's messages
+    float4 cv[CM];
+    int e = 0;
+    if (v < it.n_tips) {
+        const int code = iv.codes[(size_t)v * it.site_stride + site_c] & (kCodes - 1);
+        const float4 m = make_float4((float)(code & 1), (float)((code >> 1) & 1), (float)((code >> 2) & 1),
+                                     (float)((code >> 3) & 1));
+#pragma unroll
+        for (int k = 0; k < CM; ++k) cv[k] = m;
+    } else {
+        const int2 ch = iv.child[v];
+#pragma unroll
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                cv[k] = message(iv, b, ch.x, k, site_c, tid, sD, sED, &e);
+                if (ch.y >= 0) cv[k] = mul4(cv[k], message(iv, b, ch.y, k, site_c, tid, sD, sED, &e));
+            }
+    }
+    float l0 = 0.f, l1 = 0.f, l2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < CM; ++k)
+        if (k < C) {
+            float4 A = u_root ? make_float4((float)iv.root_w[0], (float)iv.root_w[1], (float)iv.root_w[2],
+                                            (float)iv.root_w[3])
+                              : sO[((size_t)(u - it.n_tips) * C + k) * TILE + tid];
+            if (w >= 0) A = mul4(A, message(iv, b, w, k, site_c, tid, sD, sED, &e));
+            const float Av[4] = {A.x, A.y, A.z, A.w};
+            const float cvv[4] = {cv[k].x, cv[k].y, cv[k].z, cv[k].w};
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                float a = 0.f, bb = 0.f;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    a = fmaf(Av[i], (float)Lm[i * 4 + m], a);
+                    bb = fmaf((float)Rm[m * 4 + i], cvv[i], bb);
+                }
+                const float rho = (float)(lam[m] * cat_rate[k]);
+                const float term = a * bb * expf(rho * (float)t);
+                s0 += term;
+                s1 = fmaf(rho, term, s1);
+                s2 = fmaf(rho * rho, term, s2);
+            }
+            const float wk = (float)iv.cat_w[k];
+            l0 = fmaf(wk, s0, l0);
+            l1 = fmaf(wk, s1, l1);
+            l2 = fmaf(wk, s2, l2);
+        }
+    const double g = (double)l1 / (double)l0;
+    *d1 = g;
+    *d2 = (double)l2 / (double)l0 - g * g;
+}
+
+template <int CM, bool CODES_SMEM>
+__global__ void __launch_bounds__(kPruneThreads) batch_blen_kernel(BatchDev b, BlenDev bd) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ int s_unit;
+    __shared__ double s_red[kPruneThreads / 32][32][2];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const size_t vec_slice = (size_t)b.scratch_int * b.C * TILE;
+    const size_t int_slice = (size_t)b.scratch_int * TILE;
+    float4* sD = b.scr_D + blockIdx.x * vec_slice;
+    int* sED = b.scr_ED + blockIdx.x * int_slice;
+    float4* sO = b.scr_O + blockIdx.x * vec_slice;
+    int* sEO = b.scr_EO + blockIdx.x * int_slice;
+    for (;;) {
+        if (tid == 0) s_unit = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int u_idx = s_unit;
+        if (u_idx >= b.n_units) break;
+        const int2 unit = b.units[u_idx];
+        const BatchItemDev it = b.items[unit.x];
+        ItemView iv;
+        iv.it = &it;
+        iv.P = b.P32 + (size_t)it.node_off * b.C * 16;
+        iv.tipT = b.tip32 + (size_t)it.tip_off * b.C * kCodes * 4;
+        iv.codes = b.codes + it.codes_off;
+        iv.child = b.child + it.node_off;
+        iv.root_w = b.model + it.model_off + 36;
+        iv.cat_w = b.model + it.model_off + 40 + b.C;
+        TileJob j;
+        j.ops = b.ops + it.ops_off;
+        j.n_ops = it.n_ops;
+        j.codes = iv.codes;
+        j.site_stride = it.site_stride;
+        j.n_sites = it.n_sites;
+        j.n_tips = it.n_tips;
+        j.P = iv.P;
+        j.tipT = iv.tipT;
+        j.root_w = iv.root_w;
+        j.cat_w = iv.cat_w;
+        j.C = b.C;
+        j.tile_base = unit.y * TILE;
+        j.site_lnl = nullptr;
+        j.max_depth = b.max_depth;
+        DStore ds{sD, sED};
+        double ts = 0.0, tc = 0.0;
+        run_tile<CM, 1, CODES_SMEM, true>(j, sm, ts, tc, &ds);
+        const int site = j.tile_base + tid;
+        const bool valid = site < it.n_sites;
+        const int site_c = min(site, it.site_stride - 1);
+        phase_b<CM>(iv, b, site_c, tid, sD, sED, sO, sEO);
+        const long long out_off = bd.unit_edge_off[u_idx];
+        const int n_slots = 2 * it.n_int;
+        for (int s0 = 0; s0 < n_slots; s0 += 32) {
+            const int count = min(32, n_slots - s0);
+            for (int si = 0; si < count; ++si) {
+                const int slot = s0 + si;
+                const int u = it.n_tips + slot / 2;
+                const int2 ch = iv.child[u];
+                const int v = (slot % 2 == 0) ? ch.x : ch.y;
+                const int w = (slot % 2 == 0) ? ch.y : ch.x;
+                double d1 = 0.0, d2 = 0.0;
+                if (valid && v >= 0) edge_site_derivs<CM>(iv, b, u, v, w, site_c, tid, sD, sED, sO, &d1, &d2);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    d1 += __shfl_down_sync(0xffffffffu, d1, off);
+                    d2 += __shfl_down_sync(0xffffffffu, d2, off);
+                }
+                if (lane == 0) {
+                    s_red[warp][si][0] = d1;
+                    s_red[warp][si][1] = d2;
+                }
+            }
+            __syncthreads();
+            if (tid < count) {
+                double a = 0.0, c = 0.0;
+                for (int q = 0; q < kPruneThreads / 32; ++q) {
+                    a += s_red[q][tid][0];
+                    c += s_red[q][tid][1];
+                }
+                bd.unit_edge_sums[2 * (out_off + s0 + tid)] = a;
+                bd.unit_edge_sums[2 * (out_off + s0 + tid) + 1] = c;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// one thread per (item, edge slot): the item's units in site order
+__global__ void batch_blen_reduce_kernel(BatchDev b, BlenDev bd) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= bd.total_slots) return;
+    const int item = bd.edge_item[g];
+    const int slot = g - bd.item_edge_off[item];
+    double a = 0.0, c = 0.0;
+    for (int q = b.item_unit_ptr[item]; q < b.item_unit_ptr[item + 1]; ++q) {
+        const int u = b.item_units[q];
+        const double* p = bd.unit_edge_sums + 2 * (bd.unit_edge_off[u] + slot);
+        a += p[0];
+        c += p[1];
+    }
+    bd.edge_out[2 * g] = a;
+    bd.edge_out[2 * g + 1] = c;
+}
+
+template <int CM, bool CODES_SMEM>
+cudaError_t launch_blen_t(const BatchDev& b, const BlenDev& bd, int grid, size_t smem, cudaStream_t st) {
+    auto kern = batch_blen_kernel<CM, CODES_SMEM>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kPruneThreads, smem, st>>>(b, bd);
+    return cudaGetLastError();
+}
+
 template <int CM, bool CODES_SMEM>
 cudaError_t launch_nni_t(const BatchDev& b, int grid, size_t smem, cudaStream_t st) {
     auto kern = batch_nni_kernel<CM, CODES_SMEM>;
@@ -336,6 +526,21 @@ cudaError_t launch_batch_nni(const BatchDev& b, bool codes_smem, int grid, size_
     if (cm == 1) return codes_smem ? launch_nni_t<1, true>(b, grid, smem, st) : launch_nni_t<1, false>(b, grid, smem, st);
     if (cm == 4) return codes_smem ? launch_nni_t<4, true>(b, grid, smem, st) : launch_nni_t<4, false>(b, grid, smem, st);
     return codes_smem ? launch_nni_t<8, true>(b, grid, smem, st) : launch_nni_t<8, false>(b, grid, smem, st);
+}
+
+cudaError_t launch_batch_blen(const BatchDev& b, const BlenDev& bd, bool codes_smem, int grid, size_t smem,
+                              cudaStream_t st) {
+    const int cm = b.C == 1 ? 1 : (b.C <= 4 ? 4 : 8);
+    if (cm == 1) return codes_smem ? launch_blen_t<1, true>(b, bd, grid, smem, st) : launch_blen_t<1, false>(b, bd, grid, smem, st);
+    if (cm == 4) return codes_smem ? launch_blen_t<4, true>(b, bd, grid, smem, st) : launch_blen_t<4, false>(b, bd, grid, smem, st);
+    return codes_smem ? launch_blen_t<8, true>(b, bd, grid, smem, st) : launch_blen_t<8, false>(b, bd, grid, smem, st);
+}
+
+cudaError_t launch_batch_blen_reduce(const BatchDev& b, const BlenDev& bd, cudaStream_t st) {
+    if (bd.total_slots == 0) return cudaSuccess;
+    const int threads = 128;
+    batch_blen_reduce_kernel<<<(bd.total_slots + threads - 1) / threads, threads, 0, st>>>(b, bd);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_nni_reduce(const BatchDev& b, cudaStream_t st) {

@@ -34,6 +34,7 @@ PLK_NODES_COND = 0
 PLK_NODES_MARGINAL = 1
 PLK_FIT_NELDER_MEAD = 0
 PLK_FIT_QUASI_NEWTON = 1
+PLK_FIT_NEWTON_START = 2
 
 # Every symbol include/plk.h declares (checked by the tests).
 EXPORTS = [
@@ -48,7 +49,7 @@ EXPORTS = [
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
     "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate", "plk_nni_moves_host",
     "plk_batch_features", "plk_batch_fit_gtr", "plk_batch_eval_gtr", "plk_batch_set_fit_method",
-    "plk_set_fit_method",
+    "plk_set_fit_method", "plk_batch_edge_derivatives", "plk_batch_optimize_branches", "plk_batch_branch_lengths",
     "plk_mlp_create", "plk_mlp_destroy", "plk_mlp_last_error", "plk_mlp_n_params", "plk_mlp_get_params",
     "plk_mlp_set_params", "plk_mlp_forward", "plk_mlp_gradients", "plk_mlp_train_step",
 ]
@@ -128,6 +129,9 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_eval_gtr.argtypes = [hp, dp, dp, dp]
     L.plk_batch_set_fit_method.argtypes = [hp, c_int]
     L.plk_set_fit_method.argtypes = [hp, c_int]
+    L.plk_batch_edge_derivatives.argtypes = [hp, dp]
+    L.plk_batch_optimize_branches.argtypes = [hp, c_int, c_double, dp, ip]
+    L.plk_batch_branch_lengths.argtypes = [hp, c_int, dp]
     L.plk_mlp_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64]
     L.plk_mlp_destroy.argtypes = [hp]
     L.plk_mlp_destroy.restype = None
@@ -407,6 +411,7 @@ class Batch:
         self._b = ctypes.c_void_p()
         _check(lib().plk_batch_create(ctypes.byref(self._b), int(device), int(n_cats)), None)
         self.n_cats = int(n_cats)
+        self._n_nodes = []
 
     def _check(self, status: int) -> None:
         if status != PLK_OK:
@@ -442,6 +447,7 @@ class Batch:
         self._check(lib().plk_batch_add(self._b, m.shape[0], m.shape[1], _p(m, ctypes.c_uint32), l.shape[0],
                                         _p(l, ctypes.c_int), _p(r, ctypes.c_int), _p(b, ctypes.c_double),
                                         ctypes.byref(item)))
+        self._n_nodes.append(int(l.shape[0]))
         return item.value
 
     def set_model(self, item: int, Q, freqs, cat_rates, cat_weights) -> None:
@@ -493,6 +499,31 @@ class Batch:
     def set_fit_method(self, method: int) -> None:
         """PLK_FIT_NELDER_MEAD (default) or PLK_FIT_QUASI_NEWTON for fit_gtr."""
         self._check(lib().plk_batch_set_fit_method(self._b, int(method)))
+
+    def edge_derivatives(self) -> list:
+        """Per item an [n_nodes, 2] array: d lnL / dt and d2 lnL / dt2 for the
+        edge above every node (caller's node ids; the root's row is 0)."""
+        counts = self._n_nodes
+        out = np.zeros(2 * max(sum(counts), 1))
+        self._check(lib().plk_batch_edge_derivatives(self._b, _p(out, ctypes.c_double)))
+        res, o = [], 0
+        for n in counts:
+            res.append(out[o:o + 2 * n].reshape(n, 2).copy())
+            o += 2 * n
+        return res
+
+    def optimize_branches(self, max_iter: int = 50, tol: float = 1e-4):
+        """ML branch lengths of every item; returns (lnL per item, iterations)."""
+        lnl = np.zeros(len(self))
+        iters = ctypes.c_int(0)
+        self._check(lib().plk_batch_optimize_branches(self._b, int(max_iter), float(tol), _p(lnl, ctypes.c_double),
+                                                      ctypes.byref(iters)))
+        return lnl, iters.value
+
+    def branch_lengths(self, item: int) -> np.ndarray:
+        out = np.zeros(self._n_nodes[item])
+        self._check(lib().plk_batch_branch_lengths(self._b, int(item), _p(out, ctypes.c_double)))
+        return out
 
     def eval_gtr(self, freqs, x) -> np.ndarray:
         """lnL of every item at its GTR parameter vector x[n_items, n_params]."""
