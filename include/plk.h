@@ -349,6 +349,36 @@ plk_status plk_simulate(int n_nodes, const int* left, const int* right, const do
                         const double* cat_rates, int n_sites, uint64_t seed, int n_threads,
                         uint32_t* masks_out);
 
+/* ---- input formats (host only) ----------------------------------------------
+ * Character matrix text -> state-set masks, restating the reference's
+ * matrix_parser (src/matrix_parser.cpp:27-225): FASTA ('>' name lines; a
+ * character outside the alphabet is an empty cell), relaxed PHYLIP ("n_taxa
+ * n_char" header, a name up to the first blank then the cells of the line)
+ * and the MATRIX of a NEXUS DATA block (ntax checked; in both, characters
+ * outside the alphabet are skipped).  alphabet[256]: the state set of every
+ * character, -1 outside the alphabet; NULL = the DNA alphabet with IUPAC
+ * ambiguity codes in the order A, G, C, T ('-' and '.' empty).  Empty cells
+ * (and the tails of short rows) come out as all states, as treeator sets them
+ * (src/treeator.cpp:463-466).  Two calls: with masks_out / names_out NULL
+ * only the sizes; then masks_out[n_taxa][n_sites] and the names,
+ * NUL-terminated one after another, in names_out (names_cap bytes). */
+#define PLK_FORMAT_FASTA 0
+#define PLK_FORMAT_PHYLIP 1
+#define PLK_FORMAT_NEXUS 2
+plk_status plk_parse_alignment(const char* text, size_t len, int format, const int32_t* alphabet,
+                               int* n_taxa_out, int* n_sites_out, uint32_t* masks_out, char* names_out,
+                               size_t names_cap);
+/* The first tree of Newick text -> the engine's node arrays, restating
+ * tree::tree_file_parser (src/tree.cpp:69-237): comments in [], quoted
+ * labels, branch lengths read as atof reads them, a node with a third child
+ * resolved by a zero-length node over the first two.  Tips come first: tip i
+ * is the taxon names[i] (n_taxa NUL-separated names, as plk_parse_alignment
+ * returns them) or, with names NULL, the i-th tip in the text; internal nodes
+ * follow in post-order.  Two calls: with left/right/bl NULL only
+ * *n_nodes_out. */
+plk_status plk_parse_newick(const char* text, size_t len, int n_taxa, const char* names, int* n_nodes_out,
+                            int* left, int* right, double* bl);
+
 /* ---- host helpers (FP64, no device work) ---------------------------------- */
 /* Q as sub_model::calc_Q_matrix (src/sub_model.cpp:99-114): off-diagonal
  * Q[i][j] = rates[rate_spec[pos(i,j)]] * (reversible ? freq_j : 1), diagonal =

@@ -2,8 +2,10 @@
 // and the device code (plk_kernels.cu) of libplk.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>

@@ -50,6 +50,7 @@ EXPORTS = [
     "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate", "plk_nni_moves_host",
     "plk_batch_features", "plk_batch_fit_gtr", "plk_batch_eval_gtr", "plk_batch_set_fit_method",
     "plk_set_fit_method", "plk_batch_edge_derivatives", "plk_batch_optimize_branches", "plk_batch_branch_lengths",
+    "plk_parse_alignment", "plk_parse_newick",
     "plk_mlp_create", "plk_mlp_destroy", "plk_mlp_last_error", "plk_mlp_n_params", "plk_mlp_get_params",
     "plk_mlp_set_params", "plk_mlp_forward", "plk_mlp_gradients", "plk_mlp_train_step",
 ]
@@ -132,6 +133,9 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_edge_derivatives.argtypes = [hp, dp]
     L.plk_batch_optimize_branches.argtypes = [hp, c_int, c_double, dp, ip]
     L.plk_batch_branch_lengths.argtypes = [hp, c_int, dp]
+    L.plk_parse_alignment.argtypes = [ctypes.c_char_p, ctypes.c_size_t, c_int, ctypes.POINTER(ctypes.c_int32), ip,
+                                      ip, u32p, ctypes.c_char_p, ctypes.c_size_t]
+    L.plk_parse_newick.argtypes = [ctypes.c_char_p, ctypes.c_size_t, c_int, ctypes.c_char_p, ip, ip, ip, dp]
     L.plk_mlp_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int, c_int, c_int, c_int, ctypes.c_uint64]
     L.plk_mlp_destroy.argtypes = [hp]
     L.plk_mlp_destroy.restype = None
@@ -197,6 +201,52 @@ def simulate(left, right, branch_length, Q, freqs, cat_rates, n_sites: int, seed
                               int(n_sites), ctypes.c_uint64(seed), int(threads or os.cpu_count() or 1),
                               _p(out, ctypes.c_uint32)))
     return out
+
+
+PLK_FORMAT_FASTA = 0
+PLK_FORMAT_PHYLIP = 1
+PLK_FORMAT_NEXUS = 2
+
+
+def parse_alignment(text, fmt: int = PLK_FORMAT_FASTA, alphabet=None):
+    """(names, masks[n_taxa, n_sites]) from FASTA / PHYLIP / NEXUS text
+    (alphabet: dict char -> state-set mask, default DNA with IUPAC codes)."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    table = None
+    if alphabet is not None:
+        table = np.full(256, -1, dtype=np.int32)
+        for c, m in alphabet.items():
+            table[ord(c)] = int(m)
+    tp = _p(table, ctypes.c_int32)
+    nt, ns = ctypes.c_int(0), ctypes.c_int(0)
+    _check(lib().plk_parse_alignment(data, len(data), int(fmt), tp, ctypes.byref(nt), ctypes.byref(ns), None, None, 0))
+    masks = np.zeros((nt.value, ns.value), dtype=np.uint32)
+    cap = len(data) + nt.value + 1
+    names = ctypes.create_string_buffer(cap)
+    _check(lib().plk_parse_alignment(data, len(data), int(fmt), tp, ctypes.byref(nt), ctypes.byref(ns),
+                                     _p(masks, ctypes.c_uint32), names, cap))
+    out, off = [], 0
+    raw = names.raw
+    for _ in range(nt.value):
+        end = raw.index(b"\0", off)
+        out.append(raw[off:end].decode())
+        off = end + 1
+    return out, masks
+
+
+def parse_newick(text, names=None):
+    """(left, right, bl) of the first tree; tip i = names[i] when given."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    packed = None if names is None else b"".join(n.encode() + b"\0" for n in names)
+    n_taxa = 0 if names is None else len(names)
+    nn = ctypes.c_int(0)
+    _check(lib().plk_parse_newick(data, len(data), n_taxa, packed, ctypes.byref(nn), None, None, None))
+    left = np.zeros(nn.value, dtype=np.int32)
+    right = np.zeros(nn.value, dtype=np.int32)
+    bl = np.zeros(nn.value)
+    _check(lib().plk_parse_newick(data, len(data), n_taxa, packed, ctypes.byref(nn), _p(left, ctypes.c_int),
+                                  _p(right, ctypes.c_int), _p(bl, ctypes.c_double)))
+    return left, right, bl
 
 
 def nni_moves(left, right) -> np.ndarray:

@@ -19,6 +19,12 @@ Pipeline, every step on the GPU through libplk:
   4. fit new alignments from the predicted start.  The default start stays
      the fallback: both starts are scored first and the better one is used.
 
+The fits use the quasi-Newton optimiser with a finite-difference Hessian at
+the start (``PLK_FIT_NEWTON_START``): its first step is a Newton step, so a
+start close to the optimum pays off; with Nelder-Mead (linear convergence, the
+reference's NLopt method) most evaluations go into the last decades of
+convergence whatever the start, and the comparison is reported beside it.
+
 The tree handed to the fit carries the simulated topology with branch lengths
 rescaled to a mean pairwise (tip-to-tip) path length of ``INPUT_MEAN_PATH``,
 so the tree-length scale is a real unknown; because the features are pairwise
@@ -135,10 +141,11 @@ class LabelledSet:
 
 
 def make_labelled(n_items: int, n_taxa: int, n_sites: int, seed: int, ftol: float = 1e-4, xtol: float = 1e-3,
-                  max_evals: int = 4000) -> LabelledSet:
+                  max_evals: int = 4000, method: int = plk.PLK_FIT_NEWTON_START) -> LabelledSet:
     """Simulate, extract features and label with the plain GPU ML fit."""
     b, truth = simulate_batch(n_items, n_taxa, n_sites, seed)
     try:
+        b.set_fit_method(method)
         feats = b.features()
         freqs = empirical_freqs(feats)
         t0 = time.perf_counter()
@@ -247,7 +254,7 @@ def fit_warm(b: plk.Batch, freqs, features, ws: WarmStart, ftol: float = 1e-4, x
 
 def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int = 5000, seed: int = 7,
              ftol: float = 1e-4, xtol: float = 1e-3, max_evals: int = 4000, tol: float = 1e-3,
-             method: int = plk.PLK_FIT_NELDER_MEAD) -> dict:
+             method: int = plk.PLK_FIT_NEWTON_START) -> dict:
     """Held-out comparison of the plain default-start fit and the warm fit on
     the same simulated alignments, both with the optimiser ``method``.  Two
     evaluation counts per item: until the stopping rule ends the fit, and
@@ -323,6 +330,13 @@ def main(argv=None):
     res["label_fit_s"] = data.fit_s
     res["label_evals_mean"] = float(data.evals.mean())
     res["training"] = {k: v for k, v in hist.items() if k != "train_loss"}
+    # the same comparison with the Nelder-Mead optimiser (the reference's NLopt method)
+    nm = evaluate(ws, args.eval_items, args.eval_taxa, args.eval_sites, seed=args.seed + 1000,
+                  method=plk.PLK_FIT_NELDER_MEAD)
+    res["nelder_mead"] = {k: nm[k] for k in ("plain_evals_to_optimum_mean", "warm_evals_to_plain_optimum_mean",
+                                             "evals_to_optimum_ratio_warm_over_plain", "plain_evals_mean",
+                                             "warm_evals_mean", "frac_final_within_tol_of_plain", "plain_wall_s",
+                                             "warm_wall_s")}
     print(json.dumps(res))
 
 
