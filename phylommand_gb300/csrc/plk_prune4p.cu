@@ -15,7 +15,9 @@
 // The P(t) and tip tables are read in a paired layout that relayout4p_kernel
 // writes from the FP32 copies of the P(t) kernel:
 //   P:   [node][pair q][row j][state i][2]      (P_{2q}[i][j], P_{2q+1}[i][j])
-//   tip: [tip][pair q][code][state i][2]
+//   tip: [tip][pair q][half][code][state i in the half][2]
+// (each code's row in two 16-byte planes, states 0-1 and 2-3: a 32-byte
+// stride per code would put codes 4 and 8, C and T, on the same banks)
 #include "plk_device.cuh"
 #include "plk_internal.h"
 
@@ -49,7 +51,7 @@ __device__ __forceinline__ void unpack2(u64 v, float& lo, float& hi) {
 template <int KP>
 struct alignas(16) StageP {
     u64 p[2][KP][4][4];          // [child][pair][row j][state i]
-    u64 tip[2][KP][kCodes4][4];  // [child][pair][code][state i]
+    u64 tip[2][KP][2][kCodes4][2];  // [child][pair][half][code][state in the half]
 };
 
 template <int KP, int SPT, bool CODES_SMEM>
@@ -76,11 +78,13 @@ __global__ void relayout4p_kernel(const float* __restrict__ P, const float* __re
             const int q = w / 32, j = (w / 8) % 4, i = (w / 2) % 4, h = w % 2;
             Pp[idx] = P[((node * C + 2 * q + h) * 4 + i) * 4 + j];
         } else {
-            // Tp[((tip*KP + q)*16 + code)*8 + i*2 + h] = tip[((tip*C + 2q+h)*16 + code)*4 + i]
+            // Tp[(((tip*KP + q)*2 + half)*16 + code)*4 + (i % 2)*2 + h] = tip[((tip*C + 2q+h)*16 + code)*4 + i]
+            // with half = i / 2
             const long long t = idx - n_p;
             const long long tp = t / (C * kCodes4 * 4);
             const int w = (int)(t % (C * kCodes4 * 4));
-            const int q = w / (kCodes4 * 8), code = (w / 8) % kCodes4, i = (w / 2) % 4, h = w % 2;
+            const int q = w / (kCodes4 * 8), half = (w / (kCodes4 * 4)) % 2, code = (w / 4) % kCodes4;
+            const int i = 2 * half + (w / 2) % 2, h = w % 2;
             Tp[t] = tip[((tp * C + 2 * q + h) * kCodes4 + code) * 4 + i];
         }
     }
@@ -130,11 +134,11 @@ __device__ __forceinline__ void mv4p(const u64 (*P)[4][4], const u64 x[KP][4], u
 }
 
 template <int KP>
-__device__ __forceinline__ void tip4p(const u64 (*T)[kCodes4][4], int code, u64 out[KP][4]) {
+__device__ __forceinline__ void tip4p(const u64 (*T)[2][kCodes4][2], int code, u64 out[KP][4]) {
 #pragma unroll
     for (int q = 0; q < KP; ++q) {
-        const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(&T[q][code][0]);
-        const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(&T[q][code][2]);
+        const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(&T[q][0][code][0]);
+        const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(&T[q][1][code][0]);
         out[q][0] = a.x; out[q][1] = a.y; out[q][2] = b.x; out[q][3] = b.y;
     }
 }

@@ -283,7 +283,8 @@ def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int 
     pred = ws.predict(feats)
     return {
         "n_items": n_items, "n_taxa": n_taxa, "n_sites": n_sites, "seed": seed, "tol": tol,
-        "method": "quasi-newton" if method == plk.PLK_FIT_QUASI_NEWTON else "nelder-mead",
+        "method": {plk.PLK_FIT_NELDER_MEAD: "nelder-mead", plk.PLK_FIT_QUASI_NEWTON: "quasi-newton",
+                   plk.PLK_FIT_NEWTON_START: "quasi-newton, newton start"}[method],
         "plain_evals_mean": float(plain.evals.mean()), "warm_evals_mean": float(warm.evals.mean()),
         "evals_ratio_warm_over_plain": float(warm.evals.mean() / plain.evals.mean()),
         "plain_evals_to_optimum_mean": float(plain_hit.mean()),

@@ -185,13 +185,13 @@ def test_eval_gtr_matches_single_tree_fp64():
 def test_warm_start_end_to_end_small():
     """Labels from the plain GPU fit, a network trained on them, and the
     warm fit of held-out alignments: fewer evaluations, same optimum."""
-    data = warmstart.make_labelled(800, 16, 1000, seed=21)
+    data = warmstart.make_labelled(3000, 32, 2000, seed=21)
     assert np.all(np.isfinite(data.lnl)) and np.all(np.isfinite(data.labels))
-    ws, hist = warmstart.train(data, epochs=80, seed=3)
+    ws, hist = warmstart.train(data, epochs=60, seed=3)
     assert hist["train_loss"][-1] < 0.5 * hist["train_loss"][0]
     # the network beats predicting the label mean on held-out labels
-    assert np.mean(hist["val_rmse"]) < np.mean(hist["val_rmse_mean_predictor"])
+    assert np.mean(hist["val_rmse"]) < 0.5 * np.mean(hist["val_rmse_mean_predictor"])
     # held out, and with twice the taxa of the training alignments
-    res = warmstart.evaluate(ws, n_items=120, n_taxa=32, n_sites=1000, seed=99)
-    assert res["frac_final_within_tol_of_plain"] >= 0.9, res
-    assert res["evals_to_optimum_ratio_warm_over_plain"] < 0.8, res
+    res = warmstart.evaluate(ws, n_items=200, n_taxa=64, n_sites=2000, seed=99)
+    assert res["frac_final_within_tol_of_plain"] >= 0.95, res
+    assert res["evals_to_optimum_ratio_warm_over_plain"] < 0.75, res
