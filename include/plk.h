@@ -158,11 +158,14 @@ plk_status plk_set_stream(plk_handle* h, void* cuda_stream);
  * reset, and their number. */
 plk_status plk_set_profiling(plk_handle* h, int on);
 plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int reset);
-/* The 4-state FP32 post-order kernel the autotuner chose for the current
- * tree and alignment: 0 = prune4_kernel (partials in registers, P(t) from
+/* The FP32 post-order kernel the autotuner chose for the current tree and
+ * alignment.  4 states: 0 = prune4_kernel (partials in registers, P(t) from
  * global memory), 1 / 2 = prune4s_kernel with 1 / 2 sites per thread (P(t)
- * rows and tip tables staged in shared memory); -1 = not tuned yet or another
- * kernel applies (FP64, S != 4, more than 8 categories). */
+ * rows and tip tables staged in shared memory), 3 / 4 = prune4p_kernel (the
+ * same with the categories in pairs on packed FP32x2), 5 / 6 = prune4p_kernel
+ * reading the tip codes from global memory.  20 states: 1 = prune20_kernel
+ * on CUDA cores, 2 = on tensor cores.  -1 = not tuned yet or another kernel
+ * applies (FP64, other state counts, more than 8 categories). */
 int plk_prune_variant(const plk_handle* h);
 /* Per-site log-likelihoods of the last plk_loglik (n_sites doubles). */
 plk_status plk_site_loglik(plk_handle* h, double* out);

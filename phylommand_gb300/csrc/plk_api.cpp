@@ -321,8 +321,8 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
             std::vector<int> cands = {0};
             for (int v = 1; v <= 2; ++v)
                 if (prune4s_fits(a, v)) cands.push_back(v);
-            for (int v = 3; v <= 4; ++v)
-                if (prune4p_fits(a, v - 2)) cands.push_back(v);
+            for (int v = 3; v <= 6; ++v)
+                if (prune4p_fits(a, (v + 1) % 2 + 1)) cands.push_back(v);
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }

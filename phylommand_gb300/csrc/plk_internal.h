@@ -199,7 +199,8 @@ struct PruneArgs {
     int n_tips;
     // FP32 kernel choice (picked by the autotuner).  4 states: 0 =
     // prune4_kernel, 1/2 = prune4s_kernel with 1/2 sites per thread, 3/4 =
-    // prune4p_kernel (category pairs on FP32x2) with 1/2 sites per thread.
+    // prune4p_kernel (category pairs on FP32x2) with 1/2 sites per thread,
+    // 5/6 = the same reading the tip codes from global memory.
     // 20 states: 0 = prune_generic_kernel, 1 = prune20_kernel on CUDA cores,
     // 2 = prune20_kernel on tensor cores (TF32, three-product split).
     int variant;
@@ -218,7 +219,7 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scra
 // a.scratch for the paired P(t) and tip tables.
 bool prune4p_fits(const PruneArgs& a, int spt);
 size_t prune4p_scratch_bytes(const PruneArgs& a);
-cudaError_t launch_prune4p(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);
+cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* n_blocks, cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
 bool prune4s_fits(const PruneArgs& a, int spt);
 cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);

@@ -515,8 +515,8 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
     const bool fp64 = precision == PLK_FP64;
     if (!fp64 && !store && S == 4 && a.C <= 8 && (a.variant == 1 || a.variant == 2) && prune4s_fits(a, a.variant))
         return launch_prune4s(a, a.variant, n_blocks, st);
-    if (!fp64 && !store && S == 4 && (a.variant == 3 || a.variant == 4) && prune4p_fits(a, a.variant - 2))
-        return launch_prune4p(a, a.variant - 2, n_blocks, st);
+    if (!fp64 && !store && S == 4 && a.variant >= 3 && a.variant <= 6 && prune4p_fits(a, (a.variant + 1) % 2 + 1))
+        return launch_prune4p(a, (a.variant + 1) % 2 + 1, a.variant >= 5, n_blocks, st);
     if (!fp64 && !store && S == 20 && a.variant > 0 && prune20_fits(a, a.variant))
         return launch_prune20(a, a.n_nodes, a.variant, a.scratch, n_blocks, st);
     if (S == 4 && a.C <= 8) {

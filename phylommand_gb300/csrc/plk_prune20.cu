@@ -39,11 +39,13 @@ constexpr int kMaxSlots = 32;       // live node vectors (bit mask)
 
 // staged layouts
 //  CUDA cores:   P: [j][group 4][8] (i = 5 group + r, r < 5), 640 floats
-//                tip: [code][group 4][8], 32 floats per code
+//                tip: [code][group 4][8] + 4 padding, 36 floats per code
 //  tensor cores: P: hi [j 24][i 24] then lo [j 24][i 24], 1152 floats
-//                tip: [code][24], 24 floats per code
+//                tip: [code][24] + 4 padding, 28 floats per code
 __host__ __device__ inline int p_floats(int mode) { return mode == 1 ? 640 : 2 * kRows * kRows; }
-__host__ __device__ inline int tip_floats_per_code(int mode) { return mode == 1 ? 32 : kRows; }
+// per-code strides of the tip tables padded past a multiple of 32 floats, so
+// that the codes of one warp's sites spread over the shared-memory banks
+__host__ __device__ inline int tip_floats_per_code(int mode) { return mode == 1 ? 36 : kRows + 4; }
 
 __host__ __device__ inline int child_floats(int mode, int n_codes) {
     const int p = p_floats(mode), t = n_codes * tip_floats_per_code(mode);
@@ -103,7 +105,7 @@ __global__ void relayout20_kernel(const float* __restrict__ P, const float* __re
             float v = 0.f;
             if (mode == 1) {
                 const int g = w / 8, r = w % 8;
-                if (r < 5) v = src[5 * g + r];
+                if (w < 32 && r < 5) v = src[5 * g + r];
             } else if (w < kS) {
                 v = src[w];
             }
@@ -169,9 +171,10 @@ __device__ __forceinline__ void tip_cc(const float* __restrict__ T, const uint8_
     for (int s = 0; s < 4; ++s) {
         int code = codes[sbase + s];
         code = code < n_codes ? code : 0;
-        const float4 p = *reinterpret_cast<const float4*>(T + (code * 4 + grp) * 8);
+        const float* row = T + code * tip_floats_per_code(1) + grp * 8;
+        const float4 p = *reinterpret_cast<const float4*>(row);
         m[s][0] = p.x; m[s][1] = p.y; m[s][2] = p.z; m[s][3] = p.w;
-        m[s][4] = T[(code * 4 + grp) * 8 + 4];
+        m[s][4] = row[4];
     }
 }
 
@@ -246,7 +249,7 @@ __device__ __forceinline__ void tip_tc(const float* __restrict__ T, const uint8_
             code = code < n_codes ? code : 0;
 #pragma unroll
             for (int nt = 0; nt < 3; ++nt) {
-                const float2 v = *reinterpret_cast<const float2*>(T + code * kRows + nt * 8 + 2 * t);
+                const float2 v = *reinterpret_cast<const float2*>(T + code * tip_floats_per_code(2) + nt * 8 + 2 * t);
                 acc[mt][nt][2 * h] = v.x;
                 acc[mt][nt][2 * h + 1] = v.y;
             }
@@ -511,7 +514,8 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scra
     const size_t pf = p_floats(mode);
     const size_t ps = (size_t)n_nodes * a.C * pf * sizeof(float);
     const size_t pf_max = (size_t)p_floats(2);
-    const size_t ts_max = (size_t)a.n_tips * a.C * a.n_codes * 32 * sizeof(float);
+    const size_t ts_max = (size_t)a.n_tips * a.C * a.n_codes *
+                          std::max(tip_floats_per_code(1), tip_floats_per_code(2)) * sizeof(float);
     unsigned char* base = static_cast<unsigned char*>(scratch);
     P20Args g{};
     g.a = a;

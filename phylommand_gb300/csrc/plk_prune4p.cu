@@ -318,9 +318,12 @@ cudaError_t launch4p(const PruneArgs& a, const float* Pp, const float* Tp, int* 
     return cudaGetLastError();
 }
 
+// codes_global: read the tip codes from global memory (cached) instead of
+// staging the tile's codes in shared memory, for more resident CTAs
 template <int KP, int SPT>
-cudaError_t launch4p_kp(const PruneArgs& a, const float* Pp, const float* Tp, int* n_blocks, cudaStream_t st) {
-    if (smem4p_bytes<KP, SPT, true>(a.n_ops, a.n_tips, a.max_depth) <= 160 * 1024)
+cudaError_t launch4p_kp(const PruneArgs& a, const float* Pp, const float* Tp, bool codes_global, int* n_blocks,
+                        cudaStream_t st) {
+    if (!codes_global && smem4p_bytes<KP, SPT, true>(a.n_ops, a.n_tips, a.max_depth) <= 160 * 1024)
         return launch4p<KP, SPT, true>(a, Pp, Tp, n_blocks, st);
     return launch4p<KP, SPT, false>(a, Pp, Tp, n_blocks, st);
 }
@@ -349,7 +352,7 @@ size_t prune4p_scratch_bytes(const PruneArgs& a) {
     return ((p + 255) & ~(size_t)255) + (size_t)a.n_tips * a.C * kCodes4 * 4 * sizeof(float);
 }
 
-cudaError_t launch_prune4p(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st) {
+cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* n_blocks, cudaStream_t st) {
     if (!prune4p_fits(a, spt) || a.scratch == nullptr) return cudaErrorInvalidValue;
     float* Pp = static_cast<float*>(a.scratch);
     const size_t p = (size_t)a.n_nodes * a.C * 16 * sizeof(float);
@@ -363,9 +366,12 @@ cudaError_t launch_prune4p(const PruneArgs& a, int spt, int* n_blocks, cudaStrea
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     switch (a.C / 2) {
-        case 1: return spt == 1 ? launch4p_kp<1, 1>(a, Pp, Tp, n_blocks, st) : launch4p_kp<1, 2>(a, Pp, Tp, n_blocks, st);
-        case 2: return spt == 1 ? launch4p_kp<2, 1>(a, Pp, Tp, n_blocks, st) : launch4p_kp<2, 2>(a, Pp, Tp, n_blocks, st);
-        default: return spt == 1 ? launch4p_kp<4, 1>(a, Pp, Tp, n_blocks, st) : launch4p_kp<4, 2>(a, Pp, Tp, n_blocks, st);
+        case 1: return spt == 1 ? launch4p_kp<1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
+                                : launch4p_kp<1, 2>(a, Pp, Tp, codes_global, n_blocks, st);
+        case 2: return spt == 1 ? launch4p_kp<2, 1>(a, Pp, Tp, codes_global, n_blocks, st)
+                                : launch4p_kp<2, 2>(a, Pp, Tp, codes_global, n_blocks, st);
+        default: return spt == 1 ? launch4p_kp<4, 1>(a, Pp, Tp, codes_global, n_blocks, st)
+                                 : launch4p_kp<4, 2>(a, Pp, Tp, codes_global, n_blocks, st);
     }
 }
 

@@ -391,7 +391,9 @@ class Handle:
     PRUNE_KERNELS = {
         4: {0: "prune4_kernel", 1: "prune4s_kernel (1 site/thread)", 2: "prune4s_kernel (2 sites/thread)",
             3: "prune4p_kernel (category pairs on FP32x2, 1 site/thread)",
-            4: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread)"},
+            4: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread)",
+            5: "prune4p_kernel (category pairs on FP32x2, 1 site/thread, tip codes from global)",
+            6: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes from global)"},
         20: {1: "prune20_kernel (CUDA cores)", 2: "prune20_kernel (tensor cores, split TF32)"},
     }
 

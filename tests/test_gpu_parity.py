@@ -200,7 +200,7 @@ def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
     sites = []
-    variants = ("0", "1", "2", "3", "4") if C in (2, 4, 8) else ("0", "1", "2")
+    variants = ("0", "1", "2", "3", "4", "5", "6") if C in (2, 4, 8) else ("0", "1", "2")
     for v in variants:
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
