@@ -340,8 +340,10 @@ def run_protein(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
     res = {}
-    names = {"1": "prune20_kernel, CUDA cores", "2": "prune20_kernel, tensor cores (split TF32)", "auto": "autotuned"}
-    for v in ("1", "2", "auto"):
+    names = {"1": "prune20_kernel, CUDA cores, 4 warps/tile", "2": "prune20_kernel, tensor cores (split TF32), 4 warps/tile",
+             "3": "prune20_kernel, CUDA cores, 8 warps/tile", "4": "prune20_kernel, tensor cores (split TF32), 8 warps/tile",
+             "auto": "autotuned"}
+    for v in ("1", "2", "3", "4", "auto"):
         if v == "auto":
             os.environ.pop("PLK_PRUNE_VARIANT", None)
         else:

@@ -292,7 +292,7 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     const bool fused = fused_kernel_applies(h, precision);
     std::vector<int> cands20;
     if (!store && precision == PLK_FP32S && h->S == 20)
-        for (int v = 1; v <= 2; ++v)
+        for (int v = 1; v <= 4; ++v)
             if (prune20_fits(a, v)) cands20.push_back(v);
     if (!cands20.empty()) {
         PLK_CUDA(h, h->d_work.ensure(prune20_scratch_bytes(a, h->n_nodes)), "allocate scratch");

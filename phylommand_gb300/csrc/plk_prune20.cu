@@ -35,7 +35,7 @@ constexpr int kTile = 128;          // sites per CTA
 constexpr int kLD = kTile + 8;      // row stride of a node vector (floats)
 constexpr int kRows = 24;           // node-vector rows (20 states, 4 zero rows)
 constexpr int kThreads = 128;
-constexpr int kMaxSlots = 32;       // live node vectors (bit mask)
+constexpr int kMaxSlots = 16;       // live node vectors (16-bit mask, 4-bit stack entries)
 
 // staged layouts
 //  CUDA cores:   P: [j][group 4][8] (i = 5 group + r, r < 5), 640 floats
@@ -140,35 +140,44 @@ __device__ __forceinline__ void stage_op20(float* dst, const Op& op, int k, cons
             from = g.Ps + ((size_t)(c ? op.e1 : op.e0) * C + k) * (size_t)n;
         }
         float* to = dst + c * cf;
-        for (int q = threadIdx.x; q < n / 4; q += kThreads) cp_async16(to + 4 * q, from + 4 * q);
+        for (int q = threadIdx.x; q < n / 4; q += blockDim.x) cp_async16(to + 4 * q, from + 4 * q);
     }
 }
 
-// CUDA-core child message: m[s][r] for sites sbase + s (s < 4), states 5 grp + r
+// CUDA-core child message: m[s][r] for sites sbase + s (s < SPS), states
+// 5 grp + r
+template <int SPS>
 __device__ __forceinline__ void child_cc(const float* __restrict__ V, const float* __restrict__ Pst, int sbase,
-                                         int grp, float m[4][5]) {
+                                         int grp, float m[SPS][5]) {
 #pragma unroll
-    for (int s = 0; s < 4; ++s)
+    for (int s = 0; s < SPS; ++s)
 #pragma unroll
         for (int r = 0; r < 5; ++r) m[s][r] = 0.f;
 #pragma unroll 4
     for (int j = 0; j < kS; ++j) {
-        const float4 v = *reinterpret_cast<const float4*>(V + j * kLD + sbase);
+        float vs[SPS];
+        if constexpr (SPS == 4) {
+            const float4 v = *reinterpret_cast<const float4*>(V + j * kLD + sbase);
+            vs[0] = v.x; vs[1] = v.y; vs[2] = v.z; vs[3] = v.w;
+        } else {
+            const float2 v = *reinterpret_cast<const float2*>(V + j * kLD + sbase);
+            vs[0] = v.x; vs[1] = v.y;
+        }
         const float4 p = *reinterpret_cast<const float4*>(Pst + (j * 4 + grp) * 8);
         const float p4 = Pst[(j * 4 + grp) * 8 + 4];
-        const float vs[4] = {v.x, v.y, v.z, v.w};
         const float ps[5] = {p.x, p.y, p.z, p.w, p4};
 #pragma unroll
-        for (int s = 0; s < 4; ++s)
+        for (int s = 0; s < SPS; ++s)
 #pragma unroll
             for (int r = 0; r < 5; ++r) m[s][r] = fmaf(ps[r], vs[s], m[s][r]);
     }
 }
 
+template <int SPS>
 __device__ __forceinline__ void tip_cc(const float* __restrict__ T, const uint8_t* __restrict__ codes, int sbase,
-                                       int grp, int n_codes, float m[4][5]) {
+                                       int grp, int n_codes, float m[SPS][5]) {
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
+    for (int s = 0; s < SPS; ++s) {
         int code = codes[sbase + s];
         code = code < n_codes ? code : 0;
         const float* row = T + code * tip_floats_per_code(1) + grp * 8;
@@ -178,16 +187,17 @@ __device__ __forceinline__ void tip_cc(const float* __restrict__ T, const uint8_
     }
 }
 
-// tensor-core child message for a warp's 32 sites: acc[mt][nt][4] in the
-// m16n8 accumulator layout (rows = sites mt*16 + g (+8), cols = states
+// tensor-core child message for a warp's MT x 16 sites: acc[mt][nt][4] in
+// the m16n8 accumulator layout (rows = sites mt*16 + g (+8), cols = states
 // nt*8 + 2t (+1))
+template <int MT>
 __device__ __forceinline__ void child_tc(const float* __restrict__ V, const float* __restrict__ Pst, int wbase,
-                                         int lane, float acc[2][3][4]) {
+                                         int lane, float acc[MT][3][4]) {
     const int g = lane >> 2, t = lane & 3;
     const float* Phi = Pst;
     const float* Plo = Pst + kRows * kRows;
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
+    for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 3; ++nt)
 #pragma unroll
@@ -205,7 +215,7 @@ __device__ __forceinline__ void child_tc(const float* __restrict__ V, const floa
             bl[nt][1] = __float_as_uint(Plo[j1 * kRows + i]);
         }
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
+        for (int mt = 0; mt < MT; ++mt) {
             const int r0 = wbase + mt * 16 + g, r1 = r0 + 8;
             const float x[4] = {V[j0 * kLD + r0], V[j0 * kLD + r1], V[j1 * kLD + r0], V[j1 * kLD + r1]};
             uint32_t ah[4], al[4];
@@ -238,11 +248,12 @@ __device__ __forceinline__ void child_tc(const float* __restrict__ V, const floa
     }
 }
 
+template <int MT>
 __device__ __forceinline__ void tip_tc(const float* __restrict__ T, const uint8_t* __restrict__ codes, int wbase,
-                                       int lane, int n_codes, float acc[2][3][4]) {
+                                       int lane, int n_codes, float acc[MT][3][4]) {
     const int g = lane >> 2, t = lane & 3;
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
+    for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             int code = codes[wbase + mt * 16 + g + 8 * h];
@@ -256,8 +267,15 @@ __device__ __forceinline__ void tip_tc(const float* __restrict__ T, const uint8_
         }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
+// MODE 1 = CUDA cores, 2 = tensor cores; WARPS = 4 or 8 warps per 128-site
+// tile (a warp takes 128 / WARPS sites: CUDA cores 8 site groups of SPS
+// sites x 4 state groups, tensor cores MT m16 tiles)
+template <int MODE, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) prune20_kernel(P20Args g) {
+    constexpr int NT = 32 * WARPS;
+    constexpr int SW = kTile / WARPS;  // sites per warp
+    constexpr int SPS = SW / 8;        // CUDA cores: sites per thread
+    constexpr int MT = SW / 16;        // tensor cores: m16 tiles per warp
     extern __shared__ __align__(16) unsigned char smem[];
     const PruneArgs& a = g.a;
     const int k = blockIdx.y;
@@ -278,10 +296,10 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
     sm.slots = reinterpret_cast<float*>(smem + off);
     const size_t slot_floats = (size_t)kRows * kLD;
 
-    for (int i = tid; i < a.n_ops; i += kThreads) sm.ops[i] = a.ops[i];
+    for (int i = tid; i < a.n_ops; i += NT) sm.ops[i] = a.ops[i];
     {
         constexpr int chunks = kTile / 16;
-        for (int i = tid; i < a.n_tips * chunks; i += kThreads) {
+        for (int i = tid; i < a.n_tips * chunks; i += NT) {
             const int t = i / chunks, q = i % chunks, col = tile0 + 16 * q;
             uint8_t* dst = sm.codes + (size_t)t * kTile + 16 * q;
             if (col < a.site_stride) cp_async16(dst, a.codes + (size_t)t * a.site_stride + col);
@@ -289,7 +307,7 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
         }
     }
     // rows 20..23 of every slot stay zero (the padded K rows of the tensor form)
-    for (int i = tid; i < g.n_slots * (kRows - kS) * kLD; i += kThreads) {
+    for (int i = tid; i < g.n_slots * (kRows - kS) * kLD; i += NT) {
         const int sl = i / ((kRows - kS) * kLD), q = i % ((kRows - kS) * kLD);
         sm.slots[sl * slot_floats + kS * kLD + q] = 0.f;
     }
@@ -299,14 +317,14 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
     if (a.n_ops > 1) stage_op20(sm.stage[1], sm.ops[1], k, g, cf);
     cp_async_commit();
 
-    // uniform slot bookkeeping
-    int stack[kMaxSlots];
+    // uniform slot bookkeeping: the spill stack packs 4-bit slot numbers
+    uint64_t stack = 0;
     int sp = 0, cur = -1;
     uint32_t live = 0;
 
-    // per-thread sites: CUDA cores: 4 sites (sbase..sbase+3), state group grp;
-    // tensor cores: rows g, g+8 of two m16 tiles of the warp's 32 sites
-    const int sbase = warp * 32 + (lane >> 2) * 4;
+    // per-thread sites: CUDA cores: SPS sites (sbase..), state group grp;
+    // tensor cores: rows g, g+8 of the warp's MT m16 tiles
+    const int sbase = warp * SW + (lane >> 2) * SPS;
     const int grp = lane & 3;
     int e_site[4] = {0, 0, 0, 0};
 
@@ -318,26 +336,26 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
         const Op op = sm.ops[o];
         const float* st = sm.stage[o % 3];
         int src0 = -1, src1 = -1;
-        if (op.s0 == kSrcPop) src0 = stack[--sp];
+        if (op.s0 == kSrcPop) src0 = (int)((stack >> (4 * --sp)) & 15u);
         else if (op.s0 == kSrcAcc) src0 = cur;
         if (op.s1 == kSrcAcc) src1 = cur;
         const int dst = __ffs(~live) - 1;  // a slot no live vector uses
         float* D = sm.slots + (size_t)dst * slot_floats;
 
         if constexpr (MODE == 1) {
-            float m0[4][5], m1[4][5];
-            if (op.s0 >= 0) tip_cc(st, sm.codes + (size_t)op.s0 * kTile, sbase, grp, a.n_codes, m0);
-            else child_cc(sm.slots + (size_t)src0 * slot_floats, st, sbase, grp, m0);
+            float m0[SPS][5], m1[SPS][5];
+            if (op.s0 >= 0) tip_cc<SPS>(st, sm.codes + (size_t)op.s0 * kTile, sbase, grp, a.n_codes, m0);
+            else child_cc<SPS>(sm.slots + (size_t)src0 * slot_floats, st, sbase, grp, m0);
             if (op.s1 != kSrcNone) {
-                if (op.s1 >= 0) tip_cc(st + cf, sm.codes + (size_t)op.s1 * kTile, sbase, grp, a.n_codes, m1);
-                else child_cc(sm.slots + (size_t)src1 * slot_floats, st + cf, sbase, grp, m1);
+                if (op.s1 >= 0) tip_cc<SPS>(st + cf, sm.codes + (size_t)op.s1 * kTile, sbase, grp, a.n_codes, m1);
+                else child_cc<SPS>(sm.slots + (size_t)src1 * slot_floats, st + cf, sbase, grp, m1);
 #pragma unroll
-                for (int s = 0; s < 4; ++s)
+                for (int s = 0; s < SPS; ++s)
 #pragma unroll
                     for (int r = 0; r < 5; ++r) m0[s][r] *= m1[s][r];
             }
 #pragma unroll
-            for (int s = 0; s < 4; ++s) {
+            for (int s = 0; s < SPS; ++s) {
                 float mx = m0[s][0];
 #pragma unroll
                 for (int r = 1; r < 5; ++r) mx = fmaxf(mx, m0[s][r]);
@@ -353,19 +371,21 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
                 }
             }
 #pragma unroll
-            for (int r = 0; r < 5; ++r)
-                *reinterpret_cast<float4*>(D + (5 * grp + r) * kLD + sbase) =
-                    make_float4(m0[0][r], m0[1][r], m0[2][r], m0[3][r]);
+            for (int r = 0; r < 5; ++r) {
+                float* row = D + (5 * grp + r) * kLD + sbase;
+                if constexpr (SPS == 4) *reinterpret_cast<float4*>(row) = make_float4(m0[0][r], m0[1][r], m0[2][r], m0[3][r]);
+                else *reinterpret_cast<float2*>(row) = make_float2(m0[0][r], m0[1][r]);
+            }
         } else {
-            const int wbase = warp * 32;
-            float m0[2][3][4], m1[2][3][4];
-            if (op.s0 >= 0) tip_tc(st, sm.codes + (size_t)op.s0 * kTile, wbase, lane, a.n_codes, m0);
-            else child_tc(sm.slots + (size_t)src0 * slot_floats, st, wbase, lane, m0);
+            const int wbase = warp * SW;
+            float m0[MT][3][4], m1[MT][3][4];
+            if (op.s0 >= 0) tip_tc<MT>(st, sm.codes + (size_t)op.s0 * kTile, wbase, lane, a.n_codes, m0);
+            else child_tc<MT>(sm.slots + (size_t)src0 * slot_floats, st, wbase, lane, m0);
             if (op.s1 != kSrcNone) {
-                if (op.s1 >= 0) tip_tc(st + cf, sm.codes + (size_t)op.s1 * kTile, wbase, lane, a.n_codes, m1);
-                else child_tc(sm.slots + (size_t)src1 * slot_floats, st + cf, wbase, lane, m1);
+                if (op.s1 >= 0) tip_tc<MT>(st + cf, sm.codes + (size_t)op.s1 * kTile, wbase, lane, a.n_codes, m1);
+                else child_tc<MT>(sm.slots + (size_t)src1 * slot_floats, st + cf, wbase, lane, m1);
 #pragma unroll
-                for (int mt = 0; mt < 2; ++mt)
+                for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
                     for (int nt = 0; nt < 3; ++nt)
 #pragma unroll
@@ -373,7 +393,7 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
             }
             // per-site maxima: this thread's rows are (mt, h) -> site wbase + mt*16 + g + 8h
 #pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
+            for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     float mx = 0.f;
@@ -395,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
                 }
             const int gg = lane >> 2, t = lane & 3;
 #pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
+            for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
                 for (int nt = 0; nt < 3; ++nt) {
                     const int i = nt * 8 + 2 * t;
@@ -413,7 +433,8 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
         if (src1 >= 0) live &= ~(1u << src1);
         live |= 1u << dst;
         if (op.push) {
-            stack[sp++] = dst;
+            stack = (stack & ~(15ull << (4 * sp))) | ((uint64_t)dst << (4 * sp));
+            ++sp;
             cur = -1;
         } else {
             cur = dst;
@@ -426,7 +447,7 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
     const float* R = sm.slots + (size_t)cur * slot_floats;
     if constexpr (MODE == 1) {
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < SPS; ++s) {
             double l = 0.0;
 #pragma unroll
             for (int r = 0; r < 5; ++r) l = fma((double)R[(5 * grp + r) * kLD + sbase + s], a.root_w[5 * grp + r], l);
@@ -441,10 +462,10 @@ __global__ void __launch_bounds__(kThreads) prune20_kernel(P20Args g) {
     } else {
         const int gg = lane >> 2, t = lane & 3;
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
+        for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int ls = warp * 32 + mt * 16 + gg + 8 * h;
+                const int ls = warp * SW + mt * 16 + gg + 8 * h;
                 double l = 0.0;
                 for (int i = t; i < kS; i += 4) l = fma((double)R[i * kLD + ls], a.root_w[i], l);
                 l += __shfl_xor_sync(0xffffffffu, l, 1);
@@ -492,10 +513,12 @@ size_t smem20_bytes(const PruneArgs& a, int mode) {
 
 }  // namespace
 
-bool prune20_fits(const PruneArgs& a, int mode) {
+// variant 1 / 2: CUDA cores / tensor cores with 4 warps per tile; 3 / 4: the
+// same with 8 warps per tile
+bool prune20_fits(const PruneArgs& a, int variant) {
     if (a.C < 1 || a.n_codes < 1 || a.n_ops < 1 || a.max_depth + 2 > kMaxSlots) return false;
-    if (mode != 1 && mode != 2) return false;
-    return smem20_bytes(a, mode) <= 227 * 1024;
+    if (variant < 1 || variant > 4) return false;
+    return smem20_bytes(a, (variant - 1) % 2 + 1) <= 227 * 1024;
 }
 
 size_t prune20_scratch_bytes(const PruneArgs& a, int n_nodes) {
@@ -508,9 +531,11 @@ size_t prune20_scratch_bytes(const PruneArgs& a, int n_nodes) {
     return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl;
 }
 
-cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scratch, int* n_blocks,
+cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int variant, void* scratch, int* n_blocks,
                            cudaStream_t st) {
-    if (!prune20_fits(a, mode) || scratch == nullptr) return cudaErrorInvalidValue;
+    if (!prune20_fits(a, variant) || scratch == nullptr) return cudaErrorInvalidValue;
+    const int mode = (variant - 1) % 2 + 1;
+    const int warps = variant <= 2 ? 4 : 8;
     const size_t pf = p_floats(mode);
     const size_t ps = (size_t)n_nodes * a.C * pf * sizeof(float);
     const size_t pf_max = (size_t)p_floats(2);
@@ -544,15 +569,14 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scra
     const size_t smem = smem20_bytes(a, mode);
     dim3 grid((a.n_sites + kTile - 1) / kTile, a.C);
     cudaError_t e;
-    if (mode == 1) {
-        e = cudaFuncSetAttribute(prune20_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        prune20_kernel<1><<<grid, kThreads, smem, st>>>(g);
-    } else {
-        e = cudaFuncSetAttribute(prune20_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        prune20_kernel<2><<<grid, kThreads, smem, st>>>(g);
-    }
+    auto run = [&](auto kern) -> cudaError_t {
+        cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (r != cudaSuccess) return r;
+        kern<<<grid, 32 * warps, smem, st>>>(g);
+        return cudaGetLastError();
+    };
+    if (mode == 1) e = warps == 4 ? run(prune20_kernel<1, 4>) : run(prune20_kernel<1, 8>);
+    else e = warps == 4 ? run(prune20_kernel<2, 4>) : run(prune20_kernel<2, 8>);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int blocks = (a.n_sites + kThreads - 1) / kThreads;

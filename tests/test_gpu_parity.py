@@ -240,7 +240,7 @@ def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
     masks[amb] |= np.uint32(1 << 3)                          # two-state ambiguity
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
-    for v in ("1", "2"):
+    for v in ("1", "2", "3", "4"):
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
             got = h.loglik(plk.PLK_FP32S)
