@@ -110,9 +110,19 @@ struct plk_handle {
     struct EvSet { cudaEvent_t e[4]; };
     std::vector<EvSet> evs;
     size_t ev_used = 0;
+    // pinned arena of small host-to-device uploads, and the event after the
+    // last copy out of it; a pinned word for the tip-check flag
+    char* arena = nullptr;
+    size_t arena_off = 0;
+    cudaEvent_t arena_done = nullptr;
+    int* h_flag = nullptr;
+    bool flag_pending = false;
     ~plk_handle() {
         for (auto& s : evs)
             for (auto& e : s.e) cudaEventDestroy(e);
+        if (arena) cudaFreeHost(arena);
+        if (arena_done) cudaEventDestroy(arena_done);
+        if (h_flag) cudaFreeHost(h_flag);
     }
 };
 
@@ -135,12 +145,33 @@ plk_status cuda_fail(plk_handle* h, cudaError_t e, const char* what) {
         if (_e != cudaSuccess) return cuda_fail(h, _e, what); \
     } while (0)
 
+constexpr size_t kArenaBytes = 1 << 20;
+
+// Host-to-device upload of v into b on the handle's stream.  Small arrays go
+// through the handle's pinned arena, so the copy is asynchronous (a pageable
+// copy stages synchronously); the arena starts over once the event after its
+// last copy has completed.  Larger arrays are copied from pageable memory.
 template <typename T>
-cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t st) {
+cudaError_t upload(plk_handle* h, DevBuf& b, const std::vector<T>& v) {
     cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
     if (e != cudaSuccess) return e;
     if (v.empty()) return cudaSuccess;
-    return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+    const size_t bytes = sizeof(T) * v.size();
+    if (bytes > kArenaBytes) return cudaMemcpyAsync(b.p, v.data(), bytes, cudaMemcpyHostToDevice, h->stream);
+    if (!h->arena) {
+        if ((e = cudaMallocHost(&h->arena, kArenaBytes)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&h->arena_done, cudaEventDisableTiming)) != cudaSuccess) return e;
+        h->arena_off = 0;
+    }
+    if (h->arena_off + bytes > kArenaBytes) {
+        if ((e = cudaEventSynchronize(h->arena_done)) != cudaSuccess) return e;
+        h->arena_off = 0;
+    }
+    char* src = h->arena + h->arena_off;
+    std::memcpy(src, v.data(), bytes);
+    h->arena_off = (h->arena_off + bytes + 15) & ~(size_t)15;
+    if ((e = cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) return e;
+    return cudaEventRecord(h->arena_done, h->stream);
 }
 
 plk_status ready(plk_handle* h) {
@@ -162,7 +193,7 @@ plk_status refresh_teff(plk_handle* h) {
     h->t_eff.assign(h->n_nodes, 0.0);
     effective_lengths(h->n_nodes, h->left.data(), h->right.data(), h->root, h->bl.data(), h->root_quirk,
                       h->cut_off, h->cut_rate, h->clade_of_node, h->clade_rate, h->t_eff.data());
-    PLK_CUDA(h, upload(h->d_teff, h->t_eff, h->stream), "upload effective lengths");
+    PLK_CUDA(h, upload(h, h->d_teff, h->t_eff), "upload effective lengths");
     h->teff_dirty = false;
     return PLK_OK;
 }
@@ -418,6 +449,7 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
     h->n_sites_full = n_sites;
     h->site_pattern.clear();
     h->pattern_w.clear();
+    h->flag_pending = false;
     std::vector<uint32_t> pmasks;
     if (h->patterns) {
         // distinct columns in order of first appearance, with their counts
@@ -452,7 +484,7 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
         pmasks.resize((size_t)n_tips * n_pat);
         for (int t = 0; t < n_tips; ++t)
             for (int p = 0; p < n_pat; ++p) pmasks[(size_t)t * n_pat + p] = masks[(size_t)t * n_sites + first[p]];
-        PLK_CUDA(h, upload(h->d_pattern_w, h->pattern_w, h->stream), "upload pattern weights");
+        PLK_CUDA(h, upload(h, h->d_pattern_w, h->pattern_w), "upload pattern weights");
         masks = pmasks.data();
         n_sites = n_pat;
     }
@@ -473,11 +505,11 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
         PLK_CUDA(h, launch_encode_small(h->d_mask_raw.as<uint32_t>(), n_tips, n_sites, code_stride(n_sites), all,
                                         h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->stream),
                  "encode kernel launch");
-        int flag = 0;
-        PLK_CUDA(h, cudaMemcpyAsync(&flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
-        PLK_CUDA(h, upload(h->d_code_mask, table, h->stream), "upload code table");
-        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "encode tip codes");
-        bad = flag != 0;
+        // the empty-cell flag comes back with the next result fetch (no wait here)
+        if (!h->h_flag) PLK_CUDA(h, cudaMallocHost(&h->h_flag, sizeof(int)), "allocate flag");
+        PLK_CUDA(h, cudaMemcpyAsync(h->h_flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
+        PLK_CUDA(h, upload(h, h->d_code_mask, table), "upload code table");
+        h->flag_pending = true;
     } else {
         const size_t stride = (size_t)code_stride(n_sites);
         std::vector<uint8_t> codes((size_t)n_tips * stride, 0);
@@ -495,8 +527,8 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
             } else c = it->second;
             codes[(i / n_sites) * stride + (i % n_sites)] = (uint8_t)c;
         }
-        PLK_CUDA(h, upload(h->d_codes, codes, h->stream), "upload tip codes");
-        PLK_CUDA(h, upload(h->d_code_mask, table, h->stream), "upload code table");
+        PLK_CUDA(h, upload(h, h->d_codes, codes), "upload tip codes");
+        PLK_CUDA(h, upload(h, h->d_code_mask, table), "upload code table");
         PLK_CUDA(h, cudaStreamSynchronize(h->stream), "upload tip codes");
     }
     h->n_tips = n_tips;
@@ -533,12 +565,11 @@ plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* 
     h->n_nodes = n_nodes;
     h->tree_tips = n_leaves;
     h->prog = build_program(n_leaves, n_nodes, left, right, root, rank);
-    PLK_CUDA(h, upload(h->d_ops, h->prog.ops, h->stream), "upload program");
-    PLK_CUDA(h, upload(h->d_order, post, h->stream), "upload order");
-    PLK_CUDA(h, upload(h->d_left, h->left, h->stream), "upload tree");
-    PLK_CUDA(h, upload(h->d_right, h->right, h->stream), "upload tree");
-    PLK_CUDA(h, upload(h->d_rank, rank, h->stream), "upload tree");
-    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "upload tree");
+    PLK_CUDA(h, upload(h, h->d_ops, h->prog.ops), "upload program");
+    PLK_CUDA(h, upload(h, h->d_order, post), "upload order");
+    PLK_CUDA(h, upload(h, h->d_left, h->left), "upload tree");
+    PLK_CUDA(h, upload(h, h->d_right, h->right), "upload tree");
+    PLK_CUDA(h, upload(h, h->d_rank, rank), "upload tree");
     // default rate model: the reference's empty rate_model
     h->root_quirk = true;
     h->cut_off.clear();
@@ -604,14 +635,13 @@ plk_status plk_set_model(plk_handle* h, int S, const double* Q, const double* ro
             return fail(h, PLK_ERR_ARG, "eigen form needs positive root weights (frequencies)");
         h->p_kind = 1;
     } else h->p_kind = 2;
-    PLK_CUDA(h, upload(h->d_Q, h->Q, h->stream), "upload model");
-    PLK_CUDA(h, upload(h->d_rootw, h->root_w, h->stream), "upload model");
-    PLK_CUDA(h, upload(h->d_catr, h->cat_rate, h->stream), "upload model");
-    PLK_CUDA(h, upload(h->d_catw, h->cat_w, h->stream), "upload model");
-    PLK_CUDA(h, upload(h->d_lam, h->lam, h->stream), "upload model");
-    PLK_CUDA(h, upload(h->d_L, h->L, h->stream), "upload model");
-    PLK_CUDA(h, upload(h->d_R, h->R, h->stream), "upload model");
-    PLK_CUDA(h, cudaStreamSynchronize(h->stream), "upload model");
+    PLK_CUDA(h, upload(h, h->d_Q, h->Q), "upload model");
+    PLK_CUDA(h, upload(h, h->d_rootw, h->root_w), "upload model");
+    PLK_CUDA(h, upload(h, h->d_catr, h->cat_rate), "upload model");
+    PLK_CUDA(h, upload(h, h->d_catw, h->cat_w), "upload model");
+    PLK_CUDA(h, upload(h, h->d_lam, h->lam), "upload model");
+    PLK_CUDA(h, upload(h, h->d_L, h->L), "upload model");
+    PLK_CUDA(h, upload(h, h->d_R, h->R), "upload model");
     h->have_model = true;
     h->have_lnl = false;
     return PLK_OK;
@@ -654,6 +684,11 @@ plk_status plk_loglik_result(plk_handle* h, double* lnl_out) {
     PLK_CUDA(h, cudaMemcpyAsync(&v, h->d_lnl.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy lnL");
     PLK_CUDA(h, cudaStreamSynchronize(h->stream), "likelihood kernels");
     h->lnl_pending = false;
+    if (h->flag_pending) {  // the alignment's empty-cell check, read back with this result
+        h->flag_pending = false;
+        h->bad_tip = *h->h_flag != 0;
+    }
+    if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
     *lnl_out = v;
     h->have_lnl = true;
     if (!std::isfinite(v)) return fail(h, PLK_ERR_NUMERIC, "log-likelihood is not finite");
@@ -730,6 +765,11 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
     if (!out) return fail(h, PLK_ERR_ARG, "out is NULL");
     if (mode != PLK_NODES_COND && mode != PLK_NODES_MARGINAL) return fail(h, PLK_ERR_ARG, "unknown node-state mode");
     if (precision != PLK_FP64 && precision != PLK_FP32S) return fail(h, PLK_ERR_ARG, "unknown precision");
+    if (h->flag_pending) {  // the alignment's empty-cell check
+        PLK_CUDA(h, cudaStreamSynchronize(h->stream), "tip check");
+        h->flag_pending = false;
+        h->bad_tip = *h->h_flag != 0;
+    }
     if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
     if ((s = build_pmats(h)) != PLK_OK) return s;
     void* cond = nullptr;
