@@ -243,26 +243,36 @@ def run_ours(args, world, rank, local):
 
     # end to end through the C ABI with host buffers: upload the alignment,
     # tree and model from pinned host memory, evaluate, read the lnL back
+    # (byte masks, plk_set_alignment8; the 32-bit masks of plk_set_alignment
+    # are timed the same way beside it)
     h.set_stream(None)
-    pinned = torch.empty(w.masks.shape, dtype=torch.int32, pin_memory=True)
-    masks_pinned = pinned.numpy().view(np.uint32)
-    masks_pinned[...] = w.masks
-    h2d = masks_pinned.nbytes + w.left.nbytes + w.right.nbytes + w.bl.nbytes + w.Q.nbytes + w.freqs.nbytes \
+    pinned8 = torch.empty(w.masks.shape, dtype=torch.uint8, pin_memory=True)
+    masks8 = pinned8.numpy()
+    masks8[...] = w.masks.astype(np.uint8)
+    pinned32 = torch.empty(w.masks.shape, dtype=torch.int32, pin_memory=True)
+    masks32 = pinned32.numpy().view(np.uint32)
+    masks32[...] = w.masks
+    small = w.left.nbytes + w.right.nbytes + w.bl.nbytes + w.Q.nbytes + w.freqs.nbytes \
         + w.cat_rates.nbytes + w.cat_weights.nbytes
     e2e_steps = max(3, args.steps // 2)
-    for _ in range(2):
-        h.set_alignment(masks_pinned, w.n_states)
-        h.loglik(plk.PLK_FP32S)
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        h.set_alignment(masks_pinned, w.n_states)
-        h.set_tree(w.left, w.right, w.bl)
-        h.set_rate_model(False)
-        h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
-        lnl_e2e = h.loglik(plk.PLK_FP32S)
-    e2e_s = reduce_max(world, time.perf_counter() - t0, dev)
-    e2e_value = world * e2e_steps / e2e_s
+
+    def e2e_run(masks):
+        for _ in range(2):
+            h.set_alignment(masks, w.n_states)
+            h.loglik(plk.PLK_FP32S)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            h.set_alignment(masks, w.n_states)
+            h.set_tree(w.left, w.right, w.bl)
+            h.set_rate_model(False)
+            h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
+            lnl = h.loglik(plk.PLK_FP32S)
+        return world * e2e_steps / reduce_max(world, time.perf_counter() - t0, dev), lnl
+
+    e2e_value, lnl_e2e = e2e_run(masks8)
+    e2e32_value, _ = e2e_run(masks32)
+    h2d = masks8.nbytes + small
     h.close()
 
     if rank != 0:
@@ -309,8 +319,13 @@ def run_ours(args, world, rank, local):
                          "sample": f"{sample} of {w.n_sites} sites, P(t) rebuilt per (site, edge, category) by the "
                                    f"reference's Taylor-plus-20-squarings, scaled linearly to all sites"},
         "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 12,
-                "path": "plk_set_alignment + plk_set_tree + plk_set_rate_model + plk_set_model + plk_loglik"},
-        "gpu_launches": 3 * args.steps,
+                "path": "plk_set_alignment8 (pinned byte masks) + plk_set_tree + plk_set_rate_model + "
+                        "plk_set_model + plk_loglik",
+                "with_32bit_masks": {"value": e2e32_value, "h2d_bytes_per_step": int(masks32.nbytes + small),
+                                     "path": "plk_set_alignment (pinned 32-bit masks) + the same calls"}},
+        # per evaluation: P(t), the post-order pass, the reduction, and for the
+        # paired kernel the relayout of P(t) and the tip tables
+        "gpu_launches": (4 if h_variant.startswith("prune4p") else 3) * args.steps,
         "error_vs_fp64_oracle": {"abs": abs(lnl_timed - orc.lnl), "rel": abs(lnl_timed - orc.lnl) / abs(orc.lnl),
                                  "fp64_engine_rel": abs(lnl64 - orc.lnl) / abs(orc.lnl),
                                  "e2e_rel": abs(lnl_e2e - orc.lnl) / abs(orc.lnl)},
@@ -389,6 +404,41 @@ def run_protein(args):
                          "unit": "GB/s", "frac": best["achieved_gbs_algorithmic"] / hbm_peak, "traffic": None,
                          "algorithmic_bytes_per_launch": bytes_per_eval, "peak_source": peak_src},
             "algorithmic_flops_per_eval": flops_per_eval, "variants": res}
+    print(json.dumps(line), flush=True)
+
+
+def run_warmstart(args):
+    """Time-to-ML-fit, learned vs plain: 10,000 simulated 32 x 2,000 training
+    alignments labelled by the GPU fit, the network trained on them, then
+    1,000 held-out 64 x 5,000 alignments fitted from the default start and
+    from the network's start (the Newton-start quasi-Newton fit); evaluations
+    until each fit first comes within 1e-3 of the plain fit's optimum."""
+    import tempfile
+    from phylommand_gb300 import warmstart as W
+    t0 = time.perf_counter()
+    data = W.make_labelled(args.ws_train, 32, 2000, seed=1)
+    ws, hist = W.train(data, epochs=200, seed=1)
+    prep_s = time.perf_counter() - t0
+    r = W.evaluate(ws, args.ws_eval, 64, 5000, seed=1001)
+    with tempfile.TemporaryDirectory() as d:  # the checkpoint round trip
+        ws.save(os.path.join(d, "w.npz"))
+        again = W.WarmStart.load(os.path.join(d, "w.npz"))
+        feats = np.random.default_rng(0).random((4, W.N_FEATURES)).astype(np.float32)
+        same = bool(np.array_equal(ws.predict(feats), again.predict(feats)))
+    line = {"metric": "lnL evaluations to reach the ML fit, learned start / default start",
+            "value": r["evals_to_optimum_ratio_warm_over_plain"], "unit": "ratio", "higher_is_better": False,
+            "n_gpus": 1, "dtype": "f32 lnL, bf16 network", "data": "synthetic",
+            "config": {"workload": "train 10,000 x (32 taxa, 2,000 sites); evaluate 1,000 x (64 taxa, 5,000 sites); "
+                                   "GTR+Gamma4 priors", "train_items": args.ws_train, "eval_items": args.ws_eval,
+                       "optimiser": r["method"]},
+            "plain": {"evals_to_optimum": r["plain_evals_to_optimum_mean"], "evals_to_stop": r["plain_evals_mean"],
+                      "wall_s": r["plain_wall_s"], "rounds": r["plain_rounds"]},
+            "warm": {"evals_to_plain_optimum": r["warm_evals_to_plain_optimum_mean"],
+                     "evals_to_stop": r["warm_evals_mean"], "wall_s": r["warm_wall_s"], "rounds": r["warm_rounds"]},
+            "time_to_fit_ratio": r["wall_ratio_warm_over_plain"],
+            "frac_final_within_1e-3_of_plain": r["frac_final_within_tol_of_plain"],
+            "max_lnl_deficit": r["max_lnl_deficit"], "labelling_and_training_s": prep_s,
+            "label_fit_s": data.fit_s, "train_s": hist["train_s"], "checkpoint_round_trip": same}
     print(json.dumps(line), flush=True)
 
 
@@ -481,16 +531,22 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dna", choices=["dna", "nni", "protein"],
-                    help="dna: the headline workload; nni: the uneven batch with NNI neighbours")
+    ap.add_argument("--workload", default="dna", choices=["dna", "nni", "protein", "warmstart"],
+                    help="dna: the headline workload; nni: the uneven batch with NNI neighbours; protein: 20 "
+                         "states; warmstart: time-to-ML-fit with the learned start")
     ap.add_argument("--nni-items", type=int, default=512)
     ap.add_argument("--nni-sample", type=int, default=24)
+    ap.add_argument("--ws-train", type=int, default=10000)
+    ap.add_argument("--ws-eval", type=int, default=1000)
     args = ap.parse_args()
     if args.workload == "nni":
         run_nni(args)
         return
     if args.workload == "protein":
         run_protein(args)
+        return
+    if args.workload == "warmstart":
+        run_warmstart(args)
         return
     world, rank, local = (1, 0, 0) if args.impl == "reference" else dist_setup(args.gpus)
     if args.impl == "reference":

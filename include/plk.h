@@ -96,6 +96,12 @@ int plk_api_version(void);
  * Replaces simpleML::set_char for every (tip, site). */
 plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states,
                              const uint32_t* masks);
+/* The same with one byte per cell (bit s = state s allowed), for alphabets
+ * of at most 8 states: a quarter of the host-to-device traffic.  For <= 4
+ * states without site patterns the bytes go to the device as they are and are
+ * encoded there; otherwise they are widened on the host first. */
+plk_status plk_set_alignment8(plk_handle* h, int n_tips, int n_sites, int n_states,
+                              const uint8_t* masks);
 
 /* Site patterns (off by default, as the reference evaluates every site; its
  * unfinished MLtree.h declares n_patterns / char_per_pattern for this).  On:

@@ -441,9 +441,16 @@ plk_status plk_set_patterns(plk_handle* h, int on) {
 
 int plk_n_patterns(const plk_handle* h) { return h && h->have_aln ? h->n_sites : 0; }
 
-plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states, const uint32_t* masks) {
+}  // extern "C"
+
+namespace {
+
+// plk_set_alignment with the state sets as 32-bit masks, or (masks8, only for
+// n_states <= 4 without site patterns) as bytes
+plk_status set_alignment_impl(plk_handle* h, int n_tips, int n_sites, int n_states, const uint32_t* masks,
+                              const uint8_t* masks8) {
     if (!h) return PLK_ERR_ARG;
-    if (n_tips < 1 || n_sites < 1 || n_states < 1 || n_states > kMaxStates || !masks)
+    if (n_tips < 1 || n_sites < 1 || n_states < 1 || n_states > kMaxStates || (!masks && !masks8))
         return fail(h, PLK_ERR_ARG, "alignment needs n_tips >= 1, n_sites >= 1, 1 <= n_states <= 24");
     PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     h->n_sites_full = n_sites;
@@ -496,13 +503,15 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
         // small alphabets: the code is the state set itself, encoded on the
         // device straight from the caller's masks
         for (uint32_t c = 0; c < (1u << n_states); ++c) table.push_back(c);
-        PLK_CUDA(h, h->d_mask_raw.ensure(n_cells * sizeof(uint32_t)), "allocate mask staging");
+        const int eb = masks8 ? 1 : (int)sizeof(uint32_t);
+        PLK_CUDA(h, h->d_mask_raw.ensure(n_cells * eb), "allocate mask staging");
         PLK_CUDA(h, h->d_codes.ensure((size_t)n_tips * code_stride(n_sites)), "allocate tip codes");
         PLK_CUDA(h, h->d_flag.ensure(sizeof(int)), "allocate flag");
-        PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks, n_cells * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream),
+        PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks8 ? (const void*)masks8 : (const void*)masks, n_cells * eb,
+                                    cudaMemcpyHostToDevice, h->stream),
                  "upload masks");
         PLK_CUDA(h, cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "clear flag");
-        PLK_CUDA(h, launch_encode_small(h->d_mask_raw.as<uint32_t>(), n_tips, n_sites, code_stride(n_sites), all,
+        PLK_CUDA(h, launch_encode_small(h->d_mask_raw.p, eb, n_tips, n_sites, code_stride(n_sites), all,
                                         h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->stream),
                  "encode kernel launch");
         // the empty-cell flag comes back with the next result fetch (no wait here)
@@ -541,6 +550,24 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
     h->variant = -1;
     h->have_lnl = false;
     return PLK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_states, const uint32_t* masks) {
+    return set_alignment_impl(h, n_tips, n_sites, n_states, masks, nullptr);
+}
+
+plk_status plk_set_alignment8(plk_handle* h, int n_tips, int n_sites, int n_states, const uint8_t* masks) {
+    if (!h) return PLK_ERR_ARG;
+    if (n_tips < 1 || n_sites < 1 || n_states < 1 || n_states > 8 || !masks)
+        return fail(h, PLK_ERR_ARG, "byte masks need n_tips >= 1, n_sites >= 1, 1 <= n_states <= 8");
+    if (n_states <= 4 && !h->patterns) return set_alignment_impl(h, n_tips, n_sites, n_states, nullptr, masks);
+    // more states, or patterns compressed on the host: through the 32-bit path
+    const std::vector<uint32_t> wide(masks, masks + (size_t)n_tips * n_sites);
+    return set_alignment_impl(h, n_tips, n_sites, n_states, wide.data(), nullptr);
 }
 
 plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* right, const double* bl) {

@@ -546,8 +546,9 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
 // Tip encoding for alphabets of <= 4 states: the code is the state set
 // itself; a cell with no allowed state raises the flag (check_nodes).
 // =========================================================================
-__global__ void encode_small_kernel(const uint32_t* __restrict__ masks, int n_tips, int n_sites, int stride,
-                                    uint32_t all, uint8_t* __restrict__ codes, int* __restrict__ bad) {
+template <typename M>
+__global__ void encode_small_kernel(const M* __restrict__ masks, int n_tips, int n_sites, int stride, uint32_t all,
+                                    uint8_t* __restrict__ codes, int* __restrict__ bad) {
     // one thread per 4 consecutive sites of a row; rows of `codes` are padded
     // to `stride` (a multiple of 16) and the padding is written as 0
     const int chunks = stride / 4;
@@ -556,13 +557,13 @@ __global__ void encode_small_kernel(const uint32_t* __restrict__ masks, int n_ti
     int any_bad = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += step) {
         const int t = (int)(i / chunks), s0 = (int)(i % chunks) * 4;
-        const uint32_t* row = masks + (size_t)t * n_sites;
+        const M* row = masks + (size_t)t * n_sites;
         uint8_t c[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int s = s0 + j;
             if (s < n_sites) {
-                const uint32_t m = row[s] & all;
+                const uint32_t m = (uint32_t)row[s] & all;
                 any_bad |= (m == 0);
                 c[j] = (uint8_t)m;
             } else {
@@ -574,14 +575,19 @@ __global__ void encode_small_kernel(const uint32_t* __restrict__ masks, int n_ti
     if (__any_sync(0xffffffffu, any_bad) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
 }
 
-cudaError_t launch_encode_small(const uint32_t* masks, int n_tips, int n_sites, int stride, uint32_t all,
+cudaError_t launch_encode_small(const void* masks, int elem_bytes, int n_tips, int n_sites, int stride, uint32_t all,
                                 uint8_t* codes, int* bad, cudaStream_t st) {
     const int threads = 256;
     const size_t total = (size_t)n_tips * (stride / 4);
     size_t blocks = (total + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    encode_small_kernel<<<(unsigned)blocks, threads, 0, st>>>(masks, n_tips, n_sites, stride, all, codes, bad);
+    if (elem_bytes == 1)
+        encode_small_kernel<uint8_t><<<(unsigned)blocks, threads, 0, st>>>(static_cast<const uint8_t*>(masks), n_tips,
+                                                                          n_sites, stride, all, codes, bad);
+    else
+        encode_small_kernel<uint32_t><<<(unsigned)blocks, threads, 0, st>>>(static_cast<const uint32_t*>(masks),
+                                                                           n_tips, n_sites, stride, all, codes, bad);
     return cudaGetLastError();
 }
 

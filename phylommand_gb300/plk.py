@@ -39,7 +39,7 @@ PLK_FIT_NEWTON_START = 2
 # Every symbol include/plk.h declares (checked by the tests).
 EXPORTS = [
     "plk_create", "plk_destroy", "plk_last_error", "plk_status_string", "plk_api_version",
-    "plk_set_alignment", "plk_set_tree", "plk_set_rate_model", "plk_set_model",
+    "plk_set_alignment", "plk_set_alignment8", "plk_set_tree", "plk_set_rate_model", "plk_set_model",
     "plk_loglik", "plk_site_loglik", "plk_node_states", "plk_n_internal",
     "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
@@ -88,6 +88,7 @@ def lib() -> ctypes.CDLL:
     L.plk_status_string.restype = ctypes.c_char_p
     L.plk_api_version.argtypes = []
     L.plk_set_alignment.argtypes = [hp, c_int, c_int, c_int, u32p]
+    L.plk_set_alignment8.argtypes = [hp, c_int, c_int, c_int, ctypes.POINTER(ctypes.c_uint8)]
     L.plk_set_tree.argtypes = [hp, c_int, ip, ip, dp]
     L.plk_set_rate_model.argtypes = [hp, c_int, c_int, fp, fp, ip, c_int, fp]
     L.plk_set_model.argtypes = [hp, c_int, dp, dp, c_int, c_int, dp, dp, c_int]
@@ -327,8 +328,16 @@ class Handle:
         return int(lib().plk_n_patterns(self._h))
 
     def set_alignment(self, masks: np.ndarray, n_states: int) -> None:
-        m = np.ascontiguousarray(masks, dtype=np.uint32)
-        _check(lib().plk_set_alignment(self._h, m.shape[0], m.shape[1], int(n_states), _p(m, ctypes.c_uint32)), self._h)
+        """State-set masks [n_tips, n_sites]; uint8 masks (<= 8 states) take
+        the byte path (plk_set_alignment8), anything else the 32-bit one."""
+        if isinstance(masks, np.ndarray) and masks.dtype == np.uint8 and masks.flags.c_contiguous:
+            _check(lib().plk_set_alignment8(self._h, masks.shape[0], masks.shape[1], int(n_states),
+                                            _p(masks, ctypes.c_uint8)), self._h)
+            m = masks
+        else:
+            m = np.ascontiguousarray(masks, dtype=np.uint32)
+            _check(lib().plk_set_alignment(self._h, m.shape[0], m.shape[1], int(n_states), _p(m, ctypes.c_uint32)),
+                   self._h)
         self.n_states = int(n_states)
         self.n_sites = int(m.shape[1])
 

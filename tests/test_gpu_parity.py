@@ -181,6 +181,32 @@ def test_call_order_and_argument_errors():
         assert st == plk.PLK_ERR_ARG
 
 
+@pytest.mark.parametrize("S,patterns", [(4, False), (4, True), (3, False), (6, False)])
+def test_byte_masks_match_32bit_masks(S, patterns):
+    """plk_set_alignment8 (device encoding for <= 4 states, host widening
+    otherwise or with patterns) gives the same bits as plk_set_alignment,
+    and reports an empty cell the same way."""
+    rng = np.random.default_rng(S + 10 * patterns)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 19, 777, S=S, C=4)
+    out = []
+    for m in (masks.astype(np.uint32), masks.astype(np.uint8)):
+        h = plk.Handle()
+        h.set_patterns(patterns)
+        h.set_alignment(m, S)
+        h.set_tree(left, right, bl)
+        h.set_rate_model(False)
+        h.set_model(Q, f, True, cr, cw, plk.PLK_P_EXACT)
+        out.append((h.loglik(plk.PLK_FP64), h.site_loglik(), h.loglik(plk.PLK_FP32S)))
+        bad = m.copy()
+        bad[3, 5] = 0
+        h.set_alignment(bad, S)
+        st, _ = h.loglik_status()
+        assert st == plk.PLK_ERR_TIP
+        h.close()
+    assert out[0][0] == out[1][0] and out[0][2] == out[1][2]
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
 def test_repeat_calls_are_deterministic():
     fx = H.load_fixture("syn_gtr_gamma_ambig")
     with H.engine_for_fixture(fx, p_mode=plk.PLK_P_EXACT) as h:
