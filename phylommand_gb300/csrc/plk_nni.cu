@@ -259,19 +259,14 @@ __global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
             const int mcount = min(32, it.n_moves - m0);
             for (int mi = 0; mi < mcount; ++mi) {
                 const NniMoveDev mv = b.moves[it.moves_off + m0 + mi];
-                double s = valid ? move_site_lnl<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO) : 0.0, c = 0.0;
+                // a warp's 32 site terms in plain FP64 (error ~1e-15 relative);
+                // the compensated sums start across warps and tiles
+                double s = valid ? move_site_lnl<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO) : 0.0;
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const double os = __shfl_down_sync(0xffffffffu, s, off);
-                    const double oc = __shfl_down_sync(0xffffffffu, c, off);
-                    double ns, e;
-                    two_sum(s, os, ns, e);
-                    s = ns;
-                    c = c + oc + e;
-                }
+                for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
                 if (lane == 0) {
                     s_red[warp][mi][0] = s;
-                    s_red[warp][mi][1] = c;
+                    s_red[warp][mi][1] = 0.0;
                 }
             }
             __syncthreads();
