@@ -158,7 +158,9 @@ plk_status plk_loglik_result(plk_handle* h, double* lnl_out);
  * void*); NULL returns to the handle's own stream. */
 plk_status plk_set_stream(plk_handle* h, void* cuda_stream);
 /* Kernel timing: with profiling on, every evaluation records CUDA events on
- * the handle's stream around its P(t), post-order and reduction kernels.
+ * the handle's stream around its P(t) kernel, its post-order pass (whose last
+ * CTA also adds up the total) and the site-pattern weighting (zero time
+ * without site patterns).
  * plk_kernel_times waits for the stream and returns the summed milliseconds
  * of each phase (ms_out[3]) over the evaluations recorded since the last
  * reset, and their number. */
@@ -169,8 +171,9 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * global memory), 1 / 2 = prune4s_kernel with 1 / 2 sites per thread (P(t)
  * rows and tip tables staged in shared memory), 3 / 4 = prune4p_kernel (the
  * same with the categories in pairs on packed FP32x2), 5 / 6 = prune4p_kernel
- * reading the tip codes from global memory.  20 states: 1 = prune20_kernel
- * on CUDA cores, 2 = on tensor cores.  -1 = not tuned yet or another kernel
+ * reading the tip codes from global memory.  20 states: 1 / 2 =
+ * prune20_kernel on CUDA cores / tensor cores with 4 warps per tile, 3 / 4 =
+ * the same with 8 warps.  -1 = not tuned yet or another kernel
  * applies (FP64, other state counts, more than 8 categories). */
 int plk_prune_variant(const plk_handle* h);
 /* Per-site log-likelihoods of the last plk_loglik (n_sites doubles). */
@@ -234,6 +237,11 @@ plk_status plk_batch_loglik(plk_batch* b, double* lnl_out);
  * post-order launch, and whether evaluations replay a CUDA graph. */
 plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid, double* ms,
                             int* uses_graph);
+/* The autotuned form of the post-order kernel: paired = 1 when categories
+ * go in pairs on the packed FP32x2 pipe (2, 4 or 8 categories; same per-site
+ * bits as one at a time), codes_smem = 1 when each tile's tip codes are
+ * staged in shared memory rather than read from global memory. */
+plk_status plk_batch_form(const plk_batch* b, int* paired, int* codes_smem);
 
 /* NNI neighbours of every item: the trees one nearest-neighbour interchange
  * away, with branch lengths kept on their edges -- what `treebender --nni`
@@ -331,7 +339,10 @@ plk_status plk_batch_edge_derivatives(plk_batch* b, double* out);
  * step along the slope where the curvature is not negative; lengths within
  * [1e-8, 20], at most x10 per step; of the two root edges only the first
  * moves, their sum being what counts), halving the item's steps until its lnL
- * does not drop.  An item stops when an iteration gains less than tol.
+ * does not drop.  An item stops when the Newton model predicts less than tol
+ * of lnL gain from another step (sum over its edges of d1^2 / (2 |d2|); edges
+ * held at a length bound by their slope do not count), or when no halved
+ * step keeps its lnL.
  * lnl_out[n_items] (may be NULL), iters_out = iterations run. */
 plk_status plk_batch_optimize_branches(plk_batch* b, int max_iter, double tol, double* lnl_out, int* iters_out);
 /* An item's current branch lengths in the caller's node ids. */

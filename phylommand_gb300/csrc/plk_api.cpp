@@ -95,6 +95,7 @@ struct plk_handle {
     DevBuf d_P64, d_P32, d_tip64, d_tip32;
     // results and scratch
     DevBuf d_site_lnl, d_block, d_lnl, d_work, d_cond, d_outside, d_nodes_out;
+    DevBuf d_done;  // arrival counter of finish_grid_sum, zero between launches
     DevBuf d_mask_raw, d_flag;
     bool have_lnl = false;
     bool lnl_pending = false;
@@ -319,7 +320,15 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     PLK_CUDA(h, h->d_site_lnl.ensure(sizeof(double) * h->n_sites), "allocate site lnL");
     PLK_CUDA(h, h->d_block.ensure(sizeof(double) * 2 * blocks), "allocate block sums");
     PLK_CUDA(h, h->d_lnl.ensure(sizeof(double)), "allocate lnL");
+    if (!h->d_done.p) {
+        PLK_CUDA(h, h->d_done.ensure(sizeof(unsigned)), "allocate counter");
+        PLK_CUDA(h, cudaMemsetAsync(h->d_done.p, 0, sizeof(unsigned), h->stream), "clear counter");
+    }
     PruneArgs a = prune_args(h, precision);
+    // the last CTA of the post-order pass (or of its per-site combine) adds
+    // up the block sums into d_lnl: no separate reduction launch
+    a.grid_done = h->d_done.as<unsigned>();
+    a.lnl_out = h->d_lnl.as<double>();
     const bool fused = fused_kernel_applies(h, precision);
     std::vector<int> cands20;
     if (!store && precision == PLK_FP32S && h->S == 20)
@@ -362,7 +371,6 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     int nb = 0;
     PLK_CUDA(h, launch_prune(a, h->S, precision, store != nullptr, &nb, h->stream), "post-order kernel launch");
     if (after_prune) PLK_CUDA(h, cudaEventRecord(*after_prune, h->stream), "cudaEventRecord");
-    PLK_CUDA(h, launch_reduce(a.block_sum, nb, h->d_lnl.as<double>(), h->stream), "reduce kernel launch");
     if (store) *store = a.cond;
     return PLK_OK;
 }

@@ -8,11 +8,13 @@
 //                      from an atomic counter (largest trees first) and runs
 //                      the staged post-order tile body of plk_prune4s.cuh on
 //                      it; one compensated partial sum per unit.
+//  batch_prune4p_kernel the same over the paired-category tile body of
+//                      plk_prune4p.cuh (C = 2, 4, 8; same per-site bits).
 //  batch_reduce_kernel one warp per item sums its units in a fixed order
 //                      (TwoSum), so results do not depend on scheduling.
 #include "plk_batch.h"
 #include "plk_device.cuh"
-#include "plk_prune4s.cuh"
+#include "plk_prune4p.cuh"
 
 namespace plk {
 using namespace dev;
@@ -45,12 +47,22 @@ __global__ void batch_pmat_kernel(BatchDev b) {
             for (int m = 0; m < 4; ++m) acc = fma(L[i * 4 + m] * ex[m], R[m * 4 + j], acc);
             P[i * 4 + j] = acc;
         }
-    float* dst = b.P32 + ((size_t)g * C + k) * 16;
+    if (b.write_std) {
+        float* dst = b.P32 + ((size_t)g * C + k) * 16;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) dst[q] = (float)P[q];
+        for (int q = 0; q < 16; ++q) dst[q] = (float)P[q];
+    }
+    if (b.P32p) {
+        float* dst = b.P32p + (size_t)g * C * 16;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) dst[paired_p_index(k, i, j)] = (float)P[i * 4 + j];
+    }
     const int v = nm.y;
     if (v < it.n_tips) {
-        float* tt = b.tip32 + (((size_t)(it.tip_off + v) * C + k) * kCodes) * 4;
+        float* tt = b.write_std ? b.tip32 + (((size_t)(it.tip_off + v) * C + k) * kCodes) * 4 : nullptr;
+        float* tp = b.tip32p ? b.tip32p + (size_t)(it.tip_off + v) * C * kCodes * 4 : nullptr;
         for (int code = 0; code < kCodes; ++code)
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
@@ -58,13 +70,37 @@ __global__ void batch_pmat_kernel(BatchDev b) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
                     if ((code >> j) & 1) acc += P[i * 4 + j];
-                tt[code * 4 + i] = (float)acc;
+                if (tt) tt[code * 4 + i] = (float)acc;
+                if (tp) tp[paired_tip_index(k, code, i)] = (float)acc;
             }
     }
 }
 
-template <int CM, int SPT, bool CODES_SMEM>
-__global__ void __launch_bounds__(kPruneThreads) batch_prune_kernel(BatchDev b) {
+// The tile job of work unit `unit` (P and tipT in the plain or paired layout).
+__device__ __forceinline__ TileJob unit_job(const BatchDev& b, int2 unit, int tile, bool paired) {
+    const BatchItemDev it = b.items[unit.x];
+    TileJob j;
+    j.ops = b.ops + it.ops_off;
+    j.n_ops = it.n_ops;
+    j.codes = b.codes + it.codes_off;
+    j.site_stride = it.site_stride;
+    j.n_sites = it.n_sites;
+    j.n_tips = it.n_tips;
+    j.P = (paired ? b.P32p : b.P32) + (size_t)it.node_off * b.C * 16;
+    j.tipT = (paired ? b.tip32p : b.tip32) + (size_t)it.tip_off * b.C * kCodes * 4;
+    j.root_w = b.model + it.model_off + 36;
+    j.cat_w = b.model + it.model_off + 40 + b.C;
+    j.C = b.C;
+    j.tile_base = unit.y * tile;
+    j.site_lnl = nullptr;
+    j.max_depth = b.max_depth;
+    return j;
+}
+
+// Persistent loop over work units; PAIRED selects the tile body of
+// plk_prune4p.cuh (K = pairs) or of plk_prune4s.cuh (K = category bound).
+template <bool PAIRED, int K, int SPT, bool CODES_SMEM>
+__device__ __forceinline__ void batch_prune_body(const BatchDev& b) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ int s_unit;
     constexpr int TILE = kPruneThreads * SPT;
@@ -73,25 +109,10 @@ __global__ void __launch_bounds__(kPruneThreads) batch_prune_kernel(BatchDev b) 
         __syncthreads();
         const int u = s_unit;
         if (u >= b.n_units) break;
-        const int2 unit = b.units[u];
-        const BatchItemDev it = b.items[unit.x];
-        TileJob j;
-        j.ops = b.ops + it.ops_off;
-        j.n_ops = it.n_ops;
-        j.codes = b.codes + it.codes_off;
-        j.site_stride = it.site_stride;
-        j.n_sites = it.n_sites;
-        j.n_tips = it.n_tips;
-        j.P = b.P32 + (size_t)it.node_off * b.C * 16;
-        j.tipT = b.tip32 + (size_t)it.tip_off * b.C * kCodes * 4;
-        j.root_w = b.model + it.model_off + 36;
-        j.cat_w = b.model + it.model_off + 40 + b.C;
-        j.C = b.C;
-        j.tile_base = unit.y * TILE;
-        j.site_lnl = nullptr;
-        j.max_depth = b.max_depth;
+        const TileJob j = unit_job(b, b.units[u], TILE, PAIRED);
         double ts = 0.0, tc = 0.0;
-        run_tile<CM, SPT, CODES_SMEM>(j, sm, ts, tc);
+        if constexpr (PAIRED) run_tile4p<K, SPT, CODES_SMEM>(j, sm, ts, tc);
+        else run_tile<K, SPT, CODES_SMEM>(j, sm, ts, tc);
         block_sum_pair(ts, tc);
         if (threadIdx.x == 0) {
             b.unit_sums[2 * u] = ts;
@@ -99,6 +120,16 @@ __global__ void __launch_bounds__(kPruneThreads) batch_prune_kernel(BatchDev b) 
         }
         __syncthreads();
     }
+}
+
+template <int CM, int SPT, bool CODES_SMEM>
+__global__ void __launch_bounds__(kPruneThreads) batch_prune_kernel(BatchDev b) {
+    batch_prune_body<false, CM, SPT, CODES_SMEM>(b);
+}
+
+template <int KP, int SPT, bool CODES_SMEM>
+__global__ void __launch_bounds__(kPruneThreads) batch_prune4p_kernel(BatchDev b) {
+    batch_prune_body<true, KP, SPT, CODES_SMEM>(b);
 }
 
 __global__ void batch_reduce_kernel(BatchDev b) {
@@ -126,54 +157,63 @@ __global__ void batch_reduce_kernel(BatchDev b) {
     if (lane == 0) b.lnl[item] = s + c;
 }
 
-template <int CM, int SPT, bool CODES_SMEM>
-cudaError_t launch_batch_prune_t(const BatchDev& b, int grid, size_t smem, cudaStream_t st) {
-    auto kern = batch_prune_kernel<CM, SPT, CODES_SMEM>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    kern<<<grid, kPruneThreads, smem, st>>>(b);
-    return cudaGetLastError();
+// The kernel of a form, its shared memory for the batch's largest tree.
+typedef void (*BatchKernel)(BatchDev);
+
+template <int SPT, bool CODES_SMEM>
+BatchKernel kernel_of(int C, bool paired, int max_ops, int max_tips, int max_depth, size_t* smem) {
+    if (paired) {
+        switch (C) {
+            case 2: *smem = tile4p_smem_bytes<1, SPT, CODES_SMEM>(max_ops, max_tips, max_depth);
+                    return batch_prune4p_kernel<1, SPT, CODES_SMEM>;
+            case 4: *smem = tile4p_smem_bytes<2, SPT, CODES_SMEM>(max_ops, max_tips, max_depth);
+                    return batch_prune4p_kernel<2, SPT, CODES_SMEM>;
+            case 8: *smem = tile4p_smem_bytes<4, SPT, CODES_SMEM>(max_ops, max_tips, max_depth);
+                    return batch_prune4p_kernel<4, SPT, CODES_SMEM>;
+            default: return nullptr;
+        }
+    }
+    if (C == 1) {
+        *smem = tile_smem_bytes<1, SPT, CODES_SMEM>(max_ops, max_tips, max_depth);
+        return batch_prune_kernel<1, SPT, CODES_SMEM>;
+    }
+    if (C <= 4) {
+        *smem = tile_smem_bytes<4, SPT, CODES_SMEM>(max_ops, max_tips, max_depth);
+        return batch_prune_kernel<4, SPT, CODES_SMEM>;
+    }
+    *smem = tile_smem_bytes<8, SPT, CODES_SMEM>(max_ops, max_tips, max_depth);
+    return batch_prune_kernel<8, SPT, CODES_SMEM>;
 }
 
-template <int CM, int SPT, bool CODES_SMEM>
-int occupancy_t(size_t smem) {
-    int n = 0;
-    auto kern = batch_prune_kernel<CM, SPT, CODES_SMEM>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kPruneThreads, smem) != cudaSuccess) return 0;
-    return n;
+BatchKernel form_kernel(int C, const BatchForm& f, int max_ops, int max_tips, int max_depth, size_t* smem) {
+    if (!batch_form_valid(C, f)) return nullptr;
+    if (f.spt == 1) return f.codes_smem ? kernel_of<1, true>(C, f.paired, max_ops, max_tips, max_depth, smem)
+                                        : kernel_of<1, false>(C, f.paired, max_ops, max_tips, max_depth, smem);
+    return f.codes_smem ? kernel_of<2, true>(C, f.paired, max_ops, max_tips, max_depth, smem)
+                        : kernel_of<2, false>(C, f.paired, max_ops, max_tips, max_depth, smem);
 }
 
 }  // namespace
 
-size_t batch_smem_bytes(int C, int spt, bool codes_smem, int max_ops, int max_tips, int max_depth) {
-    const int cm = C == 1 ? 1 : (C <= 4 ? 4 : 8);
-#define PLK_SMEM_CASE(CMV)                                                                                  \
-    if (cm == CMV) {                                                                                        \
-        if (spt == 1) return codes_smem ? tile_smem_bytes<CMV, 1, true>(max_ops, max_tips, max_depth)      \
-                                        : tile_smem_bytes<CMV, 1, false>(max_ops, max_tips, max_depth);    \
-        return codes_smem ? tile_smem_bytes<CMV, 2, true>(max_ops, max_tips, max_depth)                    \
-                          : tile_smem_bytes<CMV, 2, false>(max_ops, max_tips, max_depth);                  \
-    }
-    PLK_SMEM_CASE(1)
-    PLK_SMEM_CASE(4)
-    PLK_SMEM_CASE(8)
-#undef PLK_SMEM_CASE
-    return 0;
+bool batch_form_valid(int C, const BatchForm& f) {
+    if (f.spt != 1 && f.spt != 2) return false;
+    if (C < 1 || C > 8) return false;
+    return !f.paired || C == 2 || C == 4 || C == 8;
 }
 
-int batch_occupancy(int C, int spt, bool codes_smem, size_t smem) {
-    const int cm = C == 1 ? 1 : (C <= 4 ? 4 : 8);
-#define PLK_OCC_CASE(CMV)                                                                               \
-    if (cm == CMV) {                                                                                    \
-        if (spt == 1) return codes_smem ? occupancy_t<CMV, 1, true>(smem) : occupancy_t<CMV, 1, false>(smem); \
-        return codes_smem ? occupancy_t<CMV, 2, true>(smem) : occupancy_t<CMV, 2, false>(smem);         \
-    }
-    PLK_OCC_CASE(1)
-    PLK_OCC_CASE(4)
-    PLK_OCC_CASE(8)
-#undef PLK_OCC_CASE
-    return 0;
+size_t batch_smem_bytes(int C, const BatchForm& f, int max_ops, int max_tips, int max_depth) {
+    size_t smem = 0;
+    return form_kernel(C, f, max_ops, max_tips, max_depth, &smem) ? smem : 0;
+}
+
+int batch_occupancy(int C, const BatchForm& f, size_t smem) {
+    size_t unused = 0;
+    const BatchKernel kern = form_kernel(C, f, 0, 0, 0, &unused);
+    int n = 0;
+    if (!kern) return 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kPruneThreads, smem) != cudaSuccess) return 0;
+    return n;
 }
 
 cudaError_t launch_batch_pmat(const BatchDev& b, cudaStream_t st) {
@@ -185,21 +225,14 @@ cudaError_t launch_batch_pmat(const BatchDev& b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_prune(const BatchDev& b, int spt, bool codes_smem, int grid, size_t smem,
-                               cudaStream_t st) {
-    const int cm = b.C == 1 ? 1 : (b.C <= 4 ? 4 : 8);
-#define PLK_LAUNCH_CASE(CMV)                                                                                   \
-    if (cm == CMV) {                                                                                           \
-        if (spt == 1) return codes_smem ? launch_batch_prune_t<CMV, 1, true>(b, grid, smem, st)               \
-                                        : launch_batch_prune_t<CMV, 1, false>(b, grid, smem, st);             \
-        return codes_smem ? launch_batch_prune_t<CMV, 2, true>(b, grid, smem, st)                             \
-                          : launch_batch_prune_t<CMV, 2, false>(b, grid, smem, st);                           \
-    }
-    PLK_LAUNCH_CASE(1)
-    PLK_LAUNCH_CASE(4)
-    PLK_LAUNCH_CASE(8)
-#undef PLK_LAUNCH_CASE
-    return cudaErrorInvalidValue;
+cudaError_t launch_batch_prune(const BatchDev& b, const BatchForm& f, int grid, size_t smem, cudaStream_t st) {
+    size_t unused = 0;
+    const BatchKernel kern = form_kernel(b.C, f, 0, 0, 0, &unused);
+    if (!kern || (f.paired && (!b.P32p || !b.tip32p))) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kPruneThreads, smem, st>>>(b);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_reduce(const BatchDev& b, cudaStream_t st) {

@@ -47,6 +47,9 @@ struct BatchDev {
     const double* model;      // per item, see BatchItemDev::model_off
     float* P32;               // [n_nodes_total][C][16]
     float* tip32;             // [n_tips_total][C][16][4]
+    float* P32p;              // paired layout of P32 (plk_prune4p.cuh), or null
+    float* tip32p;            // paired layout of tip32, or null
+    int write_std, pad2;      // batch_pmat_kernel writes P32 / tip32 when non-zero
     const int2* units;        // [n_units] (item, tile index), largest trees first
     double* unit_sums;        // [n_units][2]
     const int* item_unit_ptr; // [n_items + 1]
@@ -68,11 +71,19 @@ struct BatchDev {
 
 inline int batch_model_stride(int C) { return 40 + 2 * C; }
 
-size_t batch_smem_bytes(int C, int spt, bool codes_smem, int max_ops, int max_tips, int max_depth);
-int batch_occupancy(int C, int spt, bool codes_smem, size_t smem);
+// One form of the batch post-order kernel: sites per thread, tip codes staged
+// in shared memory or read from global, categories in pairs on the FP32x2
+// pipe (C = 2, 4, 8; reads P32p / tip32p) or one at a time.
+struct BatchForm {
+    int spt = 1;
+    bool codes_smem = false;
+    bool paired = false;
+};
+bool batch_form_valid(int C, const BatchForm& f);
+size_t batch_smem_bytes(int C, const BatchForm& f, int max_ops, int max_tips, int max_depth);
+int batch_occupancy(int C, const BatchForm& f, size_t smem);
 cudaError_t launch_batch_pmat(const BatchDev& b, cudaStream_t st);
-cudaError_t launch_batch_prune(const BatchDev& b, int spt, bool codes_smem, int grid, size_t smem,
-                               cudaStream_t st);
+cudaError_t launch_batch_prune(const BatchDev& b, const BatchForm& f, int grid, size_t smem, cudaStream_t st);
 cudaError_t launch_batch_reduce(const BatchDev& b, cudaStream_t st);
 
 // NNI scoring (plk_nni.cu): one tile per work unit, grid CTAs with their own

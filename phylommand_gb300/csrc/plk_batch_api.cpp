@@ -82,6 +82,7 @@ struct plk_batch {
     bool layout_dirty = true;
     // device layout
     BBuf d_items, d_codes, d_ops, d_teff, d_node_item, d_child, d_model, d_P32, d_tip32, d_lnl, d_counter;
+    BBuf d_P32p, d_tip32p;  // paired layouts (C = 2, 4, 8)
     BBuf d_moves, d_move_item, d_nni_out, d_unit_move_sums, d_scr_D, d_scr_ED, d_scr_O, d_scr_EO;
     BBuf d_blen_ueo, d_blen_ues, d_blen_ieo, d_blen_ei, d_blen_out;  // branch-length derivative slots
     double* h_model = nullptr;  // pinned staging of the models
@@ -90,8 +91,8 @@ struct plk_batch {
     int n_nodes_total = 0, max_ops = 0, max_tips = 0, max_depth = 0, max_int = 0, total_moves = 0;
     UnitSet lnl_units, nni_units;
     // tuning of the lnL kernel
-    int spt = 1, grid = 0;
-    bool codes_smem = false;
+    BatchForm form;
+    int grid = 0;
     size_t smem = 0;
     double tuned_ms = 0.0;
     bool tuned = false;
@@ -140,6 +141,9 @@ BatchDev device_view(plk_batch* b, const UnitSet& us) {
     d.model = b->d_model.as<double>();
     d.P32 = b->d_P32.as<float>();
     d.tip32 = b->d_tip32.as<float>();
+    d.P32p = nullptr;  // the plain layout only, unless with_paired() asks for both
+    d.tip32p = nullptr;
+    d.write_std = 1;
     d.units = us.units.as<int2>();
     d.unit_sums = us.sums.as<double>();
     d.item_unit_ptr = us.ptr.as<int>();
@@ -157,6 +161,19 @@ BatchDev device_view(plk_batch* b, const UnitSet& us) {
     d.scr_ED = b->d_scr_ED.as<int>();
     d.scr_O = b->d_scr_O.as<float4>();
     d.scr_EO = b->d_scr_EO.as<int>();
+    return d;
+}
+
+// The view for the lnL kernels: P(t) written in the layouts that `form`
+// reads (both while tuning).
+BatchDev lnl_view(plk_batch* b, const BatchForm* form) {
+    BatchDev d = device_view(b, b->lnl_units);
+    const bool has_paired = b->d_P32p.p != nullptr && (b->C == 2 || b->C == 4 || b->C == 8);
+    if (has_paired && (!form || form->paired)) {
+        d.P32p = b->d_P32p.as<float>();
+        d.tip32p = b->d_tip32p.as<float>();
+    }
+    if (form && form->paired) d.write_std = 0;
     return d;
 }
 
@@ -262,6 +279,10 @@ plk_status build_layout(plk_batch* b) {
     PLK_BCUDA(b, b->d_model.ensure(it.size() * batch_model_stride(C) * sizeof(double)), "allocate models");
     PLK_BCUDA(b, b->d_P32.ensure((size_t)b->n_nodes_total * C * 16 * sizeof(float)), "allocate P");
     PLK_BCUDA(b, b->d_tip32.ensure((size_t)tips_total * C * 16 * 4 * sizeof(float)), "allocate tip tables");
+    if (C == 2 || C == 4 || C == 8) {
+        PLK_BCUDA(b, b->d_P32p.ensure((size_t)b->n_nodes_total * C * 16 * sizeof(float)), "allocate P");
+        PLK_BCUDA(b, b->d_tip32p.ensure((size_t)tips_total * C * 16 * 4 * sizeof(float)), "allocate tip tables");
+    }
     PLK_BCUDA(b, b->d_lnl.ensure(it.size() * sizeof(double)), "allocate lnL");
     PLK_BCUDA(b, b->d_counter.ensure(sizeof(int)), "allocate counter");
     PLK_BCUDA(b, b->d_moves.ensure(std::max<size_t>(moves.size(), 1) * sizeof(NniMoveDev)), "allocate moves");
@@ -313,13 +334,13 @@ plk_status build_layout(plk_batch* b) {
 
 // The evaluation sequence (graph body).
 plk_status enqueue_eval(plk_batch* b) {
-    const BatchDev d = device_view(b, b->lnl_units);
+    const BatchDev d = lnl_view(b, &b->form);
     const size_t mn = b->items.size() * batch_model_stride(b->C);
     PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
     PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, mn * sizeof(double), cudaMemcpyHostToDevice, b->stream),
               "upload models");
     PLK_BCUDA(b, launch_batch_pmat(d, b->stream), "batch P(t) launch");
-    PLK_BCUDA(b, launch_batch_prune(d, b->spt, b->codes_smem, b->grid, b->smem, b->stream), "batch post-order launch");
+    PLK_BCUDA(b, launch_batch_prune(d, b->form, b->grid, b->smem, b->stream), "batch post-order launch");
     PLK_BCUDA(b, launch_batch_reduce(d, b->stream), "batch reduce launch");
     PLK_BCUDA(b, cudaMemcpyAsync(b->h_lnl, b->d_lnl.p, b->items.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                  b->stream),
@@ -327,28 +348,46 @@ plk_status enqueue_eval(plk_batch* b) {
     return PLK_OK;
 }
 
-// Autotuner: sites per thread (1, 2) x CTAs per SM (1 .. occupancy), each
-// timed over two launches of the persistent kernel after a warm-up.
+// Autotuner over the kernel forms -- categories in pairs or one at a time,
+// sites per thread 1 or 2, tip codes staged in shared memory (where they fit)
+// or read from global -- times CTAs per SM 1 .. occupancy, two launches of
+// the persistent kernel after a warm-up each.  PLK_BATCH_SPT and
+// PLK_BATCH_PAIRED (0 / 1) pin those choices.
 plk_status tune(plk_batch* b) {
     cudaEvent_t e0, e1;
     PLK_BCUDA(b, cudaEventCreate(&e0), "cudaEventCreate");
     PLK_BCUDA(b, cudaEventCreate(&e1), "cudaEventCreate");
     double best = 1e30;
-    int best_spt = 1, best_grid = 0;
-    bool best_codes = false;
+    BatchForm best_form;
+    int best_grid = 0;
     size_t best_smem = 0;
     const char* force_spt = getenv("PLK_BATCH_SPT");
-    for (int spt = 1; spt <= 2; ++spt) {
-        if (force_spt && atoi(force_spt) != spt) continue;
-        size_t smem = batch_smem_bytes(b->C, spt, true, b->max_ops, b->max_tips, b->max_depth);
-        bool codes_smem = smem <= 160 * 1024;
-        if (!codes_smem) smem = batch_smem_bytes(b->C, spt, false, b->max_ops, b->max_tips, b->max_depth);
-        if (smem > 227 * 1024) continue;
-        const int occ = batch_occupancy(b->C, spt, codes_smem, smem);
+    const char* force_paired = getenv("PLK_BATCH_PAIRED");
+    std::vector<BatchForm> forms;
+    for (int paired = 0; paired <= 1; ++paired)
+        for (int spt = 1; spt <= 2; ++spt)
+            for (int codes = 1; codes >= 0; --codes) {
+                BatchForm f;
+                f.spt = spt;
+                f.codes_smem = codes != 0;
+                f.paired = paired != 0;
+                if (!batch_form_valid(b->C, f)) continue;
+                if (force_spt && atoi(force_spt) != spt) continue;
+                if (force_paired && atoi(force_paired) != paired) continue;
+                const size_t smem = batch_smem_bytes(b->C, f, b->max_ops, b->max_tips, b->max_depth);
+                if (smem == 0 || smem > 227 * 1024) continue;
+                if (f.codes_smem && smem > 160 * 1024) continue;
+                forms.push_back(f);
+            }
+    for (const BatchForm& f : forms) {
+        const size_t smem = batch_smem_bytes(b->C, f, b->max_ops, b->max_tips, b->max_depth);
+        const int occ = batch_occupancy(b->C, f, smem);
         if (occ < 1) continue;
-        plk_status s = build_units(b, b->lnl_units, spt, false);
-        if (s != PLK_OK) return s;
-        const BatchDev d = device_view(b, b->lnl_units);
+        if (b->lnl_units.spt != f.spt) {
+            plk_status s = build_units(b, b->lnl_units, f.spt, false);
+            if (s != PLK_OK) return s;
+        }
+        const BatchDev d = lnl_view(b, nullptr);
         for (int per_sm = 1; per_sm <= occ; ++per_sm) {
             const int grid = std::min(b->lnl_units.n_units, per_sm * b->n_sms);
             if (grid < 1) continue;
@@ -356,16 +395,15 @@ plk_status tune(plk_batch* b) {
             for (int rep = 0; rep < 3; ++rep) {  // warm-up, then two timed launches
                 PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
                 if (rep == 1) PLK_BCUDA(b, cudaEventRecord(e0, b->stream), "cudaEventRecord");
-                PLK_BCUDA(b, launch_batch_prune(d, spt, codes_smem, grid, smem, b->stream), "batch post-order launch");
+                PLK_BCUDA(b, launch_batch_prune(d, f, grid, smem, b->stream), "batch post-order launch");
             }
             PLK_BCUDA(b, cudaEventRecord(e1, b->stream), "cudaEventRecord");
             PLK_BCUDA(b, cudaEventSynchronize(e1), "tune");
             PLK_BCUDA(b, cudaEventElapsedTime(&ms, e0, e1), "tune");
             if (ms < best) {
                 best = ms;
-                best_spt = spt;
+                best_form = f;
                 best_grid = grid;
-                best_codes = codes_smem;
                 best_smem = smem;
             }
             if (grid == b->lnl_units.n_units) break;
@@ -374,13 +412,12 @@ plk_status tune(plk_batch* b) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_grid == 0) return bfail(b, PLK_ERR_UNSUPPORTED, "no batch kernel configuration fits these trees");
-    b->spt = best_spt;
+    b->form = best_form;
     b->grid = best_grid;
-    b->codes_smem = best_codes;
     b->smem = best_smem;
     b->tuned_ms = best / 2.0;
-    if (b->lnl_units.spt != best_spt) {
-        plk_status s = build_units(b, b->lnl_units, best_spt, false);
+    if (b->lnl_units.spt != best_form.spt) {
+        plk_status s = build_units(b, b->lnl_units, best_form.spt, false);
         if (s != PLK_OK) return s;
     }
     b->tuned = true;
@@ -411,7 +448,7 @@ plk_status prepare(plk_batch* b) {
         PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, b->items.size() * stride * sizeof(double),
                                      cudaMemcpyHostToDevice, b->stream),
                   "upload models");
-        PLK_BCUDA(b, launch_batch_pmat(device_view(b, b->lnl_units), b->stream), "batch P(t) launch");
+        PLK_BCUDA(b, launch_batch_pmat(lnl_view(b, nullptr), b->stream), "batch P(t) launch");
         s = tune(b);
         if (s != PLK_OK) return s;
     }
@@ -613,10 +650,17 @@ plk_status plk_batch_loglik(plk_batch* b, double* lnl_out) {
 
 plk_status plk_batch_tuning(const plk_batch* b, int* spt, int* grid, double* ms, int* uses_graph) {
     if (!b) return PLK_ERR_ARG;
-    if (spt) *spt = b->spt;
+    if (spt) *spt = b->form.spt;
     if (grid) *grid = b->grid;
     if (ms) *ms = b->tuned_ms;
     if (uses_graph) *uses_graph = b->exec != nullptr;
+    return PLK_OK;
+}
+
+plk_status plk_batch_form(const plk_batch* b, int* paired, int* codes_smem) {
+    if (!b) return PLK_ERR_ARG;
+    if (paired) *paired = b->form.paired ? 1 : 0;
+    if (codes_smem) *codes_smem = b->form.codes_smem ? 1 : 0;
     return PLK_OK;
 }
 
@@ -980,13 +1024,18 @@ plk_status plk_batch_optimize_branches(plk_batch* b, int max_iter, double tol, d
         if (!any) break;
         if ((s = blen_pass(b, deriv, item_edge_off)) != PLK_OK) return s;
         // one Newton step per edge (all edges of an item at once), halved
-        // until the item's lnL does not drop
+        // until the item's lnL does not drop.  An item has converged when the
+        // quadratic model predicts less than tol of gain from another step:
+        // sum over its free edges of g^2 / (2 |c|) (an edge in a convex
+        // direction counts as not converged; an edge held at a bound by its
+        // slope does not count).
         std::vector<std::vector<double>> old(n_items), step(n_items);
         for (int i = 0; i < n_items; ++i) {
             ItemHost& h = b->items[i];
             old[i] = h.t_eff;
             step[i].assign(h.n_nodes, 0.0);
             if (done[i]) continue;
+            double predicted = 0.0;
             for (int slot = 0; slot < 2 * h.n_int; ++slot) {
                 const int2 ch = h.child[h.n_tips + slot / 2];
                 const int v = (slot % 2 == 0) ? ch.x : ch.y;
@@ -996,12 +1045,23 @@ plk_status plk_batch_optimize_branches(plk_batch* b, int max_iter, double tol, d
                 if (slot / 2 == h.n_int - 1 && slot % 2 == 1) continue;
                 const double g = deriv[2 * (item_edge_off[i] + slot)], c = deriv[2 * (item_edge_off[i] + slot) + 1];
                 const double t = h.t_eff[v];
+                const bool held = (t <= t_min * 1.000001 && g <= 0.0) || (t >= t_max * 0.999999 && g >= 0.0);
+                if (!held) predicted += c < 0.0 ? g * g / (-2.0 * c) : HUGE_VAL;
                 double tn;
                 if (c < 0.0) tn = t - g / c;                 // Newton on a concave direction
                 else tn = g > 0.0 ? 2.0 * t + 1e-3 : 0.5 * t;  // otherwise move along the slope
                 tn = std::min(std::max(tn, std::max(t_min, 0.1 * t)), std::min(t_max, 10.0 * t + 0.05));
                 step[i][v] = tn - t;
             }
+            if (predicted < tol) {
+                done[i] = 1;
+                step[i].assign(h.n_nodes, 0.0);
+            }
+        }
+        {
+            bool any = false;
+            for (char d : done) any = any || !d;
+            if (!any) break;
         }
         std::vector<char> accepted(n_items, 0);
         for (int half = 0; half < 6; ++half) {
@@ -1028,7 +1088,6 @@ plk_status plk_batch_optimize_branches(plk_batch* b, int max_iter, double tol, d
                 done[i] = 1;
                 continue;
             }
-            if (trial[i] - cur[i] < tol) done[i] = 1;
             cur[i] = trial[i];
         }
         if ((s = upload_lengths(b)) != PLK_OK) return s;

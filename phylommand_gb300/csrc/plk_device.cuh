@@ -87,6 +87,53 @@ __device__ __forceinline__ void block_sum_pair(double& s, double& c) {
     }
 }
 
+// Compensated sum of the n (sum, compensation) pairs of bs by one CTA:
+// thread i folds pairs i, i + blockDim.x, ... (TwoSum), then the block
+// reduction of block_sum_pair; the result is valid in thread 0.  Loads go
+// through L2 so that pairs other CTAs of the same grid stored are seen.
+__device__ inline double cta_sum_pairs(const double* bs, int n) {
+    constexpr int U = 8;  // a thread's loads of one round, all in flight before the sums
+    double s = 0.0, c = 0.0;
+    for (int base = 0; base < n; base += U * (int)blockDim.x) {
+        double2 v[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            const int i = base + q * (int)blockDim.x + (int)threadIdx.x;
+            v[q] = i < n ? __ldcg(reinterpret_cast<const double2*>(bs) + i) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            double ns, e;
+            two_sum(s, v[q].x, ns, e);
+            s = ns;
+            c = c + v[q].y + e;
+        }
+    }
+    block_sum_pair(s, c);
+    return s + c;
+}
+
+// Epilogue of a 1-D grid whose CTAs each stored one pair at bs[2 blockIdx.x]
+// from thread 0: every CTA counts itself in with one atomicAdd after a fence,
+// and the CTA that arrives last sums all pairs in index order into *out and
+// re-arms the counter (zero between launches).  Nothing waits on another CTA.
+// Every thread of the CTA must call it, after thread 0's store.
+__device__ inline void finish_grid_sum(const double* bs, unsigned* counter, double* out) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const double t = cta_sum_pairs(bs, (int)gridDim.x);
+    if (threadIdx.x == 0) {
+        *out = t;
+        *counter = 0u;
+    }
+}
+
 // 16-byte asynchronous global-to-shared copies (sm_80+ cp.async).
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));

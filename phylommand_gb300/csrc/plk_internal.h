@@ -206,10 +206,16 @@ struct PruneArgs {
     int variant;
     int n_nodes;
     void* scratch;             // kernel-specific scratch (prune20_scratch_bytes)
+    // The last CTA of the kernel that stores the block sums adds them up into
+    // *lnl_out (finish_grid_sum), counting arrivals in *grid_done, which is
+    // zero between launches; with grid_done null only the block sums and
+    // per-site values are written.
+    unsigned* grid_done;
+    double* lnl_out;
 };
 // Fused 20-state FP32 kernels (plk_prune20.cu): mode 1 = CUDA cores, 2 =
-// tensor cores.  Launches the relayout, the pass and the per-site combine;
-// *n_blocks = the block sums left for launch_reduce.
+// tensor cores.  Launches the relayout, the pass and the per-site combine
+// (which also finishes the total); *n_blocks = the number of block sums.
 bool prune20_fits(const PruneArgs& a, int mode);
 size_t prune20_scratch_bytes(const PruneArgs& a, int n_nodes);
 cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scratch, int* n_blocks,
@@ -227,7 +233,6 @@ cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStrea
 // for the partial sums in *n_blocks.
 cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, int* n_blocks,
                          cudaStream_t st);
-cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cudaStream_t st);
 // *out = compensated sum_i w[i] x[i] (one CTA)
 cudaError_t launch_weighted_sum(const double* x, const double* w, int n, double* out, cudaStream_t st);
 // codes[t * stride + s] = masks[t * n_sites + s] & all (alphabets of <= 4

@@ -10,12 +10,12 @@
 //                   op list; partial vectors live in registers, spills in a
 //                   per-thread shared-memory stack; per-site power-of-two
 //                   scaling; root reduction (src/simpleML.h:123-141) fused;
-//                   compensated block sums of the per-site lnL.
+//                   compensated block sums of the per-site lnL, added up by
+//                   the grid's last CTA (finish_grid_sum).
 //  prune_generic    the same pass for any state count (<= 24), vectors in a
 //                   global work buffer.
 //  preorder_kernel  outside vectors from the root down and normalised
 //                   marginal posteriors (absent in the reference).
-//  reduce_kernel    compensated (TwoSum) sum of the block partial sums.
 #include <cstdio>
 
 #include "plk_device.cuh"
@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
             a.block_sum[2 * blockIdx.x + 1] = c;
         }
     }
+    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 }  // namespace
@@ -483,6 +484,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune_generic_kernel(GenericArg
             a.block_sum[2 * blockIdx.x + 1] = c;
         }
     }
+    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 }  // namespace
@@ -588,50 +590,6 @@ cudaError_t launch_encode_small(const void* masks, int elem_bytes, int n_tips, i
     else
         encode_small_kernel<uint32_t><<<(unsigned)blocks, threads, 0, st>>>(static_cast<const uint32_t*>(masks),
                                                                            n_tips, n_sites, stride, all, codes, bad);
-    return cudaGetLastError();
-}
-
-// =========================================================================
-// Final compensated reduction of the block sums
-// =========================================================================
-__global__ void reduce_kernel(const double* __restrict__ bs, int n, double* out) {
-    double s = 0.0, c = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double ns, e;
-        two_sum(s, bs[2 * i], ns, e);
-        s = ns;
-        c = c + bs[2 * i + 1] + e;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        const double os = __shfl_down_sync(0xffffffffu, s, off);
-        const double oc = __shfl_down_sync(0xffffffffu, c, off);
-        double ns, e;
-        two_sum(s, os, ns, e);
-        s = ns;
-        c = c + oc + e;
-    }
-    __shared__ double rs[32], rc[32];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { rs[warp] = s; rc[warp] = c; }
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = blockDim.x >> 5;
-        s = lane < nw ? rs[lane] : 0.0;
-        c = lane < nw ? rc[lane] : 0.0;
-        for (int off = 16; off > 0; off >>= 1) {
-            const double os = __shfl_down_sync(0xffffffffu, s, off);
-            const double oc = __shfl_down_sync(0xffffffffu, c, off);
-            double ns, e;
-            two_sum(s, os, ns, e);
-            s = ns;
-            c = c + oc + e;
-        }
-        if (lane == 0) out[0] = s + c;
-    }
-}
-
-cudaError_t launch_reduce(const double* block_sum, int n_blocks, double* out, cudaStream_t st) {
-    reduce_kernel<<<1, 256, 0, st>>>(block_sum, n_blocks, out);
     return cudaGetLastError();
 }
 

@@ -15,7 +15,11 @@
 //       L = sum_k w_k sum_s Out_u[s] D_z[s] (P_v (D_x x D_y))[s],
 //     and across the root edge (v, c): v' = (x, y), c' = (p, q),
 //       L = sum_k w_k sum_s pi_s (P_v (D_x x D_y))[s] (P_c (D_p x D_q))[s];
-//     log site likelihoods summed per warp, then per CTA in warp order.
+//     in FP32 per site (the FP64 pipe of this part is a small fraction of
+//     its FP32 rate): a site's log-likelihood is logf of the mantissa of L
+//     plus its power-of-two exponent times ln 2, the mantissa logs summed per
+//     warp with FP32 TwoSum, the exponents as integers, then per CTA in warp
+//     order in FP64.
 // A last kernel sums each (tree, move) over its tiles in site order.
 #include "plk_batch.h"
 #include "plk_device.cuh"
@@ -37,6 +41,22 @@ struct ItemView {
     const double* root_w;
     const double* cat_w;
 };
+
+// FP32 copies of an item's root and category weights (converted once per unit)
+template <int CM>
+struct Weights32 {
+    float4 root;
+    float cat[CM];
+};
+
+template <int CM>
+__device__ __forceinline__ Weights32<CM> weights32(const ItemView& iv, int C) {
+    Weights32<CM> w;
+    w.root = make_float4((float)iv.root_w[0], (float)iv.root_w[1], (float)iv.root_w[2], (float)iv.root_w[3]);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) w.cat[k] = k < C ? (float)iv.cat_w[k] : 0.0f;
+    return w;
+}
 
 // Message of node `node` to its parent at this thread's site, category k,
 // and its exponent: tip -> tip-table row of the site's code, internal ->
@@ -139,10 +159,15 @@ __device__ void phase_b(const ItemView& iv, const BatchDev& b, int site_c, int t
     }
 }
 
-// log-likelihood of one move at this thread's site
+// Likelihood of one move at this thread's site in FP32:  L = lsum 2^etot,
+// lsum = sum_k w_k sum_s Out[s] (P_v (D_x x D_y))[s] D_z[s]  (kind 0) or
+// sum_k w_k sum_s pi_s (P_v (D_x x D_y))[s] (P_c (D_p x D_q))[s]  (kind 1).
+// SCALE multiplies lsum by 2^64 (the outside / root weights scaled, exact)
+// for the rare site whose FP32 lsum would fall below the normal range.
 template <int CM>
-__device__ double move_site_lnl(const ItemView& iv, const BatchDev& b, const NniMoveDev& mv, int site_c, int tid,
-                                const float4* sD, const int* sED, const float4* sO, const int* sEO) {
+__device__ float move_site_l(const ItemView& iv, const BatchDev& b, const NniMoveDev& mv, int site_c, int tid,
+                             const float4* sD, const int* sED, const float4* sO, const int* sEO,
+                             const Weights32<CM>& w, float scale, int* etot_out) {
     const BatchItemDev& it = *iv.it;
     const int C = b.C;
     float4 t1[CM];
@@ -162,7 +187,7 @@ __device__ double move_site_lnl(const ItemView& iv, const BatchDev& b, const Nni
 #pragma unroll
         for (int k = 0; k < CM; ++k) t1[k] = scale4(t1[k], f1, f2);
     }
-    double lsum = 0.0;
+    float lsum = 0.0f;
     int etot = ex + ey + e1;
     if (mv.kind == 0) {
         const int ru = mv.u - it.n_tips;
@@ -173,17 +198,17 @@ __device__ double move_site_lnl(const ItemView& iv, const BatchDev& b, const Nni
             if (k < C) {
                 const float4 a = pmv(iv.P + ((size_t)mv.v * C + k) * 16, t1[k]);
                 const float4 z = message(iv, b, mv.z, k, site_c, tid, sD, sED, &ez);
-                const float4 o = u_root ? make_float4((float)iv.root_w[0], (float)iv.root_w[1], (float)iv.root_w[2],
-                                                      (float)iv.root_w[3])
-                                        : sO[((size_t)ru * C + k) * TILE + tid];
-                double lk = (double)o.x * ((double)a.x * (double)z.x);
-                lk = fma((double)o.y, (double)a.y * (double)z.y, lk);
-                lk = fma((double)o.z, (double)a.z * (double)z.z, lk);
-                lk = fma((double)o.w, (double)a.w * (double)z.w, lk);
-                lsum = fma(iv.cat_w[k], lk, lsum);
+                float4 o = u_root ? w.root : sO[((size_t)ru * C + k) * TILE + tid];
+                o = make_float4(o.x * scale, o.y * scale, o.z * scale, o.w * scale);
+                float lk = o.x * (a.x * z.x);
+                lk = fmaf(o.y, a.y * z.y, lk);
+                lk = fmaf(o.z, a.z * z.z, lk);
+                lk = fmaf(o.w, a.w * z.w, lk);
+                lsum = fmaf(w.cat[k], lk, lsum);
             }
         etot += ez;
     } else {
+        const float4 pi = make_float4(w.root.x * scale, w.root.y * scale, w.root.z * scale, w.root.w * scale);
 #pragma unroll
         for (int k = 0; k < CM; ++k)
             if (k < C) {
@@ -191,15 +216,52 @@ __device__ double move_site_lnl(const ItemView& iv, const BatchDev& b, const Nni
                 const float4 t4 = mul4(message(iv, b, mv.p, k, site_c, tid, sD, sED, &ep),
                                        message(iv, b, mv.q, k, site_c, tid, sD, sED, &eq));
                 const float4 c = pmv(iv.P + ((size_t)mv.c * C + k) * 16, t4);
-                double lk = iv.root_w[0] * ((double)a.x * (double)c.x);
-                lk = fma(iv.root_w[1], (double)a.y * (double)c.y, lk);
-                lk = fma(iv.root_w[2], (double)a.z * (double)c.z, lk);
-                lk = fma(iv.root_w[3], (double)a.w * (double)c.w, lk);
-                lsum = fma(iv.cat_w[k], lk, lsum);
+                float lk = pi.x * (a.x * c.x);
+                lk = fmaf(pi.y, a.y * c.y, lk);
+                lk = fmaf(pi.z, a.z * c.z, lk);
+                lk = fmaf(pi.w, a.w * c.w, lk);
+                lsum = fmaf(w.cat[k], lk, lsum);
             }
         etot += ep + eq;
     }
-    return log(lsum) + (double)etot * 0.69314718055994530942;
+    *etot_out = etot;
+    return lsum;
+}
+
+// log L of one move at this thread's site as lm + ee ln 2, lm = log of the
+// mantissa of L in [0, ln 2)
+template <int CM>
+__device__ __forceinline__ void move_site_log(const ItemView& iv, const BatchDev& b, const NniMoveDev& mv, int site_c,
+                                              int tid, const float4* sD, const int* sED, const float4* sO,
+                                              const int* sEO, const Weights32<CM>& w, float* lm, int* ee) {
+    int etot;
+    float l = move_site_l<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO, w, 1.0f, &etot);
+    if (!(l >= 1.17549435e-38f)) {  // below the normal range (or zero): again with 2^64 on the weights
+        l = move_site_l<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO, w, 1.8446744073709552e19f, &etot);
+        etot -= 64;
+    }
+    const int bits = __float_as_int(l);
+    *ee = etot + ((bits >> 23) & 255) - 127;
+    *lm = logf(__int_as_float((bits & 0x007fffff) | 0x3f800000));
+}
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// FP32 TwoSum reduction of (hi, lo) over a warp; lane 0 ends with the pair
+__device__ __forceinline__ void warp_two_sum_f(float& hi, float& lo) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, hi, off);
+        const float ol = __shfl_down_sync(0xffffffffu, lo, off);
+        float ns, e;
+        two_sum_f(hi, oh, ns, e);
+        hi = ns;
+        lo = __fadd_rn(lo, __fadd_rn(ol, e));
+    }
 }
 
 template <int CM, bool CODES_SMEM>
@@ -247,7 +309,7 @@ __global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
         j.site_lnl = nullptr;
         j.max_depth = b.max_depth;
         DStore ds{sD, sED};
-        double ts = 0.0, tc = 0.0;
+        double ts = 0.0, tc = 0.0;  // untouched with STORE_D (no root)
         run_tile<CM, 1, CODES_SMEM, true>(j, sm, ts, tc, &ds);
         // phases B and C touch only this thread's site column of the scratch
         const int site = j.tile_base + tid;
@@ -255,18 +317,21 @@ __global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
         const int site_c = min(site, it.site_stride - 1);
         phase_b<CM>(iv, b, site_c, tid, sD, sED, sO, sEO);
         const long long out_off = b.unit_move_off[u];
+        const Weights32<CM> w32 = weights32<CM>(iv, b.C);
         for (int m0 = 0; m0 < it.n_moves; m0 += 32) {
             const int mcount = min(32, it.n_moves - m0);
             for (int mi = 0; mi < mcount; ++mi) {
                 const NniMoveDev mv = b.moves[it.moves_off + m0 + mi];
-                // a warp's 32 site terms in plain FP64 (error ~1e-15 relative);
-                // the compensated sums start across warps and tiles
-                double s = valid ? move_site_lnl<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO) : 0.0;
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+                float lm = 0.0f;
+                int ee = 0;
+                if (valid) move_site_log<CM>(iv, b, mv, site_c, tid, sD, sED, sO, sEO, w32, &lm, &ee);
+                // the warp's mantissa logs with FP32 TwoSum, exponents exactly
+                float hi = lm, lo = 0.0f;
+                warp_two_sum_f(hi, lo);
+                const int esum = __reduce_add_sync(0xffffffffu, ee);
                 if (lane == 0) {
-                    s_red[warp][mi][0] = s;
-                    s_red[warp][mi][1] = 0.0;
+                    s_red[warp][mi][0] = (double)esum * 0.69314718055994530942 + (double)hi;
+                    s_red[warp][mi][1] = (double)lo;
                 }
             }
             __syncthreads();
@@ -317,19 +382,26 @@ __global__ void batch_nni_reduce_kernel(BatchDev b) {
 // d1 = L'/L and d2 = L''/L - (L'/L)^2 (the first and second derivatives of its
 // log likelihood; the power-of-two exponents cancel in the ratios).  Edge
 // slot i of an item is child i % 2 of internal node n_tips + i / 2.
+//
+// All per-site arithmetic is FP32: the model's eigenvectors and rates are
+// converted once per work unit and the factors exp(rho_km t) once per edge
+// (shared memory), the ratios are IEEE FP32 divisions, and a warp's 32 site
+// terms are summed with FP32 TwoSum before the FP64 sums across warps.
 // ---------------------------------------------------------------------------
 template <int CM>
+struct BlenModel32 {
+    float L[16], R[16];
+    float rho[CM][4];
+};
+constexpr int kBlenSlots = 32;  // edge slots per pass over the tile
+
+template <int CM>
 __device__ void edge_site_derivs(const ItemView& iv, const BatchDev& b, int u, int v, int w, int site_c, int tid,
-                                 const float4* sD, const int* sED, const float4* sO, double* d1, double* d2) {
+                                 const float4* sD, const int* sED, const float4* sO, const BlenModel32<CM>& mf,
+                                 const float* ex, const float4& root32, const float* cat32, float* d1, float* d2) {
     const BatchItemDev& it = *iv.it;
     const int C = b.C;
-    const double* mdl = b.model + it.model_off;
-    const double* lam = mdl;
-    const double* Lm = mdl + 4;
-    const double* Rm = mdl + 20;
-    const double* cat_rate = mdl + 40;
     const bool u_root = (u - it.n_tips) == it.n_int - 1;
-    const double t = b.t_eff[it.node_off + v];
     // cond(v): a tip's state set, or the product of v's children's messages
     float4 cv[CM];
     int e = 0;
@@ -352,9 +424,7 @@ __device__ void edge_site_derivs(const ItemView& iv, const BatchDev& b, int u, i
 #pragma unroll
     for (int k = 0; k < CM; ++k)
         if (k < C) {
-            float4 A = u_root ? make_float4((float)iv.root_w[0], (float)iv.root_w[1], (float)iv.root_w[2],
-                                            (float)iv.root_w[3])
-                              : sO[((size_t)(u - it.n_tips) * C + k) * TILE + tid];
+            float4 A = u_root ? root32 : sO[((size_t)(u - it.n_tips) * C + k) * TILE + tid];
             if (w >= 0) A = mul4(A, message(iv, b, w, k, site_c, tid, sD, sED, &e));
             const float Av[4] = {A.x, A.y, A.z, A.w};
             const float cvv[4] = {cv[k].x, cv[k].y, cv[k].z, cv[k].w};
@@ -364,30 +434,32 @@ __device__ void edge_site_derivs(const ItemView& iv, const BatchDev& b, int u, i
                 float a = 0.f, bb = 0.f;
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
-                    a = fmaf(Av[i], (float)Lm[i * 4 + m], a);
-                    bb = fmaf((float)Rm[m * 4 + i], cvv[i], bb);
+                    a = fmaf(Av[i], mf.L[i * 4 + m], a);
+                    bb = fmaf(mf.R[m * 4 + i], cvv[i], bb);
                 }
-                const float rho = (float)(lam[m] * cat_rate[k]);
-                const float term = a * bb * expf(rho * (float)t);
+                const float rho = mf.rho[k][m];
+                const float term = a * bb * ex[k * 4 + m];
                 s0 += term;
                 s1 = fmaf(rho, term, s1);
                 s2 = fmaf(rho * rho, term, s2);
             }
-            const float wk = (float)iv.cat_w[k];
+            const float wk = cat32[k];
             l0 = fmaf(wk, s0, l0);
             l1 = fmaf(wk, s1, l1);
             l2 = fmaf(wk, s2, l2);
         }
-    const double g = (double)l1 / (double)l0;
+    const float g = __fdiv_rn(l1, l0);
     *d1 = g;
-    *d2 = (double)l2 / (double)l0 - g * g;
+    *d2 = __fsub_rn(__fdiv_rn(l2, l0), __fmul_rn(g, g));
 }
 
 template <int CM, bool CODES_SMEM>
 __global__ void __launch_bounds__(kPruneThreads) batch_blen_kernel(BatchDev b, BlenDev bd) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ int s_unit;
-    __shared__ double s_red[kPruneThreads / 32][32][2];
+    __shared__ double s_red[kPruneThreads / 32][kBlenSlots][2];
+    __shared__ BlenModel32<CM> s_mf;
+    __shared__ float s_ex[kBlenSlots][CM * 4];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const size_t vec_slice = (size_t)b.scratch_int * b.C * TILE;
     const size_t int_slice = (size_t)b.scratch_int * TILE;
@@ -410,6 +482,15 @@ __global__ void __launch_bounds__(kPruneThreads) batch_blen_kernel(BatchDev b, B
         iv.child = b.child + it.node_off;
         iv.root_w = b.model + it.model_off + 36;
         iv.cat_w = b.model + it.model_off + 40 + b.C;
+        const double* mdl = b.model + it.model_off;
+        // the item's model in FP32: eigenvectors, rates rho_km = lambda_m r_k
+        if (tid < 16) {
+            s_mf.L[tid] = (float)mdl[4 + tid];
+            s_mf.R[tid] = (float)mdl[20 + tid];
+        } else if (tid < 16 + CM * 4) {
+            const int k = (tid - 16) / 4, m = (tid - 16) % 4;
+            s_mf.rho[k][m] = k < b.C ? (float)(mdl[m] * mdl[40 + k]) : 0.0f;
+        }
         TileJob j;
         j.ops = b.ops + it.ops_off;
         j.n_ops = it.n_ops;
@@ -426,32 +507,44 @@ __global__ void __launch_bounds__(kPruneThreads) batch_blen_kernel(BatchDev b, B
         j.site_lnl = nullptr;
         j.max_depth = b.max_depth;
         DStore ds{sD, sED};
-        double ts = 0.0, tc = 0.0;
+        double ts = 0.0, tc = 0.0;  // untouched with STORE_D (no root)
         run_tile<CM, 1, CODES_SMEM, true>(j, sm, ts, tc, &ds);
         const int site = j.tile_base + tid;
         const bool valid = site < it.n_sites;
         const int site_c = min(site, it.site_stride - 1);
         phase_b<CM>(iv, b, site_c, tid, sD, sED, sO, sEO);
+        const Weights32<CM> w32 = weights32<CM>(iv, b.C);
+        const BlenModel32<CM>& mf = s_mf;
         const long long out_off = bd.unit_edge_off[u_idx];
         const int n_slots = 2 * it.n_int;
-        for (int s0 = 0; s0 < n_slots; s0 += 32) {
-            const int count = min(32, n_slots - s0);
+        for (int s0 = 0; s0 < n_slots; s0 += kBlenSlots) {
+            const int count = min(kBlenSlots, n_slots - s0);
+            // exp(rho_km t) of every edge of this pass
+            for (int q = tid; q < count * CM * 4; q += kPruneThreads) {
+                const int si = q / (CM * 4), km = q % (CM * 4);
+                const int slot = s0 + si;
+                const int2 ch = iv.child[it.n_tips + slot / 2];
+                const int v = (slot % 2 == 0) ? ch.x : ch.y;
+                const float t = v >= 0 ? (float)b.t_eff[it.node_off + v] : 0.0f;
+                s_ex[si][km] = expf(mf.rho[km / 4][km % 4] * t);
+            }
+            __syncthreads();
             for (int si = 0; si < count; ++si) {
                 const int slot = s0 + si;
                 const int u = it.n_tips + slot / 2;
                 const int2 ch = iv.child[u];
                 const int v = (slot % 2 == 0) ? ch.x : ch.y;
                 const int w = (slot % 2 == 0) ? ch.y : ch.x;
-                double d1 = 0.0, d2 = 0.0;
-                if (valid && v >= 0) edge_site_derivs<CM>(iv, b, u, v, w, site_c, tid, sD, sED, sO, &d1, &d2);
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    d1 += __shfl_down_sync(0xffffffffu, d1, off);
-                    d2 += __shfl_down_sync(0xffffffffu, d2, off);
-                }
+                float d1 = 0.0f, d2 = 0.0f;
+                if (valid && v >= 0)
+                    edge_site_derivs<CM>(iv, b, u, v, w, site_c, tid, sD, sED, sO, mf, s_ex[si], w32.root, w32.cat,
+                                         &d1, &d2);
+                float c1 = 0.0f, c2 = 0.0f;
+                warp_two_sum_f(d1, c1);
+                warp_two_sum_f(d2, c2);
                 if (lane == 0) {
-                    s_red[warp][si][0] = d1;
-                    s_red[warp][si][1] = d2;
+                    s_red[warp][si][0] = (double)d1 + (double)c1;
+                    s_red[warp][si][1] = (double)d2 + (double)c2;
                 }
             }
             __syncthreads();

@@ -480,11 +480,13 @@ __global__ void __launch_bounds__(32 * WARPS) prune20_kernel(P20Args g) {
 }
 
 // per site: log(sum_k w_k L_k 2^e_k) with the largest exponent factored out,
-// then the compensated block sums the reduce kernel finishes
+// then the compensated block sums (added up by the last CTA when
+// grid_done is set, else by the reduce kernel)
 __global__ void __launch_bounds__(kThreads) combine20_kernel(const double* __restrict__ cat_L,
                                                              const int* __restrict__ cat_E, const double* cat_w,
                                                              int C, int n_sites, double* site_lnl,
-                                                             double* block_sum) {
+                                                             double* block_sum, unsigned* grid_done,
+                                                             double* lnl_out) {
     const int site = blockIdx.x * blockDim.x + threadIdx.x;
     double s = 0.0, c = 0.0;
     if (site < n_sites) {
@@ -502,6 +504,7 @@ __global__ void __launch_bounds__(kThreads) combine20_kernel(const double* __res
         block_sum[2 * blockIdx.x] = s;
         block_sum[2 * blockIdx.x + 1] = c;
     }
+    if (grid_done) finish_grid_sum(block_sum, grid_done, lnl_out);
 }
 
 size_t smem20_bytes(const PruneArgs& a, int mode) {
@@ -581,7 +584,7 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int variant, void* s
     if (e != cudaSuccess) return e;
     const int blocks = (a.n_sites + kThreads - 1) / kThreads;
     combine20_kernel<<<blocks, kThreads, 0, st>>>(g.cat_L, g.cat_E, a.cat_w, a.C, a.n_sites, a.site_lnl,
-                                                  a.block_sum);
+                                                  a.block_sum, a.grid_done, a.lnl_out);
     *n_blocks = blocks;
     return cudaGetLastError();
 }

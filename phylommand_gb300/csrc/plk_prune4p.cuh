@@ -1,0 +1,299 @@
+// Per-tile body of the paired-category 4-state FP32 post-order pass (see
+// plk_prune4p.cu), shared by the single-tree and the batch kernels.
+//
+// The tile walks the op list like run_tile (plk_prune4s.cuh), but every value
+// is a pair (category 2q, category 2q+1) held in one 64-bit register, so each
+// product P(t) x v, child product and rescale is one fma.rn.f32x2 /
+// mul.rn.f32x2 for two categories.  Every lane rounds exactly as the scalar
+// fmaf / fmul of run_tile in the same order, so per-site results are the
+// same bits.
+//
+// Paired layouts (one block of C x 16 floats per node, C x 64 per tip):
+//   P:   [node][pair q][row j][state i][2]      (P_{2q}[i][j], P_{2q+1}[i][j])
+//   tip: [tip][pair q][half][code][state i in the half][2]
+// Each code's tip row sits in two 16-byte planes (states 0-1 and 2-3): with
+// one 32-byte row per code, codes 4 and 8 (C and T) would share banks.
+#pragma once
+
+#include "plk_prune4s.cuh"
+
+namespace plk {
+namespace dev {
+
+typedef unsigned long long u64;
+
+__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;\n" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;\n" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 pack2(float lo, float hi) {
+    u64 r;
+    asm("mov.b64 %0, {%1, %2};\n" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(u64 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;\n" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+// Offset of P_k[i][j] inside a node's paired block.
+__host__ __device__ inline int paired_p_index(int k, int i, int j) {
+    return ((k >> 1) * 4 + j) * 8 + i * 2 + (k & 1);
+}
+// Offset of tip_k[code][i] inside a tip's paired block.
+__host__ __device__ inline int paired_tip_index(int k, int code, int i) {
+    return (((k >> 1) * 2 + (i >> 1)) * kCodes + code) * 4 + (i & 1) * 2 + (k & 1);
+}
+
+template <int KP>
+struct alignas(16) StageP {
+    u64 p[2][KP][4][4];             // [child][pair][row j][state i]
+    u64 tip[2][KP][2][kCodes][2];   // [child][pair][half][code][state in the half]
+};
+
+// Shared memory: three stage slots | ops | tip codes (optional) | spill stack.
+template <int KP, int SPT, bool CODES_SMEM>
+__host__ __device__ inline size_t tile4p_smem_bytes(int n_ops, int n_tips, int max_depth) {
+    constexpr int TILE = kPruneThreads * SPT;
+    const size_t depth = (size_t)(max_depth > 0 ? max_depth : 1);
+    size_t s = 3 * sizeof(StageP<KP>) + align16((size_t)n_ops * sizeof(Op));
+    if (CODES_SMEM) s += align16((size_t)n_tips * TILE);
+    s += depth * SPT * KP * 4 * sizeof(u64) * kPruneThreads;
+    return s;
+}
+
+inline size_t tile4p_smem_min(int C, int spt, int n_ops, int n_tips, int max_depth) {
+    switch (C) {
+        case 2: return spt == 1 ? tile4p_smem_bytes<1, 1, false>(n_ops, n_tips, max_depth)
+                                : tile4p_smem_bytes<1, 2, false>(n_ops, n_tips, max_depth);
+        case 4: return spt == 1 ? tile4p_smem_bytes<2, 1, false>(n_ops, n_tips, max_depth)
+                                : tile4p_smem_bytes<2, 2, false>(n_ops, n_tips, max_depth);
+        case 8: return spt == 1 ? tile4p_smem_bytes<4, 1, false>(n_ops, n_tips, max_depth)
+                                : tile4p_smem_bytes<4, 2, false>(n_ops, n_tips, max_depth);
+        default: return 0;
+    }
+}
+
+template <int KP>
+__device__ __forceinline__ void stage_op4p(StageP<KP>* st, const Op& op, const float* __restrict__ Pp,
+                                           const float* __restrict__ Tp) {
+    // 16-byte chunks: internal child KP * 8, tip child KP * 32
+    const int n0 = (op.s0 >= 0) ? KP * 32 : KP * 8;
+    const int n1 = (op.s1 == kSrcNone) ? 0 : ((op.s1 >= 0) ? KP * 32 : KP * 8);
+    for (int i = threadIdx.x; i < n0 + n1; i += blockDim.x) {
+        const int c = i < n0 ? 0 : 1;
+        const int q = c ? i - n0 : i;
+        const int src = c ? op.s1 : op.s0;
+        if (src >= 0) {
+            cp_async16(reinterpret_cast<float*>(st->tip[c]) + 4 * q, Tp + (size_t)src * KP * 128 + 4 * q);
+        } else {
+            const int e = c ? op.e1 : op.e0;
+            cp_async16(reinterpret_cast<float*>(st->p[c]) + 4 * q, Pp + (size_t)e * KP * 32 + 4 * q);
+        }
+    }
+}
+
+// out[q][i] = sum_j P[q][j][i] x[q][j] for both categories of every pair,
+// j ascending with the first term a product (the order of run_tile)
+template <int KP>
+__device__ __forceinline__ void mv4p(const u64 (*P)[4][4], const u64 x[KP][4], u64 out[KP][4]) {
+#pragma unroll
+    for (int q = 0; q < KP; ++q) {
+        u64 r[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(&P[q][j][0]);
+            const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(&P[q][j][2]);
+            r[j][0] = a.x; r[j][1] = a.y; r[j][2] = b.x; r[j][3] = b.y;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            u64 acc = mul2(x[q][0], r[0][i]);
+            acc = fma2(x[q][1], r[1][i], acc);
+            acc = fma2(x[q][2], r[2][i], acc);
+            acc = fma2(x[q][3], r[3][i], acc);
+            out[q][i] = acc;
+        }
+    }
+}
+
+template <int KP>
+__device__ __forceinline__ void tip4p(const u64 (*T)[2][kCodes][2], int code, u64 out[KP][4]) {
+#pragma unroll
+    for (int q = 0; q < KP; ++q) {
+        const ulonglong2 a = *reinterpret_cast<const ulonglong2*>(&T[q][0][code][0]);
+        const ulonglong2 b = *reinterpret_cast<const ulonglong2*>(&T[q][1][code][0]);
+        out[q][0] = a.x; out[q][1] = a.y; out[q][2] = b.x; out[q][3] = b.y;
+    }
+}
+
+// One tile of 128 x SPT sites of one tree with C = 2 KP categories; j.P and
+// j.tipT are the tree's paired P(t) and tip blocks.  Leaves this thread's
+// compensated partial sum of the site log-likelihoods in (tsum, tcomp) and
+// writes each site's value to j.site_lnl when it is not null.  Ends with no
+// cp.async in flight; the caller must __syncthreads() before reusing the
+// shared memory.
+template <int KP, int SPT, bool CODES_SMEM>
+__device__ void run_tile4p(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp) {
+    constexpr int TILE = kPruneThreads * SPT;
+    StageP<KP>* stages = reinterpret_cast<StageP<KP>*>(sm);
+    size_t off = 3 * sizeof(StageP<KP>);
+    Op* s_ops = reinterpret_cast<Op*>(sm + off);
+    off += align16((size_t)j.n_ops * sizeof(Op));
+    uint8_t* s_codes = sm + off;
+    if (CODES_SMEM) off += align16((size_t)j.n_tips * TILE);
+    ulonglong2* s_stack = reinterpret_cast<ulonglong2*>(sm + off);
+    const float* __restrict__ Pp = j.P;
+    const float* __restrict__ Tp = j.tipT;
+
+    const int tid = threadIdx.x;
+    for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
+    if (CODES_SMEM) {
+        constexpr int chunks = TILE / 16;
+        for (int i = tid; i < j.n_tips * chunks; i += kPruneThreads) {
+            const int t = i / chunks, q = i % chunks, col = j.tile_base + 16 * q;
+            uint8_t* dst = s_codes + (size_t)t * TILE + 16 * q;
+            if (col < j.site_stride) cp_async16(dst, j.codes + (size_t)t * j.site_stride + col);
+            else *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    __syncthreads();
+    stage_op4p<KP>(&stages[0], s_ops[0], Pp, Tp);
+    cp_async_commit();
+    if (j.n_ops > 1) stage_op4p<KP>(&stages[1], s_ops[1], Pp, Tp);
+    cp_async_commit();
+
+    u64 acc[SPT][KP][4];
+    int scale_e[SPT];
+    const u64 one2 = pack2(1.0f, 1.0f);
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+        scale_e[s] = 0;
+#pragma unroll
+        for (int q = 0; q < KP; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[s][q][i] = one2;
+    }
+    int sp = 0;
+
+    for (int o = 0; o < j.n_ops; ++o) {
+        cp_async_wait<1>();
+        __syncthreads();
+        if (o + 2 < j.n_ops) stage_op4p<KP>(&stages[(o + 2) % 3], s_ops[o + 2], Pp, Tp);
+        cp_async_commit();
+        const Op op = s_ops[o];
+        const StageP<KP>& stg = stages[o % 3];
+        if (op.s0 == kSrcPop) --sp;
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) {
+            const int lsite = tid + s * kPruneThreads;
+            u64 d0[KP][4], d1[KP][4];
+            if (op.s0 >= 0) {
+                int code;
+                if (CODES_SMEM) code = s_codes[(size_t)op.s0 * TILE + lsite];
+                else code = j.codes[(size_t)op.s0 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+                tip4p<KP>(stg.tip[0], code & (kCodes - 1), d0);
+            } else if (op.s0 == kSrcPop) {
+                u64 x[KP][4];
+#pragma unroll
+                for (int q = 0; q < KP; ++q)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const ulonglong2 v = s_stack[((size_t)((sp * SPT + s) * KP + q) * 2 + h) * kPruneThreads + tid];
+                        x[q][2 * h] = v.x;
+                        x[q][2 * h + 1] = v.y;
+                    }
+                mv4p<KP>(stg.p[0], x, d0);
+            } else {
+                mv4p<KP>(stg.p[0], acc[s], d0);
+            }
+            if (op.s1 >= 0) {
+                int code;
+                if (CODES_SMEM) code = s_codes[(size_t)op.s1 * TILE + lsite];
+                else code = j.codes[(size_t)op.s1 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+                tip4p<KP>(stg.tip[1], code & (kCodes - 1), d1);
+            } else if (op.s1 == kSrcAcc) {
+                mv4p<KP>(stg.p[1], acc[s], d1);
+            }
+            if (op.s1 == kSrcNone) {
+#pragma unroll
+                for (int q = 0; q < KP; ++q)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[s][q][i] = d0[q][i];
+            } else {
+#pragma unroll
+                for (int q = 0; q < KP; ++q)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[q][i], d1[q][i]);
+            }
+            float mx = 0.0f;
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    float lo, hi;
+                    unpack2(acc[s][q][i], lo, hi);
+                    mx = fmaxf(mx, fmaxf(lo, hi));
+                }
+            if (mx < scale_threshold<float>() && mx > 0.0f) {
+                int e;
+                float f1, f2;
+                pow2_factors(mx, &e, &f1, &f2);
+                const u64 g1 = pack2(f1, f1), g2 = pack2(f2, f2);
+#pragma unroll
+                for (int q = 0; q < KP; ++q)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(mul2(acc[s][q][i], g1), g2);
+                scale_e[s] += e;
+            }
+            if (op.push) {
+#pragma unroll
+                for (int q = 0; q < KP; ++q)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        s_stack[((size_t)((sp * SPT + s) * KP + q) * 2 + h) * kPruneThreads + tid] =
+                            make_ulonglong2(acc[s][q][2 * h], acc[s][q][2 * h + 1]);
+            }
+        }
+        if (op.push) ++sp;
+    }
+    cp_async_wait<0>();
+
+    // root: sum_k w_k sum_s L[s] root_w[s] in FP64 (categories in order)
+    tsum = 0.0;
+    tcomp = 0.0;
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+        const int site = j.tile_base + tid + s * kPruneThreads;
+        double lsum = 0.0;
+#pragma unroll
+        for (int q = 0; q < KP; ++q) {
+            float v[2][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[0][i], v[1][i]);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                double lk = (double)v[h][0] * j.root_w[0];
+#pragma unroll
+                for (int i = 1; i < 4; ++i) lk = fma((double)v[h][i], j.root_w[i], lk);
+                lsum = fma(j.cat_w[2 * q + h], lk, lsum);
+            }
+        }
+        if (site < j.n_sites) {
+            const double lnl = log(lsum) + (double)scale_e[s] * 0.69314718055994530942;
+            if (j.site_lnl) j.site_lnl[site] = lnl;
+            double ns, e;
+            two_sum(tsum, lnl, ns, e);
+            tsum = ns;
+            tcomp += e;
+        }
+    }
+}
+
+}  // namespace dev
+}  // namespace plk

@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4s_kernel(PruneArgs a) {
         a.block_sum[2 * blockIdx.x] = tsum;
         a.block_sum[2 * blockIdx.x + 1] = tcomp;
     }
+    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 template <int CM, int SPT, bool CODES_SMEM>

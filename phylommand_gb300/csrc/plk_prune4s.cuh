@@ -105,8 +105,9 @@ __device__ __forceinline__ void mv4(const float4* rows, const float x[4], float 
 // site log-likelihoods (TwoSum-compensated) to (tsum, tcomp) and writes them
 // to j.site_lnl when it is not null.  Ends with no cp.async in flight; the
 // caller must __syncthreads() before reusing the shared memory.  With
-// STORE_D, also writes the message every internal child sends to its parent
-// (and its exponent) to *ds; the per-node exponents are tracked for that.
+// STORE_D, writes instead the message every internal child sends to its
+// parent (and its exponent) to *ds, tracking the per-node exponents, and
+// skips the root (tsum and tcomp stay untouched).
 template <int CM, int SPT, bool CODES_SMEM, bool STORE_D = false>
 __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp,
                          const DStore* ds = nullptr) {
@@ -279,6 +280,7 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
         if (op.push) ++sp;
     }
     cp_async_wait<0>();
+    if constexpr (STORE_D) return;
 
     // root: sum_k w_k sum_s L[s] * root_w[s] in FP64, log, scaler exponents
 #pragma unroll

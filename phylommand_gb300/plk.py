@@ -46,7 +46,7 @@ EXPORTS = [
     "plk_sum_sites_noalloc", "plk_prune_variant", "plk_set_patterns", "plk_n_patterns",
     "plk_fit_gtr", "plk_fit_n_params",
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
-    "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning",
+    "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning", "plk_batch_form",
     "plk_batch_nni_count", "plk_batch_nni_moves", "plk_batch_nni_loglik", "plk_simulate", "plk_nni_moves_host",
     "plk_batch_features", "plk_batch_fit_gtr", "plk_batch_eval_gtr", "plk_batch_set_fit_method",
     "plk_set_fit_method", "plk_batch_edge_derivatives", "plk_batch_optimize_branches", "plk_batch_branch_lengths",
@@ -121,6 +121,7 @@ def lib() -> ctypes.CDLL:
     L.plk_batch_set_model.argtypes = [hp, c_int, dp, dp, dp, dp]
     L.plk_batch_loglik.argtypes = [hp, dp]
     L.plk_batch_tuning.argtypes = [hp, ip, ip, dp, ip]
+    L.plk_batch_form.argtypes = [hp, ip, ip]
     L.plk_batch_nni_count.argtypes = [hp, c_int]
     L.plk_batch_nni_moves.argtypes = [hp, c_int, ip]
     L.plk_batch_nni_loglik.argtypes = [hp, dp]
@@ -622,7 +623,10 @@ class Batch:
         ms = ctypes.c_double(0.0)
         self._check(lib().plk_batch_tuning(self._b, ctypes.byref(spt), ctypes.byref(grid), ctypes.byref(ms),
                                            ctypes.byref(graph)))
-        return {"sites_per_thread": spt.value, "grid": grid.value, "postorder_ms": ms.value, "graph": bool(graph.value)}
+        paired, codes = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(lib().plk_batch_form(self._b, ctypes.byref(paired), ctypes.byref(codes)))
+        return {"sites_per_thread": spt.value, "grid": grid.value, "postorder_ms": ms.value, "graph": bool(graph.value),
+                "paired": bool(paired.value), "codes_smem": bool(codes.value)}
 
 
 class MLP:

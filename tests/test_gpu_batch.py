@@ -84,6 +84,30 @@ def test_batch_paths_agree(monkeypatch, env):
     np.testing.assert_allclose(got, ref, rtol=1e-12)
 
 
+@pytest.mark.parametrize("C", [2, 4, 8])
+@pytest.mark.parametrize("spt", ["1", "2"])
+def test_paired_form_same_bits(monkeypatch, C, spt):
+    """Categories in pairs on the FP32x2 pipe round lane by lane like the
+    one-at-a-time body: with the same tile size the lnL bits agree."""
+    items = _items(seed=30 + C, C=C, shapes=SHAPES[:7])
+    monkeypatch.setenv("PLK_BATCH_SPT", spt)
+    got = {}
+    for paired in ("0", "1"):
+        monkeypatch.setenv("PLK_BATCH_PAIRED", paired)
+        with _batch(items, C) as b:
+            got[paired] = b.loglik()
+            tune = b.tuning()
+            assert tune["paired"] == (paired == "1") and tune["sites_per_thread"] == int(spt)
+            # a model update after tuning reaches the paired layouts too
+            masks, left, right, bl, Q, freqs, cr, cw = items[2]
+            b.set_model(2, Q, freqs, cr * 1.3, cw)
+            again = b.loglik()
+            assert again[2] == pytest.approx(_single(masks, left, right, bl, Q, freqs, cr * 1.3, cw), rel=1e-12)
+    assert np.array_equal(got["0"], got["1"])
+    for (masks, left, right, bl, Q, freqs, cr, cw), g in zip(items, got["1"]):
+        assert g == pytest.approx(_single(masks, left, right, bl, Q, freqs, cr, cw), rel=1e-12)
+
+
 @pytest.mark.parametrize("C", [4, 1])
 def test_nni_neighbours_match_explicit_trees(C):
     shapes = [(4, 60), (6, 129), (13, 300), (25, 77), (40, 1000)]

@@ -78,8 +78,13 @@ def test_optimize_branches_reaches_a_stationary_point():
             assert lnl[i] == pytest.approx(l64, rel=1e-6)
             # at least as good as the generating lengths (the ML point beats them)
             assert l64 >= _fp64(h, item, item[3]) - 1e-3
-            # stationary: every non-root edge longer than the floor has a small slope
+            # stationary: on every non-root edge off the length floor another
+            # Newton step would gain next to nothing, g^2 / (2 |c|), with the
+            # curvature negative (the two root edges act through their sum,
+            # so both carry the same slope)
             root = len(fitted) - 1
-            slope = np.abs(der[i][:root, 0])
+            g, c = der[i][:root, 0], der[i][:root, 1]
             free = fitted[:root] > 1e-6
-            assert np.all(slope[free] < 0.05 * np.sqrt(item[0].shape[1])), (i, slope[free].max())
+            assert np.all(c[free] < 0.0), (i, c[free].max())
+            gain = g[free] ** 2 / (2.0 * np.abs(c[free]))
+            assert gain.max() < 1e-3, (i, gain.max(), g[free][np.argmax(gain)], c[free][np.argmax(gain)])
