@@ -110,10 +110,11 @@ __device__ __forceinline__ void batch_prune_body(const BatchDev& b) {
         const int u = s_unit;
         if (u >= b.n_units) break;
         const TileJob j = unit_job(b, b.units[u], TILE, PAIRED);
-        double ts = 0.0, tc = 0.0;
-        if constexpr (PAIRED) run_tile4p<K, SPT, CODES_SMEM>(j, sm, ts, tc);
-        else run_tile<K, SPT, CODES_SMEM>(j, sm, ts, tc);
-        block_sum_pair(ts, tc);
+        SiteSum32 sum;
+        if constexpr (PAIRED) run_tile4p<K, SPT, CODES_SMEM>(j, sm, sum);
+        else run_tile<K, SPT, CODES_SMEM>(j, sm, sum);
+        double ts, tc;
+        block_sum_site32(sum, ts, tc);
         if (threadIdx.x == 0) {
             b.unit_sums[2 * u] = ts;
             b.unit_sums[2 * u + 1] = tc;

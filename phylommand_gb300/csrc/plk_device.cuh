@@ -87,6 +87,95 @@ __device__ __forceinline__ void block_sum_pair(double& s, double& c) {
     }
 }
 
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// FP32 TwoSum reduction of (hi, lo) over a warp; lane 0 ends with the pair
+__device__ __forceinline__ void warp_two_sum_f(float& hi, float& lo) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, hi, off);
+        const float ol = __shfl_down_sync(0xffffffffu, lo, off);
+        float ns, e;
+        two_sum_f(hi, oh, ns, e);
+        hi = ns;
+        lo = __fadd_rn(lo, __fadd_rn(ol, e));
+    }
+}
+
+// FP32 site log-likelihoods.  GB300's FP64 pipe retires a small fraction of
+// its FP32 rate, so the per-site root stays in FP32: a site's likelihood is
+// L = lsum 2^e (lsum the FP32 root sum, e the scaler exponent), and
+//   log L = lm + ee ln 2,   lm = log of the mantissa of lsum, in [0, ln 2),
+// so logf's error is absolute (about 6e-8), not relative to log L.
+__device__ __forceinline__ void site_log32(float lsum, int e, float& lm, int& ee) {
+    if (lsum > 0.0f && lsum < 1.17549435e-38f) {  // subnormal: exact rescale by 2^64
+        lsum *= 1.8446744073709552e19f;
+        e -= 64;
+    }
+    const int bits = __float_as_int(lsum);
+    ee = e + ((bits >> 23) & 255) - 127;
+    // zero, infinity and NaN keep logf's own result (-inf, inf, NaN)
+    lm = (lsum > 0.0f && lsum <= 3.40282347e38f) ? logf(__int_as_float((bits & 0x007fffff) | 0x3f800000))
+                                                 : logf(lsum);
+}
+
+__device__ __forceinline__ double site_lnl64(float lm, int ee) {
+    return fma((double)ee, 0.69314718055994530942, (double)lm);
+}
+
+// A thread's running sum of site log-likelihoods: the mantissa logs in FP32
+// TwoSum (hi, lo), the exponents as an integer.
+struct SiteSum32 {
+    float hi = 0.0f, lo = 0.0f;
+    int ee = 0;
+};
+
+__device__ __forceinline__ void site_sum_add(SiteSum32& a, float lm, int ee) {
+    float s, e;
+    two_sum_f(a.hi, lm, s, e);
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, e);
+    a.ee += ee;
+}
+
+// Block total of the threads' SiteSum32 as a compensated FP64 pair (s, c),
+// valid in thread 0: FP32 TwoSum and integer sums within each warp, FP64 from
+// the warp totals on.  All threads of the block must call it.
+__device__ inline void block_sum_site32(SiteSum32 a, double& s, double& c) {
+    warp_two_sum_f(a.hi, a.lo);
+    const int esum = __reduce_add_sync(0xffffffffu, a.ee);
+    __shared__ double r_s[32], r_c[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();  // an earlier call may still be reading r_s / r_c
+    if (lane == 0) {
+        double ws, we;
+        two_sum((double)esum * 0.69314718055994530942, (double)a.hi, ws, we);
+        r_s[warp] = ws;
+        r_c[warp] = we + (double)a.lo;
+    }
+    __syncthreads();
+    s = 0.0;
+    c = 0.0;
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        s = lane < nw ? r_s[lane] : 0.0;
+        c = lane < nw ? r_c[lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double os = __shfl_down_sync(0xffffffffu, s, off);
+            const double oc = __shfl_down_sync(0xffffffffu, c, off);
+            double ns, e;
+            two_sum(s, os, ns, e);
+            s = ns;
+            c = c + oc + e;
+        }
+    }
+}
+
 // Compensated sum of the n (sum, compensation) pairs of bs by one CTA:
 // thread i folds pairs i, i + blockDim.x, ... (TwoSum), then the block
 // reduction of block_sum_pair; the result is valid in thread 0.  Loads go

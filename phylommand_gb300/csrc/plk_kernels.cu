@@ -17,6 +17,7 @@
 //  preorder_kernel  outside vectors from the root down and normalised
 //                   marginal posteriors (absent in the reference).
 #include <cstdio>
+#include <type_traits>
 
 #include "plk_device.cuh"
 #include "plk_internal.h"
@@ -297,45 +298,56 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
             ++sp;
         }
     }
-    // ---- root: sum_k w_k sum_s L[s] * root_w[s]
-    double lsum = 0.0;
+    if constexpr (std::is_same<T, float>::value) {
+        // ---- root in FP32 and its log as lm + ee ln 2 (site_log32), in the
+        // operation order of run_tile: the same per-site bits as the staged
+        // kernels
+        float lsum = 0.0f;
 #pragma unroll
-    for (int k = 0; k < CM; ++k)
-        if (k < C) {
-            double lk;
-            if (EXACT) {
-                lk = __dmul_rn((double)acc[k][0], a.root_w[0]);
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                float lk = acc[k][0] * (float)a.root_w[0];
 #pragma unroll
-                for (int s = 1; s < 4; ++s) lk = __dadd_rn(lk, __dmul_rn((double)acc[k][s], a.root_w[s]));
-                lsum = (k == 0) ? __dmul_rn(a.cat_w[0], lk) : __dadd_rn(lsum, __dmul_rn(a.cat_w[k], lk));
-            } else {
-                lk = (double)acc[k][0] * a.root_w[0];
-#pragma unroll
-                for (int s = 1; s < 4; ++s) lk = fma((double)acc[k][s], a.root_w[s], lk);
-                lsum = fma(a.cat_w[k], lk, lsum);
+                for (int s = 1; s < 4; ++s) lk = fmaf(acc[k][s], (float)a.root_w[s], lk);
+                lsum = fmaf((float)a.cat_w[k], lk, lsum);
             }
+        SiteSum32 sum;
+        if (valid) {
+            float lm;
+            int ee;
+            site_log32(lsum, scale_e, lm, ee);
+            a.site_lnl[site] = site_lnl64(lm, ee);
+            site_sum_add(sum, lm, ee);
         }
-    const double lnl = valid ? log(lsum) + (double)scale_e * 0.69314718055994530942 : 0.0;
-    if (valid) a.site_lnl[site] = lnl;
-    // ---- compensated block reduction
-    double s = valid ? lnl : 0.0, c = 0.0;
+        double s, c;
+        block_sum_site32(sum, s, c);
+        if (threadIdx.x == 0) {
+            a.block_sum[2 * blockIdx.x] = s;
+            a.block_sum[2 * blockIdx.x + 1] = c;
+        }
+    } else {
+        // ---- root: sum_k w_k sum_s L[s] * root_w[s]
+        double lsum = 0.0;
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const double os = __shfl_down_sync(0xffffffffu, s, off);
-        const double oc = __shfl_down_sync(0xffffffffu, c, off);
-        double ns, e;
-        two_sum(s, os, ns, e);
-        s = ns;
-        c = c + oc + e;
-    }
-    __shared__ double red_s[32], red_c[32];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = blockDim.x >> 5;
-        s = lane < nw ? red_s[lane] : 0.0;
-        c = lane < nw ? red_c[lane] : 0.0;
+        for (int k = 0; k < CM; ++k)
+            if (k < C) {
+                double lk;
+                if (EXACT) {
+                    lk = __dmul_rn((double)acc[k][0], a.root_w[0]);
+#pragma unroll
+                    for (int s = 1; s < 4; ++s) lk = __dadd_rn(lk, __dmul_rn((double)acc[k][s], a.root_w[s]));
+                    lsum = (k == 0) ? __dmul_rn(a.cat_w[0], lk) : __dadd_rn(lsum, __dmul_rn(a.cat_w[k], lk));
+                } else {
+                    lk = (double)acc[k][0] * a.root_w[0];
+#pragma unroll
+                    for (int s = 1; s < 4; ++s) lk = fma((double)acc[k][s], a.root_w[s], lk);
+                    lsum = fma(a.cat_w[k], lk, lsum);
+                }
+            }
+        const double lnl = valid ? log(lsum) + (double)scale_e * 0.69314718055994530942 : 0.0;
+        if (valid) a.site_lnl[site] = lnl;
+        // ---- compensated block reduction
+        double s = valid ? lnl : 0.0, c = 0.0;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             const double os = __shfl_down_sync(0xffffffffu, s, off);
@@ -345,9 +357,27 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
             s = ns;
             c = c + oc + e;
         }
-        if (lane == 0) {
-            a.block_sum[2 * blockIdx.x] = s;
-            a.block_sum[2 * blockIdx.x + 1] = c;
+        __shared__ double red_s[32], red_c[32];
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) { red_s[warp] = s; red_c[warp] = c; }
+        __syncthreads();
+        if (warp == 0) {
+            const int nw = blockDim.x >> 5;
+            s = lane < nw ? red_s[lane] : 0.0;
+            c = lane < nw ? red_c[lane] : 0.0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const double os = __shfl_down_sync(0xffffffffu, s, off);
+                const double oc = __shfl_down_sync(0xffffffffu, c, off);
+                double ns, e;
+                two_sum(s, os, ns, e);
+                s = ns;
+                c = c + oc + e;
+            }
+            if (lane == 0) {
+                a.block_sum[2 * blockIdx.x] = s;
+                a.block_sum[2 * blockIdx.x + 1] = c;
+            }
         }
     }
     if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);

@@ -245,25 +245,6 @@ __device__ __forceinline__ void move_site_log(const ItemView& iv, const BatchDev
     *lm = logf(__int_as_float((bits & 0x007fffff) | 0x3f800000));
 }
 
-__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// FP32 TwoSum reduction of (hi, lo) over a warp; lane 0 ends with the pair
-__device__ __forceinline__ void warp_two_sum_f(float& hi, float& lo) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float oh = __shfl_down_sync(0xffffffffu, hi, off);
-        const float ol = __shfl_down_sync(0xffffffffu, lo, off);
-        float ns, e;
-        two_sum_f(hi, oh, ns, e);
-        hi = ns;
-        lo = __fadd_rn(lo, __fadd_rn(ol, e));
-    }
-}
-
 template <int CM, bool CODES_SMEM>
 __global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -309,8 +290,8 @@ __global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
         j.site_lnl = nullptr;
         j.max_depth = b.max_depth;
         DStore ds{sD, sED};
-        double ts = 0.0, tc = 0.0;  // untouched with STORE_D (no root)
-        run_tile<CM, 1, CODES_SMEM, true>(j, sm, ts, tc, &ds);
+        SiteSum32 unused;  // untouched with STORE_D (no root)
+        run_tile<CM, 1, CODES_SMEM, true>(j, sm, unused, &ds);
         // phases B and C touch only this thread's site column of the scratch
         const int site = j.tile_base + tid;
         const bool valid = site < it.n_sites;
@@ -507,8 +488,8 @@ __global__ void __launch_bounds__(kPruneThreads) batch_blen_kernel(BatchDev b, B
         j.site_lnl = nullptr;
         j.max_depth = b.max_depth;
         DStore ds{sD, sED};
-        double ts = 0.0, tc = 0.0;  // untouched with STORE_D (no root)
-        run_tile<CM, 1, CODES_SMEM, true>(j, sm, ts, tc, &ds);
+        SiteSum32 unused;  // untouched with STORE_D (no root)
+        run_tile<CM, 1, CODES_SMEM, true>(j, sm, unused, &ds);
         const int site = j.tile_base + tid;
         const bool valid = site < it.n_sites;
         const int site_c = min(site, it.site_stride - 1);

@@ -60,9 +60,10 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, con
     j.tile_base = blockIdx.x * kPruneThreads * SPT;
     j.site_lnl = a.site_lnl;
     j.max_depth = a.max_depth;
+    SiteSum32 sum;
+    run_tile4p<KP, SPT, CODES_SMEM>(j, sm, sum);
     double tsum, tcomp;
-    run_tile4p<KP, SPT, CODES_SMEM>(j, sm, tsum, tcomp);
-    block_sum_pair(tsum, tcomp);
+    block_sum_site32(sum, tsum, tcomp);
     if (threadIdx.x == 0) {
         a.block_sum[2 * blockIdx.x] = tsum;
         a.block_sum[2 * blockIdx.x + 1] = tcomp;

@@ -133,13 +133,13 @@ __device__ __forceinline__ void tip4p(const u64 (*T)[2][kCodes][2], int code, u6
 }
 
 // One tile of 128 x SPT sites of one tree with C = 2 KP categories; j.P and
-// j.tipT are the tree's paired P(t) and tip blocks.  Leaves this thread's
-// compensated partial sum of the site log-likelihoods in (tsum, tcomp) and
+// j.tipT are the tree's paired P(t) and tip blocks.  Adds this thread's site
+// log-likelihoods to sum (the root and log of run_tile, same bits) and
 // writes each site's value to j.site_lnl when it is not null.  Ends with no
 // cp.async in flight; the caller must __syncthreads() before reusing the
 // shared memory.
 template <int KP, int SPT, bool CODES_SMEM>
-__device__ void run_tile4p(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp) {
+__device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) {
     constexpr int TILE = kPruneThreads * SPT;
     StageP<KP>* stages = reinterpret_cast<StageP<KP>*>(sm);
     size_t off = 3 * sizeof(StageP<KP>);
@@ -264,13 +264,17 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, double& tsum, do
     }
     cp_async_wait<0>();
 
-    // root: sum_k w_k sum_s L[s] root_w[s] in FP64 (categories in order)
-    tsum = 0.0;
-    tcomp = 0.0;
+    // root: L = sum_k w_k sum_s v_k[s] root_w[s] in FP32 (categories in
+    // order, as run_tile), log L = lm + ee ln 2
+    float rw[4], cw[2 * KP];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) rw[i] = (float)j.root_w[i];
+#pragma unroll
+    for (int k = 0; k < 2 * KP; ++k) cw[k] = (float)j.cat_w[k];
 #pragma unroll
     for (int s = 0; s < SPT; ++s) {
         const int site = j.tile_base + tid + s * kPruneThreads;
-        double lsum = 0.0;
+        float lsum = 0.0f;
 #pragma unroll
         for (int q = 0; q < KP; ++q) {
             float v[2][4];
@@ -278,19 +282,18 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, double& tsum, do
             for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[0][i], v[1][i]);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                double lk = (double)v[h][0] * j.root_w[0];
+                float lk = v[h][0] * rw[0];
 #pragma unroll
-                for (int i = 1; i < 4; ++i) lk = fma((double)v[h][i], j.root_w[i], lk);
-                lsum = fma(j.cat_w[2 * q + h], lk, lsum);
+                for (int i = 1; i < 4; ++i) lk = fmaf(v[h][i], rw[i], lk);
+                lsum = fmaf(cw[2 * q + h], lk, lsum);
             }
         }
         if (site < j.n_sites) {
-            const double lnl = log(lsum) + (double)scale_e[s] * 0.69314718055994530942;
-            if (j.site_lnl) j.site_lnl[site] = lnl;
-            double ns, e;
-            two_sum(tsum, lnl, ns, e);
-            tsum = ns;
-            tcomp += e;
+            float lm;
+            int ee;
+            site_log32(lsum, scale_e[s], lm, ee);
+            if (j.site_lnl) j.site_lnl[site] = site_lnl64(lm, ee);
+            site_sum_add(sum, lm, ee);
         }
     }
 }

@@ -43,9 +43,10 @@ __global__ void __launch_bounds__(kPruneThreads) prune4s_kernel(PruneArgs a) {
     j.tile_base = blockIdx.x * kPruneThreads * SPT;
     j.site_lnl = a.site_lnl;
     j.max_depth = a.max_depth;
-    double tsum = 0.0, tcomp = 0.0;
-    run_tile<CM, SPT, CODES_SMEM>(j, sm, tsum, tcomp);
-    block_sum_pair(tsum, tcomp);
+    SiteSum32 sum;
+    run_tile<CM, SPT, CODES_SMEM>(j, sm, sum);
+    double tsum, tcomp;
+    block_sum_site32(sum, tsum, tcomp);
     if (threadIdx.x == 0) {
         a.block_sum[2 * blockIdx.x] = tsum;
         a.block_sum[2 * blockIdx.x + 1] = tcomp;

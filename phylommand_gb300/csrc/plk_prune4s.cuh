@@ -102,15 +102,14 @@ __device__ __forceinline__ void mv4(const float4* rows, const float x[4], float 
 }
 
 // Runs one tile; every thread of the CTA must call it.  Adds this thread's
-// site log-likelihoods (TwoSum-compensated) to (tsum, tcomp) and writes them
-// to j.site_lnl when it is not null.  Ends with no cp.async in flight; the
+// site log-likelihoods to sum (site_log32: FP32 root, FP32 TwoSum) and
+// writes them to j.site_lnl when it is not null.  Ends with no cp.async in flight; the
 // caller must __syncthreads() before reusing the shared memory.  With
 // STORE_D, writes instead the message every internal child sends to its
 // parent (and its exponent) to *ds, tracking the per-node exponents, and
-// skips the root (tsum and tcomp stay untouched).
+// skips the root (sum stays untouched).
 template <int CM, int SPT, bool CODES_SMEM, bool STORE_D = false>
-__device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, double& tcomp,
-                         const DStore* ds = nullptr) {
+__device__ void run_tile(const TileJob& j, unsigned char* sm, SiteSum32& sum, const DStore* ds = nullptr) {
     constexpr int TILE = kPruneThreads * SPT;
     Stage<CM>* stages = reinterpret_cast<Stage<CM>*>(sm);
     size_t off = 3 * sizeof(Stage<CM>);
@@ -282,26 +281,30 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, double& tsum, doub
     cp_async_wait<0>();
     if constexpr (STORE_D) return;
 
-    // root: sum_k w_k sum_s L[s] * root_w[s] in FP64, log, scaler exponents
+    // root: L = sum_k w_k sum_s v_k[s] root_w[s] in FP32, log L = lm + ee ln 2
+    float rw[4], cw[CM];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) rw[i] = (float)j.root_w[i];
+#pragma unroll
+    for (int k = 0; k < CM; ++k) cw[k] = k < C ? (float)j.cat_w[k] : 0.0f;
 #pragma unroll
     for (int s = 0; s < SPT; ++s) {
         const int site = j.tile_base + tid + s * kPruneThreads;
-        double lsum = 0.0;
+        float lsum = 0.0f;
 #pragma unroll
         for (int k = 0; k < CM; ++k)
             if (k < C) {
-                double lk = (double)acc[s][k][0] * j.root_w[0];
+                float lk = acc[s][k][0] * rw[0];
 #pragma unroll
-                for (int i = 1; i < 4; ++i) lk = fma((double)acc[s][k][i], j.root_w[i], lk);
-                lsum = fma(j.cat_w[k], lk, lsum);
+                for (int i = 1; i < 4; ++i) lk = fmaf(acc[s][k][i], rw[i], lk);
+                lsum = fmaf(cw[k], lk, lsum);
             }
         if (site < j.n_sites) {
-            const double lnl = log(lsum) + (double)scale_e[s] * 0.69314718055994530942;
-            if (j.site_lnl) j.site_lnl[site] = lnl;
-            double ns, e;
-            two_sum(tsum, lnl, ns, e);
-            tsum = ns;
-            tcomp += e;
+            float lm;
+            int ee;
+            site_log32(lsum, scale_e[s], lm, ee);
+            if (j.site_lnl) j.site_lnl[site] = site_lnl64(lm, ee);
+            site_sum_add(sum, lm, ee);
         }
     }
 }
