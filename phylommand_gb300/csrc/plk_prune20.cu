@@ -19,9 +19,10 @@
 // ring.  Every node vector gets a fresh slot (slots are allocated uniformly
 // across the CTA), so no op reads and writes the same shared memory.
 //
-// The root sums pi_s L[s] per (site, category) in FP64 and leaves it with
+// The root sums pi_s L[s] per (site, category) in FP32 and leaves it with
 // the category's scaler exponent; combine20_kernel forms
-// log(sum_k w_k L_k 2^e_k) per site and the compensated block sums.
+// log(sum_k w_k L_k 2^e_k) per site in FP32 (site_log32) and the compensated
+// block sums.
 #include "plk_device.cuh"
 #include "plk_internal.h"
 
@@ -57,7 +58,7 @@ struct P20Args {
     int mode;            // 1 = CUDA cores, 2 = tensor cores
     const float* Ps;     // staged P per (node, category)
     const float* Ts;     // staged tip tables per (tip, category)
-    double* cat_L;       // [C][n_sites]
+    float* cat_L;        // [C][n_sites] root sums of each category (FP32)
     int* cat_E;          // [C][n_sites]
     int n_slots;
 };
@@ -296,6 +297,8 @@ __global__ void __launch_bounds__(32 * WARPS) prune20_kernel(P20Args g) {
     sm.slots = reinterpret_cast<float*>(smem + off);
     const size_t slot_floats = (size_t)kRows * kLD;
 
+    __shared__ float s_rw[kS];  // root weights in FP32
+    if (tid < kS) s_rw[tid] = (float)a.root_w[tid];
     for (int i = tid; i < a.n_ops; i += NT) sm.ops[i] = a.ops[i];
     {
         constexpr int chunks = kTile / 16;
@@ -443,14 +446,14 @@ __global__ void __launch_bounds__(32 * WARPS) prune20_kernel(P20Args g) {
     cp_async_wait<0>();
     __syncthreads();
 
-    // root: L = sum_s pi_s R[s] per site in FP64 (this category)
+    // root: L = sum_s pi_s R[s] per site in FP32 (this category)
     const float* R = sm.slots + (size_t)cur * slot_floats;
     if constexpr (MODE == 1) {
 #pragma unroll
         for (int s = 0; s < SPS; ++s) {
-            double l = 0.0;
+            float l = 0.0f;
 #pragma unroll
-            for (int r = 0; r < 5; ++r) l = fma((double)R[(5 * grp + r) * kLD + sbase + s], a.root_w[5 * grp + r], l);
+            for (int r = 0; r < 5; ++r) l = fmaf(R[(5 * grp + r) * kLD + sbase + s], s_rw[5 * grp + r], l);
             l += __shfl_xor_sync(0xffffffffu, l, 1);
             l += __shfl_xor_sync(0xffffffffu, l, 2);
             const int site = tile0 + sbase + s;
@@ -466,8 +469,8 @@ __global__ void __launch_bounds__(32 * WARPS) prune20_kernel(P20Args g) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int ls = warp * SW + mt * 16 + gg + 8 * h;
-                double l = 0.0;
-                for (int i = t; i < kS; i += 4) l = fma((double)R[i * kLD + ls], a.root_w[i], l);
+                float l = 0.0f;
+                for (int i = t; i < kS; i += 4) l = fmaf(R[i * kLD + ls], s_rw[i], l);
                 l += __shfl_xor_sync(0xffffffffu, l, 1);
                 l += __shfl_xor_sync(0xffffffffu, l, 2);
                 const int site = tile0 + ls;
@@ -480,26 +483,30 @@ __global__ void __launch_bounds__(32 * WARPS) prune20_kernel(P20Args g) {
 }
 
 // per site: log(sum_k w_k L_k 2^e_k) with the largest exponent factored out,
-// then the compensated block sums (added up by the last CTA when
-// grid_done is set, else by the reduce kernel)
-__global__ void __launch_bounds__(kThreads) combine20_kernel(const double* __restrict__ cat_L,
+// in FP32 (site_log32), then the compensated block sums (added up by the
+// last CTA when grid_done is set)
+__global__ void __launch_bounds__(kThreads) combine20_kernel(const float* __restrict__ cat_L,
                                                              const int* __restrict__ cat_E, const double* cat_w,
                                                              int C, int n_sites, double* site_lnl,
                                                              double* block_sum, unsigned* grid_done,
                                                              double* lnl_out) {
     const int site = blockIdx.x * blockDim.x + threadIdx.x;
-    double s = 0.0, c = 0.0;
+    SiteSum32 sum;
     if (site < n_sites) {
         int E = cat_E[site];
         for (int k = 1; k < C; ++k) E = max(E, cat_E[(size_t)k * n_sites + site]);
-        double sum = 0.0;
+        float l = 0.0f;
         for (int k = 0; k < C; ++k)
-            sum = fma(cat_w[k], ldexp(cat_L[(size_t)k * n_sites + site], cat_E[(size_t)k * n_sites + site] - E), sum);
-        const double lnl = log(sum) + (double)E * 0.69314718055994530942;
-        site_lnl[site] = lnl;
-        s = lnl;
+            l = fmaf((float)cat_w[k], ldexpf(cat_L[(size_t)k * n_sites + site], cat_E[(size_t)k * n_sites + site] - E),
+                     l);
+        float lm;
+        int ee;
+        site_log32(l, E, lm, ee);
+        site_lnl[site] = site_lnl64(lm, ee);
+        site_sum_add(sum, lm, ee);
     }
-    block_sum_pair(s, c);
+    double s, c;
+    block_sum_site32(sum, s, c);
     if (threadIdx.x == 0) {
         block_sum[2 * blockIdx.x] = s;
         block_sum[2 * blockIdx.x + 1] = c;
@@ -530,7 +537,8 @@ size_t prune20_scratch_bytes(const PruneArgs& a, int n_nodes) {
                                                                                 : tip_floats_per_code(2));
     const size_t ps = (size_t)n_nodes * a.C * pf * sizeof(float);
     const size_t ts = (size_t)a.n_tips * a.C * a.n_codes * tf * sizeof(float);
-    const size_t cl = (size_t)a.C * a.n_sites * (sizeof(double) + sizeof(int));
+    const size_t cl = (((size_t)a.C * a.n_sites * sizeof(float) + 255) & ~(size_t)255) +
+                      (size_t)a.C * a.n_sites * sizeof(int);
     return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl;
 }
 
@@ -552,8 +560,8 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int variant, void* s
     size_t off = (((size_t)n_nodes * a.C * pf_max * sizeof(float)) + 255) & ~(size_t)255;
     g.Ts = reinterpret_cast<float*>(base + off);
     off += (ts_max + 255) & ~(size_t)255;
-    g.cat_L = reinterpret_cast<double*>(base + off);
-    off += (size_t)a.C * a.n_sites * sizeof(double);
+    g.cat_L = reinterpret_cast<float*>(base + off);
+    off += (((size_t)a.C * a.n_sites * sizeof(float)) + 255) & ~(size_t)255;
     g.cat_E = reinterpret_cast<int*>(base + off);
     g.n_slots = a.max_depth + 2;
     (void)ps;
