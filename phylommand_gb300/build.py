@@ -19,7 +19,7 @@ LIB = os.path.join(LIB_DIR, "libplk.so")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["plk_kernels.cu", "plk_prune4s.cu", "plk_prune4p.cu", "plk_prune20.cu", "plk_batch.cu", "plk_nni.cu", "plk_features.cu",
+CU_SOURCES = ["plk_kernels.cu", "plk_prune4s.cu", "plk_prune4p.cu", "plk_prune20.cu", "plk_prune20u.cu", "plk_batch.cu", "plk_nni.cu", "plk_features.cu",
               "plk_mlp.cu", "plk_noalloc.cu"]
 CPP_SOURCES = ["plk_api.cpp", "plk_host.cpp", "plk_fit.cpp", "plk_batch_api.cpp", "plk_sim.cpp", "plk_io.cpp"]
 

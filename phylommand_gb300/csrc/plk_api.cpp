@@ -334,8 +334,10 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     if (!store && precision == PLK_FP32S && h->S == 20)
         for (int v = 1; v <= 4; ++v)
             if (prune20_fits(a, v)) cands20.push_back(v);
+    if (!store && precision == PLK_FP32S && h->S == 20 && prune20u_fits(a)) cands20.push_back(5);
     if (!cands20.empty()) {
-        PLK_CUDA(h, h->d_work.ensure(prune20_scratch_bytes(a, h->n_nodes)), "allocate scratch");
+        PLK_CUDA(h, h->d_work.ensure(std::max(prune20_scratch_bytes(a, h->n_nodes), prune20u_scratch_bytes(a, h->n_nodes))),
+                 "allocate scratch");
         a.scratch = h->d_work.p;
         if (h->variant < 0) {
             plk_status s = autotune_prune(h, a, cands20);

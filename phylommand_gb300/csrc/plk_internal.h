@@ -201,8 +201,10 @@ struct PruneArgs {
     // prune4_kernel, 1/2 = prune4s_kernel with 1/2 sites per thread, 3/4 =
     // prune4p_kernel (category pairs on FP32x2) with 1/2 sites per thread,
     // 5/6 = the same reading the tip codes from global memory.
-    // 20 states: 0 = prune_generic_kernel, 1 = prune20_kernel on CUDA cores,
-    // 2 = prune20_kernel on tensor cores (TF32, three-product split).
+    // 20 states: 0 = prune_generic_kernel, 1 / 2 = prune20_kernel on CUDA
+    // cores / mma.sync tensor cores (TF32, three-product split) with 4 warps
+    // per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel on
+    // tcgen05 tensor cores (TMEM accumulators).
     int variant;
     int n_nodes;
     void* scratch;             // kernel-specific scratch (prune20_scratch_bytes)
@@ -220,6 +222,15 @@ bool prune20_fits(const PruneArgs& a, int mode);
 size_t prune20_scratch_bytes(const PruneArgs& a, int n_nodes);
 cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scratch, int* n_blocks,
                            cudaStream_t st);
+// Per-site log(sum_k w_k L_k 2^e_k) from the FP32 category root sums and
+// exponents ([C][n_sites] each), the block sums and the total.
+cudaError_t launch_combine20(const float* cat_L, const int* cat_E, const PruneArgs& a, int* n_blocks,
+                             cudaStream_t st);
+// 20 states on tcgen05 tensor cores with TMEM accumulators (plk_prune20u.cu):
+// the B-operand relayout, the pass and the per-site combine.
+bool prune20u_fits(const PruneArgs& a);
+size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes);
+cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int* n_blocks, cudaStream_t st);
 // Staged 4-state FP32 kernel with categories in pairs on the packed FP32x2
 // pipe (plk_prune4p.cu), C = 2, 4 or 8; needs prune4p_scratch_bytes of
 // a.scratch for the paired P(t) and tip tables.

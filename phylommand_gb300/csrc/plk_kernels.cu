@@ -549,7 +549,9 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
         return launch_prune4s(a, a.variant, n_blocks, st);
     if (!fp64 && !store && S == 4 && a.variant >= 3 && a.variant <= 6 && prune4p_fits(a, (a.variant + 1) % 2 + 1))
         return launch_prune4p(a, (a.variant + 1) % 2 + 1, a.variant >= 5, n_blocks, st);
-    if (!fp64 && !store && S == 20 && a.variant > 0 && prune20_fits(a, a.variant))
+    if (!fp64 && !store && S == 20 && a.variant == 5 && prune20u_fits(a))
+        return launch_prune20u(a, a.n_nodes, a.scratch, n_blocks, st);
+    if (!fp64 && !store && S == 20 && a.variant > 0 && a.variant < 5 && prune20_fits(a, a.variant))
         return launch_prune20(a, a.n_nodes, a.variant, a.scratch, n_blocks, st);
     if (S == 4 && a.C <= 8) {
         const size_t ops_bytes = ((size_t)a.n_ops * sizeof(Op) + 31) & ~(size_t)31;

@@ -590,9 +590,14 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int variant, void* s
     else e = warps == 4 ? run(prune20_kernel<2, 4>) : run(prune20_kernel<2, 8>);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    return launch_combine20(g.cat_L, g.cat_E, a, n_blocks, st);
+}
+
+cudaError_t launch_combine20(const float* cat_L, const int* cat_E, const PruneArgs& a, int* n_blocks,
+                             cudaStream_t st) {
     const int blocks = (a.n_sites + kThreads - 1) / kThreads;
-    combine20_kernel<<<blocks, kThreads, 0, st>>>(g.cat_L, g.cat_E, a.cat_w, a.C, a.n_sites, a.site_lnl,
-                                                  a.block_sum, a.grid_done, a.lnl_out);
+    combine20_kernel<<<blocks, kThreads, 0, st>>>(cat_L, cat_E, a.cat_w, a.C, a.n_sites, a.site_lnl, a.block_sum,
+                                                  a.grid_done, a.lnl_out);
     *n_blocks = blocks;
     return cudaGetLastError();
 }

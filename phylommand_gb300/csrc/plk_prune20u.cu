@@ -1,0 +1,464 @@
+// prune20u: the 20-state FP32 post-order pass (src/simpleML.cpp:127-197 for
+// S = 20) with the child messages on Blackwell's fifth-generation tensor
+// cores: tcgen05.mma kind::tf32 with the accumulators in tensor memory (TMEM).
+//
+// A CTA takes 128 sites of one rate category (grid = tiles x C); thread t
+// owns site t, which is lane t of the TMEM accumulators.  For an internal
+// child the message M[site][i] = sum_j V[site][j] P[i][j] is one
+// M = 128 x N = 32 x K = 24 product (20 states, padded), split in TF32 hi and
+// lo parts, V_lo P_hi + V_hi P_lo + V_hi P_hi (about FP32 accuracy): nine
+// tcgen05.mma of K = 8 issued by one thread into a TMEM accumulator and
+// completed through an mbarrier.  Operands sit in shared memory in the
+// K-major canonical layout without swizzle (8-row x 16-byte core matrices,
+// 128 bytes between row blocks (SBO), the 4-column groups LBO apart):
+//   * the running vector and a vector popped from the spill stack are written
+//     row by row by their threads as A operands (hi and lo parts);
+//   * P(t) arrives as a B operand image prepared by relayout20u_kernel and is
+//     staged through a three-slot cp.async ring, two ops ahead;
+//   * spilled vectors are thread-private rows in TMEM (tcgen05.st / ld).
+// Tip children are look-ups in the staged tip table.  The root forms
+// sum_s pi_s L[s] per site in FP32 for combine20_kernel.
+//
+// Every mbarrier wait is bounded: a wait that runs out sets the tile's sites
+// to NaN (the evaluation then fails with a numeric error) and the CTA still
+// frees its TMEM.  TMEM per CTA: 64 columns for the two accumulators plus 32
+// per spill slot, rounded up to a power of two; the dynamic shared memory is
+// padded so that no more CTAs fit on an SM than its 512 columns serve, so an
+// allocation never waits.
+#include <algorithm>
+
+#include "plk_device.cuh"
+#include "plk_internal.h"
+
+namespace plk {
+using namespace dev;
+
+namespace {
+
+constexpr int kS = 20;
+constexpr int kTile = 128;
+constexpr int kThreads = 128;
+constexpr int kN = 32;                   // MMA N: output states, padded
+constexpr int kAGroup = 16 * 128;        // bytes of a 4-column group of an A operand (LBO of A)
+constexpr int kAPart = 6 * kAGroup;      // one TF32 part of an A operand (K = 24)
+constexpr int kAOperand = 2 * kAPart;    // hi and lo
+constexpr int kBGroup = 4 * 128;         // bytes of a 4-column group of a B operand (LBO of B)
+constexpr int kBPart = 6 * kBGroup;
+constexpr int kBFloats = 2 * kBPart / 4;  // staged B image per (node, category): 1,536 floats
+constexpr int kTipStride = 28;            // floats per code in the staged tip table
+constexpr int kAccCols = 64;              // TMEM columns of the two accumulators
+constexpr int kSlotCols = 32;             // TMEM columns per spill slot (20 used)
+constexpr uint32_t kIdesc = (1u << 4)          // D: F32
+                            | (2u << 7)        // A: TF32
+                            | (2u << 10)       // B: TF32
+                            | ((kN >> 3) << 17)    // N
+                            | ((128 >> 4) << 24);  // M
+constexpr int kWaitLimit = 1 << 22;       // try_wait rounds before a wait gives up
+
+struct P20UArgs {
+    PruneArgs a;
+    const float* Ps;   // B images [node][category][kBFloats]
+    const float* Ts;   // tip tables [tip][category][code][kTipStride]
+    float* cat_L;      // [C][n_sites]
+    int* cat_E;        // [C][n_sites]
+    int child_bytes;   // bytes of one child's slot in a stage
+    int tmem_cols;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle (layout type 0),
+// descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (int i = 0; i < kWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// 20 columns of this thread's TMEM lane, the wait for the load inside the
+// same statement so that no use of x can move ahead of it (warp-collective:
+// the warp reconverges first)
+__device__ __forceinline__ void tmem_ld20(uint32_t taddr, float x[kS]) {
+    uint32_t r[kS];
+    __syncwarp();
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%20];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%21];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19])
+        : "r"(taddr), "r"(taddr + 16)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < kS; ++i) x[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_st20(uint32_t taddr, const float x[kS]) {
+    __syncwarp();
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17};\n"
+        "tcgen05.st.sync.aligned.32x32b.x4.b32 [%1], {%18,%19,%20,%21};\n"
+        "tcgen05.wait::st.sync.aligned;\n" ::"r"(taddr),
+        "r"(taddr + 16), "r"(__float_as_uint(x[0])), "r"(__float_as_uint(x[1])), "r"(__float_as_uint(x[2])),
+        "r"(__float_as_uint(x[3])), "r"(__float_as_uint(x[4])), "r"(__float_as_uint(x[5])),
+        "r"(__float_as_uint(x[6])), "r"(__float_as_uint(x[7])), "r"(__float_as_uint(x[8])),
+        "r"(__float_as_uint(x[9])), "r"(__float_as_uint(x[10])), "r"(__float_as_uint(x[11])),
+        "r"(__float_as_uint(x[12])), "r"(__float_as_uint(x[13])), "r"(__float_as_uint(x[14])),
+        "r"(__float_as_uint(x[15])), "r"(__float_as_uint(x[16])), "r"(__float_as_uint(x[17])),
+        "r"(__float_as_uint(x[18])), "r"(__float_as_uint(x[19]))
+        : "memory");
+}
+
+// row t of an A operand: TF32 hi and lo parts of the 20 values (columns
+// 20-23 stay zero from the start)
+__device__ __forceinline__ void write_operand(unsigned char* area, int t, const float x[kS]) {
+    const int row = (t >> 3) * 128 + (t & 7) * 16;
+#pragma unroll
+    for (int g = 0; g < 5; ++g) {
+        float4 h, l;
+        h.x = tf32_rna(x[4 * g]);
+        h.y = tf32_rna(x[4 * g + 1]);
+        h.z = tf32_rna(x[4 * g + 2]);
+        h.w = tf32_rna(x[4 * g + 3]);
+        l.x = tf32_rna(x[4 * g] - h.x);
+        l.y = tf32_rna(x[4 * g + 1] - h.y);
+        l.z = tf32_rna(x[4 * g + 2] - h.z);
+        l.w = tf32_rna(x[4 * g + 3] - h.w);
+        *reinterpret_cast<float4*>(area + g * kAGroup + row) = h;
+        *reinterpret_cast<float4*>(area + kAPart + g * kAGroup + row) = l;
+    }
+}
+
+// nine MMAs of one child message into the accumulator at d_tmem
+__device__ __forceinline__ void issue_child(uint32_t d_tmem, uint32_t a_addr, uint32_t b_addr) {
+#pragma unroll
+    for (int ks = 0; ks < 3; ++ks) {
+        const uint64_t a_hi = smem_desc(a_addr + ks * 2 * kAGroup, kAGroup, 128);
+        const uint64_t a_lo = smem_desc(a_addr + kAPart + ks * 2 * kAGroup, kAGroup, 128);
+        const uint64_t b_hi = smem_desc(b_addr + ks * 2 * kBGroup, kBGroup, 128);
+        const uint64_t b_lo = smem_desc(b_addr + kBPart + ks * 2 * kBGroup, kBGroup, 128);
+        umma_tf32(d_tmem, a_lo, b_hi, ks > 0 ? 1u : 0u);  // small products first
+        umma_tf32(d_tmem, a_hi, b_lo, 1u);
+        umma_tf32(d_tmem, a_hi, b_hi, 1u);
+    }
+}
+
+// P(t) as B operand images and tip tables with a 28-float stride per code
+__global__ void relayout20u_kernel(const float* __restrict__ P, const float* __restrict__ tip, int n_nodes,
+                                   int n_tips, int C, int n_codes, float* __restrict__ Ps, float* __restrict__ Ts) {
+    const long long n_p = (long long)n_nodes * C * kBFloats;
+    const long long n_t = (long long)n_tips * C * n_codes * kTipStride;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n_p + n_t;
+         idx += (long long)gridDim.x * blockDim.x) {
+        if (idx < n_p) {
+            // [part][group g][row block nb][row r][column c]: state i = 8 nb + r, j = 4 g + c
+            const long long nk = idx / kBFloats;
+            const int w = (int)(idx % kBFloats);
+            const int part = w / (kBPart / 4), q = w % (kBPart / 4);
+            const int g = q / 128, nb = (q / 32) % 4, r = (q / 4) % 8, c = q % 4;
+            const int i = 8 * nb + r, j = 4 * g + c;
+            float v = 0.0f;
+            if (i < kS && j < kS) {
+                const float x = P[nk * kS * kS + i * kS + j];
+                const float hi = tf32_rna(x);
+                v = part == 0 ? hi : tf32_rna(x - hi);
+            }
+            Ps[idx] = v;
+        } else {
+            const long long t = idx - n_p;
+            const long long nkc = t / kTipStride;
+            const int w = (int)(t % kTipStride);
+            Ts[t] = w < kS ? tip[nkc * kS + w] : 0.0f;
+        }
+    }
+}
+
+__device__ __forceinline__ void stage_op20u(unsigned char* dst, const Op& op, int k, const P20UArgs& g) {
+    const PruneArgs& a = g.a;
+    for (int c = 0; c < 2; ++c) {
+        const int src = c ? op.s1 : op.s0;
+        if (src == kSrcNone) continue;
+        const float* from;
+        int n;
+        if (src >= 0) {
+            n = a.n_codes * kTipStride;
+            from = g.Ts + ((size_t)src * a.C + k) * (size_t)n;
+        } else {
+            n = kBFloats;
+            from = g.Ps + ((size_t)(c ? op.e1 : op.e0) * a.C + k) * (size_t)kBFloats;
+        }
+        float* to = reinterpret_cast<float*>(dst + c * g.child_bytes);
+        for (int q = threadIdx.x; q < n / 4; q += kThreads) cp_async16(to + 4 * q, from + 4 * q);
+    }
+}
+
+__device__ __forceinline__ void tip_row(const unsigned char* stage_child, int code, int n_codes, float m[kS]) {
+    code = code < n_codes ? code : 0;
+    const float* row = reinterpret_cast<const float*>(stage_child) + code * kTipStride;
+#pragma unroll
+    for (int g = 0; g < 5; ++g) {
+        const float4 v = *reinterpret_cast<const float4*>(row + 4 * g);
+        m[4 * g] = v.x;
+        m[4 * g + 1] = v.y;
+        m[4 * g + 2] = v.z;
+        m[4 * g + 3] = v.w;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ uint32_t s_tmem;
+    __shared__ float s_rw[kS];
+    __shared__ int s_abort;
+    const PruneArgs& a = g.a;
+    const int k = blockIdx.y;
+    const int tile0 = blockIdx.x * kTile;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int cb = g.child_bytes;
+    unsigned char* acc_op = smem;               // A operand of the running vector
+    unsigned char* pop_op = smem + kAOperand;   // A operand of a vector popped from the stack
+    unsigned char* stages = smem + 2 * kAOperand;
+    Op* s_ops = reinterpret_cast<Op*>(stages + 3 * 2 * cb);
+    uint8_t* s_codes = reinterpret_cast<uint8_t*>(s_ops) + (((size_t)a.n_ops * sizeof(Op) + 15) & ~(size_t)15);
+    const uint32_t mbar = smem_u32(&s_mbar);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_tmem)),
+                     "r"(g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    if (tid < kS) s_rw[tid] = (float)a.root_w[tid];
+    for (int i = tid; i < a.n_ops; i += kThreads) s_ops[i] = a.ops[i];
+    {
+        constexpr int chunks = kTile / 16;
+        for (int i = tid; i < a.n_tips * chunks; i += kThreads) {
+            const int t = i / chunks, q = i % chunks, col = tile0 + 16 * q;
+            uint8_t* dst = s_codes + (size_t)t * kTile + 16 * q;
+            if (col < a.site_stride) cp_async16(dst, a.codes + (size_t)t * a.site_stride + col);
+            else *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    // columns 20-23 (group 5) of both parts of both A operands stay zero
+    for (int i = tid; i < 4 * (kAGroup / 16); i += kThreads) {
+        const int part = i / (kAGroup / 16), q = i % (kAGroup / 16);
+        unsigned char* base = (part < 2 ? acc_op : pop_op) + (part % 2) * kAPart + 5 * kAGroup;
+        reinterpret_cast<uint4*>(base)[q] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
+    stage_op20u(stages, s_ops[0], k, g);
+    cp_async_commit();
+    if (a.n_ops > 1) stage_op20u(stages + 2 * cb, s_ops[1], k, g);
+    cp_async_commit();
+
+    float m0[kS], m1[kS];
+    int e_site = 0, sp = 0;
+    uint32_t phase = 0;
+    bool pending = false;  // an MMA commit whose completion was not observed
+    for (int o = 0; o < a.n_ops; ++o) {
+        cp_async_wait<1>();
+        const Op op = s_ops[o];
+        if (op.s0 == kSrcPop) {
+            --sp;
+            tmem_ld20(lane + kAccCols + kSlotCols * sp, m0);
+            write_operand(pop_op, tid, m0);
+        }
+        fence_proxy_async();  // cp.async data and operand rows -> the tensor cores
+        tc_fence_before();
+        __syncthreads();
+        if (s_abort) break;
+        if (o + 2 < a.n_ops) stage_op20u(stages + ((o + 2) % 3) * 2 * cb, s_ops[o + 2], k, g);
+        cp_async_commit();
+        const unsigned char* st = stages + (o % 3) * 2 * cb;
+        const bool mma0 = op.s0 < 0, mma1 = op.s1 == kSrcAcc;
+        if (tid == 0 && (mma0 || mma1)) {
+            tc_fence_after();
+            if (mma0) issue_child(tmem, smem_u32(op.s0 == kSrcPop ? pop_op : acc_op), smem_u32(st));
+            if (mma1) issue_child(tmem + 32, smem_u32(acc_op), smem_u32(st + cb));
+            umma_commit(mbar);
+        }
+        if (op.s0 >= 0) tip_row(st, s_codes[(size_t)op.s0 * kTile + tid], a.n_codes, m0);
+        if (op.s1 >= 0) tip_row(st + cb, s_codes[(size_t)op.s1 * kTile + tid], a.n_codes, m1);
+        if (mma0 || mma1) {
+            pending = true;
+            if (!mbar_wait(mbar, phase)) s_abort = 1;
+            else pending = false;
+            phase ^= 1u;
+            tc_fence_after();
+            if (mma0) tmem_ld20(lane, m0);
+            if (mma1) tmem_ld20(lane + 32, m1);
+        }
+        if (op.s1 != kSrcNone) {
+#pragma unroll
+            for (int i = 0; i < kS; ++i) m0[i] *= m1[i];
+        }
+        float mx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kS; ++i) mx = fmaxf(mx, m0[i]);
+        if (mx < scale_threshold<float>() && mx > 0.0f) {
+            int e;
+            float f1, f2;
+            pow2_factors(mx, &e, &f1, &f2);
+#pragma unroll
+            for (int i = 0; i < kS; ++i) m0[i] = (m0[i] * f1) * f2;
+            e_site += e;
+        }
+        if (o == a.n_ops - 1) break;  // the root vector stays in m0
+        if (op.push) {
+            tmem_st20(lane + kAccCols + kSlotCols * sp, m0);
+            ++sp;
+        } else {
+            write_operand(acc_op, tid, m0);
+        }
+    }
+    cp_async_wait<0>();
+    if (pending) mbar_wait(mbar, phase ^ 1u);  // a commit still in flight after a timed-out wait
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(g.tmem_cols)
+                     : "memory");
+    }
+    // root: L = sum_s pi_s R[s] in FP32 (this category)
+    float l = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kS; ++i) l = fmaf(m0[i], s_rw[i], l);
+    if (s_abort) l = __int_as_float(0x7fc00000);  // NaN: the evaluation reports a numeric error
+    const int site = tile0 + tid;
+    if (site < a.n_sites) {
+        g.cat_L[(size_t)k * a.n_sites + site] = l;
+        g.cat_E[(size_t)k * a.n_sites + site] = e_site;
+    }
+}
+
+int tmem_cols_for(const PruneArgs& a) {
+    const int need = kAccCols + kSlotCols * std::max(a.max_depth, 1);
+    int cols = 32;
+    while (cols < need) cols *= 2;
+    return cols;
+}
+
+int child_bytes_for(const PruneArgs& a) {
+    const int tip = a.n_codes * kTipStride * 4;
+    return (std::max(2 * kBPart, tip) + 127) & ~127;
+}
+
+size_t smem20u_bytes(const PruneArgs& a) {
+    return (size_t)2 * kAOperand + (size_t)3 * 2 * child_bytes_for(a) +
+           (((size_t)a.n_ops * sizeof(Op) + 15) & ~(size_t)15) + (size_t)a.n_tips * kTile;
+}
+
+}  // namespace
+
+bool prune20u_fits(const PruneArgs& a) {
+    if (a.C < 1 || a.n_codes < 1 || a.n_ops < 1) return false;
+    if (tmem_cols_for(a) > 512) return false;
+    return smem20u_bytes(a) <= 200 * 1024;
+}
+
+size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes) {
+    const size_t ps = (size_t)n_nodes * a.C * kBFloats * sizeof(float);
+    const size_t ts = (size_t)a.n_tips * a.C * a.n_codes * kTipStride * sizeof(float);
+    const size_t cl = (((size_t)a.C * a.n_sites * sizeof(float) + 255) & ~(size_t)255) +
+                      (size_t)a.C * a.n_sites * sizeof(int);
+    return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl;
+}
+
+cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int* n_blocks, cudaStream_t st) {
+    if (!prune20u_fits(a) || scratch == nullptr) return cudaErrorInvalidValue;
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    P20UArgs g{};
+    g.a = a;
+    g.Ps = reinterpret_cast<float*>(base);
+    size_t off = (((size_t)n_nodes * a.C * kBFloats * sizeof(float)) + 255) & ~(size_t)255;
+    g.Ts = reinterpret_cast<float*>(base + off);
+    off += (((size_t)a.n_tips * a.C * a.n_codes * kTipStride * sizeof(float)) + 255) & ~(size_t)255;
+    g.cat_L = reinterpret_cast<float*>(base + off);
+    off += (((size_t)a.C * a.n_sites * sizeof(float)) + 255) & ~(size_t)255;
+    g.cat_E = reinterpret_cast<int*>(base + off);
+    g.child_bytes = child_bytes_for(a);
+    g.tmem_cols = tmem_cols_for(a);
+    {
+        const long long total =
+            (long long)n_nodes * a.C * kBFloats + (long long)a.n_tips * a.C * a.n_codes * kTipStride;
+        long long blocks = (total + 255) / 256;
+        if (blocks > 152 * 8) blocks = 152 * 8;
+        relayout20u_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),
+                                                              static_cast<const float*>(a.tipT), n_nodes, a.n_tips,
+                                                              a.C, a.n_codes, const_cast<float*>(g.Ps),
+                                                              const_cast<float*>(g.Ts));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    // pad the shared memory until no more CTAs fit on an SM than its TMEM serves
+    const int max_ctas = 512 / g.tmem_cols;
+    size_t smem = smem20u_bytes(a);
+    int occ = 0;
+    for (;;) {
+        cudaError_t e = cudaFuncSetAttribute(prune20u_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, prune20u_kernel, kThreads, smem);
+        if (e != cudaSuccess) return e;
+        if (occ <= max_ctas) break;
+        smem += 4096;
+        if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    }
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    dim3 grid((a.n_sites + kTile - 1) / kTile, a.C);
+    prune20u_kernel<<<grid, kThreads, smem, st>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_combine20(g.cat_L, g.cat_E, a, n_blocks, st);
+}
+
+}  // namespace plk

@@ -101,6 +101,20 @@ __device__ __forceinline__ void mv4(const float4* rows, const float x[4], float 
     }
 }
 
+// Tip codes of an op's children at this thread's SPT sites, read from global
+// memory (0 where a child is no tip).  The tile bodies load them one op ahead
+// of their use, so that the L2 latency hides behind an op's work.
+template <int SPT>
+__device__ __forceinline__ void load_op_codes(const TileJob& j, const Op& op, int tid, int (&c0)[SPT],
+                                              int (&c1)[SPT]) {
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+        const int col = min(j.tile_base + tid + s * kPruneThreads, j.site_stride - 1);
+        c0[s] = op.s0 >= 0 ? (int)__ldg(j.codes + (size_t)op.s0 * j.site_stride + col) : 0;
+        c1[s] = op.s1 >= 0 ? (int)__ldg(j.codes + (size_t)op.s1 * j.site_stride + col) : 0;
+    }
+}
+
 // Runs one tile; every thread of the CTA must call it.  Adds this thread's
 // site log-likelihoods to sum (site_log32: FP32 root, FP32 TwoSum) and
 // writes them to j.site_lnl when it is not null.  Ends with no cp.async in flight; the
@@ -158,6 +172,8 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, SiteSum32& sum, co
             for (int i = 0; i < 4; ++i) acc[s][k][i] = 1.0f;
     }
     int sp = 0;
+    int pc0[SPT], pc1[SPT];  // tip codes of op o when they are read from global memory
+    if constexpr (!CODES_SMEM) load_op_codes<SPT>(j, s_ops[0], tid, pc0, pc1);
 
     for (int o = 0; o < j.n_ops; ++o) {
         cp_async_wait<1>();
@@ -165,6 +181,9 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, SiteSum32& sum, co
         if (o + 2 < j.n_ops) stage_op<CM>(&stages[(o + 2) % 3], s_ops[o + 2], C, P, tipT);
         cp_async_commit();
         const Op op = s_ops[o];
+        int nc0[SPT] = {}, nc1[SPT] = {};
+        if constexpr (!CODES_SMEM)
+            if (o + 1 < j.n_ops) load_op_codes<SPT>(j, s_ops[o + 1], tid, nc0, nc1);
         const Stage<CM>& stg = stages[o % 3];
         if (op.s0 == kSrcPop) --sp;
 #pragma unroll
@@ -180,7 +199,7 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, SiteSum32& sum, co
             if (op.s0 >= 0) {
                 int code;
                 if (CODES_SMEM) code = s_codes[(size_t)op.s0 * TILE + lsite];
-                else code = j.codes[(size_t)op.s0 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+                else code = pc0[s];
                 code &= kCodes - 1;
 #pragma unroll
                 for (int k = 0; k < CM; ++k)
@@ -206,7 +225,7 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, SiteSum32& sum, co
             if (op.s1 >= 0) {
                 int code;
                 if (CODES_SMEM) code = s_codes[(size_t)op.s1 * TILE + lsite];
-                else code = j.codes[(size_t)op.s1 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+                else code = pc1[s];
                 code &= kCodes - 1;
 #pragma unroll
                 for (int k = 0; k < CM; ++k)
@@ -277,6 +296,13 @@ __device__ void run_tile(const TileJob& j, unsigned char* sm, SiteSum32& sum, co
             }
         }
         if (op.push) ++sp;
+        if constexpr (!CODES_SMEM) {
+#pragma unroll
+            for (int s = 0; s < SPT; ++s) {
+                pc0[s] = nc0[s];
+                pc1[s] = nc1[s];
+            }
+        }
     }
     cp_async_wait<0>();
     if constexpr (STORE_D) return;

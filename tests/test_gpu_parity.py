@@ -256,17 +256,18 @@ def test_full_size_dna_gtr_gamma_fp32_against_fp64():
 @pytest.mark.parametrize("n_tips,n_sites,C,shape", [(64, 2000, 4, "yule"), (7, 1, 1, "yule"), (33, 129, 8, "yule"),
                                                     (200, 300, 4, "caterpillar"), (16, 4099, 2, "yule")])
 def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
-    """20 states: prune20_kernel on CUDA cores (1) and on tensor cores with
-    the split-TF32 products (2) against the FP64 oracle, per site; the
-    caterpillar tree forces repeated rescaling, ambiguity codes the table
-    look-ups."""
+    """20 states: prune20_kernel on CUDA cores (1, 3) and on mma.sync tensor
+    cores with the split-TF32 products (2, 4), and prune20u_kernel on tcgen05
+    tensor cores with TMEM accumulators (5), against the FP64 oracle, per
+    site; the caterpillar tree forces repeated rescaling and spills, ambiguity
+    codes the table look-ups."""
     rng = np.random.default_rng(n_tips * 7 + n_sites)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, S=20, C=C, missing=0.03, shape=shape)
     amb = rng.random(masks.shape) < 0.02
     masks[amb] |= np.uint32(1 << 3)                          # two-state ambiguity
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
-    for v in ("1", "2", "3", "4"):
+    for v in ("5", "1", "2", "3", "4"):
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
             got = h.loglik(plk.PLK_FP32S)
