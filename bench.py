@@ -272,6 +272,21 @@ def run_ours(args, world, rank, local):
 
     e2e_value, lnl_e2e = e2e_run(masks8)
     e2e32_value, _ = e2e_run(masks32)
+    # where an end-to-end step goes: the host time of each call (the uploads
+    # are asynchronous, so their device work overlaps the calls after them;
+    # plk_loglik waits for everything)
+    calls = (("set_alignment8", lambda: h.set_alignment(masks8, w.n_states)),
+             ("set_tree", lambda: h.set_tree(w.left, w.right, w.bl)),
+             ("set_rate_model", lambda: h.set_rate_model(False)),
+             ("set_model", lambda: h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)),
+             ("loglik", lambda: h.loglik(plk.PLK_FP32S)))
+    e2e_parts = {name: 0.0 for name, _ in calls}
+    for _ in range(e2e_steps):
+        for name, call in calls:
+            t0 = time.perf_counter()
+            call()
+            e2e_parts[name] += time.perf_counter() - t0
+    e2e_parts = {name: 1e3 * t / e2e_steps for name, t in e2e_parts.items()}
     h2d = masks8.nbytes + small
     h.close()
 
@@ -322,11 +337,12 @@ def run_ours(args, world, rank, local):
                 "path": "plk_set_alignment8 (pinned byte masks) + plk_set_tree + plk_set_rate_model + "
                         "plk_set_model + plk_loglik",
                 "with_32bit_masks": {"value": e2e32_value, "h2d_bytes_per_step": int(masks32.nbytes + small),
-                                     "path": "plk_set_alignment (pinned 32-bit masks) + the same calls"}},
-        # per evaluation: P(t) and the post-order pass (whose last CTA adds up
-        # the total), and for the paired kernel the relayout of P(t) and the
-        # tip tables
-        "gpu_launches": (3 if h_variant.startswith("prune4p") else 2) * args.steps,
+                                     "path": "plk_set_alignment (pinned 32-bit masks) + the same calls"},
+                "host_ms_per_call": e2e_parts},
+        # per evaluation: P(t) (which also writes the paired layouts of the
+        # tuned prune4p form) and the post-order pass, whose last CTA adds up
+        # the total
+        "gpu_launches": 2 * args.steps,
         "error_vs_fp64_oracle": {"abs": abs(lnl_timed - orc.lnl), "rel": abs(lnl_timed - orc.lnl) / abs(orc.lnl),
                                  "fp64_engine_rel": abs(lnl64 - orc.lnl) / abs(orc.lnl),
                                  "e2e_rel": abs(lnl_e2e - orc.lnl) / abs(orc.lnl)},

@@ -47,6 +47,14 @@ struct DevBuf {
     T* as() const { return static_cast<T*>(p); }
 };
 
+// A device array inside a DevBuf block that holds a group of arrays uploaded
+// together (upload_group); not owned.
+struct DevView {
+    void* p = nullptr;
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
 }  // namespace
 
 plk_status plk::report_error(plk_status s, const std::string& msg) {
@@ -78,7 +86,8 @@ struct plk_handle {
     std::vector<int> left, right, post, rank;
     std::vector<double> bl;
     Program prog;
-    DevBuf d_ops, d_order, d_left, d_right, d_rank;
+    DevBuf d_tree_block;  // the tree's arrays, one upload (upload_group)
+    DevView d_ops, d_order, d_left, d_right, d_rank;
     // rate model
     bool root_quirk = true;
     std::vector<float> cut_off, cut_rate, clade_rate;
@@ -90,12 +99,14 @@ struct plk_handle {
     bool have_model = false;
     int C = 1, p_kind = 0, reversible = 1;
     std::vector<double> Q, root_w, cat_rate, cat_w, lam, L, R;
-    DevBuf d_Q, d_rootw, d_catr, d_catw, d_lam, d_L, d_R;
+    DevBuf d_model_block;  // the model's arrays, one upload (upload_group)
+    DevView d_Q, d_rootw, d_catr, d_catw, d_lam, d_L, d_R;
     // P(t) and tip tables
     DevBuf d_P64, d_P32, d_tip64, d_tip32;
     // results and scratch
     DevBuf d_site_lnl, d_block, d_lnl, d_work, d_cond, d_outside, d_nodes_out;
     DevBuf d_done;  // arrival counter of finish_grid_sum, zero between launches
+    bool paired_written = false;  // this evaluation's P(t) kernel also wrote prune4p's layouts
     DevBuf d_mask_raw, d_flag;
     bool have_lnl = false;
     bool lnl_pending = false;
@@ -175,6 +186,63 @@ cudaError_t upload(plk_handle* h, DevBuf& b, const std::vector<T>& v) {
     return cudaEventRecord(h->arena_done, h->stream);
 }
 
+// One part of a group upload: host data and the view that will point at its
+// device copy.
+struct UploadPart {
+    DevView* dst;
+    const void* src;
+    size_t bytes;
+};
+
+template <typename T>
+UploadPart part(DevView& dst, const std::vector<T>& v) {
+    return UploadPart{&dst, v.data(), sizeof(T) * v.size()};
+}
+
+// Uploads a group of arrays into one device block at 256-byte aligned
+// offsets with one host-to-device copy from the pinned arena (one API call
+// instead of one per array; each cudaMemcpyAsync costs microseconds of host
+// time), and points the views at their parts.  A group larger than the arena
+// is copied part by part from pageable memory.
+cudaError_t upload_group(plk_handle* h, DevBuf& block, std::initializer_list<UploadPart> parts) {
+    size_t total = 0;
+    for (const UploadPart& q : parts) total += (q.bytes + 255) & ~(size_t)255;
+    cudaError_t e = block.ensure(std::max<size_t>(total, 256));
+    if (e != cudaSuccess) return e;
+    size_t off = 0;
+    for (const UploadPart& q : parts) {
+        q.dst->p = static_cast<char*>(block.p) + off;
+        off += (q.bytes + 255) & ~(size_t)255;
+    }
+    if (total > kArenaBytes) {
+        for (const UploadPart& q : parts)
+            if (q.bytes && (e = cudaMemcpyAsync(q.dst->p, q.src, q.bytes, cudaMemcpyHostToDevice, h->stream)) !=
+                               cudaSuccess)
+                return e;
+        return cudaSuccess;
+    }
+    if (total == 0) return cudaSuccess;
+    if (!h->arena) {
+        if ((e = cudaMallocHost(&h->arena, kArenaBytes)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&h->arena_done, cudaEventDisableTiming)) != cudaSuccess) return e;
+        h->arena_off = 0;
+    }
+    h->arena_off = (h->arena_off + 255) & ~(size_t)255;
+    if (h->arena_off + total > kArenaBytes) {
+        if ((e = cudaEventSynchronize(h->arena_done)) != cudaSuccess) return e;
+        h->arena_off = 0;
+    }
+    char* src = h->arena + h->arena_off;
+    off = 0;
+    for (const UploadPart& q : parts) {
+        if (q.bytes) std::memcpy(src + off, q.src, q.bytes);
+        off += (q.bytes + 255) & ~(size_t)255;
+    }
+    h->arena_off += total;
+    if ((e = cudaMemcpyAsync(block.p, src, total, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) return e;
+    return cudaEventRecord(h->arena_done, h->stream);
+}
+
 plk_status ready(plk_handle* h) {
     if (!h) return PLK_ERR_ARG;
     if (!h->have_aln) return fail(h, PLK_ERR_STATE, "no alignment set (plk_set_alignment)");
@@ -199,7 +267,9 @@ plk_status refresh_teff(plk_handle* h) {
     return PLK_OK;
 }
 
-plk_status build_pmats(plk_handle* h) {
+// P(t) of every edge and category; with paired, also the layouts prune4p
+// reads, into its scratch (so no relayout launch follows).
+plk_status build_pmats(plk_handle* h, bool paired = false) {
     plk_status s = refresh_teff(h);
     if (s != PLK_OK) return s;
     const size_t SS = (size_t)h->S * h->S;
@@ -216,6 +286,17 @@ plk_status build_pmats(plk_handle* h) {
     m.code_mask = h->d_code_mask.as<uint32_t>();
     m.P64 = h->d_P64.as<double>(); m.P32 = h->d_P32.as<float>();
     m.tip64 = h->d_tip64.as<double>(); m.tip32 = h->d_tip32.as<float>();
+    m.P32p = nullptr;
+    m.tip32p = nullptr;
+    if (paired) {
+        PruneArgs a{};
+        a.n_nodes = h->n_nodes;
+        a.n_tips = h->n_tips;
+        a.C = h->C;
+        PLK_CUDA(h, h->d_work.ensure(prune4p_scratch_bytes(a)), "allocate scratch");
+        prune4p_scratch_parts(h->d_work.p, h->n_nodes, h->C, &m.P32p, &m.tip32p);
+    }
+    h->paired_written = paired;
     PLK_CUDA(h, launch_pmat(m, h->p_kind, h->stream), "P(t) kernel launch");
     return PLK_OK;
 }
@@ -311,6 +392,22 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
     return PLK_OK;
 }
 
+// Whether the FP32 pass of this handle's current shape will run a paired
+// form (prune4p): the tuning already chose one for the shape, or
+// PLK_PRUNE_VARIANT forces one.  Before the first tuning this is false and
+// prune4p relays the layouts out itself.
+bool tuned_paired(const plk_handle* h) {
+    if (h->S != 4 || (h->C != 2 && h->C != 4 && h->C != 8) || !fused_kernel_applies(h, PLK_FP32S)) return false;
+    int v = h->variant;
+    if (const char* f = getenv("PLK_PRUNE_VARIANT")) v = atoi(f);
+    if (v < 0) {
+        const std::array<int, 6> key = {h->n_sites, h->n_tips, (int)h->prog.ops.size(), h->prog.max_depth, h->C, h->S};
+        auto hit = h->tune_cache.find(key);
+        if (hit != h->tune_cache.end()) v = hit->second;
+    }
+    return v >= 3 && v <= 6;
+}
+
 // Runs the post-order pass (P(t) already built); store != null asks for the
 // conditional vectors of every internal node in *store.
 plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* after_prune = nullptr) {
@@ -329,6 +426,7 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     // up the block sums into d_lnl: no separate reduction launch
     a.grid_done = h->d_done.as<unsigned>();
     a.lnl_out = h->d_lnl.as<double>();
+    a.paired_ready = (precision == PLK_FP32S && h->paired_written) ? 1 : 0;
     const bool fused = fused_kernel_applies(h, precision);
     std::vector<int> cands20;
     if (!store && precision == PLK_FP32S && h->S == 20)
@@ -602,11 +700,11 @@ plk_status plk_set_tree(plk_handle* h, int n_nodes, const int* left, const int* 
     h->n_nodes = n_nodes;
     h->tree_tips = n_leaves;
     h->prog = build_program(n_leaves, n_nodes, left, right, root, rank);
-    PLK_CUDA(h, upload(h, h->d_ops, h->prog.ops), "upload program");
-    PLK_CUDA(h, upload(h, h->d_order, post), "upload order");
-    PLK_CUDA(h, upload(h, h->d_left, h->left), "upload tree");
-    PLK_CUDA(h, upload(h, h->d_right, h->right), "upload tree");
-    PLK_CUDA(h, upload(h, h->d_rank, rank), "upload tree");
+    PLK_CUDA(h,
+             upload_group(h, h->d_tree_block,
+                          {part(h->d_ops, h->prog.ops), part(h->d_order, post), part(h->d_left, h->left),
+                           part(h->d_right, h->right), part(h->d_rank, rank)}),
+             "upload tree");
     // default rate model: the reference's empty rate_model
     h->root_quirk = true;
     h->cut_off.clear();
@@ -672,13 +770,12 @@ plk_status plk_set_model(plk_handle* h, int S, const double* Q, const double* ro
             return fail(h, PLK_ERR_ARG, "eigen form needs positive root weights (frequencies)");
         h->p_kind = 1;
     } else h->p_kind = 2;
-    PLK_CUDA(h, upload(h, h->d_Q, h->Q), "upload model");
-    PLK_CUDA(h, upload(h, h->d_rootw, h->root_w), "upload model");
-    PLK_CUDA(h, upload(h, h->d_catr, h->cat_rate), "upload model");
-    PLK_CUDA(h, upload(h, h->d_catw, h->cat_w), "upload model");
-    PLK_CUDA(h, upload(h, h->d_lam, h->lam), "upload model");
-    PLK_CUDA(h, upload(h, h->d_L, h->L), "upload model");
-    PLK_CUDA(h, upload(h, h->d_R, h->R), "upload model");
+    PLK_CUDA(h,
+             upload_group(h, h->d_model_block,
+                          {part(h->d_Q, h->Q), part(h->d_rootw, h->root_w), part(h->d_catr, h->cat_rate),
+                           part(h->d_catw, h->cat_w), part(h->d_lam, h->lam), part(h->d_L, h->L),
+                           part(h->d_R, h->R)}),
+             "upload model");
     h->have_model = true;
     h->have_lnl = false;
     return PLK_OK;
@@ -700,7 +797,7 @@ plk_status plk_loglik_async(plk_handle* h, int precision) {
         ev = &h->evs[h->ev_used++];
         PLK_CUDA(h, cudaEventRecord(ev->e[0], h->stream), "cudaEventRecord");
     }
-    if ((s = build_pmats(h)) != PLK_OK) return s;
+    if ((s = build_pmats(h, precision == PLK_FP32S && tuned_paired(h))) != PLK_OK) return s;
     if (ev) PLK_CUDA(h, cudaEventRecord(ev->e[1], h->stream), "cudaEventRecord");
     if ((s = run_prune(h, precision, nullptr, ev ? &ev->e[2] : nullptr)) != PLK_OK) return s;
     if (h->patterns)  // every pattern's lnL counts once per site showing it

@@ -169,6 +169,10 @@ struct DeviceModel {
     float* P32;               // [n_nodes][C][S][S]
     double* tip64;            // [n_tips][C][n_codes][S]
     float* tip32;             // [n_tips][C][n_codes][S]
+    // when set (4 states, C = 2, 4, 8): also the paired layouts prune4p_kernel
+    // reads (plk_prune4p.cuh), so that no relayout launch is needed
+    float* P32p;
+    float* tip32p;
 };
 // p_kind: 0 taylor20, 1 eigen (reversible), 2 series (non-reversible)
 cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st);
@@ -214,6 +218,9 @@ struct PruneArgs {
     // per-site values are written.
     unsigned* grid_done;
     double* lnl_out;
+    // the paired P(t) and tip layouts are already in scratch (written by the
+    // P(t) kernel): prune4p skips its relayout
+    int paired_ready;
 };
 // Fused 20-state FP32 kernels (plk_prune20.cu): mode 1 = CUDA cores, 2 =
 // tensor cores.  Launches the relayout, the pass and the per-site combine
@@ -235,6 +242,8 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
 // pipe (plk_prune4p.cu), C = 2, 4 or 8; needs prune4p_scratch_bytes of
 // a.scratch for the paired P(t) and tip tables.
 bool prune4p_fits(const PruneArgs& a, int spt);
+// Where the paired P(t) and tip layouts sit in prune4p's scratch.
+void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float** Tp);
 size_t prune4p_scratch_bytes(const PruneArgs& a);
 cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* n_blocks, cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.

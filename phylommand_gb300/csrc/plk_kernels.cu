@@ -21,6 +21,7 @@
 
 #include "plk_device.cuh"
 #include "plk_internal.h"
+#include "plk_prune4p.cuh"
 
 namespace plk {
 
@@ -119,6 +120,7 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
     for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
         m.P64[base + idx] = A[idx];
         m.P32[base + idx] = (float)A[idx];
+        if (m.P32p) m.P32p[(size_t)v * m.C * 16 + paired_p_index(k, idx / 4, idx % 4)] = (float)A[idx];
     }
     if (v < m.n_tips) {
         // table[code][i] = sum over allowed j (ascending) of P[i][j]: what
@@ -136,6 +138,7 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
                 }
             m.tip64[tb + idx] = acc;
             m.tip32[tb + idx] = (float)acc;
+            if (m.tip32p) m.tip32p[(size_t)v * m.C * kCodes * 4 + paired_tip_index(k, c, i)] = (float)acc;
         }
     }
 }

@@ -16,7 +16,9 @@
 //   * P(t) arrives as a B operand image prepared by relayout20u_kernel and is
 //     staged through a three-slot cp.async ring, two ops ahead;
 //   * spilled vectors are thread-private rows in TMEM (tcgen05.st / ld).
-// Tip children are look-ups in the staged tip table.  The root forms
+// Tip children are look-ups in the staged tip table, laid out [state][code]
+// so that the lanes of a warp, whose sites carry different codes, read
+// different banks.  The root forms
 // sum_s pi_s L[s] per site in FP32 for combine20_kernel.
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the tile's sites
@@ -45,7 +47,6 @@ constexpr int kAOperand = 2 * kAPart;    // hi and lo
 constexpr int kBGroup = 4 * 128;         // bytes of a 4-column group of a B operand (LBO of B)
 constexpr int kBPart = 6 * kBGroup;
 constexpr int kBFloats = 2 * kBPart / 4;  // staged B image per (node, category): 1,536 floats
-constexpr int kTipStride = 28;            // floats per code in the staged tip table
 constexpr int kAccCols = 64;              // TMEM columns of the two accumulators
 constexpr int kSlotCols = 32;             // TMEM columns per spill slot (20 used)
 constexpr uint32_t kIdesc = (1u << 4)          // D: F32
@@ -58,7 +59,7 @@ constexpr int kWaitLimit = 1 << 22;       // try_wait rounds before a wait gives
 struct P20UArgs {
     PruneArgs a;
     const float* Ps;   // B images [node][category][kBFloats]
-    const float* Ts;   // tip tables [tip][category][code][kTipStride]
+    const float* Ts;   // tip tables [tip][category][state][code (n_codes padded to 4)]
     float* cat_L;      // [C][n_sites]
     int* cat_E;        // [C][n_sites]
     int child_bytes;   // bytes of one child's slot in a stage
@@ -181,11 +182,14 @@ __device__ __forceinline__ void issue_child(uint32_t d_tmem, uint32_t a_addr, ui
     }
 }
 
-// P(t) as B operand images and tip tables with a 28-float stride per code
+__host__ __device__ inline int codes_padded(int n_codes) { return (n_codes + 3) & ~3; }
+
+// P(t) as B operand images and the tip tables transposed to [state][code]
 __global__ void relayout20u_kernel(const float* __restrict__ P, const float* __restrict__ tip, int n_nodes,
                                    int n_tips, int C, int n_codes, float* __restrict__ Ps, float* __restrict__ Ts) {
+    const int ncs = codes_padded(n_codes);
     const long long n_p = (long long)n_nodes * C * kBFloats;
-    const long long n_t = (long long)n_tips * C * n_codes * kTipStride;
+    const long long n_t = (long long)n_tips * C * kS * ncs;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n_p + n_t;
          idx += (long long)gridDim.x * blockDim.x) {
         if (idx < n_p) {
@@ -204,9 +208,10 @@ __global__ void relayout20u_kernel(const float* __restrict__ P, const float* __r
             Ps[idx] = v;
         } else {
             const long long t = idx - n_p;
-            const long long nkc = t / kTipStride;
-            const int w = (int)(t % kTipStride);
-            Ts[t] = w < kS ? tip[nkc * kS + w] : 0.0f;
+            const long long nk = t / (kS * ncs);  // tip * C + k
+            const int w = (int)(t % (kS * ncs));
+            const int i = w / ncs, code = w % ncs;
+            Ts[t] = code < n_codes ? tip[(nk * n_codes + code) * kS + i] : 0.0f;
         }
     }
 }
@@ -219,7 +224,7 @@ __device__ __forceinline__ void stage_op20u(unsigned char* dst, const Op& op, in
         const float* from;
         int n;
         if (src >= 0) {
-            n = a.n_codes * kTipStride;
+            n = kS * codes_padded(a.n_codes);
             from = g.Ts + ((size_t)src * a.C + k) * (size_t)n;
         } else {
             n = kBFloats;
@@ -232,15 +237,10 @@ __device__ __forceinline__ void stage_op20u(unsigned char* dst, const Op& op, in
 
 __device__ __forceinline__ void tip_row(const unsigned char* stage_child, int code, int n_codes, float m[kS]) {
     code = code < n_codes ? code : 0;
-    const float* row = reinterpret_cast<const float*>(stage_child) + code * kTipStride;
+    const int ncs = codes_padded(n_codes);
+    const float* col = reinterpret_cast<const float*>(stage_child) + code;
 #pragma unroll
-    for (int g = 0; g < 5; ++g) {
-        const float4 v = *reinterpret_cast<const float4*>(row + 4 * g);
-        m[4 * g] = v.x;
-        m[4 * g + 1] = v.y;
-        m[4 * g + 2] = v.z;
-        m[4 * g + 3] = v.w;
-    }
+    for (int i = 0; i < kS; ++i) m[i] = col[i * ncs];
 }
 
 __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
@@ -389,7 +389,7 @@ int tmem_cols_for(const PruneArgs& a) {
 }
 
 int child_bytes_for(const PruneArgs& a) {
-    const int tip = a.n_codes * kTipStride * 4;
+    const int tip = kS * codes_padded(a.n_codes) * 4;
     return (std::max(2 * kBPart, tip) + 127) & ~127;
 }
 
@@ -408,7 +408,7 @@ bool prune20u_fits(const PruneArgs& a) {
 
 size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes) {
     const size_t ps = (size_t)n_nodes * a.C * kBFloats * sizeof(float);
-    const size_t ts = (size_t)a.n_tips * a.C * a.n_codes * kTipStride * sizeof(float);
+    const size_t ts = (size_t)a.n_tips * a.C * kS * codes_padded(a.n_codes) * sizeof(float);
     const size_t cl = (((size_t)a.C * a.n_sites * sizeof(float) + 255) & ~(size_t)255) +
                       (size_t)a.C * a.n_sites * sizeof(int);
     return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl;
@@ -422,7 +422,7 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
     g.Ps = reinterpret_cast<float*>(base);
     size_t off = (((size_t)n_nodes * a.C * kBFloats * sizeof(float)) + 255) & ~(size_t)255;
     g.Ts = reinterpret_cast<float*>(base + off);
-    off += (((size_t)a.n_tips * a.C * a.n_codes * kTipStride * sizeof(float)) + 255) & ~(size_t)255;
+    off += (((size_t)a.n_tips * a.C * kS * codes_padded(a.n_codes) * sizeof(float)) + 255) & ~(size_t)255;
     g.cat_L = reinterpret_cast<float*>(base + off);
     off += (((size_t)a.C * a.n_sites * sizeof(float)) + 255) & ~(size_t)255;
     g.cat_E = reinterpret_cast<int*>(base + off);
@@ -430,7 +430,7 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
     g.tmem_cols = tmem_cols_for(a);
     {
         const long long total =
-            (long long)n_nodes * a.C * kBFloats + (long long)a.n_tips * a.C * a.n_codes * kTipStride;
+            (long long)n_nodes * a.C * kBFloats + (long long)a.n_tips * a.C * kS * codes_padded(a.n_codes);
         long long blocks = (total + 255) / 256;
         if (blocks > 152 * 8) blocks = 152 * 8;
         relayout20u_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),

@@ -107,19 +107,26 @@ size_t prune4p_scratch_bytes(const PruneArgs& a) {
     return ((p + 255) & ~(size_t)255) + (size_t)a.n_tips * a.C * kCodes * 4 * sizeof(float);
 }
 
+void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float** Tp) {
+    const size_t p = (size_t)n_nodes * C * 16 * sizeof(float);
+    *Pp = static_cast<float*>(scratch);
+    *Tp = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + ((p + 255) & ~(size_t)255));
+}
+
 cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* n_blocks, cudaStream_t st) {
     if (!prune4p_fits(a, spt) || a.scratch == nullptr) return cudaErrorInvalidValue;
-    float* Pp = static_cast<float*>(a.scratch);
-    const size_t p = (size_t)a.n_nodes * a.C * 16 * sizeof(float);
-    float* Tp = reinterpret_cast<float*>(static_cast<unsigned char*>(a.scratch) + ((p + 255) & ~(size_t)255));
-    const long long total = (long long)a.n_nodes * a.C * 16 + (long long)a.n_tips * a.C * kCodes * 4;
-    long long blocks = (total + 255) / 256;
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    relayout4p_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),
-                                                         static_cast<const float*>(a.tipT), a.n_nodes, a.n_tips,
-                                                         a.C, Pp, Tp);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    float *Pp, *Tp;
+    prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
+    if (!a.paired_ready) {
+        const long long total = (long long)a.n_nodes * a.C * 16 + (long long)a.n_tips * a.C * kCodes * 4;
+        long long blocks = (total + 255) / 256;
+        if (blocks > 152 * 8) blocks = 152 * 8;
+        relayout4p_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),
+                                                             static_cast<const float*>(a.tipT), a.n_nodes, a.n_tips,
+                                                             a.C, Pp, Tp);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     switch (a.C / 2) {
         case 1: return spt == 1 ? launch4p_kp<1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
                                 : launch4p_kp<1, 2>(a, Pp, Tp, codes_global, n_blocks, st);

@@ -181,8 +181,9 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     }
     int sp = 0;
 
-    // (the codes are read at their use: loading them an op ahead, as run_tile
-    // does, measured slower for this body on the 128 x 100,000 benchmark)
+    // (tip codes from global memory are read at their use: loading them an op
+    // ahead, or before the op's barrier, measured slower for this body on the
+    // 128 x 100,000 benchmark)
     for (int o = 0; o < j.n_ops; ++o) {
         cp_async_wait<1>();
         __syncthreads();
