@@ -171,7 +171,9 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * global memory), 1 / 2 = prune4s_kernel with 1 / 2 sites per thread (P(t)
  * rows and tip tables staged in shared memory), 3 / 4 = prune4p_kernel (the
  * same with the categories in pairs on packed FP32x2), 5 / 6 = prune4p_kernel
- * reading the tip codes from global memory.  20 states: 1 / 2 =
+ * reading the tip codes from global memory, 7 / 8 = prune4p_kernel with two
+ * threads per site (each takes half of the category pairs; codes from global
+ * memory / staged).  20 states: 1 / 2 =
  * prune20_kernel on CUDA cores / tensor cores with 4 warps per tile, 3 / 4 =
  * the same with 8 warps.  -1 = not tuned yet or another kernel
  * applies (FP64, other state counts, more than 8 categories). */

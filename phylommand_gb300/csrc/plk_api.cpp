@@ -405,7 +405,7 @@ bool tuned_paired(const plk_handle* h) {
         auto hit = h->tune_cache.find(key);
         if (hit != h->tune_cache.end()) v = hit->second;
     }
-    return v >= 3 && v <= 6;
+    return v >= 3 && v <= 8;
 }
 
 // Runs the post-order pass (P(t) already built); store != null asks for the
@@ -413,7 +413,7 @@ bool tuned_paired(const plk_handle* h) {
 plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* after_prune = nullptr) {
     const size_t tsz = precision == PLK_FP64 ? sizeof(double) : sizeof(float);
     const size_t vec_bytes = (size_t)h->post.size() * h->C * h->n_sites * h->S * tsz;
-    const int blocks = (h->n_sites + 127) / 128;
+    const int blocks = (h->n_sites + 63) / 64;  // the smallest tile: 64 sites (prune4p, two threads per site)
     PLK_CUDA(h, h->d_site_lnl.ensure(sizeof(double) * h->n_sites), "allocate site lnL");
     PLK_CUDA(h, h->d_block.ensure(sizeof(double) * 2 * blocks), "allocate block sums");
     PLK_CUDA(h, h->d_lnl.ensure(sizeof(double)), "allocate lnL");
@@ -463,6 +463,10 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
                 if (prune4s_fits(a, v)) cands.push_back(v);
             for (int v = 3; v <= 6; ++v)
                 if (prune4p_fits(a, (v + 1) % 2 + 1)) cands.push_back(v);
+            if (prune4p_fits(a, 1, 2)) {  // two threads per site
+                cands.push_back(7);
+                cands.push_back(8);
+            }
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }

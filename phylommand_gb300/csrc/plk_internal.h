@@ -204,7 +204,9 @@ struct PruneArgs {
     // FP32 kernel choice (picked by the autotuner).  4 states: 0 =
     // prune4_kernel, 1/2 = prune4s_kernel with 1/2 sites per thread, 3/4 =
     // prune4p_kernel (category pairs on FP32x2) with 1/2 sites per thread,
-    // 5/6 = the same reading the tip codes from global memory.
+    // 5/6 = the same reading the tip codes from global memory, 7/8 =
+    // prune4p_kernel with two threads per site (codes from global memory /
+    // staged in shared memory).
     // 20 states: 0 = prune_generic_kernel, 1 / 2 = prune20_kernel on CUDA
     // cores / mma.sync tensor cores (TF32, three-product split) with 4 warps
     // per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel on
@@ -241,11 +243,12 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
 // Staged 4-state FP32 kernel with categories in pairs on the packed FP32x2
 // pipe (plk_prune4p.cu), C = 2, 4 or 8; needs prune4p_scratch_bytes of
 // a.scratch for the paired P(t) and tip tables.
-bool prune4p_fits(const PruneArgs& a, int spt);
+bool prune4p_fits(const PruneArgs& a, int spt, int tps = 1);
 // Where the paired P(t) and tip layouts sit in prune4p's scratch.
 void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float** Tp);
 size_t prune4p_scratch_bytes(const PruneArgs& a);
-cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* n_blocks, cudaStream_t st);
+cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int tps, int* n_blocks,
+                           cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
 bool prune4s_fits(const PruneArgs& a, int spt);
 cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);

@@ -41,7 +41,7 @@ __global__ void relayout4p_kernel(const float* __restrict__ P, const float* __re
     }
 }
 
-template <int KP, int SPT, bool CODES_SMEM>
+template <int KP, int SPT, bool CODES_SMEM, int TPS>
 __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, const float* __restrict__ Pp,
                                                                 const float* __restrict__ Tp) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -57,11 +57,11 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, con
     j.root_w = a.root_w;
     j.cat_w = a.cat_w;
     j.C = 2 * KP;
-    j.tile_base = blockIdx.x * kPruneThreads * SPT;
+    j.tile_base = blockIdx.x * tile4p_sites<SPT, TPS>();
     j.site_lnl = a.site_lnl;
     j.max_depth = a.max_depth;
     SiteSum32 sum;
-    run_tile4p<KP, SPT, CODES_SMEM>(j, sm, sum);
+    run_tile4p<KP, SPT, CODES_SMEM, TPS>(j, sm, sum);
     double tsum, tcomp;
     block_sum_site32(sum, tsum, tcomp);
     if (threadIdx.x == 0) {
@@ -71,14 +71,15 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, con
     if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
-template <int KP, int SPT, bool CODES_SMEM>
+template <int KP, int SPT, bool CODES_SMEM, int TPS>
 cudaError_t launch4p(const PruneArgs& a, const float* Pp, const float* Tp, int* n_blocks, cudaStream_t st) {
-    const size_t smem = tile4p_smem_bytes<KP, SPT, CODES_SMEM>(a.n_ops, a.n_tips, a.max_depth);
+    const size_t smem = tile4p_smem_bytes<KP, SPT, CODES_SMEM, TPS>(a.n_ops, a.n_tips, a.max_depth);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    auto kern = prune4p_kernel<KP, SPT, CODES_SMEM>;
+    auto kern = prune4p_kernel<KP, SPT, CODES_SMEM, TPS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int blocks = (a.n_sites + kPruneThreads * SPT - 1) / (kPruneThreads * SPT);
+    constexpr int TILE = tile4p_sites<SPT, TPS>();
+    const int blocks = (a.n_sites + TILE - 1) / TILE;
     *n_blocks = blocks;
     kern<<<blocks, kPruneThreads, smem, st>>>(a, Pp, Tp);
     return cudaGetLastError();
@@ -86,19 +87,25 @@ cudaError_t launch4p(const PruneArgs& a, const float* Pp, const float* Tp, int* 
 
 // codes_global: read the tip codes from global memory (cached) instead of
 // staging the tile's codes in shared memory, for more resident CTAs
-template <int KP, int SPT>
+template <int KP, int SPT, int TPS>
 cudaError_t launch4p_kp(const PruneArgs& a, const float* Pp, const float* Tp, bool codes_global, int* n_blocks,
                         cudaStream_t st) {
-    if (!codes_global && tile4p_smem_bytes<KP, SPT, true>(a.n_ops, a.n_tips, a.max_depth) <= 160 * 1024)
-        return launch4p<KP, SPT, true>(a, Pp, Tp, n_blocks, st);
-    return launch4p<KP, SPT, false>(a, Pp, Tp, n_blocks, st);
+    if (!codes_global && tile4p_smem_bytes<KP, SPT, true, TPS>(a.n_ops, a.n_tips, a.max_depth) <= 160 * 1024)
+        return launch4p<KP, SPT, true, TPS>(a, Pp, Tp, n_blocks, st);
+    return launch4p<KP, SPT, false, TPS>(a, Pp, Tp, n_blocks, st);
 }
 
 }  // namespace
 
-bool prune4p_fits(const PruneArgs& a, int spt) {
+bool prune4p_fits(const PruneArgs& a, int spt, int tps) {
     if (a.C != 2 && a.C != 4 && a.C != 8) return false;
-    if (spt != 1 && spt != 2) return false;
+    if (tps == 2) {
+        if (spt != 1 || a.C == 2) return false;
+        const size_t smem = a.C == 4 ? tile4p_smem_bytes<2, 1, false, 2>(a.n_ops, a.n_tips, a.max_depth)
+                                     : tile4p_smem_bytes<4, 1, false, 2>(a.n_ops, a.n_tips, a.max_depth);
+        return smem <= 227 * 1024;
+    }
+    if (tps != 1 || (spt != 1 && spt != 2)) return false;
     return tile4p_smem_min(a.C, spt, a.n_ops, a.n_tips, a.max_depth) <= 227 * 1024;
 }
 
@@ -113,8 +120,9 @@ void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float*
     *Tp = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + ((p + 255) & ~(size_t)255));
 }
 
-cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* n_blocks, cudaStream_t st) {
-    if (!prune4p_fits(a, spt) || a.scratch == nullptr) return cudaErrorInvalidValue;
+cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int tps, int* n_blocks,
+                           cudaStream_t st) {
+    if (!prune4p_fits(a, spt, tps) || a.scratch == nullptr) return cudaErrorInvalidValue;
     float *Pp, *Tp;
     prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
     if (!a.paired_ready) {
@@ -127,13 +135,17 @@ cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int* 
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
+    if (tps == 2) {
+        return a.C == 4 ? launch4p_kp<2, 1, 2>(a, Pp, Tp, codes_global, n_blocks, st)
+                        : launch4p_kp<4, 1, 2>(a, Pp, Tp, codes_global, n_blocks, st);
+    }
     switch (a.C / 2) {
-        case 1: return spt == 1 ? launch4p_kp<1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
-                                : launch4p_kp<1, 2>(a, Pp, Tp, codes_global, n_blocks, st);
-        case 2: return spt == 1 ? launch4p_kp<2, 1>(a, Pp, Tp, codes_global, n_blocks, st)
-                                : launch4p_kp<2, 2>(a, Pp, Tp, codes_global, n_blocks, st);
-        default: return spt == 1 ? launch4p_kp<4, 1>(a, Pp, Tp, codes_global, n_blocks, st)
-                                 : launch4p_kp<4, 2>(a, Pp, Tp, codes_global, n_blocks, st);
+        case 1: return spt == 1 ? launch4p_kp<1, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
+                                : launch4p_kp<1, 2, 1>(a, Pp, Tp, codes_global, n_blocks, st);
+        case 2: return spt == 1 ? launch4p_kp<2, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
+                                : launch4p_kp<2, 2, 1>(a, Pp, Tp, codes_global, n_blocks, st);
+        default: return spt == 1 ? launch4p_kp<4, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
+                                 : launch4p_kp<4, 2, 1>(a, Pp, Tp, codes_global, n_blocks, st);
     }
 }
 

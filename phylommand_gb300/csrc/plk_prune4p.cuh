@@ -56,14 +56,20 @@ struct alignas(16) StageP {
     u64 tip[2][KP][2][kCodes][2];   // [child][pair][half][code][state in the half]
 };
 
+// Sites of one tile: 128 SPT with one thread per site, 64 with two (TPS = 2:
+// lanes 2i and 2i+1 take the first and the second half of site i's category
+// pairs).
+template <int SPT, int TPS>
+__host__ __device__ constexpr int tile4p_sites() { return kPruneThreads * SPT / TPS; }
+
 // Shared memory: three stage slots | ops | tip codes (optional) | spill stack.
-template <int KP, int SPT, bool CODES_SMEM>
+template <int KP, int SPT, bool CODES_SMEM, int TPS = 1>
 __host__ __device__ inline size_t tile4p_smem_bytes(int n_ops, int n_tips, int max_depth) {
-    constexpr int TILE = kPruneThreads * SPT;
+    constexpr int TILE = tile4p_sites<SPT, TPS>();
     const size_t depth = (size_t)(max_depth > 0 ? max_depth : 1);
     size_t s = 3 * sizeof(StageP<KP>) + align16((size_t)n_ops * sizeof(Op));
     if (CODES_SMEM) s += align16((size_t)n_tips * TILE);
-    s += depth * SPT * KP * 4 * sizeof(u64) * kPruneThreads;
+    s += depth * SPT * (KP / TPS) * 4 * sizeof(u64) * kPruneThreads;
     return s;
 }
 
@@ -132,15 +138,21 @@ __device__ __forceinline__ void tip4p(const u64 (*T)[2][kCodes][2], int code, u6
     }
 }
 
-// One tile of 128 x SPT sites of one tree with C = 2 KP categories; j.P and
-// j.tipT are the tree's paired P(t) and tip blocks.  Adds this thread's site
-// log-likelihoods to sum (the root and log of run_tile, same bits) and
-// writes each site's value to j.site_lnl when it is not null.  Ends with no
-// cp.async in flight; the caller must __syncthreads() before reusing the
-// shared memory.
-template <int KP, int SPT, bool CODES_SMEM>
+// One tile of sites of one tree with C = 2 KP categories (tile4p_sites);
+// j.P and j.tipT are the tree's paired P(t) and tip blocks.  Adds this
+// thread's site log-likelihoods to sum (the root and log of run_tile, same
+// bits) and writes each site's value to j.site_lnl when it is not null.
+// With TPS = 2 a site's pairs are split over two neighbouring lanes: they
+// exchange their maxima for the rescale (both scale by the factors of the
+// site's maximum, as one thread would) and the even lane adds up the root in
+// category order with its partner's category sums, so the per-site results
+// are the bits of TPS = 1.  Ends with no cp.async in flight; the caller must
+// __syncthreads() before reusing the shared memory.
+template <int KP, int SPT, bool CODES_SMEM, int TPS = 1>
 __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) {
-    constexpr int TILE = kPruneThreads * SPT;
+    static_assert(TPS == 1 || (TPS == 2 && SPT == 1 && KP % 2 == 0), "two threads per site split the pairs");
+    constexpr int TILE = tile4p_sites<SPT, TPS>();
+    constexpr int KPT = KP / TPS;  // pairs per thread
     StageP<KP>* stages = reinterpret_cast<StageP<KP>*>(sm);
     size_t off = 3 * sizeof(StageP<KP>);
     Op* s_ops = reinterpret_cast<Op*>(sm + off);
@@ -152,6 +164,8 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     const float* __restrict__ Tp = j.tipT;
 
     const int tid = threadIdx.x;
+    const int half = TPS == 2 ? (tid & 1) : 0;   // which half of the pairs
+    const int q0 = half * KPT;                    // first pair of this thread
     for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
     if (CODES_SMEM) {
         constexpr int chunks = TILE / 16;
@@ -168,14 +182,14 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     if (j.n_ops > 1) stage_op4p<KP>(&stages[1], s_ops[1], Pp, Tp);
     cp_async_commit();
 
-    u64 acc[SPT][KP][4];
+    u64 acc[SPT][KPT][4];
     int scale_e[SPT];
     const u64 one2 = pack2(1.0f, 1.0f);
 #pragma unroll
     for (int s = 0; s < SPT; ++s) {
         scale_e[s] = 0;
 #pragma unroll
-        for (int q = 0; q < KP; ++q)
+        for (int q = 0; q < KPT; ++q)
 #pragma unroll
             for (int i = 0; i < 4; ++i) acc[s][q][i] = one2;
     }
@@ -194,72 +208,73 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
         if (op.s0 == kSrcPop) --sp;
 #pragma unroll
         for (int s = 0; s < SPT; ++s) {
-            const int lsite = tid + s * kPruneThreads;
-            u64 d0[KP][4], d1[KP][4];
+            const int lsite = TPS == 1 ? tid + s * kPruneThreads : (tid >> 1);
+            u64 d0[KPT][4], d1[KPT][4];
             if (op.s0 >= 0) {
                 int code;
                 if (CODES_SMEM) code = s_codes[(size_t)op.s0 * TILE + lsite];
                 else code = j.codes[(size_t)op.s0 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
-                tip4p<KP>(stg.tip[0], code & (kCodes - 1), d0);
+                tip4p<KPT>(stg.tip[0] + q0, code & (kCodes - 1), d0);
             } else if (op.s0 == kSrcPop) {
-                u64 x[KP][4];
+                u64 x[KPT][4];
 #pragma unroll
-                for (int q = 0; q < KP; ++q)
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const ulonglong2 v = s_stack[((size_t)((sp * SPT + s) * KP + q) * 2 + h) * kPruneThreads + tid];
+                        const ulonglong2 v = s_stack[((size_t)((sp * SPT + s) * KPT + q) * 2 + h) * kPruneThreads + tid];
                         x[q][2 * h] = v.x;
                         x[q][2 * h + 1] = v.y;
                     }
-                mv4p<KP>(stg.p[0], x, d0);
+                mv4p<KPT>(stg.p[0] + q0, x, d0);
             } else {
-                mv4p<KP>(stg.p[0], acc[s], d0);
+                mv4p<KPT>(stg.p[0] + q0, acc[s], d0);
             }
             if (op.s1 >= 0) {
                 int code;
                 if (CODES_SMEM) code = s_codes[(size_t)op.s1 * TILE + lsite];
                 else code = j.codes[(size_t)op.s1 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
-                tip4p<KP>(stg.tip[1], code & (kCodes - 1), d1);
+                tip4p<KPT>(stg.tip[1] + q0, code & (kCodes - 1), d1);
             } else if (op.s1 == kSrcAcc) {
-                mv4p<KP>(stg.p[1], acc[s], d1);
+                mv4p<KPT>(stg.p[1] + q0, acc[s], d1);
             }
             if (op.s1 == kSrcNone) {
 #pragma unroll
-                for (int q = 0; q < KP; ++q)
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int i = 0; i < 4; ++i) acc[s][q][i] = d0[q][i];
             } else {
 #pragma unroll
-                for (int q = 0; q < KP; ++q)
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[q][i], d1[q][i]);
             }
             float mx = 0.0f;
 #pragma unroll
-            for (int q = 0; q < KP; ++q)
+            for (int q = 0; q < KPT; ++q)
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     float lo, hi;
                     unpack2(acc[s][q][i], lo, hi);
                     mx = fmaxf(mx, fmaxf(lo, hi));
                 }
+            if constexpr (TPS == 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
             if (mx < scale_threshold<float>() && mx > 0.0f) {
                 int e;
                 float f1, f2;
                 pow2_factors(mx, &e, &f1, &f2);
                 const u64 g1 = pack2(f1, f1), g2 = pack2(f2, f2);
 #pragma unroll
-                for (int q = 0; q < KP; ++q)
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(mul2(acc[s][q][i], g1), g2);
                 scale_e[s] += e;
             }
             if (op.push) {
 #pragma unroll
-                for (int q = 0; q < KP; ++q)
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int h = 0; h < 2; ++h)
-                        s_stack[((size_t)((sp * SPT + s) * KP + q) * 2 + h) * kPruneThreads + tid] =
+                        s_stack[((size_t)((sp * SPT + s) * KPT + q) * 2 + h) * kPruneThreads + tid] =
                             make_ulonglong2(acc[s][q][2 * h], acc[s][q][2 * h + 1]);
             }
         }
@@ -276,22 +291,31 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     for (int k = 0; k < 2 * KP; ++k) cw[k] = (float)j.cat_w[k];
 #pragma unroll
     for (int s = 0; s < SPT; ++s) {
-        const int site = j.tile_base + tid + s * kPruneThreads;
-        float lsum = 0.0f;
+        const int lsite = TPS == 1 ? tid + s * kPruneThreads : (tid >> 1);
+        const int site = j.tile_base + lsite;
+        float lk[2 * KP];  // sum_s v_k[s] root_w[s] of every category
 #pragma unroll
-        for (int q = 0; q < KP; ++q) {
+        for (int q = 0; q < KPT; ++q) {
             float v[2][4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[0][i], v[1][i]);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                float lk = v[h][0] * rw[0];
+                float x = v[h][0] * rw[0];
 #pragma unroll
-                for (int i = 1; i < 4; ++i) lk = fmaf(v[h][i], rw[i], lk);
-                lsum = fmaf(cw[2 * q + h], lk, lsum);
+                for (int i = 1; i < 4; ++i) x = fmaf(v[h][i], rw[i], x);
+                lk[2 * q + h] = x;
             }
         }
-        if (site < j.n_sites) {
+        if constexpr (TPS == 2) {
+            // the even lane holds categories 0 .. 2 KPT - 1, its partner the rest
+#pragma unroll
+            for (int k = 0; k < 2 * KPT; ++k) lk[2 * KPT + k] = __shfl_xor_sync(0xffffffffu, lk[k], 1);
+        }
+        float lsum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2 * KP; ++k) lsum = fmaf(cw[k], lk[k], lsum);
+        if (site < j.n_sites && half == 0) {
             float lm;
             int ee;
             site_log32(lsum, scale_e[s], lm, ee);

@@ -403,7 +403,9 @@ class Handle:
             3: "prune4p_kernel (category pairs on FP32x2, 1 site/thread)",
             4: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread)",
             5: "prune4p_kernel (category pairs on FP32x2, 1 site/thread, tip codes from global)",
-            6: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes from global)"},
+            6: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes from global)",
+            7: "prune4p_kernel (category pairs on FP32x2, 2 threads/site, tip codes from global)",
+            8: "prune4p_kernel (category pairs on FP32x2, 2 threads/site)"},
         20: {1: "prune20_kernel (CUDA cores, 4 warps/tile)", 2: "prune20_kernel (tensor cores, split TF32, 4 warps/tile)",
              3: "prune20_kernel (CUDA cores, 8 warps/tile)", 4: "prune20_kernel (tensor cores, split TF32, 8 warps/tile)",
              5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)"},
