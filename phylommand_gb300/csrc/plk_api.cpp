@@ -405,7 +405,7 @@ bool tuned_paired(const plk_handle* h) {
         auto hit = h->tune_cache.find(key);
         if (hit != h->tune_cache.end()) v = hit->second;
     }
-    return v >= 3 && v <= 8;
+    return v >= 3 && v <= 9;
 }
 
 // Runs the post-order pass (P(t) already built); store != null asks for the
@@ -467,6 +467,7 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
                 cands.push_back(7);
                 cands.push_back(8);
             }
+            if (prune4p_fits(a, 1, 0)) cands.push_back(9);  // TMA-fed stage ring
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }

@@ -554,6 +554,8 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
         return launch_prune4p(a, (a.variant + 1) % 2 + 1, a.variant >= 5, 1, n_blocks, st);
     if (!fp64 && !store && S == 4 && (a.variant == 7 || a.variant == 8) && prune4p_fits(a, 1, 2))
         return launch_prune4p(a, 1, a.variant == 7, 2, n_blocks, st);
+    if (!fp64 && !store && S == 4 && a.variant == 9 && prune4p_fits(a, 1, 0))
+        return launch_prune4p(a, 1, true, 0, n_blocks, st);
     if (!fp64 && !store && S == 20 && a.variant == 5 && prune20u_fits(a))
         return launch_prune20u(a, a.n_nodes, a.scratch, n_blocks, st);
     if (!fp64 && !store && S == 20 && a.variant > 0 && a.variant < 5 && prune20_fits(a, a.variant))

@@ -71,6 +71,62 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, con
     if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
+// The TMA-fed form (run_tile4p_bulk): one site per thread, codes from global.
+template <int KP>
+__global__ void __launch_bounds__(kPruneThreads) prune4p_bulk_kernel(PruneArgs a, const float* __restrict__ Pp,
+                                                                     const float* __restrict__ Tp) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ __align__(8) uint64_t bars[6];  // full[3], empty[3]
+    __shared__ int s_abort;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 3; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&bars[q])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(&bars[3 + q])),
+                         "r"(kPruneThreads / 32)
+                         : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    TileJob j;
+    j.ops = a.ops;
+    j.n_ops = a.n_ops;
+    j.codes = a.codes;
+    j.site_stride = a.site_stride;
+    j.n_sites = a.n_sites;
+    j.n_tips = a.n_tips;
+    j.P = Pp;
+    j.tipT = Tp;
+    j.root_w = a.root_w;
+    j.cat_w = a.cat_w;
+    j.C = 2 * KP;
+    j.tile_base = blockIdx.x * kPruneThreads;
+    j.site_lnl = a.site_lnl;
+    j.max_depth = a.max_depth;
+    SiteSum32 sum;
+    run_tile4p_bulk<KP>(j, sm, bars, &s_abort, sum);
+    double tsum, tcomp;
+    block_sum_site32(sum, tsum, tcomp);
+    if (threadIdx.x == 0) {
+        a.block_sum[2 * blockIdx.x] = tsum;
+        a.block_sum[2 * blockIdx.x + 1] = tcomp;
+    }
+    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+}
+
+template <int KP>
+cudaError_t launch4p_bulk(const PruneArgs& a, const float* Pp, const float* Tp, int* n_blocks, cudaStream_t st) {
+    const size_t smem = tile4p_bulk_smem_bytes<KP>(a.n_ops, a.max_depth);
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    auto kern = prune4p_bulk_kernel<KP>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int blocks = (a.n_sites + kPruneThreads - 1) / kPruneThreads;
+    *n_blocks = blocks;
+    kern<<<blocks, kPruneThreads, smem, st>>>(a, Pp, Tp);
+    return cudaGetLastError();
+}
+
 template <int KP, int SPT, bool CODES_SMEM, int TPS>
 cudaError_t launch4p(const PruneArgs& a, const float* Pp, const float* Tp, int* n_blocks, cudaStream_t st) {
     const size_t smem = tile4p_smem_bytes<KP, SPT, CODES_SMEM, TPS>(a.n_ops, a.n_tips, a.max_depth);
@@ -99,6 +155,13 @@ cudaError_t launch4p_kp(const PruneArgs& a, const float* Pp, const float* Tp, bo
 
 bool prune4p_fits(const PruneArgs& a, int spt, int tps) {
     if (a.C != 2 && a.C != 4 && a.C != 8) return false;
+    if (tps == 0) {
+        if (spt != 1) return false;
+        const size_t smem = a.C == 2   ? tile4p_bulk_smem_bytes<1>(a.n_ops, a.max_depth)
+                            : a.C == 4 ? tile4p_bulk_smem_bytes<2>(a.n_ops, a.max_depth)
+                                       : tile4p_bulk_smem_bytes<4>(a.n_ops, a.max_depth);
+        return smem <= 227 * 1024;
+    }
     if (tps == 2) {
         if (spt != 1 || a.C == 2) return false;
         const size_t smem = a.C == 4 ? tile4p_smem_bytes<2, 1, false, 2>(a.n_ops, a.n_tips, a.max_depth)
@@ -122,6 +185,7 @@ void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float*
 
 cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int tps, int* n_blocks,
                            cudaStream_t st) {
+    // tps 0: the TMA-fed form (one site per thread, codes from global)
     if (!prune4p_fits(a, spt, tps) || a.scratch == nullptr) return cudaErrorInvalidValue;
     float *Pp, *Tp;
     prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
@@ -138,6 +202,13 @@ cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int t
     if (tps == 2) {
         return a.C == 4 ? launch4p_kp<2, 1, 2>(a, Pp, Tp, codes_global, n_blocks, st)
                         : launch4p_kp<4, 1, 2>(a, Pp, Tp, codes_global, n_blocks, st);
+    }
+    if (tps == 0) {
+        switch (a.C / 2) {
+            case 1: return launch4p_bulk<1>(a, Pp, Tp, n_blocks, st);
+            case 2: return launch4p_bulk<2>(a, Pp, Tp, n_blocks, st);
+            default: return launch4p_bulk<4>(a, Pp, Tp, n_blocks, st);
+        }
     }
     switch (a.C / 2) {
         case 1: return spt == 1 ? launch4p_kp<1, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)

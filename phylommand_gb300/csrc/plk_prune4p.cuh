@@ -325,5 +325,236 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same tile body with the stage ring fed by TMA: one thread issues 1-D
+// bulk copies (cp.async.bulk, completion counted in bytes on the slot's
+// "full" mbarrier) three ops ahead, and every warp releases a slot through
+// its "empty" mbarrier once it has read it, so no CTA-wide barrier stands
+// between ops.  One site per thread, tip codes from global memory, the
+// arithmetic of run_tile4p (same bits).  Every wait is bounded; a wait that
+// runs out sets *abort and the tile's sites come out NaN.
+// ---------------------------------------------------------------------------
+constexpr int kBulkWaitLimit = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool mbar_try_wait_bounded(uint32_t mbar, uint32_t parity) {
+    for (int i = 0; i < kBulkWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// bytes one op stages: each child's tip table or P(t) rows
+template <int KP>
+__device__ __forceinline__ uint32_t bulk_op_bytes(const Op& op) {
+    const uint32_t tip = KP * 128 * 4, p = KP * 32 * 4;
+    uint32_t b = op.s0 >= 0 ? tip : p;
+    if (op.s1 != kSrcNone) b += op.s1 >= 0 ? tip : p;
+    return b;
+}
+
+// issued by one thread: the op's data into a stage slot, completing on full
+template <int KP>
+__device__ __forceinline__ void bulk_stage_op(StageP<KP>* st, const Op& op, const float* __restrict__ Pp,
+                                              const float* __restrict__ Tp, uint32_t full) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full), "r"(bulk_op_bytes<KP>(op))
+                 : "memory");
+    for (int c = 0; c < 2; ++c) {
+        const int src = c ? op.s1 : op.s0;
+        if (src == kSrcNone) continue;
+        const void* from;
+        void* to;
+        uint32_t bytes;
+        if (src >= 0) {
+            from = Tp + (size_t)src * KP * 128;
+            to = st->tip[c];
+            bytes = KP * 128 * 4;
+        } else {
+            from = Pp + (size_t)(c ? op.e1 : op.e0) * KP * 32;
+            to = st->p[c];
+            bytes = KP * 32 * 4;
+        }
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                smem_addr(to)),
+            "l"(from), "r"(bytes), "r"(full)
+            : "memory");
+    }
+}
+
+// Shared memory: three stage slots | ops | spill stack (the mbarriers are
+// static shared memory of the kernel).
+template <int KP>
+__host__ __device__ inline size_t tile4p_bulk_smem_bytes(int n_ops, int max_depth) {
+    const size_t depth = (size_t)(max_depth > 0 ? max_depth : 1);
+    return 3 * sizeof(StageP<KP>) + align16((size_t)n_ops * sizeof(Op)) + depth * KP * 4 * sizeof(u64) * kPruneThreads;
+}
+
+// bars: 6 mbarriers (full[3], empty[3]) initialised by the caller before
+// its first __syncthreads: full with 1 arrival, empty with one per warp.
+template <int KP>
+__device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* bars, int* abort, SiteSum32& sum) {
+    StageP<KP>* stages = reinterpret_cast<StageP<KP>*>(sm);
+    size_t off = 3 * sizeof(StageP<KP>);
+    Op* s_ops = reinterpret_cast<Op*>(sm + off);
+    off += align16((size_t)j.n_ops * sizeof(Op));
+    ulonglong2* s_stack = reinterpret_cast<ulonglong2*>(sm + off);
+    const float* __restrict__ Pp = j.P;
+    const float* __restrict__ Tp = j.tipT;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t bar0 = smem_addr(bars);  // full[q] at bar0 + 8 q, empty[q] at bar0 + 24 + 8 q
+    for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
+    __syncthreads();
+    if (tid == 0)
+        for (int o = 0; o < 3 && o < j.n_ops; ++o) bulk_stage_op<KP>(&stages[o], s_ops[o], Pp, Tp, bar0 + 8 * o);
+
+    u64 acc[KP][4];
+    int scale_e = 0;
+    const u64 one2 = pack2(1.0f, 1.0f);
+#pragma unroll
+    for (int q = 0; q < KP; ++q)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[q][i] = one2;
+    int sp = 0;
+    const int lsite = tid;
+    for (int o = 0; o < j.n_ops; ++o) {
+        const int slot = o % 3;
+        const uint32_t parity = (uint32_t)(o / 3) & 1u;
+        const uint32_t full = bar0 + 8 * slot, empty = bar0 + 24 + 8 * slot;
+        if (*reinterpret_cast<volatile int*>(abort)) break;
+        if (!mbar_try_wait_bounded(full, parity)) {
+            *reinterpret_cast<volatile int*>(abort) = 1;
+            break;
+        }
+        const Op op = s_ops[o];
+        const StageP<KP>& stg = stages[slot];
+        if (op.s0 == kSrcPop) --sp;
+        u64 d0[KP][4], d1[KP][4];
+        if (op.s0 >= 0) {
+            const int code = j.codes[(size_t)op.s0 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+            tip4p<KP>(stg.tip[0], code & (kCodes - 1), d0);
+        } else if (op.s0 == kSrcPop) {
+            u64 x[KP][4];
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const ulonglong2 v = s_stack[((size_t)(sp * KP + q) * 2 + h) * kPruneThreads + tid];
+                    x[q][2 * h] = v.x;
+                    x[q][2 * h + 1] = v.y;
+                }
+            mv4p<KP>(stg.p[0], x, d0);
+        } else {
+            mv4p<KP>(stg.p[0], acc, d0);
+        }
+        if (op.s1 >= 0) {
+            const int code = j.codes[(size_t)op.s1 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
+            tip4p<KP>(stg.tip[1], code & (kCodes - 1), d1);
+        } else if (op.s1 == kSrcAcc) {
+            mv4p<KP>(stg.p[1], acc, d1);
+        }
+        // the slot is read: release it (one arrival per warp)
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(empty) : "memory");
+        // the producer refills it with op o + 3 once every warp has let go
+        if (tid == 0 && o + 3 < j.n_ops) {
+            if (mbar_try_wait_bounded(empty, parity))
+                bulk_stage_op<KP>(&stages[slot], s_ops[o + 3], Pp, Tp, full);
+            else
+                *reinterpret_cast<volatile int*>(abort) = 1;
+        }
+        if (op.s1 == kSrcNone) {
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[q][i] = d0[q][i];
+        } else {
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[q][i] = mul2(d0[q][i], d1[q][i]);
+        }
+        float mx = 0.0f;
+#pragma unroll
+        for (int q = 0; q < KP; ++q)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                float lo, hi;
+                unpack2(acc[q][i], lo, hi);
+                mx = fmaxf(mx, fmaxf(lo, hi));
+            }
+        if (mx < scale_threshold<float>() && mx > 0.0f) {
+            int e;
+            float f1, f2;
+            pow2_factors(mx, &e, &f1, &f2);
+            const u64 g1 = pack2(f1, f1), g2 = pack2(f2, f2);
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[q][i] = mul2(mul2(acc[q][i], g1), g2);
+            scale_e += e;
+        }
+        if (op.push) {
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    s_stack[((size_t)(sp * KP + q) * 2 + h) * kPruneThreads + tid] =
+                        make_ulonglong2(acc[q][2 * h], acc[q][2 * h + 1]);
+            ++sp;
+        }
+    }
+    // every issued copy was waited for by the consumers unless a wait ran out;
+    // then give the copies of the remaining slots a bounded chance to land
+    __syncthreads();
+    if (*reinterpret_cast<volatile int*>(abort) && tid == 0) {
+        for (int o = 0; o < j.n_ops; ++o)
+            if (!mbar_try_wait_bounded(bar0 + 8 * (o % 3), (uint32_t)(o / 3) & 1u)) break;
+    }
+
+    // root: as run_tile4p
+    float rw[4], cw[2 * KP];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) rw[i] = (float)j.root_w[i];
+#pragma unroll
+    for (int k = 0; k < 2 * KP; ++k) cw[k] = (float)j.cat_w[k];
+    const int site = j.tile_base + lsite;
+    float lk[2 * KP];
+#pragma unroll
+    for (int q = 0; q < KP; ++q) {
+        float v[2][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) unpack2(acc[q][i], v[0][i], v[1][i]);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float x = v[h][0] * rw[0];
+#pragma unroll
+            for (int i = 1; i < 4; ++i) x = fmaf(v[h][i], rw[i], x);
+            lk[2 * q + h] = x;
+        }
+    }
+    float lsum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 2 * KP; ++k) lsum = fmaf(cw[k], lk[k], lsum);
+    if (*reinterpret_cast<volatile int*>(abort)) lsum = __int_as_float(0x7fc00000);
+    if (site < j.n_sites) {
+        float lm;
+        int ee;
+        site_log32(lsum, scale_e, lm, ee);
+        if (j.site_lnl) j.site_lnl[site] = site_lnl64(lm, ee);
+        site_sum_add(sum, lm, ee);
+    }
+}
+
 }  // namespace dev
 }  // namespace plk

@@ -227,8 +227,8 @@ def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
     sites = []
-    variants = {1: ("0", "1", "2"), 2: ("0", "1", "2", "3", "4", "5", "6")}.get(
-        C, ("0", "1", "2", "3", "4", "5", "6", "7", "8"))
+    variants = {1: ("0", "1", "2"), 2: ("0", "1", "2", "3", "4", "5", "6", "9")}.get(
+        C, ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9"))
     for v in variants:
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
