@@ -425,7 +425,7 @@ def run_protein(args):
 
 
 def run_warmstart(args):
-    """Time-to-ML-fit, learned vs plain: 10,000 simulated 32 x 2,000 training
+    """Time-to-ML-fit, learned vs plain: 20,000 simulated 32 x 2,000 training
     alignments labelled by the GPU fit, the network trained on them, then
     1,000 held-out 64 x 5,000 alignments fitted from the default start and
     from the network's start (the Newton-start quasi-Newton fit); evaluations
@@ -445,7 +445,8 @@ def run_warmstart(args):
     line = {"metric": "lnL evaluations to reach the ML fit, learned start / default start",
             "value": r["evals_to_optimum_ratio_warm_over_plain"], "unit": "ratio", "higher_is_better": False,
             "n_gpus": 1, "dtype": "f32 lnL, bf16 network", "data": "synthetic",
-            "config": {"workload": "train 10,000 x (32 taxa, 2,000 sites); evaluate 1,000 x (64 taxa, 5,000 sites); "
+            "config": {"workload": f"train {args.ws_train:,} x (32 taxa, 2,000 sites); evaluate {args.ws_eval:,} x "
+                                   "(64 taxa, 5,000 sites); "
                                    "GTR+Gamma4 priors", "train_items": args.ws_train, "eval_items": args.ws_eval,
                        "optimiser": r["method"]},
             "plain": {"evals_to_optimum": r["plain_evals_to_optimum_mean"], "evals_to_stop": r["plain_evals_mean"],
@@ -553,7 +554,7 @@ def main():
                          "states; warmstart: time-to-ML-fit with the learned start")
     ap.add_argument("--nni-items", type=int, default=512)
     ap.add_argument("--nni-sample", type=int, default=24)
-    ap.add_argument("--ws-train", type=int, default=10000)
+    ap.add_argument("--ws-train", type=int, default=20000)
     ap.add_argument("--ws-eval", type=int, default=1000)
     args = ap.parse_args()
     if args.workload == "nni":

@@ -305,7 +305,7 @@ def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int 
 def main(argv=None):
     ap = argparse.ArgumentParser(description="train and evaluate the learned warm start")
     ap.add_argument("--cache", default="warmstart_cache", help="directory of the labelled set and the weights")
-    ap.add_argument("--train-items", type=int, default=10000)
+    ap.add_argument("--train-items", type=int, default=20000)
     ap.add_argument("--train-taxa", type=int, default=32)
     ap.add_argument("--train-sites", type=int, default=2000)
     ap.add_argument("--eval-items", type=int, default=1000)
