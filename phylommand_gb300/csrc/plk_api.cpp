@@ -129,6 +129,7 @@ struct plk_handle {
     cudaEvent_t arena_done = nullptr;
     int* h_flag = nullptr;
     bool flag_pending = false;
+    int flag_gen = 0;  // value the encode kernel stores for an empty cell of the current alignment
     ~plk_handle() {
         for (auto& s : evs)
             for (auto& e : s.e) cudaEventDestroy(e);
@@ -283,7 +284,7 @@ plk_status build_pmats(plk_handle* h, bool paired = false) {
     m.S = h->S; m.C = h->C; m.n_nodes = h->n_nodes; m.n_tips = h->n_tips; m.n_codes = h->n_codes;
     m.t_eff = h->d_teff.as<double>(); m.cat_rate = h->d_catr.as<double>(); m.Q = h->d_Q.as<double>();
     m.eig_lam = h->d_lam.as<double>(); m.eig_L = h->d_L.as<double>(); m.eig_R = h->d_R.as<double>();
-    m.code_mask = h->d_code_mask.as<uint32_t>();
+    m.code_mask = h->S <= 4 ? nullptr : h->d_code_mask.as<uint32_t>();  // <= 4 states: code = state set
     m.P64 = h->d_P64.as<double>(); m.P32 = h->d_P32.as<float>();
     m.tip64 = h->d_tip64.as<double>(); m.tip32 = h->d_tip32.as<float>();
     m.P32p = nullptr;
@@ -619,18 +620,22 @@ plk_status set_alignment_impl(plk_handle* h, int n_tips, int n_sites, int n_stat
         const int eb = masks8 ? 1 : (int)sizeof(uint32_t);
         PLK_CUDA(h, h->d_mask_raw.ensure(n_cells * eb), "allocate mask staging");
         PLK_CUDA(h, h->d_codes.ensure((size_t)n_tips * code_stride(n_sites)), "allocate tip codes");
-        PLK_CUDA(h, h->d_flag.ensure(sizeof(int)), "allocate flag");
+        if (!h->d_flag.p) {  // zero once; every alignment then marks with its own generation
+            PLK_CUDA(h, h->d_flag.ensure(sizeof(int)), "allocate flag");
+            PLK_CUDA(h, cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "clear flag");
+        }
+        h->flag_gen = h->flag_gen == 0x7fffffff ? 1 : h->flag_gen + 1;
         PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks8 ? (const void*)masks8 : (const void*)masks, n_cells * eb,
                                     cudaMemcpyHostToDevice, h->stream),
                  "upload masks");
-        PLK_CUDA(h, cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "clear flag");
         PLK_CUDA(h, launch_encode_small(h->d_mask_raw.p, eb, n_tips, n_sites, code_stride(n_sites), all,
-                                        h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->stream),
+                                        h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->flag_gen, h->stream),
                  "encode kernel launch");
-        // the empty-cell flag comes back with the next result fetch (no wait here)
+        // the empty-cell flag comes back with the next result fetch (no wait
+        // here); the code table is the identity, so none is uploaded (the
+        // P(t) kernel takes the code as the state set)
         if (!h->h_flag) PLK_CUDA(h, cudaMallocHost(&h->h_flag, sizeof(int)), "allocate flag");
         PLK_CUDA(h, cudaMemcpyAsync(h->h_flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
-        PLK_CUDA(h, upload(h, h->d_code_mask, table), "upload code table");
         h->flag_pending = true;
     } else {
         const size_t stride = (size_t)code_stride(n_sites);
@@ -825,7 +830,7 @@ plk_status plk_loglik_result(plk_handle* h, double* lnl_out) {
     h->lnl_pending = false;
     if (h->flag_pending) {  // the alignment's empty-cell check, read back with this result
         h->flag_pending = false;
-        h->bad_tip = *h->h_flag != 0;
+        h->bad_tip = *h->h_flag == h->flag_gen;
     }
     if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
     *lnl_out = v;
@@ -907,7 +912,7 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
     if (h->flag_pending) {  // the alignment's empty-cell check
         PLK_CUDA(h, cudaStreamSynchronize(h->stream), "tip check");
         h->flag_pending = false;
-        h->bad_tip = *h->h_flag != 0;
+        h->bad_tip = *h->h_flag == h->flag_gen;
     }
     if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
     if ((s = build_pmats(h)) != PLK_OK) return s;

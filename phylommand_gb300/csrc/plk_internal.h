@@ -262,7 +262,7 @@ cudaError_t launch_weighted_sum(const double* x, const double* w, int n, double*
 // states; masks of elem_bytes 4 or 1), padding bytes 0; *bad |= 1 if a cell
 // allows no state.
 cudaError_t launch_encode_small(const void* masks, int elem_bytes, int n_tips, int n_sites, int stride, uint32_t all,
-                                uint8_t* codes, int* bad, cudaStream_t st);
+                                uint8_t* codes, int* bad, int gen, cudaStream_t st);
 // Row stride of the tip-code matrix: n_sites rounded up to 16 bytes.
 inline int code_stride(int n_sites) { return (n_sites + 15) & ~15; }
 

@@ -128,7 +128,7 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
         const size_t tb = ((size_t)v * m.C + k) * m.n_codes * S;
         for (int idx = threadIdx.x; idx < m.n_codes * S; idx += blockDim.x) {
             const int c = idx / S, i = idx % S;
-            const uint32_t mask = m.code_mask[c];
+            const uint32_t mask = m.code_mask ? m.code_mask[c] : (uint32_t)c;
             double acc = 0.0;
             bool first = true;
             for (int j = 0; j < S; ++j)
@@ -585,11 +585,13 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
 
 // =========================================================================
 // Tip encoding for alphabets of <= 4 states: the code is the state set
-// itself; a cell with no allowed state raises the flag (check_nodes).
+// itself; a cell with no allowed state sets the flag to the alignment's
+// generation number gen (check_nodes), so the flag needs no clearing between
+// alignments.
 // =========================================================================
 template <typename M>
 __global__ void encode_small_kernel(const M* __restrict__ masks, int n_tips, int n_sites, int stride, uint32_t all,
-                                    uint8_t* __restrict__ codes, int* __restrict__ bad) {
+                                    uint8_t* __restrict__ codes, int* __restrict__ bad, int gen) {
     // one thread per 4 consecutive sites of a row; rows of `codes` are padded
     // to `stride` (a multiple of 16) and the padding is written as 0
     const int chunks = stride / 4;
@@ -613,11 +615,11 @@ __global__ void encode_small_kernel(const M* __restrict__ masks, int n_tips, int
         }
         reinterpret_cast<uchar4*>(codes + (size_t)t * stride)[s0 / 4] = make_uchar4(c[0], c[1], c[2], c[3]);
     }
-    if (__any_sync(0xffffffffu, any_bad) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+    if (__any_sync(0xffffffffu, any_bad) && (threadIdx.x & 31) == 0) *reinterpret_cast<volatile int*>(bad) = gen;
 }
 
 cudaError_t launch_encode_small(const void* masks, int elem_bytes, int n_tips, int n_sites, int stride, uint32_t all,
-                                uint8_t* codes, int* bad, cudaStream_t st) {
+                                uint8_t* codes, int* bad, int gen, cudaStream_t st) {
     const int threads = 256;
     const size_t total = (size_t)n_tips * (stride / 4);
     size_t blocks = (total + threads - 1) / threads;
@@ -625,10 +627,10 @@ cudaError_t launch_encode_small(const void* masks, int elem_bytes, int n_tips, i
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (elem_bytes == 1)
         encode_small_kernel<uint8_t><<<(unsigned)blocks, threads, 0, st>>>(static_cast<const uint8_t*>(masks), n_tips,
-                                                                          n_sites, stride, all, codes, bad);
+                                                                          n_sites, stride, all, codes, bad, gen);
     else
         encode_small_kernel<uint32_t><<<(unsigned)blocks, threads, 0, st>>>(static_cast<const uint32_t*>(masks),
-                                                                           n_tips, n_sites, stride, all, codes, bad);
+                                                                           n_tips, n_sites, stride, all, codes, bad, gen);
     return cudaGetLastError();
 }
 

@@ -215,7 +215,8 @@ def test_repeat_calls_are_deterministic():
         assert a[0] == a[1] == a[2] and b[0] == b[1] == b[2]
 
 
-@pytest.mark.parametrize("n_tips,n_sites,C", [(128, 1000, 4), (40, 257, 1), (1300, 300, 4), (60, 129, 8)])
+@pytest.mark.parametrize("n_tips,n_sites,C", [(128, 1000, 4), (40, 257, 1), (1300, 300, 4), (60, 129, 8),
+                                             (20, 33, 4), (5, 1, 2)])
 def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
     """Every candidate of the autotuner (prune4_kernel, prune4s_kernel with 1
     and 2 sites per thread, prune4p_kernel with category pairs on FP32x2 where
