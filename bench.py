@@ -256,30 +256,58 @@ def run_ours(args, world, rank, local):
         + w.cat_rates.nbytes + w.cat_weights.nbytes
     e2e_steps = max(3, args.steps // 2)
 
+    # The steps call the C ABI (include/plk.h) as a C or C++ caller such as
+    # the simpleML drop-in does: the ctypes argument objects are built once,
+    # every step passes the same host buffers and the library copies them
+    # again (alignment, tree, rate model, model) before the evaluation.
+    import ctypes
+    L, hh = plk.lib(), h.raw
+    c_i, c_d = ctypes.c_int, ctypes.c_double
+    tl, tr = np.ascontiguousarray(w.left, np.int32), np.ascontiguousarray(w.right, np.int32)
+    tb = np.ascontiguousarray(w.bl, np.float64)
+    mq, mf = np.ascontiguousarray(w.Q, np.float64), np.ascontiguousarray(w.freqs, np.float64)
+    mr, mw = np.ascontiguousarray(w.cat_rates, np.float64), np.ascontiguousarray(w.cat_weights, np.float64)
+    tree_args = (hh, len(tl), tl.ctypes.data_as(ctypes.POINTER(c_i)), tr.ctypes.data_as(ctypes.POINTER(c_i)),
+                 tb.ctypes.data_as(ctypes.POINTER(c_d)))
+    rate_args = (hh, 0, 0, None, None, None, 0, None)
+    model_args = (hh, mq.shape[0], mq.ctypes.data_as(ctypes.POINTER(c_d)), mf.ctypes.data_as(ctypes.POINTER(c_d)), 1,
+                  len(mr), mr.ctypes.data_as(ctypes.POINTER(c_d)), mw.ctypes.data_as(ctypes.POINTER(c_d)),
+                  plk.PLK_P_EXACT)
+    out = ctypes.c_double(0.0)
+
     def e2e_run(masks):
+        if masks.dtype == np.uint8:
+            aln = (L.plk_set_alignment8, (hh, masks.shape[0], masks.shape[1], w.n_states,
+                                          masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        else:
+            aln = (L.plk_set_alignment, (hh, masks.shape[0], masks.shape[1], w.n_states,
+                                         masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
         for _ in range(2):
             h.set_alignment(masks, w.n_states)
             h.loglik(plk.PLK_FP32S)
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            h.set_alignment(masks, w.n_states)
-            h.set_tree(w.left, w.right, w.bl)
-            h.set_rate_model(False)
-            h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
-            lnl = h.loglik(plk.PLK_FP32S)
-        return world * e2e_steps / reduce_max(world, time.perf_counter() - t0, dev), lnl
+            st = aln[0](*aln[1])
+            st |= L.plk_set_tree(*tree_args)
+            st |= L.plk_set_rate_model(*rate_args)
+            st |= L.plk_set_model(*model_args)
+            st |= L.plk_loglik(hh, plk.PLK_FP32S, ctypes.byref(out))
+            if st != plk.PLK_OK:
+                raise plk.PlkError(st, (L.plk_last_error(hh) or b"").decode())
+        return world * e2e_steps / reduce_max(world, time.perf_counter() - t0, dev), out.value
 
     e2e_value, lnl_e2e = e2e_run(masks8)
     e2e32_value, _ = e2e_run(masks32)
     # where an end-to-end step goes: the host time of each call (the uploads
     # are asynchronous, so their device work overlaps the calls after them;
     # plk_loglik waits for everything)
-    calls = (("set_alignment8", lambda: h.set_alignment(masks8, w.n_states)),
-             ("set_tree", lambda: h.set_tree(w.left, w.right, w.bl)),
-             ("set_rate_model", lambda: h.set_rate_model(False)),
-             ("set_model", lambda: h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)),
-             ("loglik", lambda: h.loglik(plk.PLK_FP32S)))
+    aln8 = (hh, masks8.shape[0], masks8.shape[1], w.n_states, masks8.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    calls = (("set_alignment8", lambda: L.plk_set_alignment8(*aln8)),
+             ("set_tree", lambda: L.plk_set_tree(*tree_args)),
+             ("set_rate_model", lambda: L.plk_set_rate_model(*rate_args)),
+             ("set_model", lambda: L.plk_set_model(*model_args)),
+             ("loglik", lambda: L.plk_loglik(hh, plk.PLK_FP32S, ctypes.byref(out))))
     e2e_parts = {name: 0.0 for name, _ in calls}
     for _ in range(e2e_steps):
         for name, call in calls:
@@ -334,8 +362,8 @@ def run_ours(args, world, rank, local):
                          "sample": f"{sample} of {w.n_sites} sites, P(t) rebuilt per (site, edge, category) by the "
                                    f"reference's Taylor-plus-20-squarings, scaled linearly to all sites"},
         "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 12,
-                "path": "plk_set_alignment8 (pinned byte masks) + plk_set_tree + plk_set_rate_model + "
-                        "plk_set_model + plk_loglik",
+                "path": "C ABI: plk_set_alignment8 (pinned byte masks) + plk_set_tree + plk_set_rate_model + "
+                        "plk_set_model + plk_loglik, every step",
                 "with_32bit_masks": {"value": e2e32_value, "h2d_bytes_per_step": int(masks32.nbytes + small),
                                      "path": "plk_set_alignment (pinned 32-bit masks) + the same calls"},
                 "host_ms_per_call": e2e_parts},
