@@ -90,6 +90,8 @@ cudaError_t launch_batch_reduce(const BatchDev& b, cudaStream_t st);
 // scratch slices; then the per-(item, move) reduction.
 size_t nni_smem_bytes(int C, bool codes_smem, int max_ops, int max_tips, int max_depth);
 cudaError_t launch_batch_nni(const BatchDev& b, bool codes_smem, int grid, size_t smem, cudaStream_t st);
+// resident CTAs per SM of the NNI (blen = false) or branch-length kernel
+int nni_occupancy(int C, bool codes_smem, size_t smem, bool blen);
 cudaError_t launch_batch_nni_reduce(const BatchDev& b, cudaStream_t st);
 
 // Branch-length derivatives of every edge of every item (plk_nni.cu): per

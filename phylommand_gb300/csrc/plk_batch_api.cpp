@@ -141,7 +141,7 @@ BatchDev device_view(plk_batch* b, const UnitSet& us) {
     d.model = b->d_model.as<double>();
     d.P32 = b->d_P32.as<float>();
     d.tip32 = b->d_tip32.as<float>();
-    d.P32p = nullptr;  // the plain layout only, unless with_paired() asks for both
+    d.P32p = nullptr;  // the plain layout only, unless lnl_view asks for the paired one
     d.tip32p = nullptr;
     d.write_std = 1;
     d.units = us.units.as<int2>();
@@ -873,11 +873,17 @@ plk_status plk_batch_nni_loglik(plk_batch* b, double* out) {
         s = build_units(b, b->nni_units, 1, true);
         if (s != PLK_OK) return s;
     }
-    size_t smem = nni_smem_bytes(b->C, true, b->max_ops, b->max_tips, b->max_depth);
-    bool codes_smem = smem <= 160 * 1024;
-    if (!codes_smem) smem = nni_smem_bytes(b->C, false, b->max_ops, b->max_tips, b->max_depth);
-    if (smem > 227 * 1024) return bfail(b, PLK_ERR_UNSUPPORTED, "trees too large for NNI scoring");
-    const int grid = std::max(1, std::min(b->nni_units.n_units, 2 * b->n_sms));
+    // tip codes staged in shared memory or read from global, whichever lets
+    // more CTAs share an SM; one persistent CTA per resident slot
+    const size_t smem_staged = nni_smem_bytes(b->C, true, b->max_ops, b->max_tips, b->max_depth);
+    const size_t smem_global = nni_smem_bytes(b->C, false, b->max_ops, b->max_tips, b->max_depth);
+    if (smem_global > 227 * 1024) return bfail(b, PLK_ERR_UNSUPPORTED, "trees too large for NNI scoring");
+    const int occ_staged = smem_staged <= 227 * 1024 ? nni_occupancy(b->C, true, smem_staged, false) : 0;
+    const int occ_global = nni_occupancy(b->C, false, smem_global, false);
+    const bool codes_smem = occ_staged >= occ_global && occ_staged > 0;
+    const size_t smem = codes_smem ? smem_staged : smem_global;
+    const int per_sm = std::max(1, codes_smem ? occ_staged : occ_global);
+    const int grid = std::max(1, std::min(b->nni_units.n_units, per_sm * b->n_sms));
     const size_t slice = (size_t)b->max_int * kThreads;
     PLK_BCUDA(b, b->d_scr_D.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate NNI scratch");
     PLK_BCUDA(b, b->d_scr_O.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate NNI scratch");
@@ -916,11 +922,16 @@ plk_status blen_pass(plk_batch* b, std::vector<double>& deriv, std::vector<int>&
         s = build_units(b, b->nni_units, 1, true);
         if (s != PLK_OK) return s;
     }
-    size_t smem = nni_smem_bytes(b->C, true, b->max_ops, b->max_tips, b->max_depth);
-    bool codes_smem = smem <= 160 * 1024;
-    if (!codes_smem) smem = nni_smem_bytes(b->C, false, b->max_ops, b->max_tips, b->max_depth);
-    if (smem > 227 * 1024) return bfail(b, PLK_ERR_UNSUPPORTED, "trees too large for branch-length derivatives");
-    const int grid = std::max(1, std::min(b->nni_units.n_units, 2 * b->n_sms));
+    // as for NNI scoring: staged or global tip codes by resident CTAs per SM
+    const size_t smem_staged = nni_smem_bytes(b->C, true, b->max_ops, b->max_tips, b->max_depth);
+    const size_t smem_global = nni_smem_bytes(b->C, false, b->max_ops, b->max_tips, b->max_depth);
+    if (smem_global > 227 * 1024) return bfail(b, PLK_ERR_UNSUPPORTED, "trees too large for branch-length derivatives");
+    const int occ_staged = smem_staged <= 227 * 1024 ? nni_occupancy(b->C, true, smem_staged, true) : 0;
+    const int occ_global = nni_occupancy(b->C, false, smem_global, true);
+    const bool codes_smem = occ_staged >= occ_global && occ_staged > 0;
+    const size_t smem = codes_smem ? smem_staged : smem_global;
+    const int per_sm = std::max(1, codes_smem ? occ_staged : occ_global);
+    const int grid = std::max(1, std::min(b->nni_units.n_units, per_sm * b->n_sms));
     const size_t slice = (size_t)b->max_int * kThreads;
     PLK_BCUDA(b, b->d_scr_D.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate scratch");
     PLK_BCUDA(b, b->d_scr_O.ensure((size_t)grid * slice * b->C * sizeof(float4)), "allocate scratch");

@@ -245,8 +245,10 @@ __device__ __forceinline__ void move_site_log(const ItemView& iv, const BatchDev
     *lm = logf(__int_as_float((bits & 0x007fffff) | 0x3f800000));
 }
 
+// registers capped for three CTAs per SM (168; a few bytes spill): with the
+// tip codes read from global memory three CTAs fit beside each other
 template <int CM, bool CODES_SMEM>
-__global__ void __launch_bounds__(kPruneThreads) batch_nni_kernel(BatchDev b) {
+__global__ void __launch_bounds__(kPruneThreads, 3) batch_nni_kernel(BatchDev b) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ int s_unit;
     __shared__ double s_red[kPruneThreads / 32][32][2];
@@ -434,8 +436,9 @@ __device__ void edge_site_derivs(const ItemView& iv, const BatchDev& b, int u, i
     *d2 = __fsub_rn(__fdiv_rn(l2, l0), __fmul_rn(g, g));
 }
 
+// registers capped for three CTAs per SM, as batch_nni_kernel
 template <int CM, bool CODES_SMEM>
-__global__ void __launch_bounds__(kPruneThreads) batch_blen_kernel(BatchDev b, BlenDev bd) {
+__global__ void __launch_bounds__(kPruneThreads, 3) batch_blen_kernel(BatchDev b, BlenDev bd) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ int s_unit;
     __shared__ double s_red[kPruneThreads / 32][kBlenSlots][2];
@@ -588,6 +591,26 @@ size_t nni_smem_bytes(int C, bool codes_smem, int max_ops, int max_tips, int max
                                    : tile_smem_bytes<4, 1, false, true>(max_ops, max_tips, max_depth);
     return codes_smem ? tile_smem_bytes<8, 1, true, true>(max_ops, max_tips, max_depth)
                       : tile_smem_bytes<8, 1, false, true>(max_ops, max_tips, max_depth);
+}
+
+template <typename K>
+int occupancy_of(K kern, size_t smem) {
+    int n = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kPruneThreads, smem) != cudaSuccess) return 0;
+    return n;
+}
+
+int nni_occupancy(int C, bool codes_smem, size_t smem, bool blen) {
+    const int cm = C == 1 ? 1 : (C <= 4 ? 4 : 8);
+    if (blen) {
+        if (cm == 1) return codes_smem ? occupancy_of(batch_blen_kernel<1, true>, smem) : occupancy_of(batch_blen_kernel<1, false>, smem);
+        if (cm == 4) return codes_smem ? occupancy_of(batch_blen_kernel<4, true>, smem) : occupancy_of(batch_blen_kernel<4, false>, smem);
+        return codes_smem ? occupancy_of(batch_blen_kernel<8, true>, smem) : occupancy_of(batch_blen_kernel<8, false>, smem);
+    }
+    if (cm == 1) return codes_smem ? occupancy_of(batch_nni_kernel<1, true>, smem) : occupancy_of(batch_nni_kernel<1, false>, smem);
+    if (cm == 4) return codes_smem ? occupancy_of(batch_nni_kernel<4, true>, smem) : occupancy_of(batch_nni_kernel<4, false>, smem);
+    return codes_smem ? occupancy_of(batch_nni_kernel<8, true>, smem) : occupancy_of(batch_nni_kernel<8, false>, smem);
 }
 
 cudaError_t launch_batch_nni(const BatchDev& b, bool codes_smem, int grid, size_t smem, cudaStream_t st) {
