@@ -107,6 +107,7 @@ struct plk_handle {
     DevBuf d_site_lnl, d_block, d_lnl, d_work, d_cond, d_outside, d_nodes_out;
     DevBuf d_done;  // arrival counter of finish_grid_sum, zero between launches
     bool paired_written = false;  // this evaluation's P(t) kernel also wrote prune4p's layouts
+    bool withhold_stage = false;  // plk_test_withhold_stage: armed for the next FP32 pass
     DevBuf d_mask_raw, d_flag;
     bool have_lnl = false;
     bool lnl_pending = false;
@@ -428,6 +429,8 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     a.grid_done = h->d_done.as<unsigned>();
     a.lnl_out = h->d_lnl.as<double>();
     a.paired_ready = (precision == PLK_FP32S && h->paired_written) ? 1 : 0;
+    a.withhold_first_stage = (precision == PLK_FP32S && h->withhold_stage) ? 1 : 0;
+    if (precision == PLK_FP32S) h->withhold_stage = false;
     const bool fused = fused_kernel_applies(h, precision);
     std::vector<int> cands20;
     if (!store && precision == PLK_FP32S && h->S == 20)
@@ -881,6 +884,12 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
 }
 
 int plk_prune_variant(const plk_handle* h) { return h ? h->variant : -1; }
+
+plk_status plk_test_withhold_stage(plk_handle* h) {
+    if (!h) return PLK_ERR_ARG;
+    h->withhold_stage = true;
+    return PLK_OK;
+}
 
 plk_status plk_site_loglik(plk_handle* h, double* out) {
     if (!h) return PLK_ERR_ARG;

@@ -223,6 +223,9 @@ struct PruneArgs {
     // the paired P(t) and tip layouts are already in scratch (written by the
     // P(t) kernel): prune4p skips its relayout
     int paired_ready;
+    // test of the failure path (plk_test_withhold_stage): the TMA-fed form
+    // never stages its first op, so its bounded waits run out
+    int withhold_first_stage;
 };
 // Fused 20-state FP32 kernels (plk_prune20.cu): mode 1 = CUDA cores, 2 =
 // tensor cores.  Launches the relayout, the pass and the per-site combine

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_bulk_kernel(PruneArgs a
     j.site_lnl = a.site_lnl;
     j.max_depth = a.max_depth;
     SiteSum32 sum;
-    run_tile4p_bulk<KP>(j, sm, bars, &s_abort, sum);
+    run_tile4p_bulk<KP>(j, sm, bars, &s_abort, sum, a.withhold_first_stage != 0);
     double tsum, tcomp;
     block_sum_site32(sum, tsum, tcomp);
     if (threadIdx.x == 0) {

@@ -334,7 +334,7 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
 // arithmetic of run_tile4p (same bits).  Every wait is bounded; a wait that
 // runs out sets *abort and the tile's sites come out NaN.
 // ---------------------------------------------------------------------------
-constexpr int kBulkWaitLimit = 1 << 22;
+constexpr int kBulkWaitLimit = 1 << 20;  // try_wait rounds (each may suspend briefly); a copy lands in microseconds
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -402,8 +402,11 @@ __host__ __device__ inline size_t tile4p_bulk_smem_bytes(int n_ops, int max_dept
 
 // bars: 6 mbarriers (full[3], empty[3]) initialised by the caller before
 // its first __syncthreads: full with 1 arrival, empty with one per warp.
+// withhold_first (a test of the failure path): the producer never stages op
+// 0, so every wait for it runs out.
 template <int KP>
-__device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* bars, int* abort, SiteSum32& sum) {
+__device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* bars, int* abort, SiteSum32& sum,
+                                bool withhold_first = false) {
     StageP<KP>* stages = reinterpret_cast<StageP<KP>*>(sm);
     size_t off = 3 * sizeof(StageP<KP>);
     Op* s_ops = reinterpret_cast<Op*>(sm + off);
@@ -415,8 +418,14 @@ __device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* b
     const uint32_t bar0 = smem_addr(bars);  // full[q] at bar0 + 8 q, empty[q] at bar0 + 24 + 8 q
     for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
     __syncthreads();
-    if (tid == 0)
-        for (int o = 0; o < 3 && o < j.n_ops; ++o) bulk_stage_op<KP>(&stages[o], s_ops[o], Pp, Tp, bar0 + 8 * o);
+    // the producer (thread 0) tracks the staged ops [seen, issued) whose
+    // completion it has not observed yet
+    int issued = 0, seen = 0;
+    if (tid == 0) {
+        for (int o = 0; o < 3 && o < j.n_ops; ++o)
+            if (!(withhold_first && o == 0)) bulk_stage_op<KP>(&stages[o], s_ops[o], Pp, Tp, bar0 + 8 * o);
+        issued = j.n_ops < 3 ? j.n_ops : 3;
+    }
 
     u64 acc[KP][4];
     int scale_e = 0;
@@ -436,6 +445,7 @@ __device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* b
             *reinterpret_cast<volatile int*>(abort) = 1;
             break;
         }
+        seen = o + 1;
         const Op op = s_ops[o];
         const StageP<KP>& stg = stages[slot];
         if (op.s0 == kSrcPop) --sp;
@@ -468,10 +478,12 @@ __device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* b
         if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(empty) : "memory");
         // the producer refills it with op o + 3 once every warp has let go
         if (tid == 0 && o + 3 < j.n_ops) {
-            if (mbar_try_wait_bounded(empty, parity))
+            if (mbar_try_wait_bounded(empty, parity)) {
                 bulk_stage_op<KP>(&stages[slot], s_ops[o + 3], Pp, Tp, full);
-            else
+                issued = o + 4;
+            } else {
                 *reinterpret_cast<volatile int*>(abort) = 1;
+            }
         }
         if (op.s1 == kSrcNone) {
 #pragma unroll
@@ -515,11 +527,13 @@ __device__ void run_tile4p_bulk(const TileJob& j, unsigned char* sm, uint64_t* b
         }
     }
     // every issued copy was waited for by the consumers unless a wait ran out;
-    // then give the copies of the remaining slots a bounded chance to land
+    // then the producer gives the copies it issued and has not seen land a
+    // bounded chance to, before the CTA's shared memory goes
     __syncthreads();
     if (*reinterpret_cast<volatile int*>(abort) && tid == 0) {
-        for (int o = 0; o < j.n_ops; ++o)
-            if (!mbar_try_wait_bounded(bar0 + 8 * (o % 3), (uint32_t)(o / 3) & 1u)) break;
+        for (int o = seen; o < issued; ++o)
+            if (!(withhold_first && o == 0))
+                if (!mbar_try_wait_bounded(bar0 + 8 * (o % 3), (uint32_t)(o / 3) & 1u)) break;
     }
 
     // root: as run_tile4p

@@ -43,7 +43,7 @@ EXPORTS = [
     "plk_loglik", "plk_site_loglik", "plk_node_states", "plk_n_internal",
     "plk_q_matrix", "plk_pmat_host", "plk_discrete_gamma", "plk_effective_lengths",
     "plk_loglik_async", "plk_loglik_result", "plk_set_stream", "plk_set_profiling", "plk_kernel_times",
-    "plk_sum_sites_noalloc", "plk_prune_variant", "plk_set_patterns", "plk_n_patterns",
+    "plk_sum_sites_noalloc", "plk_prune_variant", "plk_test_withhold_stage", "plk_set_patterns", "plk_n_patterns",
     "plk_fit_gtr", "plk_fit_n_params",
     "plk_batch_create", "plk_batch_destroy", "plk_batch_last_error", "plk_batch_n_items", "plk_batch_add",
     "plk_batch_set_model", "plk_batch_loglik", "plk_batch_tuning", "plk_batch_form",
@@ -106,6 +106,7 @@ def lib() -> ctypes.CDLL:
     L.plk_set_profiling.argtypes = [hp, c_int]
     L.plk_kernel_times.argtypes = [hp, dp, ip, c_int]
     L.plk_prune_variant.argtypes = [hp]
+    L.plk_test_withhold_stage.argtypes = [hp]
     L.plk_set_patterns.argtypes = [hp, c_int]
     L.plk_n_patterns.argtypes = [hp]
     L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
@@ -411,6 +412,11 @@ class Handle:
              3: "prune20_kernel (CUDA cores, 8 warps/tile)", 4: "prune20_kernel (tensor cores, split TF32, 8 warps/tile)",
              5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)"},
     }
+
+    def test_withhold_stage(self) -> None:
+        """Arm the failure-path test of the TMA-fed post-order form (see
+        plk_test_withhold_stage)."""
+        _check(lib().plk_test_withhold_stage(self._h), self._h)
 
     def prune_kernel(self) -> str:
         """Name of the autotuned FP32 post-order kernel, or 'other' where no

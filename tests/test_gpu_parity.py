@@ -325,3 +325,25 @@ def test_site_patterns(S, n_tips, n_sites, C):
     np.testing.assert_array_equal(res[True][4], res[False][4])
     # FP32: the autotuner may pick another 20-state form for the other column count
     np.testing.assert_allclose(res[True][3], res[False][3], rtol=1e-6)
+
+
+def test_withheld_stage_times_out_and_the_handle_recovers(monkeypatch):
+    """Failure path of the TMA-fed post-order form: with its first stage
+    withheld every bounded mbarrier wait runs out, the evaluation reports
+    PLK_ERR_NUMERIC, and the next evaluation on the same handle is exact."""
+    import time
+    rng = np.random.default_rng(77)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 24, 700, C=4)
+    monkeypatch.setenv("PLK_PRUNE_VARIANT", "9")
+    with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
+        good = h.loglik(plk.PLK_FP32S)
+        assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[4][9]
+        h.test_withhold_stage()
+        t0 = time.perf_counter()
+        with pytest.raises(plk.PlkError) as err:
+            h.loglik(plk.PLK_FP32S)
+        waited = time.perf_counter() - t0
+        assert err.value.status == plk.PLK_ERR_NUMERIC
+        assert waited < 120.0
+        assert h.loglik(plk.PLK_FP32S) == good
+
