@@ -178,11 +178,13 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * the same with 8 warps.  -1 = not tuned yet or another kernel
  * applies (FP64, other state counts, more than 8 categories). */
 int plk_prune_variant(const plk_handle* h);
-/* Test of the failure path: the next FP32 evaluation that runs the TMA-fed
- * post-order form (candidate 9) withholds the first stage of every tile, so
- * every bounded mbarrier wait of that launch runs out; the tiles' sites come
- * out NaN, the evaluation fails with PLK_ERR_NUMERIC, and the handle stays
- * usable.  No effect on the other forms. */
+/* Test of the failure path: the next FP32 evaluation that runs one of the
+ * mbarrier-driven post-order forms -- the TMA-fed 4-state form (candidate 9)
+ * or the tcgen05 20-state form (candidate 5) -- withholds the first stage
+ * (respectively the first MMA commit) of every tile, so every bounded
+ * mbarrier wait of that launch runs out; the tiles' sites come out NaN, the
+ * evaluation fails with PLK_ERR_NUMERIC, and the handle stays usable.  No
+ * effect on the other forms. */
 plk_status plk_test_withhold_stage(plk_handle* h);
 /* Per-site log-likelihoods of the last plk_loglik (n_sites doubles). */
 plk_status plk_site_loglik(plk_handle* h, double* out);

@@ -54,7 +54,7 @@ constexpr uint32_t kIdesc = (1u << 4)          // D: F32
                             | (2u << 10)       // B: TF32
                             | ((kN >> 3) << 17)    // N
                             | ((128 >> 4) << 24);  // M
-constexpr int kWaitLimit = 1 << 22;       // try_wait rounds before a wait gives up
+constexpr int kWaitLimit = 1 << 20;       // try_wait rounds before a wait gives up (MMAs land in microseconds)
 
 struct P20UArgs {
     PruneArgs a;
@@ -303,6 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
     int e_site = 0, sp = 0;
     uint32_t phase = 0;
     bool pending = false;  // an MMA commit whose completion was not observed
+    bool withheld = false;  // the failure-path test withholds the first commit
     for (int o = 0; o < a.n_ops; ++o) {
         cp_async_wait<1>();
         const Op op = s_ops[o];
@@ -323,8 +324,9 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
             tc_fence_after();
             if (mma0) issue_child(tmem, smem_u32(op.s0 == kSrcPop ? pop_op : acc_op), smem_u32(st));
             if (mma1) issue_child(tmem + 32, smem_u32(acc_op), smem_u32(st + cb));
-            umma_commit(mbar);
+            if (!(a.withhold_first_stage && !withheld)) umma_commit(mbar);
         }
+        if ((mma0 || mma1) && a.withhold_first_stage) withheld = true;
         if (op.s0 >= 0) tip_row(st, s_codes[(size_t)op.s0 * kTile + tid], a.n_codes, m0);
         if (op.s1 >= 0) tip_row(st + cb, s_codes[(size_t)op.s1 * kTile + tid], a.n_codes, m1);
         if (mma0 || mma1) {
@@ -360,7 +362,8 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
         }
     }
     cp_async_wait<0>();
-    if (pending) mbar_wait(mbar, phase ^ 1u);  // a commit still in flight after a timed-out wait
+    // a commit still in flight after a timed-out wait (none when it was withheld)
+    if (pending && !a.withhold_first_stage) mbar_wait(mbar, phase ^ 1u);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {

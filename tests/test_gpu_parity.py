@@ -347,3 +347,23 @@ def test_withheld_stage_times_out_and_the_handle_recovers(monkeypatch):
         assert waited < 120.0
         assert h.loglik(plk.PLK_FP32S) == good
 
+
+def test_withheld_mma_commit_times_out_and_the_handle_recovers(monkeypatch):
+    """Failure path of the tcgen05 20-state form: with the first MMA commit
+    withheld every bounded mbarrier wait runs out, the evaluation reports
+    PLK_ERR_NUMERIC (TMEM still freed), and the next evaluation is exact."""
+    import time
+    rng = np.random.default_rng(78)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 16, 300, S=20, C=4)
+    monkeypatch.setenv("PLK_PRUNE_VARIANT", "5")
+    with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
+        good = h.loglik(plk.PLK_FP32S)
+        assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[20][5]
+        h.test_withhold_stage()
+        t0 = time.perf_counter()
+        with pytest.raises(plk.PlkError) as err:
+            h.loglik(plk.PLK_FP32S)
+        assert err.value.status == plk.PLK_ERR_NUMERIC
+        assert time.perf_counter() - t0 < 120.0
+        assert h.loglik(plk.PLK_FP32S) == good
+
