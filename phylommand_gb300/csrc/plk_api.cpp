@@ -131,12 +131,20 @@ struct plk_handle {
     int* h_flag = nullptr;
     bool flag_pending = false;
     int flag_gen = 0;  // value the encode kernel stores for an empty cell of the current alignment
+    // the tip masks' copy and encode run on copy_stream, so that the tree and
+    // model uploads and the P(t) kernel on the main stream overlap them; the
+    // main stream waits for codes_ready just before the post-order pass
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t main_done = nullptr, codes_ready = nullptr;
+    bool codes_pending = false;
     ~plk_handle() {
         for (auto& s : evs)
             for (auto& e : s.e) cudaEventDestroy(e);
         if (arena) cudaFreeHost(arena);
         if (arena_done) cudaEventDestroy(arena_done);
         if (h_flag) cudaFreeHost(h_flag);
+        if (main_done) cudaEventDestroy(main_done);
+        if (codes_ready) cudaEventDestroy(codes_ready);
     }
 };
 
@@ -413,6 +421,10 @@ bool tuned_paired(const plk_handle* h) {
 // Runs the post-order pass (P(t) already built); store != null asks for the
 // conditional vectors of every internal node in *store.
 plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* after_prune = nullptr) {
+    if (h->codes_pending) {  // the tip codes come from the copy stream
+        PLK_CUDA(h, cudaStreamWaitEvent(h->stream, h->codes_ready, 0), "cudaStreamWaitEvent");
+        h->codes_pending = false;
+    }
     const size_t tsz = precision == PLK_FP64 ? sizeof(double) : sizeof(float);
     const size_t vec_bytes = (size_t)h->post.size() * h->C * h->n_sites * h->S * tsz;
     const int blocks = (h->n_sites + 63) / 64;  // the smallest tile: 64 sites (prune4p, two threads per site)
@@ -542,6 +554,10 @@ void plk_destroy(plk_handle* h) {
     if (!h) return;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->copy_stream) {
+        cudaStreamSynchronize(h->copy_stream);
+        cudaStreamDestroy(h->copy_stream);
+    }
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -570,6 +586,10 @@ plk_status set_alignment_impl(plk_handle* h, int n_tips, int n_sites, int n_stat
     if (n_tips < 1 || n_sites < 1 || n_states < 1 || n_states > kMaxStates || (!masks && !masks8))
         return fail(h, PLK_ERR_ARG, "alignment needs n_tips >= 1, n_sites >= 1, 1 <= n_states <= 24");
     PLK_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->codes_pending) {  // an earlier alignment's copy and encode are still on the copy stream
+        PLK_CUDA(h, cudaStreamWaitEvent(h->stream, h->codes_ready, 0), "cudaStreamWaitEvent");
+        h->codes_pending = false;
+    }
     h->n_sites_full = n_sites;
     h->site_pattern.clear();
     h->pattern_w.clear();
@@ -623,22 +643,34 @@ plk_status set_alignment_impl(plk_handle* h, int n_tips, int n_sites, int n_stat
         const int eb = masks8 ? 1 : (int)sizeof(uint32_t);
         PLK_CUDA(h, h->d_mask_raw.ensure(n_cells * eb), "allocate mask staging");
         PLK_CUDA(h, h->d_codes.ensure((size_t)n_tips * code_stride(n_sites)), "allocate tip codes");
+        if (!h->copy_stream) {
+            PLK_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "create copy stream");
+            PLK_CUDA(h, cudaEventCreateWithFlags(&h->main_done, cudaEventDisableTiming), "cudaEventCreate");
+            PLK_CUDA(h, cudaEventCreateWithFlags(&h->codes_ready, cudaEventDisableTiming), "cudaEventCreate");
+        }
         if (!h->d_flag.p) {  // zero once; every alignment then marks with its own generation
             PLK_CUDA(h, h->d_flag.ensure(sizeof(int)), "allocate flag");
             PLK_CUDA(h, cudaMemsetAsync(h->d_flag.p, 0, sizeof(int), h->stream), "clear flag");
         }
+        if (!h->h_flag) PLK_CUDA(h, cudaMallocHost(&h->h_flag, sizeof(int)), "allocate flag");
         h->flag_gen = h->flag_gen == 0x7fffffff ? 1 : h->flag_gen + 1;
+        // the copy stream starts after all work already on the main stream
+        // (earlier passes still reading the masks or codes, the flag clear)
+        PLK_CUDA(h, cudaEventRecord(h->main_done, h->stream), "cudaEventRecord");
+        PLK_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->main_done, 0), "cudaStreamWaitEvent");
         PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks8 ? (const void*)masks8 : (const void*)masks, n_cells * eb,
-                                    cudaMemcpyHostToDevice, h->stream),
+                                    cudaMemcpyHostToDevice, h->copy_stream),
                  "upload masks");
         PLK_CUDA(h, launch_encode_small(h->d_mask_raw.p, eb, n_tips, n_sites, code_stride(n_sites), all,
-                                        h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->flag_gen, h->stream),
+                                        h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->flag_gen, h->copy_stream),
                  "encode kernel launch");
         // the empty-cell flag comes back with the next result fetch (no wait
         // here); the code table is the identity, so none is uploaded (the
         // P(t) kernel takes the code as the state set)
-        if (!h->h_flag) PLK_CUDA(h, cudaMallocHost(&h->h_flag, sizeof(int)), "allocate flag");
-        PLK_CUDA(h, cudaMemcpyAsync(h->h_flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
+        PLK_CUDA(h, cudaMemcpyAsync(h->h_flag, h->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, h->copy_stream),
+                 "read flag");
+        PLK_CUDA(h, cudaEventRecord(h->codes_ready, h->copy_stream), "cudaEventRecord");
+        h->codes_pending = true;
         h->flag_pending = true;
     } else {
         const size_t stride = (size_t)code_stride(n_sites);

@@ -367,3 +367,36 @@ def test_withheld_mma_commit_times_out_and_the_handle_recovers(monkeypatch):
         assert time.perf_counter() - t0 < 120.0
         assert h.loglik(plk.PLK_FP32S) == good
 
+
+def test_back_to_back_alignments_on_one_handle():
+    """The byte masks travel and are encoded on the handle's copy stream:
+    replacing the alignment before evaluating, or with a host-encoded
+    20-state one, must leave no stale or half-written tip codes."""
+    rng = np.random.default_rng(91)
+    left, right, bl, m1, Q, f, cr, cw = _random_case(rng, 30, 2000, C=4)
+    m2 = m1[:, ::-1].copy()
+    teff = plk.effective_lengths(left, right, bl, False)
+    want1 = O.loglik(left, right, m1, teff, Q, f, cr, cw, p_mode=O.P_EXACT).lnl
+    want2 = O.loglik(left, right, m2, teff, Q, f, cr, cw, p_mode=O.P_EXACT).lnl
+    l20, r20, b20, m20, Q20, f20, cr20, cw20 = _random_case(rng, 30, 500, S=20, C=4)
+    with plk.Handle() as h:
+        h.set_tree(left, right, bl)
+        for _ in range(3):
+            h.set_alignment(m1.astype(np.uint8), 4)
+            h.set_alignment(m2.astype(np.uint8), 4)   # replaced before any evaluation
+            h.set_tree(left, right, bl)
+            h.set_rate_model(False)
+            h.set_model(Q, f, True, cr, cw, plk.PLK_P_EXACT)
+            assert h.loglik(plk.PLK_FP32S) == pytest.approx(want2, rel=FP32_REL)
+            h.set_alignment(m1.astype(np.uint8), 4)
+            assert h.loglik(plk.PLK_FP32S) == pytest.approx(want1, rel=FP32_REL)
+        # a host-encoded 20-state alignment right after a byte-mask one
+        h.set_alignment(m1.astype(np.uint8), 4)
+        h.set_alignment(m20, 20)
+        h.set_tree(l20, r20, b20)
+        h.set_rate_model(False)
+        h.set_model(Q20, f20, True, cr20, cw20, plk.PLK_P_EXACT)
+        t20 = plk.effective_lengths(l20, r20, b20, False)
+        want20 = O.loglik(l20, r20, m20, t20, Q20, f20, cr20, cw20, p_mode=O.P_EXACT).lnl
+        assert h.loglik(plk.PLK_FP32S) == pytest.approx(want20, rel=FP32_REL)
+
