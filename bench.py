@@ -402,8 +402,9 @@ def run_protein(args):
     res = {}
     names = {"1": "prune20_kernel, CUDA cores, 4 warps/tile", "2": "prune20_kernel, tensor cores (split TF32), 4 warps/tile",
              "3": "prune20_kernel, CUDA cores, 8 warps/tile", "4": "prune20_kernel, tensor cores (split TF32), 8 warps/tile",
-             "5": "prune20u_kernel, tcgen05 tensor cores (split TF32, TMEM accumulators)", "auto": "autotuned"}
-    for v in ("1", "2", "3", "4", "5", "auto"):
+             "5": "prune20u_kernel, tcgen05 tensor cores (split TF32, TMEM accumulators)",
+             "6": "prune20v_kernel, tcgen05 tensor cores, compact form (three CTAs per SM)", "auto": "autotuned"}
+    for v in ("1", "2", "3", "4", "5", "6", "auto"):
         if v == "auto":
             os.environ.pop("PLK_PRUNE_VARIANT", None)
         else:

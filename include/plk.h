@@ -173,14 +173,17 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * same with the categories in pairs on packed FP32x2), 5 / 6 = prune4p_kernel
  * reading the tip codes from global memory, 7 / 8 = prune4p_kernel with two
  * threads per site (each takes half of the category pairs; codes from global
- * memory / staged).  20 states: 1 / 2 =
- * prune20_kernel on CUDA cores / tensor cores with 4 warps per tile, 3 / 4 =
- * the same with 8 warps.  -1 = not tuned yet or another kernel
+ * memory / staged), 9 = prune4p_bulk_kernel (TMA-fed stage ring).  20
+ * states: 1 / 2 = prune20_kernel on CUDA cores / mma.sync tensor cores with
+ * 4 warps per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel
+ * (tcgen05 tensor cores, TMEM accumulators, spill stack in TMEM), 6 =
+ * prune20v_kernel (its compact form: three CTAs per SM, spills in global
+ * memory).  -1 = not tuned yet or another kernel
  * applies (FP64, other state counts, more than 8 categories). */
 int plk_prune_variant(const plk_handle* h);
 /* Test of the failure path: the next FP32 evaluation that runs one of the
  * mbarrier-driven post-order forms -- the TMA-fed 4-state form (candidate 9)
- * or the tcgen05 20-state form (candidate 5) -- withholds the first stage
+ * or the tcgen05 20-state forms (candidates 5 and 6) -- withholds the first stage
  * (respectively the first MMA commit) of every tile, so every bounded
  * mbarrier wait of that launch runs out; the tiles' sites come out NaN, the
  * evaluation fails with PLK_ERR_NUMERIC, and the handle stays usable.  No

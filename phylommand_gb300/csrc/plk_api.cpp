@@ -448,7 +448,9 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     if (!store && precision == PLK_FP32S && h->S == 20)
         for (int v = 1; v <= 4; ++v)
             if (prune20_fits(a, v)) cands20.push_back(v);
-    if (!store && precision == PLK_FP32S && h->S == 20 && prune20u_fits(a)) cands20.push_back(5);
+    if (!store && precision == PLK_FP32S && h->S == 20)
+        for (int form = 0; form < 2; ++form)
+            if (prune20u_fits(a, form)) cands20.push_back(5 + form);
     if (!cands20.empty()) {
         PLK_CUDA(h, h->d_work.ensure(std::max(prune20_scratch_bytes(a, h->n_nodes), prune20u_scratch_bytes(a, h->n_nodes))),
                  "allocate scratch");

@@ -210,7 +210,8 @@ struct PruneArgs {
     // 20 states: 0 = prune_generic_kernel, 1 / 2 = prune20_kernel on CUDA
     // cores / mma.sync tensor cores (TF32, three-product split) with 4 warps
     // per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel on
-    // tcgen05 tensor cores (TMEM accumulators).
+    // tcgen05 tensor cores (TMEM accumulators), 6 = its compact form
+    // prune20v_kernel (three CTAs per SM).
     int variant;
     int n_nodes;
     void* scratch;             // kernel-specific scratch (prune20_scratch_bytes)
@@ -239,10 +240,14 @@ cudaError_t launch_prune20(const PruneArgs& a, int n_nodes, int mode, void* scra
 cudaError_t launch_combine20(const float* cat_L, const int* cat_E, const PruneArgs& a, int* n_blocks,
                              cudaStream_t st);
 // 20 states on tcgen05 tensor cores with TMEM accumulators (plk_prune20u.cu):
-// the B-operand relayout, the pass and the per-site combine.
-bool prune20u_fits(const PruneArgs& a);
+// the B-operand relayout, the pass and the per-site combine.  form 0 =
+// prune20u_kernel (spill stack in TMEM, three-slot stage ring), 1 =
+// prune20v_kernel (the compact form: three CTAs per SM, spills in global
+// memory).
+bool prune20u_fits(const PruneArgs& a, int form);
 size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes);
-cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int* n_blocks, cudaStream_t st);
+cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int form, int* n_blocks,
+                            cudaStream_t st);
 // Staged 4-state FP32 kernel with categories in pairs on the packed FP32x2
 // pipe (plk_prune4p.cu), C = 2, 4 or 8; needs prune4p_scratch_bytes of
 // a.scratch for the paired P(t) and tip tables.

@@ -556,8 +556,8 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
         return launch_prune4p(a, 1, a.variant == 7, 2, n_blocks, st);
     if (!fp64 && !store && S == 4 && a.variant == 9 && prune4p_fits(a, 1, 0))
         return launch_prune4p(a, 1, true, 0, n_blocks, st);
-    if (!fp64 && !store && S == 20 && a.variant == 5 && prune20u_fits(a))
-        return launch_prune20u(a, a.n_nodes, a.scratch, n_blocks, st);
+    if (!fp64 && !store && S == 20 && (a.variant == 5 || a.variant == 6) && prune20u_fits(a, a.variant - 5))
+        return launch_prune20u(a, a.n_nodes, a.scratch, a.variant - 5, n_blocks, st);
     if (!fp64 && !store && S == 20 && a.variant > 0 && a.variant < 5 && prune20_fits(a, a.variant))
         return launch_prune20(a, a.n_nodes, a.variant, a.scratch, n_blocks, st);
     if (S == 4 && a.C <= 8) {

@@ -44,6 +44,8 @@ constexpr int kN = 32;                   // MMA N: output states, padded
 constexpr int kAGroup = 16 * 128;        // bytes of a 4-column group of an A operand (LBO of A)
 constexpr int kAPart = 6 * kAGroup;      // one TF32 part of an A operand (K = 24)
 constexpr int kAOperand = 2 * kAPart;    // hi and lo
+constexpr int kAPart5 = 5 * kAGroup;      // one TF32 part without its zero group (compact form)
+constexpr int kAOperand5 = 2 * kAPart5;
 constexpr int kBGroup = 4 * 128;         // bytes of a 4-column group of a B operand (LBO of B)
 constexpr int kBPart = 6 * kBGroup;
 constexpr int kBFloats = 2 * kBPart / 4;  // staged B image per (node, category): 1,536 floats
@@ -62,6 +64,7 @@ struct P20UArgs {
     const float* Ts;   // tip tables [tip][category][state][code (n_codes padded to 4)]
     float* cat_L;      // [C][n_sites]
     int* cat_E;        // [C][n_sites]
+    float* spill;      // compact form: spilled vectors [CTA][slot][state][site of the tile]
     int child_bytes;   // bytes of one child's slot in a stage
     int tmem_cols;
 };
@@ -148,8 +151,13 @@ __device__ __forceinline__ void tmem_st20(uint32_t taddr, const float x[kS]) {
         : "memory");
 }
 
-// row t of an A operand: TF32 hi and lo parts of the 20 values (columns
-// 20-23 stay zero from the start)
+// row t of an A operand: TF32 hi and lo parts of the 20 values, the lo part
+// APART bytes after the hi part.  With APART = kAPart the columns 20-23 of
+// each part are a group of their own that stays zero; with APART = kAPart5
+// the K step over columns 16-23 reads the next part's first group (or the
+// zero pad after the last operand) as columns 20-23: finite values that meet
+// the zero rows 20-23 of every B image, so they add exact zeros.
+template <int APART>
 __device__ __forceinline__ void write_operand(unsigned char* area, int t, const float x[kS]) {
     const int row = (t >> 3) * 128 + (t & 7) * 16;
 #pragma unroll
@@ -164,16 +172,18 @@ __device__ __forceinline__ void write_operand(unsigned char* area, int t, const 
         l.z = tf32_rna(x[4 * g + 2] - h.z);
         l.w = tf32_rna(x[4 * g + 3] - h.w);
         *reinterpret_cast<float4*>(area + g * kAGroup + row) = h;
-        *reinterpret_cast<float4*>(area + kAPart + g * kAGroup + row) = l;
+        *reinterpret_cast<float4*>(area + APART + g * kAGroup + row) = l;
     }
 }
 
-// nine MMAs of one child message into the accumulator at d_tmem
+// nine MMAs of one child message into the accumulator at d_tmem (A's lo
+// part APART bytes after its hi part)
+template <int APART>
 __device__ __forceinline__ void issue_child(uint32_t d_tmem, uint32_t a_addr, uint32_t b_addr) {
 #pragma unroll
     for (int ks = 0; ks < 3; ++ks) {
         const uint64_t a_hi = smem_desc(a_addr + ks * 2 * kAGroup, kAGroup, 128);
-        const uint64_t a_lo = smem_desc(a_addr + kAPart + ks * 2 * kAGroup, kAGroup, 128);
+        const uint64_t a_lo = smem_desc(a_addr + APART + ks * 2 * kAGroup, kAGroup, 128);
         const uint64_t b_hi = smem_desc(b_addr + ks * 2 * kBGroup, kBGroup, 128);
         const uint64_t b_lo = smem_desc(b_addr + kBPart + ks * 2 * kBGroup, kBGroup, 128);
         umma_tf32(d_tmem, a_lo, b_hi, ks > 0 ? 1u : 0u);  // small products first
@@ -310,7 +320,7 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
         if (op.s0 == kSrcPop) {
             --sp;
             tmem_ld20(lane + kAccCols + kSlotCols * sp, m0);
-            write_operand(pop_op, tid, m0);
+            write_operand<kAPart>(pop_op, tid, m0);
         }
         fence_proxy_async();  // cp.async data and operand rows -> the tensor cores
         tc_fence_before();
@@ -322,8 +332,8 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
         const bool mma0 = op.s0 < 0, mma1 = op.s1 == kSrcAcc;
         if (tid == 0 && (mma0 || mma1)) {
             tc_fence_after();
-            if (mma0) issue_child(tmem, smem_u32(op.s0 == kSrcPop ? pop_op : acc_op), smem_u32(st));
-            if (mma1) issue_child(tmem + 32, smem_u32(acc_op), smem_u32(st + cb));
+            if (mma0) issue_child<kAPart>(tmem, smem_u32(op.s0 == kSrcPop ? pop_op : acc_op), smem_u32(st));
+            if (mma1) issue_child<kAPart>(tmem + 32, smem_u32(acc_op), smem_u32(st + cb));
             if (!(a.withhold_first_stage && !withheld)) umma_commit(mbar);
         }
         if ((mma0 || mma1) && a.withhold_first_stage) withheld = true;
@@ -358,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
             tmem_st20(lane + kAccCols + kSlotCols * sp, m0);
             ++sp;
         } else {
-            write_operand(acc_op, tid, m0);
+            write_operand<kAPart>(acc_op, tid, m0);
         }
     }
     cp_async_wait<0>();
@@ -384,7 +394,168 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
     }
 }
 
-int tmem_cols_for(const PruneArgs& a) {
+// The compact form of prune20u_kernel: the same MMAs and scaling with less
+// shared memory and TMEM per CTA, so that three CTAs share an SM instead of
+// two (a 128-site tile's op chain is latency-bound, and the grid is
+// tiles x categories of such chains):
+//   * A operands without their zero column group (20 KB instead of 24 KB,
+//     one zero group after the last operand);
+//   * a two-slot stage ring, one op ahead (24 KB instead of 36 KB);
+//   * spilled vectors in global memory (an L2-resident scratch written at a
+//     push and read back one op before the pop, by the thread that wrote
+//     them), so that TMEM holds only the two accumulators (64 columns);
+//   * tip codes read from global memory one op ahead instead of staged.
+__global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ uint32_t s_tmem;
+    __shared__ float s_rw[kS];
+    __shared__ int s_abort;
+    const PruneArgs& a = g.a;
+    const int k = blockIdx.y;
+    const int tile0 = blockIdx.x * kTile;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int cb = g.child_bytes;
+    unsigned char* acc_op = smem;                // A operand of the running vector
+    unsigned char* pop_op = smem + kAOperand5;   // A operand of a vector popped from the stack
+    unsigned char* stages = smem + 2 * kAOperand5 + kAGroup;  // after the zero group
+    Op* s_ops = reinterpret_cast<Op*>(stages + 2 * 2 * cb);
+    const uint32_t mbar = smem_u32(&s_mbar);
+    const int site = tile0 + tid;
+    const bool has_code = site < a.site_stride;
+    float* spill = g.spill + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * (size_t)(a.max_depth > 1 ? a.max_depth : 1) *
+                                 (kS * kTile) + tid;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_tmem)),
+                     "r"(g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    if (tid < kS) s_rw[tid] = (float)a.root_w[tid];
+    for (int i = tid; i < a.n_ops; i += kThreads) s_ops[i] = a.ops[i];
+    // both A operands and the zero group after them: every column an MMA
+    // reads is finite from the start
+    for (int i = tid; i < (2 * kAOperand5 + kAGroup) / 16; i += kThreads)
+        reinterpret_cast<uint4*>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
+    stage_op20u(stages, s_ops[0], k, g);
+    cp_async_commit();
+
+    auto code_of = [&](int src) -> int {
+        return (src >= 0 && has_code) ? (int)__ldg(a.codes + (size_t)src * a.site_stride + site) : 0;
+    };
+    int c0 = code_of(s_ops[0].s0), c1 = code_of(s_ops[0].s1);
+    float m0[kS], m1[kS], pre[kS];
+    int e_site = 0, sp = 0;
+    uint32_t phase = 0;
+    bool pending = false;   // an MMA commit whose completion was not observed
+    bool withheld = false;  // the failure-path test withholds the first commit
+    for (int o = 0; o < a.n_ops; ++o) {
+        cp_async_wait<0>();
+        const Op op = s_ops[o];
+        const bool has_next = o + 1 < a.n_ops;
+        int n0 = 0, n1 = 0;
+        bool next_pops = false;
+        if (has_next) {
+            const Op nx = s_ops[o + 1];
+            n0 = code_of(nx.s0);
+            n1 = code_of(nx.s1);
+            next_pops = nx.s0 == kSrcPop;
+        }
+        if (op.s0 == kSrcPop) {
+            --sp;
+            write_operand<kAPart5>(pop_op, tid, pre);
+        }
+        fence_proxy_async();  // cp.async data and operand rows -> the tensor cores
+        tc_fence_before();
+        __syncthreads();
+        if (s_abort) break;
+        if (has_next) stage_op20u(stages + ((o + 1) & 1) * 2 * cb, s_ops[o + 1], k, g);
+        cp_async_commit();
+        // the vector the next op pops (this op does not push when the next pops)
+        if (next_pops) {
+#pragma unroll
+            for (int i = 0; i < kS; ++i) pre[i] = spill[(size_t)((sp - 1) * kS + i) * kTile];
+        }
+        const unsigned char* st = stages + (o & 1) * 2 * cb;
+        const bool mma0 = op.s0 < 0, mma1 = op.s1 == kSrcAcc;
+        if (tid == 0 && (mma0 || mma1)) {
+            tc_fence_after();
+            if (mma0) issue_child<kAPart5>(tmem, smem_u32(op.s0 == kSrcPop ? pop_op : acc_op), smem_u32(st));
+            if (mma1) issue_child<kAPart5>(tmem + 32, smem_u32(acc_op), smem_u32(st + cb));
+            if (!(a.withhold_first_stage && !withheld)) umma_commit(mbar);
+        }
+        if ((mma0 || mma1) && a.withhold_first_stage) withheld = true;
+        if (op.s0 >= 0) tip_row(st, c0, a.n_codes, m0);
+        if (op.s1 >= 0) tip_row(st + cb, c1, a.n_codes, m1);
+        if (mma0 || mma1) {
+            pending = true;
+            if (!mbar_wait(mbar, phase)) s_abort = 1;
+            else pending = false;
+            phase ^= 1u;
+            tc_fence_after();
+            if (mma0) tmem_ld20(lane, m0);
+            if (mma1) tmem_ld20(lane + 32, m1);
+        }
+        if (op.s1 != kSrcNone) {
+#pragma unroll
+            for (int i = 0; i < kS; ++i) m0[i] *= m1[i];
+        }
+        float mx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kS; ++i) mx = fmaxf(mx, m0[i]);
+        if (mx < scale_threshold<float>() && mx > 0.0f) {
+            int e;
+            float f1, f2;
+            pow2_factors(mx, &e, &f1, &f2);
+#pragma unroll
+            for (int i = 0; i < kS; ++i) m0[i] = (m0[i] * f1) * f2;
+            e_site += e;
+        }
+        if (o == a.n_ops - 1) break;  // the root vector stays in m0
+        if (op.push) {
+#pragma unroll
+            for (int i = 0; i < kS; ++i) spill[(size_t)(sp * kS + i) * kTile] = m0[i];
+            ++sp;
+        } else {
+            write_operand<kAPart5>(acc_op, tid, m0);
+        }
+        c0 = n0;
+        c1 = n1;
+    }
+    cp_async_wait<0>();
+    // a commit still in flight after a timed-out wait (none when it was withheld)
+    if (pending && !a.withhold_first_stage) mbar_wait(mbar, phase ^ 1u);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(g.tmem_cols)
+                     : "memory");
+    }
+    float l = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kS; ++i) l = fmaf(m0[i], s_rw[i], l);
+    if (s_abort) l = __int_as_float(0x7fc00000);
+    if (site < a.n_sites) {
+        g.cat_L[(size_t)k * a.n_sites + site] = l;
+        g.cat_E[(size_t)k * a.n_sites + site] = e_site;
+    }
+}
+
+int tmem_cols_for(const PruneArgs& a, int form) {
+    if (form == 1) return kAccCols;
     const int need = kAccCols + kSlotCols * std::max(a.max_depth, 1);
     int cols = 32;
     while (cols < need) cols *= 2;
@@ -396,29 +567,36 @@ int child_bytes_for(const PruneArgs& a) {
     return (std::max(2 * kBPart, tip) + 127) & ~127;
 }
 
-size_t smem20u_bytes(const PruneArgs& a) {
-    return (size_t)2 * kAOperand + (size_t)3 * 2 * child_bytes_for(a) +
-           (((size_t)a.n_ops * sizeof(Op) + 15) & ~(size_t)15) + (size_t)a.n_tips * kTile;
+size_t smem20u_bytes(const PruneArgs& a, int form) {
+    const size_t ops = ((size_t)a.n_ops * sizeof(Op) + 15) & ~(size_t)15;
+    if (form == 1) return (size_t)2 * kAOperand5 + kAGroup + (size_t)2 * 2 * child_bytes_for(a) + ops;
+    return (size_t)2 * kAOperand + (size_t)3 * 2 * child_bytes_for(a) + ops + (size_t)a.n_tips * kTile;
+}
+
+size_t spill_bytes(const PruneArgs& a) {
+    const size_t tiles = (size_t)(a.n_sites + kTile - 1) / kTile;
+    return tiles * a.C * (size_t)std::max(a.max_depth, 1) * kS * kTile * sizeof(float);
 }
 
 }  // namespace
 
-bool prune20u_fits(const PruneArgs& a) {
-    if (a.C < 1 || a.n_codes < 1 || a.n_ops < 1) return false;
-    if (tmem_cols_for(a) > 512) return false;
-    return smem20u_bytes(a) <= 200 * 1024;
+bool prune20u_fits(const PruneArgs& a, int form) {
+    if (a.C < 1 || a.n_codes < 1 || a.n_ops < 1 || form < 0 || form > 1) return false;
+    if (tmem_cols_for(a, form) > 512) return false;
+    return smem20u_bytes(a, form) <= 200 * 1024;
 }
 
 size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes) {
     const size_t ps = (size_t)n_nodes * a.C * kBFloats * sizeof(float);
     const size_t ts = (size_t)a.n_tips * a.C * kS * codes_padded(a.n_codes) * sizeof(float);
     const size_t cl = (((size_t)a.C * a.n_sites * sizeof(float) + 255) & ~(size_t)255) +
-                      (size_t)a.C * a.n_sites * sizeof(int);
-    return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl;
+                      (((size_t)a.C * a.n_sites * sizeof(int) + 255) & ~(size_t)255);
+    return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl + spill_bytes(a);
 }
 
-cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int* n_blocks, cudaStream_t st) {
-    if (!prune20u_fits(a) || scratch == nullptr) return cudaErrorInvalidValue;
+cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int form, int* n_blocks,
+                            cudaStream_t st) {
+    if (!prune20u_fits(a, form) || scratch == nullptr) return cudaErrorInvalidValue;
     unsigned char* base = static_cast<unsigned char*>(scratch);
     P20UArgs g{};
     g.a = a;
@@ -429,8 +607,10 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
     g.cat_L = reinterpret_cast<float*>(base + off);
     off += (((size_t)a.C * a.n_sites * sizeof(float)) + 255) & ~(size_t)255;
     g.cat_E = reinterpret_cast<int*>(base + off);
+    off += (((size_t)a.C * a.n_sites * sizeof(int)) + 255) & ~(size_t)255;
+    g.spill = reinterpret_cast<float*>(base + off);
     g.child_bytes = child_bytes_for(a);
-    g.tmem_cols = tmem_cols_for(a);
+    g.tmem_cols = tmem_cols_for(a, form);
     {
         const long long total =
             (long long)n_nodes * a.C * kBFloats + (long long)a.n_tips * a.C * kS * codes_padded(a.n_codes);
@@ -443,14 +623,15 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
+    void (*kern)(P20UArgs) = form == 1 ? prune20v_kernel : prune20u_kernel;
     // pad the shared memory until no more CTAs fit on an SM than its TMEM serves
     const int max_ctas = 512 / g.tmem_cols;
-    size_t smem = smem20u_bytes(a);
+    size_t smem = smem20u_bytes(a, form);
     int occ = 0;
     for (;;) {
-        cudaError_t e = cudaFuncSetAttribute(prune20u_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, prune20u_kernel, kThreads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, smem);
         if (e != cudaSuccess) return e;
         if (occ <= max_ctas) break;
         smem += 4096;
@@ -458,7 +639,7 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int*
     }
     if (occ < 1) return cudaErrorInvalidConfiguration;
     dim3 grid((a.n_sites + kTile - 1) / kTile, a.C);
-    prune20u_kernel<<<grid, kThreads, smem, st>>>(g);
+    kern<<<grid, kThreads, smem, st>>>(g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_combine20(g.cat_L, g.cat_E, a, n_blocks, st);

@@ -410,7 +410,8 @@ class Handle:
             9: "prune4p_bulk_kernel (category pairs on FP32x2, TMA bulk-copy stage ring, mbarrier pipeline)"},
         20: {1: "prune20_kernel (CUDA cores, 4 warps/tile)", 2: "prune20_kernel (tensor cores, split TF32, 4 warps/tile)",
              3: "prune20_kernel (CUDA cores, 8 warps/tile)", 4: "prune20_kernel (tensor cores, split TF32, 8 warps/tile)",
-             5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)"},
+             5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)",
+             6: "prune20v_kernel (tcgen05 tensor cores, compact: three CTAs per SM, split TF32)"},
     }
 
     def test_withhold_stage(self) -> None:

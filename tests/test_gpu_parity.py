@@ -68,6 +68,21 @@ def test_exact_pmat_mode_matches_oracle(name):
 def _random_case(rng, n_tips, n_sites, S=4, C=1, missing=0.02, shape="yule"):
     if shape == "yule":
         left, right, bl = synth.yule_tree(n_tips, 0.1, rng)
+    elif shape == "balanced":  # tips paired level by level: the deepest spill stack
+        n_nodes = 2 * n_tips - 1
+        left = np.full(n_nodes, -1, dtype=np.int32)
+        right = np.full(n_nodes, -1, dtype=np.int32)
+        level, u = list(range(n_tips)), n_tips
+        while len(level) > 1:
+            nxt = []
+            for i in range(0, len(level) - 1, 2):
+                left[u], right[u] = level[i], level[i + 1]
+                nxt.append(u)
+                u += 1
+            if len(level) % 2:
+                nxt.append(level[-1])
+            level = nxt
+        bl = rng.exponential(0.1, n_nodes)
     else:  # caterpillar: ((((t0,t1),t2),t3)...)
         n_nodes = 2 * n_tips - 1
         left = np.full(n_nodes, -1, dtype=np.int32)
@@ -257,20 +272,23 @@ def test_full_size_dna_gtr_gamma_fp32_against_fp64():
 
 
 @pytest.mark.parametrize("n_tips,n_sites,C,shape", [(64, 2000, 4, "yule"), (7, 1, 1, "yule"), (33, 129, 8, "yule"),
-                                                    (200, 300, 4, "caterpillar"), (16, 4099, 2, "yule")])
+                                                    (200, 300, 4, "caterpillar"), (16, 4099, 2, "yule"),
+                                                    (128, 700, 4, "balanced"), (45, 257, 3, "balanced")])
 def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
     """20 states: prune20_kernel on CUDA cores (1, 3) and on mma.sync tensor
-    cores with the split-TF32 products (2, 4), and prune20u_kernel on tcgen05
-    tensor cores with TMEM accumulators (5), against the FP64 oracle, per
-    site; the caterpillar tree forces repeated rescaling and spills, ambiguity
-    codes the table look-ups."""
+    cores with the split-TF32 products (2, 4), and on tcgen05 tensor cores
+    with TMEM accumulators prune20u_kernel (5, spill stack in TMEM) and its
+    compact form prune20v_kernel (6, spills in global memory), against the
+    FP64 oracle, per site; the caterpillar tree forces repeated rescaling,
+    the balanced trees the deepest spill stacks, ambiguity codes the table
+    look-ups."""
     rng = np.random.default_rng(n_tips * 7 + n_sites)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, S=20, C=C, missing=0.03, shape=shape)
     amb = rng.random(masks.shape) < 0.02
     masks[amb] |= np.uint32(1 << 3)                          # two-state ambiguity
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
-    for v in ("5", "1", "2", "3", "4"):
+    for v in ("5", "6", "1", "2", "3", "4"):
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
             got = h.loglik(plk.PLK_FP32S)
@@ -348,17 +366,18 @@ def test_withheld_stage_times_out_and_the_handle_recovers(monkeypatch):
         assert h.loglik(plk.PLK_FP32S) == good
 
 
-def test_withheld_mma_commit_times_out_and_the_handle_recovers(monkeypatch):
-    """Failure path of the tcgen05 20-state form: with the first MMA commit
+@pytest.mark.parametrize("variant", [5, 6])
+def test_withheld_mma_commit_times_out_and_the_handle_recovers(monkeypatch, variant):
+    """Failure path of the tcgen05 20-state forms: with the first MMA commit
     withheld every bounded mbarrier wait runs out, the evaluation reports
     PLK_ERR_NUMERIC (TMEM still freed), and the next evaluation is exact."""
     import time
     rng = np.random.default_rng(78)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 16, 300, S=20, C=4)
-    monkeypatch.setenv("PLK_PRUNE_VARIANT", "5")
+    monkeypatch.setenv("PLK_PRUNE_VARIANT", str(variant))
     with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
         good = h.loglik(plk.PLK_FP32S)
-        assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[20][5]
+        assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[20][variant]
         h.test_withhold_stage()
         t0 = time.perf_counter()
         with pytest.raises(plk.PlkError) as err:
