@@ -73,6 +73,14 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// the same rounding in integer arithmetic (round to nearest, ties away from
+// zero, at TF32's 10-bit mantissa: half of the last kept bit added to the
+// magnitude, the 13 dropped bits cleared); equal to cvt.rna.tf32.f32 for
+// every finite value that does not round past the largest float
+__device__ __forceinline__ float tf32_round_int(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
 __device__ __forceinline__ float tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
@@ -163,14 +171,14 @@ __device__ __forceinline__ void write_operand(unsigned char* area, int t, const 
 #pragma unroll
     for (int g = 0; g < 5; ++g) {
         float4 h, l;
-        h.x = tf32_rna(x[4 * g]);
-        h.y = tf32_rna(x[4 * g + 1]);
-        h.z = tf32_rna(x[4 * g + 2]);
-        h.w = tf32_rna(x[4 * g + 3]);
-        l.x = tf32_rna(x[4 * g] - h.x);
-        l.y = tf32_rna(x[4 * g + 1] - h.y);
-        l.z = tf32_rna(x[4 * g + 2] - h.z);
-        l.w = tf32_rna(x[4 * g + 3] - h.w);
+        h.x = tf32_round_int(x[4 * g]);
+        h.y = tf32_round_int(x[4 * g + 1]);
+        h.z = tf32_round_int(x[4 * g + 2]);
+        h.w = tf32_round_int(x[4 * g + 3]);
+        l.x = tf32_round_int(x[4 * g] - h.x);
+        l.y = tf32_round_int(x[4 * g + 1] - h.y);
+        l.z = tf32_round_int(x[4 * g + 2] - h.z);
+        l.w = tf32_round_int(x[4 * g + 3] - h.w);
         *reinterpret_cast<float4*>(area + g * kAGroup + row) = h;
         *reinterpret_cast<float4*>(area + APART + g * kAGroup + row) = l;
     }
@@ -188,6 +196,33 @@ __device__ __forceinline__ void issue_child(uint32_t d_tmem, uint32_t a_addr, ui
         const uint64_t b_lo = smem_desc(b_addr + kBPart + ks * 2 * kBGroup, kBGroup, 128);
         umma_tf32(d_tmem, a_lo, b_hi, ks > 0 ? 1u : 0u);  // small products first
         umma_tf32(d_tmem, a_hi, b_lo, 1u);
+        umma_tf32(d_tmem, a_hi, b_hi, 1u);
+    }
+}
+
+// The same nine MMAs from precomputed descriptor low words: a descriptor's
+// high word (SBO 128 B, version bit) is the same for every operand here, and
+// its low word is (address >> 4) | (LBO >> 4) << 16, so an operand at base +
+// off has the low word of base plus off >> 4 (shared-memory addresses stay
+// below 2^18: no carry into the LBO field).
+constexpr uint32_t kDescHi = (128u >> 4) | (1u << 14);
+
+__device__ __forceinline__ uint32_t desc_lo(uint32_t addr, uint32_t lbo) {
+    return ((addr >> 4) & 0x3FFFu) | (((lbo >> 4) & 0x3FFFu) << 16);
+}
+
+__device__ __forceinline__ uint64_t desc_of(uint32_t lo) { return ((uint64_t)kDescHi << 32) | lo; }
+
+template <int APART>
+__device__ __forceinline__ void issue_child_lo(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo) {
+#pragma unroll
+    for (int ks = 0; ks < 3; ++ks) {
+        const uint64_t a_hi = desc_of(a_lo + ks * 2 * kAGroup / 16);
+        const uint64_t a_l = desc_of(a_lo + (APART + ks * 2 * kAGroup) / 16);
+        const uint64_t b_hi = desc_of(b_lo + ks * 2 * kBGroup / 16);
+        const uint64_t b_l = desc_of(b_lo + (kBPart + ks * 2 * kBGroup) / 16);
+        umma_tf32(d_tmem, a_l, b_hi, ks > 0 ? 1u : 0u);  // small products first
+        umma_tf32(d_tmem, a_hi, b_l, 1u);
         umma_tf32(d_tmem, a_hi, b_hi, 1u);
     }
 }
@@ -245,12 +280,52 @@ __device__ __forceinline__ void stage_op20u(unsigned char* dst, const Op& op, in
     }
 }
 
+// the same with the table's code stride NCS known at compile time (NCS = 0:
+// read it from n_codes)
+template <int NCS>
+__device__ __forceinline__ void tip_row_n(const unsigned char* stage_child, int code, int n_codes, float m[kS]) {
+    code = code < n_codes ? code : 0;
+    const int ncs = NCS > 0 ? NCS : codes_padded(n_codes);
+    const float* col = reinterpret_cast<const float*>(stage_child) + code;
+#pragma unroll
+    for (int i = 0; i < kS; ++i) m[i] = col[i * ncs];
+}
+
 __device__ __forceinline__ void tip_row(const unsigned char* stage_child, int code, int n_codes, float m[kS]) {
     code = code < n_codes ? code : 0;
     const int ncs = codes_padded(n_codes);
     const float* col = reinterpret_cast<const float*>(stage_child) + code;
 #pragma unroll
     for (int i = 0; i < kS; ++i) m[i] = col[i * ncs];
+}
+
+// issued by one thread: an op's children (B images or tip tables) into a
+// stage slot as 1-D bulk copies, completing in bytes on the slot's mbarrier
+__device__ __forceinline__ void bulk_stage20(unsigned char* dst, const Op& op, int k, const P20UArgs& g,
+                                             uint32_t full) {
+    const PruneArgs& a = g.a;
+    const uint32_t tip_bytes = kS * codes_padded(a.n_codes) * 4, b_bytes = kBFloats * 4;
+    uint32_t total = op.s0 >= 0 ? tip_bytes : b_bytes;
+    if (op.s1 != kSrcNone) total += op.s1 >= 0 ? tip_bytes : b_bytes;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full), "r"(total) : "memory");
+    for (int c = 0; c < 2; ++c) {
+        const int src = c ? op.s1 : op.s0;
+        if (src == kSrcNone) continue;
+        const float* from;
+        uint32_t bytes;
+        if (src >= 0) {
+            bytes = tip_bytes;
+            from = g.Ts + ((size_t)src * a.C + k) * (size_t)(tip_bytes / 4);
+        } else {
+            bytes = b_bytes;
+            from = g.Ps + ((size_t)(c ? op.e1 : op.e0) * a.C + k) * (size_t)kBFloats;
+        }
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                smem_u32(dst + c * g.child_bytes)),
+            "l"(from), "r"(bytes), "r"(full)
+            : "memory");
+    }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
@@ -400,14 +475,18 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
 // tiles x categories of such chains):
 //   * A operands without their zero column group (20 KB instead of 24 KB,
 //     one zero group after the last operand);
-//   * a two-slot stage ring, one op ahead (24 KB instead of 36 KB);
+//   * a two-slot stage ring, one op ahead (24 KB instead of 36 KB), fed by
+//     1-D bulk copies that one thread issues (completion counted in bytes
+//     on the slot's mbarrier) instead of every thread's cp.async;
 //   * spilled vectors in global memory (an L2-resident scratch written at a
 //     push and read back one op before the pop, by the thread that wrote
 //     them), so that TMEM holds only the two accumulators (64 columns);
 //   * tip codes read from global memory one op ahead instead of staged.
+template <int NCS>
 __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ __align__(8) uint64_t s_full[2];  // stage slots: bulk copies landed
     __shared__ uint32_t s_tmem;
     __shared__ float s_rw[kS];
     __shared__ int s_abort;
@@ -421,6 +500,7 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     unsigned char* stages = smem + 2 * kAOperand5 + kAGroup;  // after the zero group
     Op* s_ops = reinterpret_cast<Op*>(stages + 2 * 2 * cb);
     const uint32_t mbar = smem_u32(&s_mbar);
+    const uint32_t full0 = smem_u32(&s_full[0]);  // slot j's barrier: full0 + 8 j
     const int site = tile0 + tid;
     const bool has_code = site < a.site_stride;
     float* spill = g.spill + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * (size_t)(a.max_depth > 1 ? a.max_depth : 1) *
@@ -434,6 +514,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full0 + 8) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         s_abort = 0;
     }
@@ -448,8 +530,9 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     tc_fence_after();
     const uint32_t tmem = s_tmem;
     const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
-    stage_op20u(stages, s_ops[0], k, g);
-    cp_async_commit();
+    if (tid == 0) bulk_stage20(stages, s_ops[0], k, g, full0);
+    const uint32_t acc_lo = desc_lo(smem_u32(acc_op), kAGroup), pop_lo = desc_lo(smem_u32(pop_op), kAGroup);
+    const uint32_t stage_lo = desc_lo(smem_u32(stages), kBGroup);  // slot j, child c: + (2 j + c) cb / 16
 
     auto code_of = [&](int src) -> int {
         return (src >= 0 && has_code) ? (int)__ldg(a.codes + (size_t)src * a.site_stride + site) : 0;
@@ -460,8 +543,12 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     uint32_t phase = 0;
     bool pending = false;   // an MMA commit whose completion was not observed
     bool withheld = false;  // the failure-path test withholds the first commit
+    int lost = -1;  // the op whose stage wait ran out: its copy may still land
     for (int o = 0; o < a.n_ops; ++o) {
-        cp_async_wait<0>();
+        if (!mbar_wait(full0 + 8 * (o & 1), (uint32_t)(o >> 1) & 1u)) {
+            lost = o;
+            s_abort = 1;
+        }
         const Op op = s_ops[o];
         const bool has_next = o + 1 < a.n_ops;
         int n0 = 0, n1 = 0;
@@ -476,12 +563,13 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
             --sp;
             write_operand<kAPart5>(pop_op, tid, pre);
         }
-        fence_proxy_async();  // cp.async data and operand rows -> the tensor cores
+        fence_proxy_async();  // operand rows written by the threads -> the tensor cores
         tc_fence_before();
         __syncthreads();
         if (s_abort) break;
-        if (has_next) stage_op20u(stages + ((o + 1) & 1) * 2 * cb, s_ops[o + 1], k, g);
-        cp_async_commit();
+        // the slot op o-1 used: its MMAs completed and its tip rows were read
+        // before the barrier
+        if (tid == 0 && has_next) bulk_stage20(stages + ((o + 1) & 1) * 2 * cb, s_ops[o + 1], k, g, full0 + 8 * ((o + 1) & 1));
         // the vector the next op pops (this op does not push when the next pops)
         if (next_pops) {
 #pragma unroll
@@ -491,13 +579,14 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         const bool mma0 = op.s0 < 0, mma1 = op.s1 == kSrcAcc;
         if (tid == 0 && (mma0 || mma1)) {
             tc_fence_after();
-            if (mma0) issue_child<kAPart5>(tmem, smem_u32(op.s0 == kSrcPop ? pop_op : acc_op), smem_u32(st));
-            if (mma1) issue_child<kAPart5>(tmem + 32, smem_u32(acc_op), smem_u32(st + cb));
+            const uint32_t b0 = stage_lo + (uint32_t)((o & 1) * 2 * cb) / 16;
+            if (mma0) issue_child_lo<kAPart5>(tmem, op.s0 == kSrcPop ? pop_lo : acc_lo, b0);
+            if (mma1) issue_child_lo<kAPart5>(tmem + 32, acc_lo, b0 + (uint32_t)cb / 16);
             if (!(a.withhold_first_stage && !withheld)) umma_commit(mbar);
         }
         if ((mma0 || mma1) && a.withhold_first_stage) withheld = true;
-        if (op.s0 >= 0) tip_row(st, c0, a.n_codes, m0);
-        if (op.s1 >= 0) tip_row(st + cb, c1, a.n_codes, m1);
+        if (op.s0 >= 0) tip_row_n<NCS>(st, c0, a.n_codes, m0);
+        if (op.s1 >= 0) tip_row_n<NCS>(st + cb, c1, a.n_codes, m1);
         if (mma0 || mma1) {
             pending = true;
             if (!mbar_wait(mbar, phase)) s_abort = 1;
@@ -511,9 +600,15 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
 #pragma unroll
             for (int i = 0; i < kS; ++i) m0[i] *= m1[i];
         }
-        float mx = 0.0f;
+        float mx;
+        {  // a tree of maxima instead of a chain of twenty
+            float t[10];
 #pragma unroll
-        for (int i = 0; i < kS; ++i) mx = fmaxf(mx, m0[i]);
+            for (int i = 0; i < 10; ++i) t[i] = fmaxf(m0[i], m0[i + 10]);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) t[i] = fmaxf(t[i], t[i + 5]);
+            mx = fmaxf(fmaxf(fmaxf(t[0], t[1]), fmaxf(t[2], t[3])), t[4]);
+        }
         if (mx < scale_threshold<float>() && mx > 0.0f) {
             int e;
             float f1, f2;
@@ -533,7 +628,9 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         c0 = n0;
         c1 = n1;
     }
-    cp_async_wait<0>();
+    // every issued stage was waited for, unless a wait ran out: give that
+    // copy one more bounded wait before the shared memory is given up
+    if (lost >= 0) mbar_wait(full0 + 8 * (lost & 1), (uint32_t)(lost >> 1) & 1u);
     // a commit still in flight after a timed-out wait (none when it was withheld)
     if (pending && !a.withhold_first_stage) mbar_wait(mbar, phase ^ 1u);
     tc_fence_before();
@@ -623,7 +720,11 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    void (*kern)(P20UArgs) = form == 1 ? prune20v_kernel : prune20u_kernel;
+    void (*kern)(P20UArgs) = prune20u_kernel;
+    if (form == 1) {
+        const int ncs = codes_padded(a.n_codes);
+        kern = ncs == 20 ? prune20v_kernel<20> : ncs == 24 ? prune20v_kernel<24> : prune20v_kernel<0>;
+    }
     // pad the shared memory until no more CTAs fit on an SM than its TMEM serves
     const int max_ctas = 512 / g.tmem_cols;
     size_t smem = smem20u_bytes(a, form);
