@@ -415,7 +415,7 @@ bool tuned_paired(const plk_handle* h) {
         auto hit = h->tune_cache.find(key);
         if (hit != h->tune_cache.end()) v = hit->second;
     }
-    return v >= 3 && v <= 9;
+    return v >= 3 && v <= 11;
 }
 
 // Runs the post-order pass (P(t) already built); store != null asks for the
@@ -486,6 +486,8 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
                 cands.push_back(8);
             }
             if (prune4p_fits(a, 1, 0)) cands.push_back(9);  // TMA-fed stage ring
+            for (int v = 10; v <= 11; ++v)  // codes staged with each op
+                if (prune4p_fits(a, v - 9)) cands.push_back(v);
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }

@@ -206,7 +206,9 @@ struct PruneArgs {
     // prune4p_kernel (category pairs on FP32x2) with 1/2 sites per thread,
     // 5/6 = the same reading the tip codes from global memory, 7/8 =
     // prune4p_kernel with two threads per site (codes from global memory /
-    // staged in shared memory).
+    // staged in shared memory), 9 = prune4p_bulk_kernel (TMA-fed stage ring),
+    // 10/11 = prune4p_kernel with 1/2 sites per thread and each op's tip
+    // codes staged with its tables.
     // 20 states: 0 = prune_generic_kernel, 1 / 2 = prune20_kernel on CUDA
     // cores / mma.sync tensor cores (TF32, three-product split) with 4 warps
     // per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel on
@@ -255,8 +257,11 @@ bool prune4p_fits(const PruneArgs& a, int spt, int tps = 1);
 // Where the paired P(t) and tip layouts sit in prune4p's scratch.
 void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float** Tp);
 size_t prune4p_scratch_bytes(const PruneArgs& a);
-cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int tps, int* n_blocks,
-                           cudaStream_t st);
+// codes: 0 = the tile's tip codes staged in shared memory (global memory when
+// they do not fit), 1 = read from global memory at their use, 2 = each op's
+// codes staged with its tables (tps 1).  tps: threads per site, 0 = the
+// TMA-fed form.
+cudaError_t launch_prune4p(const PruneArgs& a, int spt, int codes, int tps, int* n_blocks, cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
 bool prune4s_fits(const PruneArgs& a, int spt);
 cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);

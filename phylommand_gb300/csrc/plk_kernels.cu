@@ -551,11 +551,13 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
     if (!fp64 && !store && S == 4 && a.C <= 8 && (a.variant == 1 || a.variant == 2) && prune4s_fits(a, a.variant))
         return launch_prune4s(a, a.variant, n_blocks, st);
     if (!fp64 && !store && S == 4 && a.variant >= 3 && a.variant <= 6 && prune4p_fits(a, (a.variant + 1) % 2 + 1))
-        return launch_prune4p(a, (a.variant + 1) % 2 + 1, a.variant >= 5, 1, n_blocks, st);
+        return launch_prune4p(a, (a.variant + 1) % 2 + 1, a.variant >= 5 ? 1 : 0, 1, n_blocks, st);
     if (!fp64 && !store && S == 4 && (a.variant == 7 || a.variant == 8) && prune4p_fits(a, 1, 2))
-        return launch_prune4p(a, 1, a.variant == 7, 2, n_blocks, st);
+        return launch_prune4p(a, 1, a.variant == 7 ? 1 : 0, 2, n_blocks, st);
     if (!fp64 && !store && S == 4 && a.variant == 9 && prune4p_fits(a, 1, 0))
-        return launch_prune4p(a, 1, true, 0, n_blocks, st);
+        return launch_prune4p(a, 1, 1, 0, n_blocks, st);
+    if (!fp64 && !store && S == 4 && (a.variant == 10 || a.variant == 11) && prune4p_fits(a, a.variant - 9))
+        return launch_prune4p(a, a.variant - 9, 2, 1, n_blocks, st);
     if (!fp64 && !store && S == 20 && (a.variant == 5 || a.variant == 6) && prune20u_fits(a, a.variant - 5))
         return launch_prune20u(a, a.n_nodes, a.scratch, a.variant - 5, n_blocks, st);
     if (!fp64 && !store && S == 20 && a.variant > 0 && a.variant < 5 && prune20_fits(a, a.variant))

@@ -41,7 +41,7 @@ __global__ void relayout4p_kernel(const float* __restrict__ P, const float* __re
     }
 }
 
-template <int KP, int SPT, bool CODES_SMEM, int TPS>
+template <int KP, int SPT, int CODES, int TPS>
 __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, const float* __restrict__ Pp,
                                                                 const float* __restrict__ Tp) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, con
     j.site_lnl = a.site_lnl;
     j.max_depth = a.max_depth;
     SiteSum32 sum;
-    run_tile4p<KP, SPT, CODES_SMEM, TPS>(j, sm, sum);
+    run_tile4p<KP, SPT, CODES, TPS>(j, sm, sum);
     double tsum, tcomp;
     block_sum_site32(sum, tsum, tcomp);
     if (threadIdx.x == 0) {
@@ -127,11 +127,11 @@ cudaError_t launch4p_bulk(const PruneArgs& a, const float* Pp, const float* Tp, 
     return cudaGetLastError();
 }
 
-template <int KP, int SPT, bool CODES_SMEM, int TPS>
+template <int KP, int SPT, int CODES, int TPS>
 cudaError_t launch4p(const PruneArgs& a, const float* Pp, const float* Tp, int* n_blocks, cudaStream_t st) {
-    const size_t smem = tile4p_smem_bytes<KP, SPT, CODES_SMEM, TPS>(a.n_ops, a.n_tips, a.max_depth);
+    const size_t smem = tile4p_smem_bytes<KP, SPT, CODES, TPS>(a.n_ops, a.n_tips, a.max_depth);
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    auto kern = prune4p_kernel<KP, SPT, CODES_SMEM, TPS>;
+    auto kern = prune4p_kernel<KP, SPT, CODES, TPS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     constexpr int TILE = tile4p_sites<SPT, TPS>();
@@ -141,14 +141,19 @@ cudaError_t launch4p(const PruneArgs& a, const float* Pp, const float* Tp, int* 
     return cudaGetLastError();
 }
 
-// codes_global: read the tip codes from global memory (cached) instead of
-// staging the tile's codes in shared memory, for more resident CTAs
+// codes: 0 = stage the tile's codes of every tip in shared memory (global
+// memory when they do not fit), 1 = read them from global memory at their use
+// (more resident CTAs), 2 = stage each op's codes with its tables (one site
+// per thread)
 template <int KP, int SPT, int TPS>
-cudaError_t launch4p_kp(const PruneArgs& a, const float* Pp, const float* Tp, bool codes_global, int* n_blocks,
+cudaError_t launch4p_kp(const PruneArgs& a, const float* Pp, const float* Tp, int codes, int* n_blocks,
                         cudaStream_t st) {
-    if (!codes_global && tile4p_smem_bytes<KP, SPT, true, TPS>(a.n_ops, a.n_tips, a.max_depth) <= 160 * 1024)
-        return launch4p<KP, SPT, true, TPS>(a, Pp, Tp, n_blocks, st);
-    return launch4p<KP, SPT, false, TPS>(a, Pp, Tp, n_blocks, st);
+    if constexpr (TPS == 1) {
+        if (codes == 2) return launch4p<KP, SPT, 2, TPS>(a, Pp, Tp, n_blocks, st);
+    }
+    if (codes == 0 && tile4p_smem_bytes<KP, SPT, 1, TPS>(a.n_ops, a.n_tips, a.max_depth) <= 160 * 1024)
+        return launch4p<KP, SPT, 1, TPS>(a, Pp, Tp, n_blocks, st);
+    return launch4p<KP, SPT, 0, TPS>(a, Pp, Tp, n_blocks, st);
 }
 
 }  // namespace
@@ -164,8 +169,8 @@ bool prune4p_fits(const PruneArgs& a, int spt, int tps) {
     }
     if (tps == 2) {
         if (spt != 1 || a.C == 2) return false;
-        const size_t smem = a.C == 4 ? tile4p_smem_bytes<2, 1, false, 2>(a.n_ops, a.n_tips, a.max_depth)
-                                     : tile4p_smem_bytes<4, 1, false, 2>(a.n_ops, a.n_tips, a.max_depth);
+        const size_t smem = a.C == 4 ? tile4p_smem_bytes<2, 1, 0, 2>(a.n_ops, a.n_tips, a.max_depth)
+                                     : tile4p_smem_bytes<4, 1, 0, 2>(a.n_ops, a.n_tips, a.max_depth);
         return smem <= 227 * 1024;
     }
     if (tps != 1 || (spt != 1 && spt != 2)) return false;
@@ -183,8 +188,7 @@ void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float*
     *Tp = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + ((p + 255) & ~(size_t)255));
 }
 
-cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int tps, int* n_blocks,
-                           cudaStream_t st) {
+cudaError_t launch_prune4p(const PruneArgs& a, int spt, int codes, int tps, int* n_blocks, cudaStream_t st) {
     // tps 0: the TMA-fed form (one site per thread, codes from global)
     if (!prune4p_fits(a, spt, tps) || a.scratch == nullptr) return cudaErrorInvalidValue;
     float *Pp, *Tp;
@@ -200,8 +204,8 @@ cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int t
         if (e != cudaSuccess) return e;
     }
     if (tps == 2) {
-        return a.C == 4 ? launch4p_kp<2, 1, 2>(a, Pp, Tp, codes_global, n_blocks, st)
-                        : launch4p_kp<4, 1, 2>(a, Pp, Tp, codes_global, n_blocks, st);
+        return a.C == 4 ? launch4p_kp<2, 1, 2>(a, Pp, Tp, codes, n_blocks, st)
+                        : launch4p_kp<4, 1, 2>(a, Pp, Tp, codes, n_blocks, st);
     }
     if (tps == 0) {
         switch (a.C / 2) {
@@ -211,12 +215,12 @@ cudaError_t launch_prune4p(const PruneArgs& a, int spt, bool codes_global, int t
         }
     }
     switch (a.C / 2) {
-        case 1: return spt == 1 ? launch4p_kp<1, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
-                                : launch4p_kp<1, 2, 1>(a, Pp, Tp, codes_global, n_blocks, st);
-        case 2: return spt == 1 ? launch4p_kp<2, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
-                                : launch4p_kp<2, 2, 1>(a, Pp, Tp, codes_global, n_blocks, st);
-        default: return spt == 1 ? launch4p_kp<4, 1, 1>(a, Pp, Tp, codes_global, n_blocks, st)
-                                 : launch4p_kp<4, 2, 1>(a, Pp, Tp, codes_global, n_blocks, st);
+        case 1: return spt == 1 ? launch4p_kp<1, 1, 1>(a, Pp, Tp, codes, n_blocks, st)
+                                : launch4p_kp<1, 2, 1>(a, Pp, Tp, codes, n_blocks, st);
+        case 2: return spt == 1 ? launch4p_kp<2, 1, 1>(a, Pp, Tp, codes, n_blocks, st)
+                                : launch4p_kp<2, 2, 1>(a, Pp, Tp, codes, n_blocks, st);
+        default: return spt == 1 ? launch4p_kp<4, 1, 1>(a, Pp, Tp, codes, n_blocks, st)
+                                 : launch4p_kp<4, 2, 1>(a, Pp, Tp, codes, n_blocks, st);
     }
 }
 

@@ -62,25 +62,37 @@ struct alignas(16) StageP {
 template <int SPT, int TPS>
 __host__ __device__ constexpr int tile4p_sites() { return kPruneThreads * SPT / TPS; }
 
-// Shared memory: three stage slots | ops | tip codes (optional) | spill stack.
-template <int KP, int SPT, bool CODES_SMEM, int TPS = 1>
+// Where the tip codes come from (CODES): 0 = global memory at their use, 1 =
+// the tile's codes of every tip staged in shared memory at the start, 2 = an
+// op's codes staged with its tables, two ops ahead, in a ring beside the stage
+// slots (2 x TILE bytes per slot).
+// Shared memory: three stage slots | ops | tip codes (CODES 1) or the code
+// ring (CODES 2) | spill stack.  With CODES 2 and one site per thread the
+// ops are read from global memory (L1-cached, the same address in every lane)
+// instead of staged, which keeps the ring within the shared memory of the
+// other one-site forms (six CTAs per SM on 128 x 100,000; 768 bytes more cost
+// one of them); with two sites per thread the ops stay staged (the op loads
+// would sit on the critical path of fewer warps).
+template <int KP, int SPT, int CODES, int TPS = 1>
 __host__ __device__ inline size_t tile4p_smem_bytes(int n_ops, int n_tips, int max_depth) {
     constexpr int TILE = tile4p_sites<SPT, TPS>();
     const size_t depth = (size_t)(max_depth > 0 ? max_depth : 1);
-    size_t s = 3 * sizeof(StageP<KP>) + align16((size_t)n_ops * sizeof(Op));
-    if (CODES_SMEM) s += align16((size_t)n_tips * TILE);
+    constexpr bool ops_global = CODES == 2 && SPT == 1;
+    size_t s = 3 * sizeof(StageP<KP>) + (ops_global ? 0 : align16((size_t)n_ops * sizeof(Op)));
+    if (CODES == 1) s += align16((size_t)n_tips * TILE);
+    if (CODES == 2) s += 3 * 2 * TILE;
     s += depth * SPT * (KP / TPS) * 4 * sizeof(u64) * kPruneThreads;
     return s;
 }
 
 inline size_t tile4p_smem_min(int C, int spt, int n_ops, int n_tips, int max_depth) {
     switch (C) {
-        case 2: return spt == 1 ? tile4p_smem_bytes<1, 1, false>(n_ops, n_tips, max_depth)
-                                : tile4p_smem_bytes<1, 2, false>(n_ops, n_tips, max_depth);
-        case 4: return spt == 1 ? tile4p_smem_bytes<2, 1, false>(n_ops, n_tips, max_depth)
-                                : tile4p_smem_bytes<2, 2, false>(n_ops, n_tips, max_depth);
-        case 8: return spt == 1 ? tile4p_smem_bytes<4, 1, false>(n_ops, n_tips, max_depth)
-                                : tile4p_smem_bytes<4, 2, false>(n_ops, n_tips, max_depth);
+        case 2: return spt == 1 ? tile4p_smem_bytes<1, 1, 0>(n_ops, n_tips, max_depth)
+                                : tile4p_smem_bytes<1, 2, 0>(n_ops, n_tips, max_depth);
+        case 4: return spt == 1 ? tile4p_smem_bytes<2, 1, 0>(n_ops, n_tips, max_depth)
+                                : tile4p_smem_bytes<2, 2, 0>(n_ops, n_tips, max_depth);
+        case 8: return spt == 1 ? tile4p_smem_bytes<4, 1, 0>(n_ops, n_tips, max_depth)
+                                : tile4p_smem_bytes<4, 2, 0>(n_ops, n_tips, max_depth);
         default: return 0;
     }
 }
@@ -102,6 +114,24 @@ __device__ __forceinline__ void stage_op4p(StageP<KP>* st, const Op& op, const f
             cp_async16(reinterpret_cast<float*>(st->p[c]) + 4 * q, Pp + (size_t)e * KP * 32 + 4 * q);
         }
     }
+}
+
+// the op's tip codes of the tile's sites into a ring slot (CODES 2), issued
+// by the last 2 TILE / 16 threads of the CTA as 16-byte cp.async; a chunk
+// past the end of the code rows reads the rows' last chunk instead (those
+// sites are beyond n_sites and never summed)
+template <int TILE>
+__device__ __forceinline__ void stage_codes4p(uint8_t* dst, const Op& op, const uint8_t* __restrict__ codes,
+                                              int site_stride, int tile_base) {
+    constexpr int CH = TILE / 16;
+    static_assert(2 * CH <= kPruneThreads, "one chunk per thread");
+    const int t = (int)threadIdx.x - (kPruneThreads - 2 * CH);
+    if (t < 0) return;
+    const int c = t / CH, q = t % CH;
+    const int src = c ? op.s1 : op.s0;
+    if (src < 0) return;
+    const int col = min(tile_base + 16 * q, site_stride - 16);
+    cp_async16(dst + c * TILE + 16 * q, codes + (size_t)src * site_stride + col);
 }
 
 // out[q][i] = sum_j P[q][j][i] x[q][j] for both categories of every pair,
@@ -148,7 +178,7 @@ __device__ __forceinline__ void tip4p(const u64 (*T)[2][kCodes][2], int code, u6
 // category order with its partner's category sums, so the per-site results
 // are the bits of TPS = 1.  Ends with no cp.async in flight; the caller must
 // __syncthreads() before reusing the shared memory.
-template <int KP, int SPT, bool CODES_SMEM, int TPS = 1>
+template <int KP, int SPT, int CODES, int TPS = 1>
 __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) {
     static_assert(TPS == 1 || (TPS == 2 && SPT == 1 && KP % 2 == 0), "two threads per site split the pairs");
     constexpr int TILE = tile4p_sites<SPT, TPS>();
@@ -156,9 +186,12 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     StageP<KP>* stages = reinterpret_cast<StageP<KP>*>(sm);
     size_t off = 3 * sizeof(StageP<KP>);
     Op* s_ops = reinterpret_cast<Op*>(sm + off);
-    off += align16((size_t)j.n_ops * sizeof(Op));
+    constexpr bool ops_global = CODES == 2 && SPT == 1;
+    if (!ops_global) off += align16((size_t)j.n_ops * sizeof(Op));
+    const Op* __restrict__ ops = ops_global ? j.ops : s_ops;
     uint8_t* s_codes = sm + off;
-    if (CODES_SMEM) off += align16((size_t)j.n_tips * TILE);
+    if (CODES == 1) off += align16((size_t)j.n_tips * TILE);
+    if (CODES == 2) off += 3 * 2 * TILE;
     ulonglong2* s_stack = reinterpret_cast<ulonglong2*>(sm + off);
     const float* __restrict__ Pp = j.P;
     const float* __restrict__ Tp = j.tipT;
@@ -166,8 +199,9 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     const int tid = threadIdx.x;
     const int half = TPS == 2 ? (tid & 1) : 0;   // which half of the pairs
     const int q0 = half * KPT;                    // first pair of this thread
-    for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
-    if (CODES_SMEM) {
+    if (!ops_global)
+        for (int i = tid; i < j.n_ops; i += kPruneThreads) s_ops[i] = j.ops[i];
+    if (CODES == 1) {
         constexpr int chunks = TILE / 16;
         for (int i = tid; i < j.n_tips * chunks; i += kPruneThreads) {
             const int t = i / chunks, q = i % chunks, col = j.tile_base + 16 * q;
@@ -177,9 +211,13 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
         }
     }
     __syncthreads();
-    stage_op4p<KP>(&stages[0], s_ops[0], Pp, Tp);
+    stage_op4p<KP>(&stages[0], ops[0], Pp, Tp);
+    if (CODES == 2) stage_codes4p<TILE>(s_codes, ops[0], j.codes, j.site_stride, j.tile_base);
     cp_async_commit();
-    if (j.n_ops > 1) stage_op4p<KP>(&stages[1], s_ops[1], Pp, Tp);
+    if (j.n_ops > 1) {
+        stage_op4p<KP>(&stages[1], ops[1], Pp, Tp);
+        if (CODES == 2) stage_codes4p<TILE>(s_codes + 2 * TILE, ops[1], j.codes, j.site_stride, j.tile_base);
+    }
     cp_async_commit();
 
     u64 acc[SPT][KPT][4];
@@ -201,10 +239,17 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     for (int o = 0; o < j.n_ops; ++o) {
         cp_async_wait<1>();
         __syncthreads();
-        if (o + 2 < j.n_ops) stage_op4p<KP>(&stages[(o + 2) % 3], s_ops[o + 2], Pp, Tp);
+        if (o + 2 < j.n_ops) {
+            const Op nx = ops[o + 2];
+            stage_op4p<KP>(&stages[(o + 2) % 3], nx, Pp, Tp);
+            if (CODES == 2)
+                stage_codes4p<TILE>(s_codes + ((o + 2) % 3) * 2 * TILE, nx, j.codes, j.site_stride,
+                                    j.tile_base);
+        }
         cp_async_commit();
-        const Op op = s_ops[o];
+        const Op op = ops[o];
         const StageP<KP>& stg = stages[o % 3];
+        const uint8_t* ring = s_codes + (o % 3) * 2 * TILE;  // CODES 2: this op's codes
         if (op.s0 == kSrcPop) --sp;
 #pragma unroll
         for (int s = 0; s < SPT; ++s) {
@@ -212,7 +257,8 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
             u64 d0[KPT][4], d1[KPT][4];
             if (op.s0 >= 0) {
                 int code;
-                if (CODES_SMEM) code = s_codes[(size_t)op.s0 * TILE + lsite];
+                if (CODES == 1) code = s_codes[(size_t)op.s0 * TILE + lsite];
+                else if (CODES == 2) code = ring[lsite];
                 else code = j.codes[(size_t)op.s0 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
                 tip4p<KPT>(stg.tip[0] + q0, code & (kCodes - 1), d0);
             } else if (op.s0 == kSrcPop) {
@@ -231,7 +277,8 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
             }
             if (op.s1 >= 0) {
                 int code;
-                if (CODES_SMEM) code = s_codes[(size_t)op.s1 * TILE + lsite];
+                if (CODES == 1) code = s_codes[(size_t)op.s1 * TILE + lsite];
+                else if (CODES == 2) code = ring[TILE + lsite];
                 else code = j.codes[(size_t)op.s1 * j.site_stride + min(j.tile_base + lsite, j.site_stride - 1)];
                 tip4p<KPT>(stg.tip[1] + q0, code & (kCodes - 1), d1);
             } else if (op.s1 == kSrcAcc) {

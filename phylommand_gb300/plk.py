@@ -407,7 +407,9 @@ class Handle:
             6: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes from global)",
             7: "prune4p_kernel (category pairs on FP32x2, 2 threads/site, tip codes from global)",
             8: "prune4p_kernel (category pairs on FP32x2, 2 threads/site)",
-            9: "prune4p_bulk_kernel (category pairs on FP32x2, TMA bulk-copy stage ring, mbarrier pipeline)"},
+            9: "prune4p_bulk_kernel (category pairs on FP32x2, TMA bulk-copy stage ring, mbarrier pipeline)",
+            10: "prune4p_kernel (category pairs on FP32x2, 1 site/thread, tip codes staged with each op)",
+            11: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes staged with each op)"},
         20: {1: "prune20_kernel (CUDA cores, 4 warps/tile)", 2: "prune20_kernel (tensor cores, split TF32, 4 warps/tile)",
              3: "prune20_kernel (CUDA cores, 8 warps/tile)", 4: "prune20_kernel (tensor cores, split TF32, 8 warps/tile)",
              5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)",

@@ -237,14 +237,15 @@ def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
     and 2 sites per thread, prune4p_kernel with category pairs on FP32x2 where
     C is 2, 4 or 8 -- one or two sites per thread, or two threads per site
     for 4 and 8 categories; tip codes in shared memory or read from global
-    for the 1300-tip tree) gives the same per-site values."""
+    for the 1300-tip tree, or staged with each op's tables) gives the same
+    per-site values."""
     rng = np.random.default_rng(n_tips + n_sites)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, C=C)
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
     sites = []
-    variants = {1: ("0", "1", "2"), 2: ("0", "1", "2", "3", "4", "5", "6", "9")}.get(
-        C, ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9"))
+    variants = {1: ("0", "1", "2"), 2: ("0", "1", "2", "3", "4", "5", "6", "9", "10", "11")}.get(
+        C, ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9", "10", "11"))
     for v in variants:
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
