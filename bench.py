@@ -29,6 +29,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "cfg2"
+ORACLE_CELLS = 20_000_000  # tip cells up to which the DNA bench runs the FP64 oracle on the full workload
 SEED = 2
 FALLBACK_HBM_GBS = 6800.0
 FALLBACK_BF16_TFLOPS = 1900.0
@@ -164,7 +165,7 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     from phylommand_gb300 import synth
-    w = synth.make(WORKLOAD, seed=SEED)
+    w = synth.make(WORKLOAD, seed=SEED, n_sites=args.sites, n_tips=args.taxa)
     threads = os.cpu_count() or 1
     sample = max(threads * 40, 256)
     for _ in range(args.warmup):
@@ -188,7 +189,7 @@ def run_reference(args, world, rank):
 
 
 def workload_config(w):
-    return {"workload": "DNA GTR+Gamma4, 128-taxon Yule tree, 100,000 sites, 2% missing cells",
+    return {"workload": f"DNA GTR+Gamma4, {w.n_tips}-taxon Yule tree, {w.n_sites:,} sites, 2% missing cells",
             "n_taxa": w.n_tips, "n_sites": w.n_sites, "n_states": w.n_states, "n_categories": len(w.cat_rates),
             "alpha": w.alpha, "branch_lengths": "Exp(mean 0.05)", "seed": w.seed,
             "p_matrix": "FP64 eigen form", "partials": "FP32, per-site power-of-two scaling",
@@ -200,7 +201,7 @@ def run_ours(args, world, rank, local):
     from phylommand_gb300 import plk, synth
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = synth.make(WORKLOAD, seed=SEED)
+    w = synth.make(WORKLOAD, seed=SEED, n_sites=args.sites, n_tips=args.taxa)
     h = plk.Handle(local)
     h.set_alignment(w.masks, w.n_states)
     h.set_tree(w.left, w.right, w.bl)
@@ -335,11 +336,22 @@ def run_ours(args, world, rank, local):
     cpu_s = cpu_port_seconds(w, sample, 1)
     cpu_value = 1.0 / (cpu_s * w.n_sites / sample)
 
-    # error of the timed FP32 result against the FP64 oracle
-    from oracle import oracle as O
-    teff = plk.effective_lengths(w.left, w.right, w.bl, False)
-    orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights, p_mode=O.P_EXACT,
-                   threads=os.cpu_count() or 1)
+    # error of the timed FP32 result against the FP64 oracle (above
+    # ORACLE_CELLS tip cells the oracle would take minutes: against the FP64
+    # engine, which the tests hold to the oracle within 1e-11)
+    if w.n_tips * w.n_sites <= ORACLE_CELLS:
+        from oracle import oracle as O
+        teff = plk.effective_lengths(w.left, w.right, w.bl, False)
+        ref_lnl = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights,
+                           p_mode=O.P_EXACT, threads=os.cpu_count() or 1).lnl
+        ref_name = "error_vs_fp64_oracle"
+    else:
+        ref_lnl = lnl64
+        ref_name = "error_vs_fp64_engine"
+    err = {"abs": abs(lnl_timed - ref_lnl), "rel": abs(lnl_timed - ref_lnl) / abs(ref_lnl),
+           "e2e_rel": abs(lnl_e2e - ref_lnl) / abs(ref_lnl)}
+    if ref_name == "error_vs_fp64_oracle":
+        err["fp64_engine_rel"] = abs(lnl64 - ref_lnl) / abs(ref_lnl)
     line = {
         "metric": "lnL evals/s", "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -371,9 +383,7 @@ def run_ours(args, world, rank, local):
         # tuned prune4p form) and the post-order pass, whose last CTA adds up
         # the total
         "gpu_launches": 2 * args.steps,
-        "error_vs_fp64_oracle": {"abs": abs(lnl_timed - orc.lnl), "rel": abs(lnl_timed - orc.lnl) / abs(orc.lnl),
-                                 "fp64_engine_rel": abs(lnl64 - orc.lnl) / abs(orc.lnl),
-                                 "e2e_rel": abs(lnl_e2e - orc.lnl) / abs(orc.lnl)},
+        ref_name: err,
         "clocks": clk,
     }
     del lnl32
@@ -581,6 +591,8 @@ def main():
     ap.add_argument("--workload", default="dna", choices=["dna", "nni", "protein", "warmstart"],
                     help="dna: the headline workload; nni: the uneven batch with NNI neighbours; protein: 20 "
                          "states; warmstart: time-to-ML-fit with the learned start")
+    ap.add_argument("--taxa", type=int, default=None, help="dna workload: taxa (default 128)")
+    ap.add_argument("--sites", type=int, default=None, help="dna workload: sites (default 100,000)")
     ap.add_argument("--nni-items", type=int, default=512)
     ap.add_argument("--nni-sample", type=int, default=24)
     ap.add_argument("--ws-train", type=int, default=20000)
