@@ -173,7 +173,9 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * same with the categories in pairs on packed FP32x2), 5 / 6 = prune4p_kernel
  * reading the tip codes from global memory, 7 / 8 = prune4p_kernel with two
  * threads per site (each takes half of the category pairs; codes from global
- * memory / staged), 9 = prune4p_bulk_kernel (TMA-fed stage ring).  20
+ * memory / staged), 9 = prune4p_bulk_kernel (TMA-fed stage ring), 10 / 11 =
+ * prune4p_kernel with 1 / 2 sites per thread and each op's tip codes staged
+ * with its tables two ops ahead (the fast forms when the codes exceed L2).  20
  * states: 1 / 2 = prune20_kernel on CUDA cores / mma.sync tensor cores with
  * 4 warps per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel
  * (tcgen05 tensor cores, TMEM accumulators, spill stack in TMEM), 6 =
