@@ -376,27 +376,52 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
     cudaEvent_t e0, e1;
     PLK_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
     PLK_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
+    // two passes over the candidates, each candidate's best pass counts (an
+    // early candidate may run before the clocks and caches settle)
+    std::vector<float> cand_ms(cands.size(), 1e30f);
+    cudaError_t err = cudaSuccess;
+    for (int pass = 0; pass < 2 && err == cudaSuccess; ++pass) {
+        for (size_t i = 0; i < cands.size(); ++i) {
+            const int v = cands[i];
+            if (err != cudaSuccess) break;
+            a.variant = v;
+            int nb = 0;
+            err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
+            if (err != cudaSuccess) break;
+            err = cudaEventRecord(e0, h->stream);
+            for (int r = 0; r < 3 && err == cudaSuccess; ++r)
+                err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
+            if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (err == cudaSuccess) cand_ms[i] = std::min(cand_ms[i], ms);
+        }
+    }
     float best = 1e30f;
     int best_v = cands[0];
-    cudaError_t err = cudaSuccess;
-    for (int v : cands) {
-        if (err != cudaSuccess) break;
-        a.variant = v;
-        int nb = 0;
-        err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
-        if (err != cudaSuccess) break;
-        err = cudaEventRecord(e0, h->stream);
-        for (int r = 0; r < 3 && err == cudaSuccess; ++r) err = launch_prune(a, h->S, PLK_FP32S, false, &nb, h->stream);
-        if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
-        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-        float ms = 0.f;
-        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-        if (v >= 0 && v < 3) h->tune_ms[v] = ms / 3.0f;
-        if (err == cudaSuccess && ms < best) { best = ms; best_v = v; }
+    float best_staged = 1e30f;  // the fastest form that stages each op's tip codes
+    int best_staged_v = -1;
+    for (size_t i = 0; i < cands.size(); ++i) {
+        const int v = cands[i];
+        if (v >= 0 && v < 3) h->tune_ms[v] = cand_ms[i] / 3.0f;
+        if (cand_ms[i] < best) { best = cand_ms[i]; best_v = v; }
+        if (h->S == 4 && (v == 10 || v == 11) && cand_ms[i] < best_staged) {
+            best_staged = cand_ms[i];
+            best_staged_v = v;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (err != cudaSuccess) return cuda_fail(h, err, "autotune post-order kernel");
+    // The timed launches run back to back with the tip codes warm in L2.  A
+    // form that stages each op's codes with its tables does not depend on
+    // that (its codes arrive two ops ahead): within 3 % of the fastest it is
+    // taken, since other work between evaluations (other partitions, other
+    // alignments) evicts the codes that the faster form reads at use.  On
+    // 128 x 100,000 the two are level warm (0.155 ms), and with the codes
+    // evicted the staged form takes 0.148 against 0.159 ms.
+    if (best_staged_v >= 0 && best_staged <= best * 1.03f) best_v = best_staged_v;
     h->variant = best_v;
     h->tune_cache[key] = best_v;
     return PLK_OK;

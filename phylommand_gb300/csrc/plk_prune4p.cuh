@@ -237,17 +237,21 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     // ahead, or before the op's barrier, measured slower for this body on the
     // 128 x 100,000 benchmark)
     for (int o = 0; o < j.n_ops; ++o) {
+        // this op and the one to stage, loaded before the wait and the
+        // barrier so that their latency (L1 when the ops are not staged)
+        // hides behind them
+        const Op op = ops[o];
+        Op nx{};
+        if (o + 2 < j.n_ops) nx = ops[o + 2];
         cp_async_wait<1>();
         __syncthreads();
         if (o + 2 < j.n_ops) {
-            const Op nx = ops[o + 2];
             stage_op4p<KP>(&stages[(o + 2) % 3], nx, Pp, Tp);
             if (CODES == 2)
                 stage_codes4p<TILE>(s_codes + ((o + 2) % 3) * 2 * TILE, nx, j.codes, j.site_stride,
                                     j.tile_base);
         }
         cp_async_commit();
-        const Op op = ops[o];
         const StageP<KP>& stg = stages[o % 3];
         const uint8_t* ring = s_codes + (o % 3) * 2 * TILE;  // CODES 2: this op's codes
         if (op.s0 == kSrcPop) --sp;
