@@ -4,7 +4,9 @@
 // Same structure as prune4s (plk_prune4s.cu): a CTA walks the op list over a
 // tile of 128 x SPT sites, op o+2's P(t) rows and tip tables travel into a
 // three-slot shared-memory ring by cp.async while op o computes, spilled
-// vectors sit in a per-thread shared-memory stack.  The tile body
+// vectors sit in a per-thread shared-memory stack.  The tip codes are read
+// from global memory at their use, staged for the whole tile, or staged
+// with each op in a ring beside the stage slots (CODES 0 / 1 / 2).  The tile body
 // (run_tile4p, plk_prune4p.cuh) keeps every value as a pair (category 2q,
 // category 2q+1), so each product is one fma.rn.f32x2 / mul.rn.f32x2 for two
 // categories, rounding lane by lane exactly as prune4s: the per-site results

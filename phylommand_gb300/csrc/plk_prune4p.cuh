@@ -233,9 +233,10 @@ __device__ void run_tile4p(const TileJob& j, unsigned char* sm, SiteSum32& sum) 
     }
     int sp = 0;
 
-    // (tip codes from global memory are read at their use: loading them an op
-    // ahead, or before the op's barrier, measured slower for this body on the
-    // 128 x 100,000 benchmark)
+    // (with CODES 0 the tip codes are read from global memory at their use:
+    // loading them into registers an op ahead, or before the op's barrier,
+    // measured slower for this body on the 128 x 100,000 benchmark; CODES 2
+    // stages them with the op instead)
     for (int o = 0; o < j.n_ops; ++o) {
         // this op and the one to stage, loaded before the wait and the
         // barrier so that their latency (L1 when the ops are not staged)
