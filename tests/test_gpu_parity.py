@@ -196,13 +196,17 @@ def test_call_order_and_argument_errors():
         assert st == plk.PLK_ERR_ARG
 
 
-@pytest.mark.parametrize("S,patterns", [(4, False), (4, True), (3, False), (6, False)])
-def test_byte_masks_match_32bit_masks(S, patterns):
-    """plk_set_alignment8 (device encoding for <= 4 states, host widening
-    otherwise or with patterns) gives the same bits as plk_set_alignment,
-    and reports an empty cell the same way."""
-    rng = np.random.default_rng(S + 10 * patterns)
-    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 19, 777, S=S, C=4)
+@pytest.mark.parametrize("S,patterns,n_sites", [(4, False, 777), (4, True, 777), (3, False, 777), (6, False, 777),
+                                                (4, False, 784), (3, False, 1600)])
+def test_byte_masks_match_32bit_masks(S, patterns, n_sites):
+    """plk_set_alignment8 (device encoding for <= 4 states -- 16 cells per
+    thread when rows are a multiple of 16 sites --, host widening otherwise
+    or with patterns) gives the same bits as plk_set_alignment, ignores the
+    bits above the alphabet, and reports an empty cell (no state bit left)
+    the same way."""
+    rng = np.random.default_rng(S + 10 * patterns + n_sites)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 19, n_sites, S=S, C=4)
+    masks[rng.random(masks.shape) < 0.05] |= np.uint32(0x40)  # bits above the alphabet
     out = []
     for m in (masks.astype(np.uint32), masks.astype(np.uint8)):
         h = plk.Handle()
@@ -212,11 +216,12 @@ def test_byte_masks_match_32bit_masks(S, patterns):
         h.set_rate_model(False)
         h.set_model(Q, f, True, cr, cw, plk.PLK_P_EXACT)
         out.append((h.loglik(plk.PLK_FP64), h.site_loglik(), h.loglik(plk.PLK_FP32S)))
-        bad = m.copy()
-        bad[3, 5] = 0
-        h.set_alignment(bad, S)
-        st, _ = h.loglik_status()
-        assert st == plk.PLK_ERR_TIP
+        for cell in (0, 0x40):  # no bit at all / only bits above the alphabet
+            bad = m.copy()
+            bad[3, 5] = cell
+            h.set_alignment(bad, S)
+            st, _ = h.loglik_status()
+            assert st == plk.PLK_ERR_TIP
         h.close()
     assert out[0][0] == out[1][0] and out[0][2] == out[1][2]
     np.testing.assert_array_equal(out[0][1], out[1][1])
