@@ -30,6 +30,8 @@ using namespace dev;
 // =========================================================================
 // P(t)
 // =========================================================================
+constexpr int kPmatOut = 4;  // P(t) entries per thread at most (see launch_pmat)
+
 __global__ void pmat_kernel(DeviceModel m, int p_kind) {
     const int v = blockIdx.x / m.C, k = blockIdx.x % m.C;
     const int S = m.S, SS = S * S;
@@ -58,13 +60,32 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
             double* tmp = A; A = B; B = tmp;
         }
     } else if (p_kind == 1) {
-        for (int i = threadIdx.x; i < S; i += blockDim.x) X[i] = exp(m.eig_lam[i] * t);
+        // P = L diag(exp(lambda t)) R with L diag(.) and R staged in shared
+        // memory (B: the exponentials, X: L diag(.), A: R, then P); each
+        // product rounded before its FMA, as in the oracle
+        for (int i = threadIdx.x; i < S; i += blockDim.x) B[i] = exp(m.eig_lam[i] * t);
+        for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) A[idx] = m.eig_R[idx];
         __syncthreads();
-        for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) {
-            const int i = idx / S, j = idx % S;
-            double acc = 0.0;
-            for (int mm = 0; mm < S; ++mm) acc = fma(m.eig_L[i * S + mm] * X[mm], m.eig_R[mm * S + j], acc);
-            A[idx] = acc;
+        for (int idx = threadIdx.x; idx < SS; idx += blockDim.x) X[idx] = m.eig_L[idx] * B[idx % S];
+        __syncthreads();
+        // launch_pmat gives every thread at most kPmatOut entries (S <= 24:
+        // 576 entries over 256 threads, < 256 over 64, < 64 over 32)
+        double out[kPmatOut];
+#pragma unroll
+        for (int r = 0; r < kPmatOut; ++r) {
+            const int idx = threadIdx.x + r * blockDim.x;
+            if (idx < SS) {
+                const int i = idx / S, j = idx % S;
+                double acc = 0.0;
+                for (int mm = 0; mm < S; ++mm) acc = fma(X[i * S + mm], A[mm * S + j], acc);
+                out[r] = acc;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kPmatOut; ++r) {
+            const int idx = threadIdx.x + r * blockDim.x;
+            if (idx < SS) A[idx] = out[r];
         }
         __syncthreads();
     } else {
@@ -147,6 +168,7 @@ cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st) {
     const int SS = m.S * m.S;
     const size_t smem = sizeof(double) * (size_t)(3 * SS);
     const int threads = SS >= 256 ? 256 : (SS >= 64 ? 64 : 32);
+    if ((SS + threads - 1) / threads > kPmatOut) return cudaErrorInvalidConfiguration;
     pmat_kernel<<<m.n_nodes * m.C, threads, smem, st>>>(m, p_kind);
     return cudaGetLastError();
 }
