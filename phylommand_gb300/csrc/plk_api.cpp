@@ -279,7 +279,24 @@ plk_status refresh_teff(plk_handle* h) {
 
 // P(t) of every edge and category; with paired, also the layouts prune4p
 // reads, into its scratch (so no relayout launch follows).
-plk_status build_pmats(plk_handle* h, bool paired = false) {
+PruneArgs prune_args(plk_handle* h, int precision);
+
+// 20 states: whether the tuned post-order form is one of the tcgen05 forms
+// (5, 6), whose B-operand images and transposed tip tables the P(t) kernel
+// then writes itself (no relayout launch)
+bool tuned_tc20(const plk_handle* h) {
+    if (h->S != 20) return false;
+    int v = h->variant;
+    if (const char* f = getenv("PLK_PRUNE_VARIANT")) v = atoi(f);
+    if (v < 0) {
+        const std::array<int, 6> key = {h->n_sites, h->n_tips, (int)h->prog.ops.size(), h->prog.max_depth, h->C, h->S};
+        auto hit = h->tune_cache.find(key);
+        if (hit != h->tune_cache.end()) v = hit->second;
+    }
+    return v == 5 || v == 6;
+}
+
+plk_status build_pmats(plk_handle* h, bool paired = false, bool tc20 = false) {
     plk_status s = refresh_teff(h);
     if (s != PLK_OK) return s;
     const size_t SS = (size_t)h->S * h->S;
@@ -306,7 +323,20 @@ plk_status build_pmats(plk_handle* h, bool paired = false) {
         PLK_CUDA(h, h->d_work.ensure(prune4p_scratch_bytes(a)), "allocate scratch");
         prune4p_scratch_parts(h->d_work.p, h->n_nodes, h->C, &m.P32p, &m.tip32p);
     }
-    h->paired_written = paired;
+    m.B20 = nullptr;
+    m.T20 = nullptr;
+    m.ncs20 = 0;
+    if (tc20) {
+        // the scratch as the post-order launch sizes it, so that it does not
+        // move between this kernel and the pass
+        const PruneArgs a = prune_args(h, PLK_FP32S);
+        PLK_CUDA(h, h->d_work.ensure(std::max(prune20_scratch_bytes(a, h->n_nodes),
+                                               prune20u_scratch_bytes(a, h->n_nodes))),
+                 "allocate scratch");
+        prune20u_scratch_parts(h->d_work.p, a, h->n_nodes, &m.B20, &m.T20);
+        m.ncs20 = prune20u_codes_padded(h->n_codes);
+    }
+    h->paired_written = paired || tc20;
     PLK_CUDA(h, launch_pmat(m, h->p_kind, h->stream), "P(t) kernel launch");
     return PLK_OK;
 }
@@ -871,7 +901,9 @@ plk_status plk_loglik_async(plk_handle* h, int precision) {
         ev = &h->evs[h->ev_used++];
         PLK_CUDA(h, cudaEventRecord(ev->e[0], h->stream), "cudaEventRecord");
     }
-    if ((s = build_pmats(h, precision == PLK_FP32S && tuned_paired(h))) != PLK_OK) return s;
+    if ((s = build_pmats(h, precision == PLK_FP32S && tuned_paired(h), precision == PLK_FP32S && tuned_tc20(h))) !=
+        PLK_OK)
+        return s;
     if (ev) PLK_CUDA(h, cudaEventRecord(ev->e[1], h->stream), "cudaEventRecord");
     if ((s = run_prune(h, precision, nullptr, ev ? &ev->e[2] : nullptr)) != PLK_OK) return s;
     if (h->patterns)  // every pattern's lnL counts once per site showing it

@@ -173,6 +173,12 @@ struct DeviceModel {
     // reads (plk_prune4p.cuh), so that no relayout launch is needed
     float* P32p;
     float* tip32p;
+    // when set (20 states, the tcgen05 forms tuned): also their B-operand
+    // images and [state][code] tip tables (plk_prune20u.cu), ncs20 codes per
+    // row (n_codes rounded up to 4)
+    float* B20;
+    float* T20;
+    int ncs20;
 };
 // p_kind: 0 taylor20, 1 eigen (reversible), 2 series (non-reversible)
 cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st);
@@ -247,6 +253,10 @@ cudaError_t launch_combine20(const float* cat_L, const int* cat_E, const PruneAr
 // prune20v_kernel (the compact form: three CTAs per SM, spills in global
 // memory).
 bool prune20u_fits(const PruneArgs& a, int form);
+// Where the B-operand images and the transposed tip tables sit in the
+// scratch, and their row length (n_codes rounded up to 4).
+void prune20u_scratch_parts(void* scratch, const PruneArgs& a, int n_nodes, float** B, float** T);
+int prune20u_codes_padded(int n_codes);
 size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes);
 cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int form, int* n_blocks,
                             cudaStream_t st);

@@ -32,6 +32,13 @@ using namespace dev;
 // =========================================================================
 constexpr int kPmatOut = 4;  // P(t) entries per thread at most (see launch_pmat)
 
+// FP32 to TF32, round to nearest with ties away from zero (the tcgen05 B images)
+__device__ __forceinline__ float tf32_rna_dev(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
 __global__ void pmat_kernel(DeviceModel m, int p_kind) {
     const int v = blockIdx.x / m.C, k = blockIdx.x % m.C;
     const int S = m.S, SS = S * S;
@@ -143,6 +150,25 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
         m.P32[base + idx] = (float)A[idx];
         if (m.P32p) m.P32p[(size_t)v * m.C * 16 + paired_p_index(k, idx / 4, idx % 4)] = (float)A[idx];
     }
+    if (m.B20 && S == 20) {
+        // the tcgen05 B-operand image of this (node, category): [part][4-column
+        // group g][8-row block nb][row r][column c], state i = 8 nb + r, j =
+        // 4 g + c, TF32 hi and lo parts of the FP32 P (zero outside 20 x 20),
+        // as relayout20u_kernel writes it
+        float* Bv = m.B20 + ((size_t)v * m.C + k) * 1536;
+        for (int w = threadIdx.x; w < 1536; w += blockDim.x) {
+            const int part = w / 768, q = w % 768;
+            const int g = q / 128, nb = (q / 32) % 4, r = (q / 4) % 8, c = q % 4;
+            const int i = 8 * nb + r, j = 4 * g + c;
+            float val = 0.0f;
+            if (i < 20 && j < 20) {
+                const float x = (float)A[i * 20 + j];
+                const float hi = tf32_rna_dev(x);
+                val = part == 0 ? hi : tf32_rna_dev(x - hi);
+            }
+            Bv[w] = val;
+        }
+    }
     if (v < m.n_tips) {
         // table[code][i] = sum over allowed j (ascending) of P[i][j]: what
         // branch_likelihood gives for a 0/1 tip vector (0 * P adds nothing).
@@ -160,6 +186,13 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
             m.tip64[tb + idx] = acc;
             m.tip32[tb + idx] = (float)acc;
             if (m.tip32p) m.tip32p[(size_t)v * m.C * kCodes * 4 + paired_tip_index(k, c, i)] = (float)acc;
+            if (m.T20) m.T20[((size_t)v * m.C + k) * (20 * m.ncs20) + (size_t)i * m.ncs20 + c] = (float)acc;
+        }
+        if (m.T20) {  // the padding codes of every state row
+            const int pad = m.ncs20 - m.n_codes;
+            for (int idx = threadIdx.x; idx < 20 * pad; idx += blockDim.x)
+                m.T20[((size_t)v * m.C + k) * (20 * m.ncs20) + (size_t)(idx / pad) * m.ncs20 + m.n_codes + idx % pad] =
+                    0.0f;
         }
     }
 }

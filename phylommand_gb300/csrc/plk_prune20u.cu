@@ -683,6 +683,14 @@ bool prune20u_fits(const PruneArgs& a, int form) {
     return smem20u_bytes(a, form) <= 200 * 1024;
 }
 
+void prune20u_scratch_parts(void* scratch, const PruneArgs& a, int n_nodes, float** B, float** T) {
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    *B = reinterpret_cast<float*>(base);
+    *T = reinterpret_cast<float*>(base + ((((size_t)n_nodes * a.C * kBFloats * sizeof(float)) + 255) & ~(size_t)255));
+}
+
+int prune20u_codes_padded(int n_codes) { return codes_padded(n_codes); }
+
 size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes) {
     const size_t ps = (size_t)n_nodes * a.C * kBFloats * sizeof(float);
     const size_t ts = (size_t)a.n_tips * a.C * kS * codes_padded(a.n_codes) * sizeof(float);
@@ -708,7 +716,7 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
     g.spill = reinterpret_cast<float*>(base + off);
     g.child_bytes = child_bytes_for(a);
     g.tmem_cols = tmem_cols_for(a, form);
-    {
+    if (!a.paired_ready) {  // else the P(t) kernel wrote both layouts
         const long long total =
             (long long)n_nodes * a.C * kBFloats + (long long)a.n_tips * a.C * kS * codes_padded(a.n_codes);
         long long blocks = (total + 255) / 256;
