@@ -105,7 +105,7 @@ struct plk_handle {
     DevBuf d_P64, d_P32, d_tip64, d_tip32;
     // results and scratch
     DevBuf d_site_lnl, d_block, d_lnl, d_work, d_cond, d_outside, d_nodes_out;
-    DevBuf d_done;  // arrival counter of finish_grid_sum, zero between launches
+    DevBuf d_done;  // arrival counters (finish_grid_sum, then one per 128-site tile), zero between launches
     bool paired_written = false;  // this evaluation's P(t) kernel also wrote prune4p's layouts
     bool withhold_stage = false;  // plk_test_withhold_stage: armed for the next FP32 pass
     DevBuf d_mask_raw, d_flag;
@@ -486,14 +486,18 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     PLK_CUDA(h, h->d_site_lnl.ensure(sizeof(double) * h->n_sites), "allocate site lnL");
     PLK_CUDA(h, h->d_block.ensure(sizeof(double) * 2 * blocks), "allocate block sums");
     PLK_CUDA(h, h->d_lnl.ensure(sizeof(double)), "allocate lnL");
-    if (!h->d_done.p) {
-        PLK_CUDA(h, h->d_done.ensure(sizeof(unsigned)), "allocate counter");
-        PLK_CUDA(h, cudaMemsetAsync(h->d_done.p, 0, sizeof(unsigned), h->stream), "clear counter");
+    // arrival counters, zero between launches: the grid's, then one per
+    // 128-site tile (the 20-state compact form's in-kernel combine)
+    const size_t counters = (1 + (size_t)(h->n_sites + 127) / 128) * sizeof(unsigned);
+    if (h->d_done.bytes < counters) {
+        PLK_CUDA(h, h->d_done.ensure(counters), "allocate counters");
+        PLK_CUDA(h, cudaMemsetAsync(h->d_done.p, 0, counters, h->stream), "clear counters");
     }
     PruneArgs a = prune_args(h, precision);
     // the last CTA of the post-order pass (or of its per-site combine) adds
     // up the block sums into d_lnl: no separate reduction launch
     a.grid_done = h->d_done.as<unsigned>();
+    a.tile_done = h->d_done.as<unsigned>() + 1;
     a.lnl_out = h->d_lnl.as<double>();
     a.paired_ready = (precision == PLK_FP32S && h->paired_written) ? 1 : 0;
     a.withhold_first_stage = (precision == PLK_FP32S && h->withhold_stage) ? 1 : 0;

@@ -229,6 +229,10 @@ struct PruneArgs {
     // per-site values are written.
     unsigned* grid_done;
     double* lnl_out;
+    // one arrival counter per 128-site tile, zero between launches: with it
+    // the 20-state compact form combines the categories of a tile in the
+    // tile's last CTA (no combine launch)
+    unsigned* tile_done;
     // the paired P(t) and tip layouts are already in scratch (written by the
     // P(t) kernel): prune4p skips its relayout
     int paired_ready;

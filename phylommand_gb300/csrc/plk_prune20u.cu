@@ -649,6 +649,41 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         g.cat_L[(size_t)k * a.n_sites + site] = l;
         g.cat_E[(size_t)k * a.n_sites + site] = e_site;
     }
+    if (!a.tile_done) return;
+    // the last of the tile's category CTAs combines them per site (the
+    // arithmetic and block grouping of combine20_kernel: the same bits) and,
+    // as the last tile, adds up the block sums
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(a.tile_done + blockIdx.x, 1u) == gridDim.y - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    SiteSum32 sum;
+    if (site < a.n_sites) {
+        int E = __ldcg(g.cat_E + site);
+        for (int kk = 1; kk < a.C; ++kk) E = max(E, __ldcg(g.cat_E + (size_t)kk * a.n_sites + site));
+        float lsum = 0.0f;
+        for (int kk = 0; kk < a.C; ++kk)
+            lsum = fmaf((float)a.cat_w[kk],
+                        ldexpf(__ldcg(g.cat_L + (size_t)kk * a.n_sites + site),
+                               __ldcg(g.cat_E + (size_t)kk * a.n_sites + site) - E),
+                        lsum);
+        float lm;
+        int ee;
+        site_log32(lsum, E, lm, ee);
+        if (a.site_lnl) a.site_lnl[site] = site_lnl64(lm, ee);
+        site_sum_add(sum, lm, ee);
+    }
+    double bs, bc;
+    block_sum_site32(sum, bs, bc);
+    if (tid == 0) {
+        a.block_sum[2 * blockIdx.x] = bs;
+        a.block_sum[2 * blockIdx.x + 1] = bc;
+        a.tile_done[blockIdx.x] = 0u;  // re-armed for the next launch
+    }
+    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 int tmem_cols_for(const PruneArgs& a, int form) {
@@ -751,6 +786,10 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
     kern<<<grid, kThreads, smem, st>>>(g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (form == 1 && a.tile_done) {  // combined in the kernel
+        *n_blocks = (int)grid.x;
+        return cudaSuccess;
+    }
     return launch_combine20(g.cat_L, g.cat_E, a, n_blocks, st);
 }
 
