@@ -281,11 +281,10 @@ plk_status refresh_teff(plk_handle* h) {
 // reads, into its scratch (so no relayout launch follows).
 PruneArgs prune_args(plk_handle* h, int precision);
 
-// 20 states: whether the tuned post-order form is one of the tcgen05 forms
-// (5, 6), whose B-operand images and transposed tip tables the P(t) kernel
-// then writes itself (no relayout launch)
-bool tuned_tc20(const plk_handle* h) {
-    if (h->S != 20) return false;
+// The post-order form the next FP32 evaluation will run: forced by
+// PLK_PRUNE_VARIANT, tuned on this handle, or cached for the shape (-1: not
+// tuned yet).
+int tuned_variant(const plk_handle* h) {
     int v = h->variant;
     if (const char* f = getenv("PLK_PRUNE_VARIANT")) v = atoi(f);
     if (v < 0) {
@@ -293,6 +292,15 @@ bool tuned_tc20(const plk_handle* h) {
         auto hit = h->tune_cache.find(key);
         if (hit != h->tune_cache.end()) v = hit->second;
     }
+    return v;
+}
+
+// 20 states: whether the tuned post-order form is one of the tcgen05 forms
+// (5, 6), whose B-operand images and transposed tip tables the P(t) kernel
+// then writes itself (no relayout launch)
+bool tuned_tc20(const plk_handle* h) {
+    if (h->S != 20) return false;
+    const int v = tuned_variant(h);
     return v == 5 || v == 6;
 }
 
@@ -463,13 +471,7 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
 // prune4p relays the layouts out itself.
 bool tuned_paired(const plk_handle* h) {
     if (h->S != 4 || (h->C != 2 && h->C != 4 && h->C != 8) || !fused_kernel_applies(h, PLK_FP32S)) return false;
-    int v = h->variant;
-    if (const char* f = getenv("PLK_PRUNE_VARIANT")) v = atoi(f);
-    if (v < 0) {
-        const std::array<int, 6> key = {h->n_sites, h->n_tips, (int)h->prog.ops.size(), h->prog.max_depth, h->C, h->S};
-        auto hit = h->tune_cache.find(key);
-        if (hit != h->tune_cache.end()) v = hit->second;
-    }
+    const int v = tuned_variant(h);
     return v >= 3 && v <= 11;
 }
 
