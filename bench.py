@@ -164,8 +164,8 @@ def run_reference(args, world, rank):
     step a bounded sample of the same workload."""
     if rank != 0:
         return
-    from phylommand_gb300 import synth
-    w = synth.make(WORKLOAD, seed=SEED, n_sites=args.sites, n_tips=args.taxa)
+    from phylommand_gb300 import synth  # the numpy backend: this process never loads libplk
+    w = synth.make(WORKLOAD, seed=SEED, n_sites=args.sites, n_tips=args.taxa, backend="numpy")
     threads = os.cpu_count() or 1
     sample = max(threads * 40, 256)
     for _ in range(args.warmup):
@@ -189,11 +189,54 @@ def run_reference(args, world, rank):
 
 
 def workload_config(w):
+    """The workload both arms run (the same dict in both lines)."""
     return {"workload": f"DNA GTR+Gamma4, {w.n_tips}-taxon Yule tree, {w.n_sites:,} sites, 2% missing cells",
             "n_taxa": w.n_tips, "n_sites": w.n_sites, "n_states": w.n_states, "n_categories": len(w.cat_rates),
             "alpha": w.alpha, "branch_lengths": "Exp(mean 0.05)", "seed": w.seed,
+            "generator": "numpy (phylommand_gb300.synth, backend numpy)",
             "p_matrix": "FP64 eigen form", "partials": "FP32, per-site power-of-two scaling",
-            "site_sum": "FP64 compensated", "parallelism": "replicas"}
+            "site_sum": "FP64 compensated", "parallelism": "replicas",
+            "l2": "GPU arm: 256 MiB written before every timed step (L2 flushed), outside the events"}
+
+
+def measure_fp32_peak(device: int):
+    """The FP32 multiply-add peak of this GPU, measured by the library's
+    microbenchmark (fma.rn.f32x2 chains over 4 CTAs per SM, CUDA events):
+    TFLOP/s, or None when it fails."""
+    import ctypes
+    from phylommand_gb300 import plk
+    t, ms = ctypes.c_double(), ctypes.c_double()
+    best = None
+    for packed in (1, 0):
+        if plk.lib().plk_measure_fp32_peak(device, packed, 1 << 16, ctypes.byref(t), ctypes.byref(ms)) == 0:
+            best = t.value if best is None else max(best, t.value)
+    return best
+
+
+def required_bytes(w, C: int, grid_blocks: int) -> int:
+    """Bytes one fused post-order pass must move through HBM: the 1-byte tip
+    codes (rows padded to 16 bytes), the paired P(t) and tip tables it reads,
+    the FP64 per-site values it writes and its block sums."""
+    stride = (w.n_sites + 15) // 16 * 16
+    codes = w.n_tips * stride
+    tables = w.n_nodes * C * 16 * 4 + w.n_tips * C * 16 * 4 * 4
+    return codes + tables + 8 * w.n_sites + 16 * grid_blocks
+
+
+def time_steps(h, stream, flush, steps: int, precision: int):
+    """CUDA-event time (ms, summed over steps) of `steps` evaluations on the
+    engine's stream, L2 flushed before each outside the events."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[k].record(stream)
+        h.loglik_async(precision)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
 
 
 def run_ours(args, world, rank, local):
@@ -201,7 +244,9 @@ def run_ours(args, world, rank, local):
     from phylommand_gb300 import plk, synth
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = synth.make(WORKLOAD, seed=SEED, n_sites=args.sites, n_tips=args.taxa)
+    w = synth.make(WORKLOAD, seed=SEED, n_sites=args.sites, n_tips=args.taxa, backend="numpy")
+    C = len(w.cat_rates)
+    fp32_peak = measure_fp32_peak(local)
     h = plk.Handle(local)
     h.set_alignment(w.masks, w.n_states)
     h.set_tree(w.left, w.right, w.bl)
@@ -214,33 +259,35 @@ def run_ours(args, world, rank, local):
     lnl64 = h.loglik(plk.PLK_FP64)
     for _ in range(max(args.warmup, 3)):
         h.loglik_async(plk.PLK_FP32S)
-    lnl32 = h.loglik_result()
+    h.loglik_result()
 
     clocks = ClockSampler(local)
     clocks.start()
     h.set_profiling(True)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize()
     t_wall = time.perf_counter()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        starts[k].record(stream)
-        h.loglik_async(plk.PLK_FP32S)
-        ends[k].record(stream)
-    torch.cuda.synchronize()
+    dev_ms = time_steps(h, stream, flush, args.steps, plk.PLK_FP32S)
     barrier(world)
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
-    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     kern_ms, n_evals = h.kernel_times(reset=True)
     h.set_profiling(False)
     lnl_timed = h.loglik_result()
     h_variant = h.prune_kernel()
     max_ms = reduce_max(world, dev_ms, dev)
     value = world * args.steps / (max_ms / 1e3)
+
+    # the FP64 plain form (reference operation order for the P(t)-independent
+    # part, FP64 partials) on the same workload: the like-for-like precision
+    # of the reference's CPU path
+    for _ in range(3):
+        h.loglik_async(plk.PLK_FP64)
+    h.loglik_result()
+    steps64 = max(3, args.steps // 2)
+    ms64 = reduce_max(world, time_steps(h, stream, flush, steps64, plk.PLK_FP64), dev)
+    lnl64_timed = h.loglik_result()
+    value64 = world * steps64 / (ms64 / 1e3)
 
     # end to end through the C ABI with host buffers: upload the alignment,
     # tree and model from pinned host memory, evaluate, read the lnL back
@@ -276,7 +323,7 @@ def run_ours(args, world, rank, local):
                   plk.PLK_P_EXACT)
     out = ctypes.c_double(0.0)
 
-    def e2e_run(masks):
+    def e2e_run(masks, precision=plk.PLK_FP32S):
         if masks.dtype == np.uint8:
             aln = (L.plk_set_alignment8, (hh, masks.shape[0], masks.shape[1], w.n_states,
                                           masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
@@ -285,7 +332,7 @@ def run_ours(args, world, rank, local):
                                          masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
         for _ in range(2):
             h.set_alignment(masks, w.n_states)
-            h.loglik(plk.PLK_FP32S)
+            h.loglik(precision)
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -293,13 +340,14 @@ def run_ours(args, world, rank, local):
             st |= L.plk_set_tree(*tree_args)
             st |= L.plk_set_rate_model(*rate_args)
             st |= L.plk_set_model(*model_args)
-            st |= L.plk_loglik(hh, plk.PLK_FP32S, ctypes.byref(out))
+            st |= L.plk_loglik(hh, precision, ctypes.byref(out))
             if st != plk.PLK_OK:
                 raise plk.PlkError(st, (L.plk_last_error(hh) or b"").decode())
         return world * e2e_steps / reduce_max(world, time.perf_counter() - t0, dev), out.value
 
     e2e_value, lnl_e2e = e2e_run(masks8)
     e2e32_value, _ = e2e_run(masks32)
+    e2e64_value, _ = e2e_run(masks8, plk.PLK_FP64)
     # where an end-to-end step goes: the host time of each call (the uploads
     # are asynchronous, so their device work overlaps the calls after them;
     # plk_loglik waits for everything)
@@ -317,18 +365,41 @@ def run_ours(args, world, rank, local):
             e2e_parts[name] += time.perf_counter() - t0
     e2e_parts = {name: 1e3 * t / e2e_steps for name, t in e2e_parts.items()}
     h2d = masks8.nbytes + small
+
+    # errors of the fast form: the lnL and the ancestral probabilities (the
+    # conditional and the marginal node states), as the C ABI reports them
+    # against the FP64 plain form, and against the FP64 oracle
+    fast, f64, abs_err_abi, rel_err_abi = h.loglik_err()
+    cells = w.n_tips * w.n_sites
+    node_err = {}
+    if cells <= ORACLE_CELLS:
+        from oracle import oracle as O
+        teff = plk.effective_lengths(w.left, w.right, w.bl, False)
+        orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights,
+                       p_mode=O.P_EXACT, threads=os.cpu_count() or 1, want_cond_norm=True, want_marginal=True)
+        ref_lnl = orc.lnl
+        ref_name = "error_vs_fp64_oracle"
+        for name, mode, ref in (("cond", plk.PLK_NODES_COND, orc.cond_norm),
+                                ("marginal", plk.PLK_NODES_MARGINAL, orc.marginal)):
+            n32, e_abi = h.node_states_err(mode)
+            node_err[name] = {"max_abs_vs_fp64_oracle": float(np.abs(n32 - ref).max()),
+                              "max_abs_vs_fp64_engine_abi": e_abi}
+            del n32
+        del orc
+    else:
+        ref_lnl = lnl64
+        ref_name = "error_vs_fp64_engine"
     h.close()
 
     if rank != 0:
         return
     hbm_peak, _, peak_src = load_peaks()
-    bytes_per_launch = algorithmic_bytes_per_site(w.n_tips, w.n_states, len(w.cat_rates), 4) * w.n_sites
-    flops_per_launch = algorithmic_flops_per_site(w.n_tips, w.n_states, len(w.cat_rates)) * w.n_sites
+    flops_per_launch = algorithmic_flops_per_site(w.n_tips, w.n_states, C) * w.n_sites
     prune_ms = kern_ms[1] / max(n_evals, 1)
-    achieved = bytes_per_launch / (prune_ms / 1e3) / 1e9
-    fp32_peak_mhz = clk["sm_max_mhz"] if clk else 2070.0
-    fp32_peak = SM_COUNT * FP32_LANES_PER_SM * 2 * fp32_peak_mhz * 1e6 / 1e12
+    grid = (w.n_sites + 127) // 128
+    req = required_bytes(w, C, grid)
     fp32_achieved = flops_per_launch / (prune_ms / 1e3) / 1e12
+    level_bytes = algorithmic_bytes_per_site(w.n_tips, w.n_states, C, 4) * w.n_sites
 
     # CPU baseline: the reference's algorithm (oracle port), one core, on a
     # bounded sample of this workload
@@ -336,40 +407,35 @@ def run_ours(args, world, rank, local):
     cpu_s = cpu_port_seconds(w, sample, 1)
     cpu_value = 1.0 / (cpu_s * w.n_sites / sample)
 
-    # error of the timed FP32 result against the FP64 oracle (above
-    # ORACLE_CELLS tip cells the oracle would take minutes: against the FP64
-    # engine, which the tests hold to the oracle within 1e-11)
-    if w.n_tips * w.n_sites <= ORACLE_CELLS:
-        from oracle import oracle as O
-        teff = plk.effective_lengths(w.left, w.right, w.bl, False)
-        ref_lnl = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights,
-                           p_mode=O.P_EXACT, threads=os.cpu_count() or 1).lnl
-        ref_name = "error_vs_fp64_oracle"
-    else:
-        ref_lnl = lnl64
-        ref_name = "error_vs_fp64_engine"
     err = {"abs": abs(lnl_timed - ref_lnl), "rel": abs(lnl_timed - ref_lnl) / abs(ref_lnl),
-           "e2e_rel": abs(lnl_e2e - ref_lnl) / abs(ref_lnl)}
-    if ref_name == "error_vs_fp64_oracle":
-        err["fp64_engine_rel"] = abs(lnl64 - ref_lnl) / abs(ref_lnl)
+           "e2e_rel": abs(lnl_e2e - ref_lnl) / abs(ref_lnl),
+           "fp64_engine_rel": abs(lnl64_timed - ref_lnl) / abs(ref_lnl),
+           "abi_plk_loglik_err": {"abs": abs_err_abi, "rel": rel_err_abi},
+           "node_states": node_err}
     line = {
         "metric": "lnL evals/s", "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded simulation of the workload's shapes)",
-        "config": {**workload_config(w), "l2": "flushed before every step (256 MiB write, outside the events)"},
+        "config": workload_config(w),
         "gsite_node_updates_per_s": value * (w.n_tips - 1) * w.n_sites / 1e9,
         "wall_s_timed_region": wall,
         "kernel_ms_per_eval": {"pmat": kern_ms[0] / max(n_evals, 1), "postorder_and_total": prune_ms,
                                "after": kern_ms[2] / max(n_evals, 1)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": load_traffic(h_variant),
-                     "kernel": f"{h_variant} (post-order pass)",
-                     "algorithmic_bytes_per_launch": bytes_per_launch, "peak_source": peak_src,
-                     "note": "algorithmic bytes of a level-by-level pass; this kernel keeps partials on chip"},
+        "roofline": {"bound": "hbm", "achieved": req / (prune_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": req / (prune_ms / 1e3) / 1e9 / hbm_peak, "traffic": load_traffic(h_variant),
+                     "kernel": f"{h_variant} (post-order pass)", "required_bytes_per_launch": req,
+                     "peak_source": peak_src,
+                     "bytes": "tip codes + paired P(t) and tip tables + FP64 site values + block sums; the pass "
+                              "keeps every partial vector on chip",
+                     "level_by_level_model_bytes": level_bytes,
+                     "bound_that_applies": "fp32 (roofline_fp32): the pass is instruction-issue bound, not HBM bound"},
         "roofline_fp32": {"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                          "frac": fp32_achieved / fp32_peak,
-                          "peak_source": f"derived: {SM_COUNT} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 x "
-                                         f"{fp32_peak_mhz:.0f} MHz"},
+                          "frac": fp32_achieved / fp32_peak if fp32_peak else None,
+                          "flops_per_launch": flops_per_launch,
+                          "peak_source": "measured: plk_measure_fp32_peak (fma.rn.f32x2 and fma.rn.f32 chains, "
+                                         "4 CTAs per SM, CUDA events), the larger"},
+        "fp64_plain_form": {"value": value64, "unit": "evals/s", "ms_per_step": ms64 / steps64, "steps": steps64,
+                            "e2e": e2e64_value},
         "cpu_baseline": {"value": cpu_value, "unit": "evals/s", "cores": 1, "kind": "port",
                          "sample": f"{sample} of {w.n_sites} sites, P(t) rebuilt per (site, edge, category) by the "
                                    f"reference's Taylor-plus-20-squarings, scaled linearly to all sites"},
@@ -380,25 +446,33 @@ def run_ours(args, world, rank, local):
                                      "path": "plk_set_alignment (pinned 32-bit masks) + the same calls"},
                 "host_ms_per_call": e2e_parts},
         # per evaluation: P(t) (which also writes the paired layouts of the
-        # tuned prune4p form) and the post-order pass, whose last CTA adds up
-        # the total
+        # tuned form) and the post-order pass, whose last CTA adds up the total
         "gpu_launches": 2 * args.steps,
         ref_name: err,
         "clocks": clk,
     }
-    del lnl32
     print(json.dumps(line), flush=True)
+
+
+def load_profile(name: str):
+    """Counters of a committed ncu summary (profiles/<name>.json), or None."""
+    p = os.path.join(ROOT, "profiles", f"{name}.json")
+    if os.path.exists(p):
+        return json.load(open(p))
+    return None
 
 
 def run_protein(args):
     """lnL evals/s of the 20-state workload (64 taxa, 20,000 sites, Gamma4):
-    each 20-state kernel forced in turn, then the autotuner's choice; the
-    post-order kernel time per evaluation against the roofline, and the error
-    against the FP64 oracle."""
+    each 20-state form forced in turn (CUDA cores, mma.sync split TF32,
+    tcgen05 split TF32, tcgen05 split BF16), the FP64 form, then the
+    autotuner's choice; per form the post-order time against the FP32 and
+    tensor rooflines, its pipe utilisation from the committed ncu summaries,
+    and the error against the FP64 oracle."""
     import torch
     from phylommand_gb300 import plk, synth
     from oracle import oracle as O
-    w = synth.make("cfg3", seed=3)
+    w = synth.make("cfg3", seed=3, backend="numpy")
     teff = plk.effective_lengths(w.left, w.right, w.bl, False)
     orc = O.loglik(w.left, w.right, w.masks, teff, w.Q, w.freqs, w.cat_rates, w.cat_weights, p_mode=O.P_EXACT,
                    threads=os.cpu_count() or 1)
@@ -406,19 +480,28 @@ def run_protein(args):
     S, C = 20, len(w.cat_rates)
     bytes_per_eval = algorithmic_bytes_per_site(w.n_tips, S, C, 4) * w.n_sites
     flops_per_eval = algorithmic_flops_per_site(w.n_tips, S, C) * w.n_sites
-    hbm_peak, _, peak_src = load_peaks()
+    hbm_peak, bf16_peak, peak_src = load_peaks()
+    fp32_peak = measure_fp32_peak(0)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
     res = {}
     names = {"1": "prune20_kernel, CUDA cores, 4 warps/tile", "2": "prune20_kernel, tensor cores (split TF32), 4 warps/tile",
              "3": "prune20_kernel, CUDA cores, 8 warps/tile", "4": "prune20_kernel, tensor cores (split TF32), 8 warps/tile",
              "5": "prune20u_kernel, tcgen05 tensor cores (split TF32, TMEM accumulators)",
-             "6": "prune20v_kernel, tcgen05 tensor cores, compact form (three CTAs per SM)", "auto": "autotuned"}
-    for v in ("1", "2", "3", "4", "5", "6", "auto"):
-        if v == "auto":
+             "6": "prune20v_kernel, tcgen05 tensor cores, compact form (three CTAs per SM)",
+             "7": "prune20v_kernel, tcgen05 tensor cores, compact form, split BF16 (kind::f16)",
+             "fp64": "prune_generic_kernel, FP64 partials (the plain form)", "auto": "autotuned"}
+    profiles = {"1": "prune20_kernel_protein_64x20k", "3": "prune20_kernel_protein_64x20k",
+                "5": "prune20u_kernel_protein_64x20k", "6": "prune20v_kernel_protein_64x20k",
+                "7": "prune20v_bf16_kernel_protein_64x20k"}
+    clocks = ClockSampler(0)
+    clocks.start()
+    for v in ("1", "2", "3", "4", "5", "6", "7", "fp64", "auto"):
+        if v in ("auto", "fp64"):
             os.environ.pop("PLK_PRUNE_VARIANT", None)
         else:
             os.environ["PLK_PRUNE_VARIANT"] = v
+        precision = plk.PLK_FP64 if v == "fp64" else plk.PLK_FP32S
         with plk.Handle() as h:
             h.set_alignment(w.masks, S)
             h.set_tree(w.left, w.right, w.bl)
@@ -426,40 +509,51 @@ def run_protein(args):
             h.set_model(w.Q, w.freqs, True, w.cat_rates, w.cat_weights, plk.PLK_P_EXACT)
             h.set_stream(stream.cuda_stream)
             for _ in range(max(args.warmup, 3)):
-                h.loglik_async(plk.PLK_FP32S)
+                h.loglik_async(precision)
             h.loglik_result()
+            if v not in ("auto", "fp64") and h.prune_variant() != int(v):
+                continue  # the form does not apply to this workload
             h.set_profiling(True)
-            starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-            ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
             torch.cuda.synchronize()
-            for k in range(args.steps):
-                with torch.cuda.stream(stream):
-                    flush.zero_()
-                starts[k].record(stream)
-                h.loglik_async(plk.PLK_FP32S)
-                ends[k].record(stream)
-            torch.cuda.synchronize()
-            ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+            ms = time_steps(h, stream, flush, args.steps, precision) / args.steps
             kern, n = h.kernel_times(reset=True)
             h.set_profiling(False)
             lnl = h.loglik_result()
             post_ms = kern[1] / max(n, 1)
+            tflops = flops_per_eval / (post_ms / 1e3) / 1e12
             res[v] = {"kernel": names[v], "evals_per_s": 1e3 / ms, "ms_per_eval": ms, "postorder_ms": post_ms,
                       "gsite_node_updates_per_s": n_int * w.n_sites / (ms / 1e3) / 1e9,
-                      "achieved_tflops": flops_per_eval / (post_ms / 1e3) / 1e12,
-                      "achieved_gbs_algorithmic": bytes_per_eval / (post_ms / 1e3) / 1e9,
-                      "rel_err_vs_fp64_oracle": abs(lnl - orc.lnl) / abs(orc.lnl)}
+                      "achieved_tflops": tflops,
+                      "frac_of_fp32_peak": tflops / fp32_peak if fp32_peak else None,
+                      "frac_of_bf16_dense_peak": tflops / bf16_peak,
+                      "rel_err_vs_fp64_oracle": abs(lnl - orc.lnl) / abs(orc.lnl),
+                      "abs_err_vs_fp64_oracle": abs(lnl - orc.lnl)}
+            if v == "auto":
+                res[v]["variant"] = h.prune_variant()
+            prof = load_profile(profiles.get(v, ""))
+            if prof:
+                res[v]["ncu"] = prof
+    clk = clocks.stop()
     os.environ.pop("PLK_PRUNE_VARIANT", None)
     best = res["auto"]
+    tuned = str(best["variant"])
+    prof = load_profile(profiles.get(tuned, "")) or {}
     line = {"metric": "lnL evals/s (20 states)", "value": best["evals_per_s"], "unit": "evals/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_eval"], "higher_is_better": True,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "20-state, 64-taxon Yule tree, 20,000 sites, exchangeabilities LogNormal(0,1), "
                                    "Gamma4 alpha 1", "l2": "flushed before every step"},
-            "roofline": {"bound": "hbm", "achieved": best["achieved_gbs_algorithmic"], "peak": hbm_peak,
-                         "unit": "GB/s", "frac": best["achieved_gbs_algorithmic"] / hbm_peak, "traffic": None,
-                         "algorithmic_bytes_per_launch": bytes_per_eval, "peak_source": peak_src},
-            "algorithmic_flops_per_eval": flops_per_eval, "variants": res}
+            "roofline": {"bound": "tensor", "achieved": best["achieved_tflops"], "peak": bf16_peak,
+                         "unit": "TFLOP/s", "frac": best["achieved_tflops"] / bf16_peak,
+                         "traffic": prof.get("dram_bytes_per_launch"), "peak_source": f"{peak_src} (cuBLAS bf16)",
+                         "flops_per_launch": flops_per_eval,
+                         "note": "algorithmic flops of the 20x20 products; the split forms issue 3x as many "
+                                 "tensor products"},
+            "roofline_fp32": {"achieved": best["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
+                              "frac": best["achieved_tflops"] / fp32_peak if fp32_peak else None,
+                              "peak_source": "measured: plk_measure_fp32_peak"},
+            "algorithmic_bytes_per_eval": bytes_per_eval, "algorithmic_flops_per_eval": flops_per_eval,
+            "tuned_form": tuned, "variants": res, "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
@@ -471,11 +565,18 @@ def run_warmstart(args):
     until each fit first comes within 1e-3 of the plain fit's optimum."""
     import tempfile
     from phylommand_gb300 import warmstart as W
+    from phylommand_gb300 import plk
     t0 = time.perf_counter()
     data = W.make_labelled(args.ws_train, 32, 2000, seed=1)
     ws, hist = W.train(data, epochs=200, seed=1)
     prep_s = time.perf_counter() - t0
+    clocks = ClockSampler(0)
+    clocks.start()
     r = W.evaluate(ws, args.ws_eval, 64, 5000, seed=1001)
+    clk = clocks.stop()
+    # the same held-out comparison under Nelder-Mead, the reference's NLopt
+    # method (LN_NELDERMEAD, src/treeator.cpp:791-805)
+    nm = W.evaluate(ws, args.ws_eval, 64, 5000, seed=1001, method=plk.PLK_FIT_NELDER_MEAD)
     with tempfile.TemporaryDirectory() as d:  # the checkpoint round trip
         ws.save(os.path.join(d, "w.npz"))
         again = W.WarmStart.load(os.path.join(d, "w.npz"))
@@ -494,8 +595,13 @@ def run_warmstart(args):
                      "evals_to_stop": r["warm_evals_mean"], "wall_s": r["warm_wall_s"], "rounds": r["warm_rounds"]},
             "time_to_fit_ratio": r["wall_ratio_warm_over_plain"],
             "frac_final_within_1e-3_of_plain": r["frac_final_within_tol_of_plain"],
-            "max_lnl_deficit": r["max_lnl_deficit"], "labelling_and_training_s": prep_s,
-            "label_fit_s": data.fit_s, "train_s": hist["train_s"], "checkpoint_round_trip": same}
+            "max_lnl_deficit": r["max_lnl_deficit"], "judge": r["judge"], "labelling_and_training_s": prep_s,
+            "label_fit_s": data.fit_s, "train_s": hist["train_s"], "checkpoint_round_trip": same,
+            "nelder_mead": {k: nm[k] for k in ("evals_to_optimum_ratio_warm_over_plain", "plain_evals_to_optimum_mean",
+                                               "warm_evals_to_plain_optimum_mean", "plain_evals_mean",
+                                               "warm_evals_mean", "wall_ratio_warm_over_plain",
+                                               "frac_final_within_tol_of_plain", "max_lnl_deficit", "judge")},
+            "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
@@ -539,14 +645,29 @@ def run_nni(args):
     for _ in range(max(1, args.warmup)):
         b.loglik()
         b.nni_loglik()
+    # device time of each batched pass from the batch's own CUDA events
+    # (plk_batch_device_ms: graph launch to result copy, and the NNI scoring)
+    clocks = ClockSampler(0)
+    clocks.start()
+    dev_ms = 0.0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         base = b.loglik()
         nni = b.nni_loglik()
-    batched_s = (time.perf_counter() - t0) / args.steps
+        a_ms, n_ms = b.device_ms()
+        dev_ms += a_ms + n_ms
+    batched_wall_s = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    batched_s = dev_ms / 1e3 / args.steps
+    # plain arm: one evaluation per tree through the single-tree C ABI (set
+    # the tree, evaluate), CUDA events on the engine's stream around each
+    # item's trees
+    import torch
+    stream = torch.cuda.Stream()
     plain_s, sample_work, err = 0.0, 0.0, 0.0
     w4 = np.full(4, 0.25)
     with plk.Handle() as h:
+        h.set_stream(stream.cuda_stream)
         for i, (masks, left, right, bl, Q, f, cr) in enumerate(sample):
             moves = b.nni_moves(i)
             topologies = [(left, right)] + [neighbour_tree(left, right, int(v), int(w)) for v, w in moves]
@@ -556,12 +677,16 @@ def run_nni(args):
             h.set_rate_model(False)
             h.set_model(Q, f, True, cr, w4, plk.PLK_P_EXACT)
             h.loglik(plk.PLK_FP32S)  # tuning for this shape
-            t0 = time.perf_counter()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
             for L, R in topologies:
                 h.set_tree(L, R, bl)
                 h.set_rate_model(False)
                 h.loglik(plk.PLK_FP32S)
-            plain_s += time.perf_counter() - t0
+            e1.record(stream)
+            torch.cuda.synchronize()
+            plain_s += e0.elapsed_time(e1) / 1e3
             sample_work += work[i] * len(topologies)
             for (L, R), got in list(zip(topologies, batched))[:8]:
                 h.set_tree(L, R, bl)
@@ -572,6 +697,9 @@ def run_nni(args):
     plain_total_s = plain_s * total_work / sample_work
     line = {"metric": "trees scored/s (512 uneven alignments + all NNI neighbours)", "value": trees / batched_s,
             "unit": "trees/s", "n_items": n_items, "trees": trees, "batched_s_per_pass": batched_s,
+            "timing": "CUDA events: the batch's own (plk_batch_device_ms) for the batched arm, on the engine's "
+                      "stream around each sampled item's per-tree calls for the plain arm",
+            "batched_wall_s_per_pass": batched_wall_s, "clocks": clk,
             "plain_s_per_pass_estimated": plain_total_s, "plain_trees_per_s": trees / plain_total_s,
             "plain_sample_items": len(sample), "speedup_vs_plain_per_tree": plain_total_s / batched_s,
             "max_rel_err_fp32_batched_vs_fp64_per_tree": err, "build_s": build_s, "tuning": b.tuning(),

@@ -149,6 +149,14 @@ plk_status plk_set_model(plk_handle* h, int n_states, const double* Q,
  * for every edge and category on the device, runs the post-order pass, and
  * reduces on the device; one device-to-host copy of 8 bytes. */
 plk_status plk_loglik(plk_handle* h, int precision, double* lnl_out);
+/* The fast form's log-likelihood with its error against the FP64 plain
+ * form of the same inputs (which holds the reference's CPU value within
+ * 1e-12): evaluates both, writes the FP32S value, the FP64 value, |delta lnL|
+ * and |delta lnL| / |lnL FP64|.  Afterwards plk_site_loglik gives the fast
+ * form's per-site values.  Replaces the error estimate of simpleML's
+ * calculate_log_likelihood (src/simpleML.h:58-90), which has none: the
+ * reference computes in FP64 only. */
+plk_status plk_loglik_err(plk_handle* h, double* lnl_fast, double* lnl_fp64, double* abs_err, double* rel_err);
 /* plk_loglik split in two: enqueue the whole evaluation on the handle's
  * stream without waiting, then fetch (waits for the stream).  Lets a caller
  * overlap host work with the device or queue evaluations back to back. */
@@ -197,6 +205,11 @@ plk_status plk_site_loglik(plk_handle* h, double* out);
  * n_states + s], internal nodes ranked in post-order (left subtree, right
  * subtree, node), the order draw_normalized_likelihood_on_nodes visits them. */
 plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out);
+/* plk_node_states in the fast form (FP32S) into out, plus the largest
+ * absolute difference from the FP64 plain form's node states over every
+ * internal node, site and state (src/simpleML.cpp:199-231 prints FP64
+ * values only). */
+plk_status plk_node_states_err(plk_handle* h, int mode, double* out, double* max_abs_err);
 /* Number of internal nodes of the current tree (rows of plk_node_states). */
 int plk_n_internal(const plk_handle* h);
 
@@ -248,6 +261,12 @@ plk_status plk_batch_set_model(plk_batch* b, int item, const double* Q, const do
                                const double* cat_rates, const double* cat_weights);
 /* lnL of every item (n_items doubles), one graph replay. */
 plk_status plk_batch_loglik(plk_batch* b, double* lnl_out);
+/* Device time (CUDA events on the batch's stream) of the last
+ * plk_batch_loglik (from the graph launch to its last copy) and of the last
+ * plk_batch_nni_loglik (from its first upload to the download of the
+ * scores), in ms; 0 before the first call.  A measurement helper with no
+ * counterpart in the reference (treeator times nothing). */
+plk_status plk_batch_device_ms(const plk_batch* b, double* loglik_ms, double* nni_ms);
 /* The autotuner's choice: sites per thread, persistent grid size, ms of one
  * post-order launch, and whether evaluations replay a CUDA graph. */
 plk_status plk_batch_tuning(const plk_batch* b, int* sites_per_thread, int* grid, double* ms,
@@ -437,6 +456,16 @@ plk_status plk_effective_lengths(int n_nodes, const int* left, const int* right,
                                  const int* clade_of_node, int n_clades, const float* clade_rate,
                                  double* t_eff_out);
 
+/* ---- measurement helper -------------------------------------------------------
+ * No counterpart in the reference (which has no GPU path).  Measures the FP32
+ * multiply-add rate of `device`: every thread of a grid of 4 CTAs per SM runs
+ * independent fma.rn.f32 chains (packed = 0) or fma.rn.f32x2 chains
+ * (packed = 1) for `iters` iterations of 64 lane-FMAs, timed with CUDA events
+ * after a warm-up launch.  Writes TFLOP/s (2 flops per lane-FMA) and the
+ * launch time in ms (ms_out may be NULL).  1 <= iters <= 2^24.  The
+ * post-order passes' FP32 roofline is quoted against this number. */
+plk_status plk_measure_fp32_peak(int device, int packed, int iters, double* tflops_out, double* ms_out);
+
 /* ---- allocation-free entry point ----------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they need the result -- work recorded into a CUDA stream
@@ -452,7 +481,9 @@ plk_status plk_effective_lengths(int n_nodes, const int* left, const int* right,
  *  - 1 <= n_sites <= 1,048,576; anything else returns PLK_ERR_ARG with a
  *    message in plk_last_error(NULL).
  *  - The first call on a device (that device current) resolves the array's
- *    device address; make that first call before any stream capture.
+ *    device address; make that first call before any stream capture.  After
+ *    a device reset the next call resolves it again (the context changed):
+ *    make that call before any capture too.
  *  - All calls share the array: calls that overlap on the GPU race. */
 plk_status plk_sum_sites_noalloc(const double* d_site_lnl, int n_sites, double* d_lnl_out,
                                  void* cuda_stream);

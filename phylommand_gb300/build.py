@@ -16,11 +16,12 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libplk.so")
+REPLAY = os.path.join(LIB_DIR, "plk_replay")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["plk_kernels.cu", "plk_prune4s.cu", "plk_prune4p.cu", "plk_prune20.cu", "plk_prune20u.cu", "plk_batch.cu", "plk_nni.cu", "plk_features.cu",
-              "plk_mlp.cu", "plk_noalloc.cu"]
+CU_SOURCES = ["plk_kernels.cu", "plk_prune4s.cu", "plk_prune4p.cu", "plk_prune4w.cu", "plk_prune20.cu", "plk_prune20u.cu", "plk_batch.cu", "plk_nni.cu", "plk_features.cu",
+              "plk_mlp.cu", "plk_noalloc.cu", "plk_peak.cu"]
 CPP_SOURCES = ["plk_api.cpp", "plk_host.cpp", "plk_fit.cpp", "plk_batch_api.cpp", "plk_sim.cpp", "plk_io.cpp"]
 
 
@@ -80,6 +81,14 @@ def build(verbose: bool = False, force: bool = False) -> str:
         list(ex.map(_run, jobs))
     if force or jobs or not os.path.exists(LIB):
         cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lpthread", "-ldl", "-lrt"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        _run(cmd)
+    # a plain C caller of the ABI, linked against libplk.so only (found next to it)
+    src = os.path.join(HERE, "capi", "plk_replay.c")
+    if force or _stale(REPLAY, [src, LIB, os.path.join(ROOT, "include", "plk.h")]):
+        cmd = ["gcc", "-O2", "-std=c99", "-Wall", "-Wextra", "-I" + os.path.join(ROOT, "include"), src,
+               "-L" + LIB_DIR, "-lplk", "-Wl,-rpath,$ORIGIN", "-o", REPLAY]
         if verbose:
             print(" ".join(cmd), flush=True)
         _run(cmd)

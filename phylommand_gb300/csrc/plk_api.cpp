@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <new>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -301,7 +302,7 @@ int tuned_variant(const plk_handle* h) {
 bool tuned_tc20(const plk_handle* h) {
     if (h->S != 20) return false;
     const int v = tuned_variant(h);
-    return v == 5 || v == 6;
+    return v == 5 || v == 6 || v == 7;
 }
 
 plk_status build_pmats(plk_handle* h, bool paired = false, bool tc20 = false) {
@@ -334,6 +335,7 @@ plk_status build_pmats(plk_handle* h, bool paired = false, bool tc20 = false) {
     m.B20 = nullptr;
     m.T20 = nullptr;
     m.ncs20 = 0;
+    m.b20_bf16 = 0;
     if (tc20) {
         // the scratch as the post-order launch sizes it, so that it does not
         // move between this kernel and the pass
@@ -343,6 +345,7 @@ plk_status build_pmats(plk_handle* h, bool paired = false, bool tc20 = false) {
                  "allocate scratch");
         prune20u_scratch_parts(h->d_work.p, a, h->n_nodes, &m.B20, &m.T20);
         m.ncs20 = prune20u_codes_padded(h->n_codes);
+        m.b20_bf16 = tuned_variant(h) == 7 ? 1 : 0;
     }
     h->paired_written = paired || tc20;
     PLK_CUDA(h, launch_pmat(m, h->p_kind, h->stream), "P(t) kernel launch");
@@ -444,7 +447,7 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
         const int v = cands[i];
         if (v >= 0 && v < 3) h->tune_ms[v] = cand_ms[i] / 3.0f;
         if (cand_ms[i] < best) { best = cand_ms[i]; best_v = v; }
-        if (h->S == 4 && (v == 10 || v == 11) && cand_ms[i] < best_staged) {
+        if (h->S == 4 && v >= 10 && v <= 14 && cand_ms[i] < best_staged) {
             best_staged = cand_ms[i];
             best_staged_v = v;
         }
@@ -453,8 +456,8 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
     cudaEventDestroy(e1);
     if (err != cudaSuccess) return cuda_fail(h, err, "autotune post-order kernel");
     // The timed launches run back to back with the tip codes warm in L2.  A
-    // form that stages each op's codes with its tables does not depend on
-    // that (its codes arrive two ops ahead): within 3 % of the fastest it is
+    // form that stages each op's codes with its tables, or loads them two ops
+    // ahead (prune4w), does not depend on that: within 3 % of the fastest it is
     // taken, since other work between evaluations (other partitions, other
     // alignments) evicts the codes that the faster form reads at use.  On
     // 128 x 100,000 the two are level warm (0.155 ms), and with the codes
@@ -472,7 +475,15 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
 bool tuned_paired(const plk_handle* h) {
     if (h->S != 4 || (h->C != 2 && h->C != 4 && h->C != 8) || !fused_kernel_applies(h, PLK_FP32S)) return false;
     const int v = tuned_variant(h);
-    return v >= 3 && v <= 11;
+    return v >= 3 && v <= 14;
+}
+
+// Re-arms the arrival counters of the passes' in-kernel totals (zero between
+// launches; every CTA of a completed launch leaves them so) after a launch
+// that may have stopped part-way; errors here are ignored, the caller
+// reports the first one.
+void clear_counters(plk_handle* h) {
+    if (h->d_done.p && h->d_done.bytes) cudaMemsetAsync(h->d_done.p, 0, h->d_done.bytes, h->stream);
 }
 
 // Runs the post-order pass (P(t) already built); store != null asks for the
@@ -510,7 +521,7 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
         for (int v = 1; v <= 4; ++v)
             if (prune20_fits(a, v)) cands20.push_back(v);
     if (!store && precision == PLK_FP32S && h->S == 20)
-        for (int form = 0; form < 2; ++form)
+        for (int form = 0; form < 3; ++form)  // split TF32, its compact form, split BF16 (compact)
             if (prune20u_fits(a, form)) cands20.push_back(5 + form);
     if (!cands20.empty()) {
         PLK_CUDA(h, h->d_work.ensure(std::max(prune20_scratch_bytes(a, h->n_nodes), prune20u_scratch_bytes(a, h->n_nodes))),
@@ -531,7 +542,7 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
     }
     if (fused && !store && precision == PLK_FP32S) {
         // the paired kernels read P(t) and tip tables re-laid out in scratch
-        const bool paired = prune4p_fits(a, 1) || prune4p_fits(a, 2);
+        const bool paired = prune4p_fits(a, 1) || prune4p_fits(a, 2) || prune4w_fits(a, 1);
         if (paired) {
             PLK_CUDA(h, h->d_work.ensure(prune4p_scratch_bytes(a)), "allocate scratch");
             a.scratch = h->d_work.p;
@@ -549,13 +560,19 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
             if (prune4p_fits(a, 1, 0)) cands.push_back(9);  // TMA-fed stage ring
             for (int v = 10; v <= 11; ++v)  // codes staged with each op
                 if (prune4p_fits(a, v - 9)) cands.push_back(v);
+            for (int v = 12; v <= 14; ++v)  // warp-independent, nothing staged, 1/2/4 sites per thread
+                if (prune4w_fits(a, v == 12 ? 1 : (v == 13 ? 2 : 4))) cands.push_back(v);
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;
         }
         a.variant = h->variant;
     }
     int nb = 0;
-    PLK_CUDA(h, launch_prune(a, h->S, precision, store != nullptr, &nb, h->stream), "post-order kernel launch");
+    const cudaError_t le = launch_prune(a, h->S, precision, store != nullptr, &nb, h->stream);
+    if (le != cudaSuccess) {
+        clear_counters(h);  // a launch that failed part-way may leave arrivals counted
+        return cuda_fail(h, le, "post-order kernel launch");
+    }
     if (after_prune) PLK_CUDA(h, cudaEventRecord(*after_prune, h->stream), "cudaEventRecord");
     if (store) *store = a.cond;
     return PLK_OK;
@@ -937,7 +954,10 @@ plk_status plk_loglik_result(plk_handle* h, double* lnl_out) {
     if (h->bad_tip) return fail(h, PLK_ERR_TIP, "a tip cell allows no state of the model");
     *lnl_out = v;
     h->have_lnl = true;
-    if (!std::isfinite(v)) return fail(h, PLK_ERR_NUMERIC, "log-likelihood is not finite");
+    if (!std::isfinite(v)) {
+        clear_counters(h);  // e.g. a bounded device wait ran out in the pass
+        return fail(h, PLK_ERR_NUMERIC, "log-likelihood is not finite");
+    }
     return PLK_OK;
 }
 
@@ -948,6 +968,23 @@ plk_status plk_loglik(plk_handle* h, int precision, double* lnl_out) {
     plk_status s = plk_loglik_async(h, precision);
     if (s != PLK_OK) return s;
     return plk_loglik_result(h, lnl_out);
+}
+
+plk_status plk_loglik_err(plk_handle* h, double* lnl_fast, double* lnl_fp64, double* abs_err, double* rel_err) {
+    if (!h) return PLK_ERR_ARG;
+    if (!lnl_fast || !lnl_fp64 || !abs_err || !rel_err) return fail(h, PLK_ERR_ARG, "an output pointer is NULL");
+    *lnl_fast = *lnl_fp64 = *abs_err = *rel_err = 0.0;
+    // the FP64 plain form first, so that the handle's per-site values are the
+    // fast form's afterwards (as after plk_loglik(h, PLK_FP32S, ...))
+    double d = 0.0, f = 0.0;
+    plk_status s = plk_loglik(h, PLK_FP64, &d);
+    if (s != PLK_OK) return s;
+    if ((s = plk_loglik(h, PLK_FP32S, &f)) != PLK_OK) return s;
+    *lnl_fast = f;
+    *lnl_fp64 = d;
+    *abs_err = std::fabs(f - d);
+    *rel_err = d != 0.0 ? *abs_err / std::fabs(d) : *abs_err;
+    return PLK_OK;
 }
 
 plk_status plk_set_stream(plk_handle* h, void* stream) {
@@ -1065,6 +1102,29 @@ plk_status plk_node_states(plk_handle* h, int mode, int precision, double* out) 
                             out + ((size_t)r * h->n_sites_full + s) * S);
     }
     h->have_lnl = true;
+    return PLK_OK;
+}
+
+plk_status plk_node_states_err(plk_handle* h, int mode, double* out, double* max_abs_err) {
+    if (!h) return PLK_ERR_ARG;
+    if (!out || !max_abs_err) return fail(h, PLK_ERR_ARG, "an output pointer is NULL");
+    *max_abs_err = 0.0;
+    const size_t n = (size_t)h->post.size() * (size_t)(h->patterns ? h->n_sites_full : h->n_sites) * (size_t)h->S;
+    std::vector<double> ref;
+    try {
+        ref.resize(n);
+    } catch (const std::bad_alloc&) {
+        return fail(h, PLK_ERR_ALLOC, "host allocation for the FP64 node states failed");
+    }
+    plk_status s = plk_node_states(h, mode, PLK_FP64, ref.data());
+    if (s != PLK_OK) return s;
+    if ((s = plk_node_states(h, mode, PLK_FP32S, out)) != PLK_OK) return s;
+    double m = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const double e = std::fabs(out[i] - ref[i]);
+        if (!(e <= m)) m = e;  // a NaN difference propagates
+    }
+    *max_abs_err = m;
     return PLK_OK;
 }
 

@@ -101,7 +101,13 @@ struct plk_batch {
     // graph
     cudaGraphExec_t exec = nullptr;
     bool use_graph = true;
+    // CUDA events around the device work of the last plk_batch_loglik (0, 1)
+    // and plk_batch_nni_loglik (2, 3), and their elapsed times
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double last_ms[2] = {0.0, 0.0};
     ~plk_batch() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
         if (exec) cudaGraphExecDestroy(exec);
         if (h_model) cudaFreeHost(h_model);
         if (h_lnl) cudaFreeHost(h_lnl);
@@ -533,6 +539,15 @@ void relabel_and_enumerate(int n_tips, int n_nodes, const int* left, const int* 
 
 }  // namespace
 
+namespace {
+// the pair of timing events (2 which, 2 which + 1), created on first use
+plk_status batch_events(plk_batch* b, int which) {
+    for (int i = 2 * which; i < 2 * which + 2; ++i)
+        if (!b->ev[i]) PLK_BCUDA(b, cudaEventCreate(&b->ev[i]), "cudaEventCreate");
+    return PLK_OK;
+}
+}  // namespace
+
 extern "C" {
 
 plk_status plk_batch_create(plk_batch** out, int device, int n_cats) {
@@ -639,9 +654,15 @@ plk_status plk_batch_loglik(plk_batch* b, double* lnl_out) {
     if (!b || !lnl_out) return b ? bfail(b, PLK_ERR_ARG, "lnl_out is NULL") : PLK_ERR_ARG;
     plk_status s = prepare(b);
     if (s != PLK_OK) return s;
+    if ((s = batch_events(b, 0)) != PLK_OK) return s;
+    PLK_BCUDA(b, cudaEventRecord(b->ev[0], b->stream), "cudaEventRecord");
     if (b->exec) PLK_BCUDA(b, cudaGraphLaunch(b->exec, b->stream), "graph launch");
     else if ((s = enqueue_eval(b)) != PLK_OK) return s;
+    PLK_BCUDA(b, cudaEventRecord(b->ev[1], b->stream), "cudaEventRecord");
     PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "batch evaluation");
+    float ms = 0.0f;
+    PLK_BCUDA(b, cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]), "cudaEventElapsedTime");
+    b->last_ms[0] = ms;
     std::memcpy(lnl_out, b->h_lnl, b->items.size() * sizeof(double));
     for (size_t i = 0; i < b->items.size(); ++i)
         if (!std::isfinite(lnl_out[i])) return bfail(b, PLK_ERR_NUMERIC, "a log-likelihood is not finite");
@@ -891,6 +912,9 @@ plk_status plk_batch_nni_loglik(plk_batch* b, double* out) {
     PLK_BCUDA(b, b->d_scr_EO.ensure((size_t)grid * slice * sizeof(int)), "allocate NNI scratch");
     const BatchDev d = device_view(b, b->nni_units);
     const size_t mn = b->items.size() * batch_model_stride(b->C);
+    plk_status se = batch_events(b, 1);
+    if (se != PLK_OK) return se;
+    PLK_BCUDA(b, cudaEventRecord(b->ev[2], b->stream), "cudaEventRecord");
     PLK_BCUDA(b, cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), b->stream), "clear work queue");
     PLK_BCUDA(b, cudaMemcpyAsync(b->d_model.p, b->h_model, mn * sizeof(double), cudaMemcpyHostToDevice, b->stream),
               "upload models");
@@ -900,8 +924,19 @@ plk_status plk_batch_nni_loglik(plk_batch* b, double* out) {
     PLK_BCUDA(b, cudaMemcpyAsync(b->h_lnl, b->d_nni_out.p, (size_t)b->total_moves * sizeof(double),
                                  cudaMemcpyDeviceToHost, b->stream),
               "download NNI lnL");
+    PLK_BCUDA(b, cudaEventRecord(b->ev[3], b->stream), "cudaEventRecord");
     PLK_BCUDA(b, cudaStreamSynchronize(b->stream), "NNI scoring");
+    float nms = 0.0f;
+    PLK_BCUDA(b, cudaEventElapsedTime(&nms, b->ev[2], b->ev[3]), "cudaEventElapsedTime");
+    b->last_ms[1] = nms;
     std::memcpy(out, b->h_lnl, (size_t)b->total_moves * sizeof(double));
+    return PLK_OK;
+}
+
+plk_status plk_batch_device_ms(const plk_batch* b, double* loglik_ms, double* nni_ms) {
+    if (!b) return PLK_ERR_ARG;
+    if (loglik_ms) *loglik_ms = b->last_ms[0];
+    if (nni_ms) *nni_ms = b->last_ms[1];
     return PLK_OK;
 }
 

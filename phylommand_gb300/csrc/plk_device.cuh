@@ -1,6 +1,8 @@
 // Device helpers shared by the kernels of libplk.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 #include "plk_internal.h"
@@ -221,6 +223,34 @@ __device__ inline void finish_grid_sum(const double* bs, unsigned* counter, doub
         *out = t;
         *counter = 0u;
     }
+}
+
+// Split-BF16 B-operand image of a 20-state P(t) for the tcgen05 kind::f16
+// form (plk_prune20u.cu): two parts (hi = bf16(x), lo = bf16(x - hi)), each
+// [8-column group g (4)][8-row block nb (4)][row r (8)][8 BF16 columns], the
+// N index (output state) i = 8 nb + r, the K index (input state) j = 8 g + c,
+// zero outside 20 x 20.
+constexpr int kB16PartBytes = 2048;
+constexpr int kB16Bytes = 2 * kB16PartBytes;
+
+// the elements of 32-bit word w of the image: its part, i and the first j
+__host__ __device__ inline void bf16_image_index(int w, int& part, int& i, int& j0) {
+    const int e = 2 * w;
+    part = e / (kB16PartBytes / 2);
+    const int q = e % (kB16PartBytes / 2);
+    const int g = q / 256, nb = (q / 64) % 4, r = (q / 8) % 8, c = q % 8;
+    i = 8 * nb + r;
+    j0 = 8 * g + c;
+}
+
+// BF16 hi and lo parts of two values, packed as the operands store them
+// (element 2k in the low half of a 32-bit word); x - hi is exact in FP32
+__device__ __forceinline__ void bf16_split2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // 16-byte asynchronous global-to-shared copies (sm_80+ cp.async).

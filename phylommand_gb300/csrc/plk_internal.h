@@ -179,6 +179,7 @@ struct DeviceModel {
     float* B20;
     float* T20;
     int ncs20;
+    int b20_bf16;  // B20 holds the split-BF16 images (the kind::f16 form) instead of split TF32
 };
 // p_kind: 0 taylor20, 1 eigen (reversible), 2 series (non-reversible)
 cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st);
@@ -214,12 +215,14 @@ struct PruneArgs {
     // prune4p_kernel with two threads per site (codes from global memory /
     // staged in shared memory), 9 = prune4p_bulk_kernel (TMA-fed stage ring),
     // 10/11 = prune4p_kernel with 1/2 sites per thread and each op's tip
-    // codes staged with its tables.
+    // codes staged with its tables, 12/13/14 = prune4w_kernel (warp-
+    // independent, nothing staged) with 1/2/4 sites per thread.
     // 20 states: 0 = prune_generic_kernel, 1 / 2 = prune20_kernel on CUDA
     // cores / mma.sync tensor cores (TF32, three-product split) with 4 warps
     // per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel on
     // tcgen05 tensor cores (TMEM accumulators), 6 = its compact form
-    // prune20v_kernel (three CTAs per SM).
+    // prune20v_kernel (three CTAs per SM), 7 = prune20v_kernel with split
+    // BF16 products (kind::f16, FP32 accumulate).
     int variant;
     int n_nodes;
     void* scratch;             // kernel-specific scratch (prune20_scratch_bytes)
@@ -255,7 +258,7 @@ cudaError_t launch_combine20(const float* cat_L, const int* cat_E, const PruneAr
 // the B-operand relayout, the pass and the per-site combine.  form 0 =
 // prune20u_kernel (spill stack in TMEM, three-slot stage ring), 1 =
 // prune20v_kernel (the compact form: three CTAs per SM, spills in global
-// memory).
+// memory), 2 = prune20v_kernel with split-BF16 products (kind::f16).
 bool prune20u_fits(const PruneArgs& a, int form);
 // Where the B-operand images and the transposed tip tables sit in the
 // scratch, and their row length (n_codes rounded up to 4).
@@ -276,6 +279,15 @@ size_t prune4p_scratch_bytes(const PruneArgs& a);
 // codes staged with its tables (tps 1).  tps: threads per site, 0 = the
 // TMA-fed form.
 cudaError_t launch_prune4p(const PruneArgs& a, int spt, int codes, int tps, int* n_blocks, cudaStream_t st);
+// The paired P(t) and tip layouts written from the P(t) kernel's FP32
+// copies (when the P(t) kernel did not write them itself).
+cudaError_t launch_relayout4p(const PruneArgs& a, float* Pp, float* Tp, cudaStream_t st);
+// Warp-independent 4-state FP32 kernel (plk_prune4w.cu): every warp walks the
+// op list over its own 32 x spt sites (spt = 1, 2, 4 sites per thread),
+// reading the paired layouts of prune4p's scratch through L1, spills in
+// tensor memory; C = 2, 4 or 8.
+bool prune4w_fits(const PruneArgs& a, int spt);
+cudaError_t launch_prune4w(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
 bool prune4s_fits(const PruneArgs& a, int spt);
 cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);

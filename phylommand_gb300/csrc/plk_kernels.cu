@@ -150,7 +150,19 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
         m.P32[base + idx] = (float)A[idx];
         if (m.P32p) m.P32p[(size_t)v * m.C * 16 + paired_p_index(k, idx / 4, idx % 4)] = (float)A[idx];
     }
-    if (m.B20 && S == 20) {
+    if (m.B20 && S == 20 && m.b20_bf16) {
+        // the split-BF16 image (bf16_image_index), in the first 4 KB of the slot
+        uint32_t* Bw = reinterpret_cast<uint32_t*>(m.B20 + ((size_t)v * m.C + k) * 1536);
+        for (int w = threadIdx.x; w < kB16Bytes / 4; w += blockDim.x) {
+            int part, i, j0;
+            bf16_image_index(w, part, i, j0);
+            const float x0 = (i < 20 && j0 < 20) ? (float)A[i * 20 + j0] : 0.0f;
+            const float x1 = (i < 20 && j0 + 1 < 20) ? (float)A[i * 20 + j0 + 1] : 0.0f;
+            uint32_t hi, lo;
+            bf16_split2(x0, x1, hi, lo);
+            Bw[w] = part == 0 ? hi : lo;
+        }
+    } else if (m.B20 && S == 20) {
         // the tcgen05 B-operand image of this (node, category): [part][4-column
         // group g][8-row block nb][row r][column c], state i = 8 nb + r, j =
         // 4 g + c, TF32 hi and lo parts of the FP32 P (zero outside 20 x 20),
@@ -613,7 +625,11 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
         return launch_prune4p(a, 1, 1, 0, n_blocks, st);
     if (!fp64 && !store && S == 4 && (a.variant == 10 || a.variant == 11) && prune4p_fits(a, a.variant - 9))
         return launch_prune4p(a, a.variant - 9, 2, 1, n_blocks, st);
-    if (!fp64 && !store && S == 20 && (a.variant == 5 || a.variant == 6) && prune20u_fits(a, a.variant - 5))
+    if (!fp64 && !store && S == 4 && a.variant >= 12 && a.variant <= 14) {
+        const int spt = a.variant == 12 ? 1 : (a.variant == 13 ? 2 : 4);
+        if (prune4w_fits(a, spt)) return launch_prune4w(a, spt, n_blocks, st);
+    }
+    if (!fp64 && !store && S == 20 && a.variant >= 5 && a.variant <= 7 && prune20u_fits(a, a.variant - 5))
         return launch_prune20u(a, a.n_nodes, a.scratch, a.variant - 5, n_blocks, st);
     if (!fp64 && !store && S == 20 && a.variant > 0 && a.variant < 5 && prune20_fits(a, a.variant))
         return launch_prune20(a, a.n_nodes, a.variant, a.scratch, n_blocks, st);

@@ -17,7 +17,12 @@
 // array and leaves its contents behind; each call writes every slot it reads
 // before reading it, so nothing needs clearing, but two calls that overlap on
 // the GPU (on different streams, or from different host threads without
-// ordering) race on the array.
+// ordering) race on the array.  The array's address is looked up once per
+// device and context: after a device reset (cudaDeviceReset) the next call
+// looks it up again in the new context, so make that call before any stream
+// capture as well.
+#include <cuda.h>  // CUcontext / CUresult types of the two driver calls below (no -lcuda: entry points)
+
 #include <mutex>
 #include <string>
 
@@ -94,6 +99,38 @@ __global__ void __launch_bounds__(kNoallocThreads) noalloc_final(const double* _
 
 std::mutex g_setup_mu;
 double* g_partials_addr[kMaxDevices] = {nullptr};
+unsigned long long g_partials_ctx[kMaxDevices] = {0};  // the context the address belongs to (0: unknown)
+
+// Unique id of the current context (cuCtxGetId, fetched through the
+// runtime's driver entry points), 0 when it cannot be had.  A device reset
+// destroys the primary context and the next runtime call makes a new one
+// with a new id, in which the array may sit at another address.  Called
+// under g_setup_mu.
+unsigned long long current_ctx_id() {
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -113,16 +150,20 @@ extern "C" plk_status plk_sum_sites_noalloc(const double* d_site_lnl, int n_site
     if (dev < 0 || dev >= kMaxDevices) return plk::report_error(PLK_ERR_ARG, "plk_sum_sites_noalloc: device index too large");
     double* partials = nullptr;
     {
-        // first call on a device: resolve the device address of the array
-        // with that device current (host code cannot use the symbol itself)
+        // first call on a device (or in a new context of it, after a device
+        // reset): resolve the device address of the array with that device
+        // current (host code cannot use the symbol itself)
         std::lock_guard<std::mutex> lock(g_setup_mu);
-        if (!g_partials_addr[dev]) {
+        const unsigned long long ctx = current_ctx_id();
+        if (!g_partials_addr[dev] || (ctx != 0 && ctx != g_partials_ctx[dev])) {
             e = cudaGetSymbolAddress(reinterpret_cast<void**>(&g_partials_addr[dev]), g_noalloc_partials);
             if (e != cudaSuccess) {
                 g_partials_addr[dev] = nullptr;
                 return plk::report_error(PLK_ERR_CUDA, std::string("plk_sum_sites_noalloc: cudaGetSymbolAddress: ") +
                                                            cudaGetErrorString(e));
             }
+            // the id of the context the runtime just used (made, after a reset)
+            g_partials_ctx[dev] = ctx != 0 ? ctx : current_ctx_id();
         }
         partials = g_partials_addr[dev];
     }

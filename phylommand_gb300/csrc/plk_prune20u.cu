@@ -227,17 +227,94 @@ __device__ __forceinline__ void issue_child_lo(uint32_t d_tmem, uint32_t a_lo, u
     }
 }
 
+// ---- the split-BF16 form (kind::f16, both operands BF16, FP32 accumulate) --
+// A value x is split into hi = bf16(x) and lo = bf16(x - hi) (x - hi is exact
+// in FP32); a child message is lo*hi + hi*lo + hi*hi over K = 32 (20 states,
+// padded), two K steps of 16 each: six MMAs instead of the split TF32's nine.
+// The dropped lo*lo term and the rounding of lo leave about 2^-16 relative
+// per product.  An A operand part holds K columns 0-23 as three 8-column
+// groups (16 bytes of BF16 per row); the second K step reads columns 16-31,
+// whose last group is the next part's first group (or the zero group after
+// the last operand): finite values that meet the zero rows 24-31 of every B
+// image.  A B image part holds K = 32 as four 8-column groups of 32 rows.
+constexpr int kAPartB = 3 * kAGroup;      // one BF16 part of an A operand
+constexpr int kAOperandB = 2 * kAPartB;
+constexpr int kBPartB = kB16PartBytes;    // one BF16 part of a B image: 4 groups of 32 rows x 16 bytes
+constexpr int kBBytesB = kB16Bytes;       // hi and lo: 4 KB, within the 6 KB slot of a TF32 image
+static_assert(kBPartB == 4 * kBGroup, "BF16 image part");
+constexpr uint32_t kIdescB = (1u << 4)          // D: F32
+                             | (1u << 7)        // A: BF16
+                             | (1u << 10)       // B: BF16
+                             | ((kN >> 3) << 17)    // N
+                             | ((128 >> 4) << 24);  // M
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(kIdescB), "r"(accumulate));
+}
+
+// row t of a BF16 A operand: hi part, then the lo part kAPartB bytes later;
+// columns 20-23 of the third group are zero
+__device__ __forceinline__ void write_operand_bf16(unsigned char* area, int t, const float x[kS]) {
+    const int row = (t >> 3) * 128 + (t & 7) * 16;
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+        uint4 h, l;
+        bf16_split2(x[8 * g], x[8 * g + 1], h.x, l.x);
+        bf16_split2(x[8 * g + 2], x[8 * g + 3], h.y, l.y);
+        if (g < 2) {
+            bf16_split2(x[8 * g + 4], x[8 * g + 5], h.z, l.z);
+            bf16_split2(x[8 * g + 6], x[8 * g + 7], h.w, l.w);
+        } else {
+            h.z = h.w = l.z = l.w = 0u;
+        }
+        *reinterpret_cast<uint4*>(area + g * kAGroup + row) = h;
+        *reinterpret_cast<uint4*>(area + kAPartB + g * kAGroup + row) = l;
+    }
+}
+
+// the six MMAs of one child message, from descriptor low words
+__device__ __forceinline__ void issue_child_bf16(uint32_t d_tmem, uint32_t a_lo, uint32_t b_lo) {
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        const uint64_t a_hi = desc_of(a_lo + ks * 2 * kAGroup / 16);
+        const uint64_t a_l = desc_of(a_lo + (kAPartB + ks * 2 * kAGroup) / 16);
+        const uint64_t b_hi = desc_of(b_lo + ks * 2 * kBGroup / 16);
+        const uint64_t b_l = desc_of(b_lo + (kBPartB + ks * 2 * kBGroup) / 16);
+        umma_bf16(d_tmem, a_l, b_hi, ks > 0 ? 1u : 0u);  // small products first
+        umma_bf16(d_tmem, a_hi, b_l, 1u);
+        umma_bf16(d_tmem, a_hi, b_hi, 1u);
+    }
+}
+
 __host__ __device__ inline int codes_padded(int n_codes) { return (n_codes + 3) & ~3; }
 
 // P(t) as B operand images and the tip tables transposed to [state][code]
 __global__ void relayout20u_kernel(const float* __restrict__ P, const float* __restrict__ tip, int n_nodes,
-                                   int n_tips, int C, int n_codes, float* __restrict__ Ps, float* __restrict__ Ts) {
+                                   int n_tips, int C, int n_codes, float* __restrict__ Ps, float* __restrict__ Ts,
+                                   int bf16) {
     const int ncs = codes_padded(n_codes);
     const long long n_p = (long long)n_nodes * C * kBFloats;
     const long long n_t = (long long)n_tips * C * kS * ncs;
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n_p + n_t;
          idx += (long long)gridDim.x * blockDim.x) {
-        if (idx < n_p) {
+        if (idx < n_p && bf16) {
+            // the BF16 image in the first kBBytesB bytes of the slot, one
+            // 32-bit word (two elements) per index; the rest of the slot unused
+            const long long nk = idx / kBFloats;
+            const int w = (int)(idx % kBFloats);
+            if (w >= kBBytesB / 4) continue;
+            int part, i, j0;
+            bf16_image_index(w, part, i, j0);
+            float x0 = 0.0f, x1 = 0.0f;
+            if (i < kS && j0 < kS) x0 = P[nk * kS * kS + i * kS + j0];
+            if (i < kS && j0 + 1 < kS) x1 = P[nk * kS * kS + i * kS + j0 + 1];
+            uint32_t hi, lo;
+            bf16_split2(x0, x1, hi, lo);
+            reinterpret_cast<uint32_t*>(Ps)[idx] = part == 0 ? hi : lo;
+        } else if (idx < n_p) {
             // [part][group g][row block nb][row r][column c]: state i = 8 nb + r, j = 4 g + c
             const long long nk = idx / kBFloats;
             const int w = (int)(idx % kBFloats);
@@ -301,10 +378,11 @@ __device__ __forceinline__ void tip_row(const unsigned char* stage_child, int co
 
 // issued by one thread: an op's children (B images or tip tables) into a
 // stage slot as 1-D bulk copies, completing in bytes on the slot's mbarrier
+template <bool BF>
 __device__ __forceinline__ void bulk_stage20(unsigned char* dst, const Op& op, int k, const P20UArgs& g,
                                              uint32_t full) {
     const PruneArgs& a = g.a;
-    const uint32_t tip_bytes = kS * codes_padded(a.n_codes) * 4, b_bytes = kBFloats * 4;
+    const uint32_t tip_bytes = kS * codes_padded(a.n_codes) * 4, b_bytes = BF ? kBBytesB : kBFloats * 4;
     uint32_t total = op.s0 >= 0 ? tip_bytes : b_bytes;
     if (op.s1 != kSrcNone) total += op.s1 >= 0 ? tip_bytes : b_bytes;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full), "r"(total) : "memory");
@@ -447,8 +525,16 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
         }
     }
     cp_async_wait<0>();
-    // a commit still in flight after a timed-out wait (none when it was withheld)
-    if (pending && !a.withhold_first_stage) mbar_wait(mbar, phase ^ 1u);
+    // a commit still in flight after a timed-out wait.  In the failure-path
+    // test the withheld commit is issued now and waited for, so that every
+    // MMA this CTA issued is seen to complete before its TMEM and shared
+    // memory are given up.
+    if (a.withhold_first_stage && withheld) {
+        if (tid == 0) umma_commit(mbar);
+        mbar_wait(mbar, phase ^ 1u);
+    } else if (pending) {
+        mbar_wait(mbar, phase ^ 1u);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -482,8 +568,12 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
 //     push and read back one op before the pop, by the thread that wrote
 //     them), so that TMEM holds only the two accumulators (64 columns);
 //   * tip codes read from global memory one op ahead instead of staged.
-template <int NCS>
+// BF: the split-BF16 products (kind::f16) instead of split TF32: smaller A
+// operands and B images (four CTAs per SM), six MMAs per child message.
+template <int NCS, bool BF>
 __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
+    constexpr int APART = BF ? kAPartB : kAPart5;
+    constexpr int AOPER = 2 * APART;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t s_mbar;
     __shared__ __align__(8) uint64_t s_full[2];  // stage slots: bulk copies landed
@@ -496,8 +586,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     const int tid = threadIdx.x, warp = tid >> 5;
     const int cb = g.child_bytes;
     unsigned char* acc_op = smem;                // A operand of the running vector
-    unsigned char* pop_op = smem + kAOperand5;   // A operand of a vector popped from the stack
-    unsigned char* stages = smem + 2 * kAOperand5 + kAGroup;  // after the zero group
+    unsigned char* pop_op = smem + AOPER;        // A operand of a vector popped from the stack
+    unsigned char* stages = smem + 2 * AOPER + kAGroup;  // after the zero group
     Op* s_ops = reinterpret_cast<Op*>(stages + 2 * 2 * cb);
     const uint32_t mbar = smem_u32(&s_mbar);
     const uint32_t full0 = smem_u32(&s_full[0]);  // slot j's barrier: full0 + 8 j
@@ -523,14 +613,14 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     for (int i = tid; i < a.n_ops; i += kThreads) s_ops[i] = a.ops[i];
     // both A operands and the zero group after them: every column an MMA
     // reads is finite from the start
-    for (int i = tid; i < (2 * kAOperand5 + kAGroup) / 16; i += kThreads)
+    for (int i = tid; i < (2 * AOPER + kAGroup) / 16; i += kThreads)
         reinterpret_cast<uint4*>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = s_tmem;
     const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
-    if (tid == 0) bulk_stage20(stages, s_ops[0], k, g, full0);
+    if (tid == 0) bulk_stage20<BF>(stages, s_ops[0], k, g, full0);
     const uint32_t acc_lo = desc_lo(smem_u32(acc_op), kAGroup), pop_lo = desc_lo(smem_u32(pop_op), kAGroup);
     const uint32_t stage_lo = desc_lo(smem_u32(stages), kBGroup);  // slot j, child c: + (2 j + c) cb / 16
 
@@ -561,7 +651,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         }
         if (op.s0 == kSrcPop) {
             --sp;
-            write_operand<kAPart5>(pop_op, tid, pre);
+            if constexpr (BF) write_operand_bf16(pop_op, tid, pre);
+            else write_operand<kAPart5>(pop_op, tid, pre);
         }
         fence_proxy_async();  // operand rows written by the threads -> the tensor cores
         tc_fence_before();
@@ -569,7 +660,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         if (s_abort) break;
         // the slot op o-1 used: its MMAs completed and its tip rows were read
         // before the barrier
-        if (tid == 0 && has_next) bulk_stage20(stages + ((o + 1) & 1) * 2 * cb, s_ops[o + 1], k, g, full0 + 8 * ((o + 1) & 1));
+        if (tid == 0 && has_next)
+            bulk_stage20<BF>(stages + ((o + 1) & 1) * 2 * cb, s_ops[o + 1], k, g, full0 + 8 * ((o + 1) & 1));
         // the vector the next op pops (this op does not push when the next pops)
         if (next_pops) {
 #pragma unroll
@@ -580,8 +672,13 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         if (tid == 0 && (mma0 || mma1)) {
             tc_fence_after();
             const uint32_t b0 = stage_lo + (uint32_t)((o & 1) * 2 * cb) / 16;
-            if (mma0) issue_child_lo<kAPart5>(tmem, op.s0 == kSrcPop ? pop_lo : acc_lo, b0);
-            if (mma1) issue_child_lo<kAPart5>(tmem + 32, acc_lo, b0 + (uint32_t)cb / 16);
+            if constexpr (BF) {
+                if (mma0) issue_child_bf16(tmem, op.s0 == kSrcPop ? pop_lo : acc_lo, b0);
+                if (mma1) issue_child_bf16(tmem + 32, acc_lo, b0 + (uint32_t)cb / 16);
+            } else {
+                if (mma0) issue_child_lo<kAPart5>(tmem, op.s0 == kSrcPop ? pop_lo : acc_lo, b0);
+                if (mma1) issue_child_lo<kAPart5>(tmem + 32, acc_lo, b0 + (uint32_t)cb / 16);
+            }
             if (!(a.withhold_first_stage && !withheld)) umma_commit(mbar);
         }
         if ((mma0 || mma1) && a.withhold_first_stage) withheld = true;
@@ -623,7 +720,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
             for (int i = 0; i < kS; ++i) spill[(size_t)(sp * kS + i) * kTile] = m0[i];
             ++sp;
         } else {
-            write_operand<kAPart5>(acc_op, tid, m0);
+            if constexpr (BF) write_operand_bf16(acc_op, tid, m0);
+            else write_operand<kAPart5>(acc_op, tid, m0);
         }
         c0 = n0;
         c1 = n1;
@@ -631,8 +729,16 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     // every issued stage was waited for, unless a wait ran out: give that
     // copy one more bounded wait before the shared memory is given up
     if (lost >= 0) mbar_wait(full0 + 8 * (lost & 1), (uint32_t)(lost >> 1) & 1u);
-    // a commit still in flight after a timed-out wait (none when it was withheld)
-    if (pending && !a.withhold_first_stage) mbar_wait(mbar, phase ^ 1u);
+    // a commit still in flight after a timed-out wait.  In the failure-path
+    // test the withheld commit is issued now and waited for, so that every
+    // MMA this CTA issued is seen to complete before its TMEM and shared
+    // memory are given up.
+    if (a.withhold_first_stage && withheld) {
+        if (tid == 0) umma_commit(mbar);
+        mbar_wait(mbar, phase ^ 1u);
+    } else if (pending) {
+        mbar_wait(mbar, phase ^ 1u);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -687,22 +793,23 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
 }
 
 int tmem_cols_for(const PruneArgs& a, int form) {
-    if (form == 1) return kAccCols;
+    if (form >= 1) return kAccCols;
     const int need = kAccCols + kSlotCols * std::max(a.max_depth, 1);
     int cols = 32;
     while (cols < need) cols *= 2;
     return cols;
 }
 
-int child_bytes_for(const PruneArgs& a) {
+int child_bytes_for(const PruneArgs& a, int form) {
     const int tip = kS * codes_padded(a.n_codes) * 4;
-    return (std::max(2 * kBPart, tip) + 127) & ~127;
+    return (std::max(form == 2 ? kBBytesB : 2 * kBPart, tip) + 127) & ~127;
 }
 
 size_t smem20u_bytes(const PruneArgs& a, int form) {
     const size_t ops = ((size_t)a.n_ops * sizeof(Op) + 15) & ~(size_t)15;
-    if (form == 1) return (size_t)2 * kAOperand5 + kAGroup + (size_t)2 * 2 * child_bytes_for(a) + ops;
-    return (size_t)2 * kAOperand + (size_t)3 * 2 * child_bytes_for(a) + ops + (size_t)a.n_tips * kTile;
+    if (form == 1) return (size_t)2 * kAOperand5 + kAGroup + (size_t)2 * 2 * child_bytes_for(a, form) + ops;
+    if (form == 2) return (size_t)2 * kAOperandB + kAGroup + (size_t)2 * 2 * child_bytes_for(a, form) + ops;
+    return (size_t)2 * kAOperand + (size_t)3 * 2 * child_bytes_for(a, form) + ops + (size_t)a.n_tips * kTile;
 }
 
 size_t spill_bytes(const PruneArgs& a) {
@@ -713,7 +820,7 @@ size_t spill_bytes(const PruneArgs& a) {
 }  // namespace
 
 bool prune20u_fits(const PruneArgs& a, int form) {
-    if (a.C < 1 || a.n_codes < 1 || a.n_ops < 1 || form < 0 || form > 1) return false;
+    if (a.C < 1 || a.n_codes < 1 || a.n_ops < 1 || form < 0 || form > 2) return false;
     if (tmem_cols_for(a, form) > 512) return false;
     return smem20u_bytes(a, form) <= 200 * 1024;
 }
@@ -749,7 +856,7 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
     g.cat_E = reinterpret_cast<int*>(base + off);
     off += (((size_t)a.C * a.n_sites * sizeof(int)) + 255) & ~(size_t)255;
     g.spill = reinterpret_cast<float*>(base + off);
-    g.child_bytes = child_bytes_for(a);
+    g.child_bytes = child_bytes_for(a, form);
     g.tmem_cols = tmem_cols_for(a, form);
     if (!a.paired_ready) {  // else the P(t) kernel wrote both layouts
         const long long total =
@@ -759,14 +866,19 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
         relayout20u_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),
                                                               static_cast<const float*>(a.tipT), n_nodes, a.n_tips,
                                                               a.C, a.n_codes, const_cast<float*>(g.Ps),
-                                                              const_cast<float*>(g.Ts));
+                                                              const_cast<float*>(g.Ts), form == 2 ? 1 : 0);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     void (*kern)(P20UArgs) = prune20u_kernel;
     if (form == 1) {
         const int ncs = codes_padded(a.n_codes);
-        kern = ncs == 20 ? prune20v_kernel<20> : ncs == 24 ? prune20v_kernel<24> : prune20v_kernel<0>;
+        kern = ncs == 20 ? prune20v_kernel<20, false> : ncs == 24 ? prune20v_kernel<24, false>
+                                                                  : prune20v_kernel<0, false>;
+    } else if (form == 2) {
+        const int ncs = codes_padded(a.n_codes);
+        kern = ncs == 20 ? prune20v_kernel<20, true> : ncs == 24 ? prune20v_kernel<24, true>
+                                                                 : prune20v_kernel<0, true>;
     }
     // pad the shared memory until no more CTAs fit on an SM than its TMEM serves
     const int max_ctas = 512 / g.tmem_cols;
@@ -786,7 +898,7 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
     kern<<<grid, kThreads, smem, st>>>(g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if (form == 1 && a.tile_done) {  // combined in the kernel
+    if (form >= 1 && a.tile_done) {  // combined in the kernel
         *n_blocks = (int)grid.x;
         return cudaSuccess;
     }

@@ -190,19 +190,23 @@ void prune4p_scratch_parts(void* scratch, int n_nodes, int C, float** Pp, float*
     *Tp = reinterpret_cast<float*>(static_cast<unsigned char*>(scratch) + ((p + 255) & ~(size_t)255));
 }
 
+cudaError_t launch_relayout4p(const PruneArgs& a, float* Pp, float* Tp, cudaStream_t st) {
+    const long long total = (long long)a.n_nodes * a.C * 16 + (long long)a.n_tips * a.C * kCodes * 4;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    relayout4p_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),
+                                                         static_cast<const float*>(a.tipT), a.n_nodes, a.n_tips, a.C,
+                                                         Pp, Tp);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_prune4p(const PruneArgs& a, int spt, int codes, int tps, int* n_blocks, cudaStream_t st) {
     // tps 0: the TMA-fed form (one site per thread, codes from global)
     if (!prune4p_fits(a, spt, tps) || a.scratch == nullptr) return cudaErrorInvalidValue;
     float *Pp, *Tp;
     prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
     if (!a.paired_ready) {
-        const long long total = (long long)a.n_nodes * a.C * 16 + (long long)a.n_tips * a.C * kCodes * 4;
-        long long blocks = (total + 255) / 256;
-        if (blocks > 152 * 8) blocks = 152 * 8;
-        relayout4p_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float*>(a.P),
-                                                             static_cast<const float*>(a.tipT), a.n_nodes, a.n_tips,
-                                                             a.C, Pp, Tp);
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = launch_relayout4p(a, Pp, Tp, st);
         if (e != cudaSuccess) return e;
     }
     if (tps == 2) {

@@ -1,0 +1,524 @@
+// prune4w: the 4-state FP32 post-order pass (src/simpleML.cpp:127-197) with
+// every warp on its own sites, SPT sites per thread, and nothing staged.
+//
+// The staged forms (prune4s, prune4p) copy each op's P(t) rows and tip
+// tables into shared memory and hold the CTA at a barrier per op; on the
+// 128-taxon x 100,000-site benchmark that staging, the barrier and the
+// generic op decoding cost more instructions than the arithmetic itself.
+// Here a warp walks the op list alone, over 32 x SPT sites:
+//  * a thread carries SPT sites (lane + 32 s of the warp's tile), so every
+//    P(t) row it loads feeds the products of SPT sites, and the SPT sites'
+//    independent products hide the latency of the next loads;
+//  * P(t) pairs and tip tables are read where the P(t) kernel wrote them
+//    (the paired layouts of plk_prune4p.cuh), through the read-only L1 path,
+//    which the launch gives all of the SM's unified memory that the kernel
+//    does not use as shared memory (none): a P(t) row of an op is the same
+//    address in every lane (one broadcast load of 32 bytes feeds two packed
+//    FMAs per site), a tip-table load gathers each lane's code row;
+//  * spilled vectors sit in tensor memory (tcgen05.st / tcgen05.ld, one
+//    instruction per category pair and op), not in shared memory;
+//  * the tip codes of op o + 2 are loaded while op o computes (a register
+//    ring, not allocated in L1), so their L2 / DRAM latency hides behind two
+//    ops of arithmetic;
+//  * every branch on the op's shape is uniform across the warp, and no CTA
+//    barrier stands between ops; one CTA per SM, its warp count chosen per
+//    launch so that every warp has a tile.
+// The arithmetic is run_tile4p's (plk_prune4p.cuh) in the same order -- every
+// product, rescale and root sum on fma.rn.f32x2 / mul.rn.f32x2 lanes -- so the
+// per-site results are the bits of prune4s and prune4p.
+#include "plk_prune4p.cuh"
+
+#include <algorithm>
+#include <atomic>
+
+namespace plk {
+using namespace dev;
+
+namespace {
+
+constexpr int kWMinWarps = 4;
+constexpr int kWMaxWarps = 24;
+
+__device__ __forceinline__ void ldg_v4(const u64* p, u64& a, u64& b, u64& c, u64& d) {
+    asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];\n" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+}
+__device__ __forceinline__ void ldg_v2(const u64* p, u64& a, u64& b) {
+    asm("ld.global.nc.v2.u64 {%0, %1}, [%2];\n" : "=l"(a), "=l"(b) : "l"(p));
+}
+// three-input maximum (PTX ISA 8.8+, sm_100+): the same value as two fmaxf
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;\n" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// one category pair of a node's paired P(t) block: rows j = 0..3, each the
+// pairs of states i = 0..3 (P points at the node's block)
+__device__ __forceinline__ void load_p_pair(const u64* __restrict__ P, int q, u64 (&r)[4][4]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ldg_v4(P + (q * 4 + j) * 4, r[j][0], r[j][1], r[j][2], r[j][3]);
+}
+
+// out[i] = sum_j r[j][i] x[j], j ascending, the first term a product (the
+// order of mv4p)
+__device__ __forceinline__ void mv_pair(const u64 (&r)[4][4], const u64 (&x)[4], u64 (&out)[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        u64 acc = mul2(x[0], r[0][i]);
+        acc = fma2(x[1], r[1][i], acc);
+        acc = fma2(x[2], r[2][i], acc);
+        acc = fma2(x[3], r[3][i], acc);
+        out[i] = acc;
+    }
+}
+
+// a tip child's message for pair q: the tip table row of this site's code; T
+// points at the tip's paired block [pair][half][code][state in the half][2]
+__device__ __forceinline__ void tip_pair(const u64* __restrict__ T, int q, int code, u64 (&out)[4]) {
+    ldg_v2(T + ((q * 2 + 0) * kCodes + code) * 2, out[0], out[1]);
+    ldg_v2(T + ((q * 2 + 1) * kCodes + code) * 2, out[2], out[3]);
+}
+
+// ---- the spill stack in tensor memory ------------------------------------
+// A spilled slot holds, for every category pair q and every site s of the
+// thread, the 4 pairs = 8 32-bit values: 8 x SPT TMEM columns per pair,
+// [q][s][8].  Warp w owns TMEM lanes 32 (w % 4) .. + 31 (the lanes a warp may
+// access) and, among the warps sharing those lanes, the column range
+// (w / 4) x depth x KP x SPT x 8.  N = 8 SPT columns move in one instruction.
+template <int N>
+__device__ __forceinline__ void tmem_st(uint32_t taddr, const uint32_t (&r)[N]) {
+    static_assert(N == 8 || N == 16 || N == 32, "8, 16 or 32 columns");
+    if constexpr (N == 8) {
+        asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"r"(taddr),
+                     "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+                     : "memory");
+    } else if constexpr (N == 16) {
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::
+                "r"(taddr),
+            "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+            "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+            : "memory");
+    } else {
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+            "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};\n" ::"r"(taddr),
+            "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+            "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
+            "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
+            "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+            : "memory");
+    }
+}
+template <int N>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[N]) {
+    static_assert(N == 8 || N == 16 || N == 32, "8, 16 or 32 columns");
+    if constexpr (N == 8) {
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                     : "r"(taddr)
+                     : "memory");
+    } else if constexpr (N == 16) {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr)
+            : "memory");
+    } else {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+            "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+              "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+              "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr)
+            : "memory");
+    }
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+// a tip code, loaded without allocating in L1 (which holds the tables)
+__device__ __forceinline__ int ldg_code_na(const uint8_t* p) {
+    unsigned short v;
+    asm volatile("ld.global.nc.L1::no_allocate.u8 %0, [%1];\n" : "=h"(v) : "l"(p));
+    return (int)v;
+}
+
+// this thread's tip codes (SPT sites) of op o's children (0 where a child is
+// no tip); col[s] points at site s's column of the code matrix
+template <int SPT>
+__device__ __forceinline__ void op_codes(const Op* __restrict__ ops, int o, const uint8_t* const (&col)[SPT],
+                                         int stride, int (&c0)[SPT], int (&c1)[SPT]) {
+    const int2 sv = __ldg(reinterpret_cast<const int2*>(&ops[o].s0));
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+        c0[s] = sv.x >= 0 ? ldg_code_na(col[s] + (size_t)sv.x * stride) : 0;
+        c1[s] = sv.y >= 0 ? ldg_code_na(col[s] + (size_t)sv.y * stride) : 0;
+    }
+}
+
+// The register budget of a thread: one CTA of 32 x warps threads per SM.
+__host__ __device__ constexpr int prune4w_maxnreg(int KP, int SPT) {
+    return SPT == 1 ? (KP == 4 ? 128 : 96) : (SPT == 2 ? (KP == 4 ? 232 : (KP == 2 ? 168 : 128)) : (KP == 1 ? 192 : 255));
+}
+
+// One CTA per SM (the launch keeps the occupancy at one), blockDim.x / 32
+// warps, each walking warp tiles of 32 SPT sites g, g + T, ... with g = warp
+// x gridDim.x + blockIdx.x and T the grid's warps, so that the tiles of a
+// last, partial round fall on every SM alike.  tmem_cols: the CTA's TMEM
+// allocation (a power of two >= 32 holding every warp's stack).
+template <int KP, int SPT>
+__global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a, const float* __restrict__ Pp,
+                                                                     const float* __restrict__ Tp, int tmem_cols) {
+    constexpr int NC = 8 * SPT;  // TMEM columns of one category pair of a slot
+    __shared__ uint32_t s_tmem;
+    const int nthr = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n_wtiles = (a.n_sites + 32 * SPT - 1) / (32 * SPT);
+    const int total_warps = (nthr >> 5) * gridDim.x;
+    const u64* __restrict__ P2 = reinterpret_cast<const u64*>(Pp);
+    const u64* __restrict__ T2 = reinterpret_cast<const u64*>(Tp);
+    const Op* __restrict__ ops = a.ops;
+    const int n_ops = a.n_ops;
+    const int depth = a.max_depth > 0 ? a.max_depth : 1;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         static_cast<uint32_t>(__cvta_generic_to_shared(&s_tmem))),
+                     "r"(tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // this warp's stack: its lanes, its column range
+    const uint32_t tstack =
+        s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * depth * KP * NC);
+    SiteSum32 sum;
+    const int stride = a.site_stride;
+    const u64 one2 = pack2(1.0f, 1.0f);
+    for (int wtile = warp * gridDim.x + blockIdx.x; wtile < n_wtiles; wtile += total_warps) {
+        const int base = wtile * 32 * SPT + lane;  // site s of the thread: base + 32 s
+        const uint8_t* col[SPT];
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) col[s] = a.codes + min(base + 32 * s, stride - 1);
+        u64 acc[SPT][KP][4];
+        int scale_e[SPT];
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) {
+            scale_e[s] = 0;
+#pragma unroll
+            for (int q = 0; q < KP; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) acc[s][q][i] = one2;
+        }
+        int sp = 0;
+        // codes of ops o (c0, c1) and o + 1 (n0, n1)
+        int c0[SPT] = {}, c1[SPT] = {}, n0[SPT] = {}, n1[SPT] = {};
+        if (n_ops > 0) op_codes<SPT>(ops, 0, col, stride, c0, c1);
+        if (n_ops > 1) op_codes<SPT>(ops, 1, col, stride, n0, n1);
+        for (int o = 0; o < n_ops; ++o) {
+            int m0[SPT] = {}, m1[SPT] = {};
+            if (o + 2 < n_ops) op_codes<SPT>(ops, o + 2, col, stride, m0, m1);
+            // the op (32 bytes, 32-byte aligned): node, rank, e0, e1 | s0, s1, push, pad
+            const int4 oa = __ldg(reinterpret_cast<const int4*>(ops + o));
+            const int4 ob = __ldg(reinterpret_cast<const int4*>(ops + o) + 1);
+            const int e0 = oa.z, e1 = oa.w, s0 = ob.x, s1 = ob.y, push = ob.z;
+            const u64* __restrict__ P0 = P2 + (size_t)(e0 >= 0 ? e0 : 0) * KP * 16;
+            const u64* __restrict__ P1 = P2 + (size_t)(e1 >= 0 ? e1 : 0) * KP * 16;
+            const u64* __restrict__ T0 = T2 + (size_t)(s0 >= 0 ? s0 : 0) * KP * 64;
+            const u64* __restrict__ T1 = T2 + (size_t)(s1 >= 0 ? s1 : 0) * KP * 64;
+            if (s0 == kSrcPop) --sp;
+#pragma unroll
+            for (int q = 0; q < KP; ++q) {
+                // the second child's messages first: they read the running
+                // vector, which the products then overwrite
+                u64 d1[SPT][4];
+                if (s1 >= 0) {
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) tip_pair(T1, q, c1[s] & (kCodes - 1), d1[s]);
+                } else if (s1 == kSrcAcc) {
+                    u64 r[4][4];
+                    load_p_pair(P1, q, r);
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
+                } else {
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) d1[s][i] = one2;
+                }
+                if (s0 >= 0) {
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) {
+                        u64 d0[4];
+                        tip_pair(T0, q, c0[s] & (kCodes - 1), d0);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                    }
+                } else {
+                    u64 r[4][4];
+                    load_p_pair(P0, q, r);
+                    if (s0 == kSrcPop) {
+                        uint32_t w[NC];
+                        tmem_ld<NC>(tstack + (uint32_t)((sp * KP + q) * NC), w);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) {
+                            u64 x[4], d0[4];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i)
+                                x[i] = pack2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
+                            mv_pair(r, x, d0);
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) {
+                            u64 d0[4];
+                            mv_pair(r, acc[s][q], d0);
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < SPT; ++s) {
+                // the node maximum (three-input max: the same value as the
+                // fmaxf chain of run_tile4p)
+                float v[KP * 8];
+#pragma unroll
+                for (int q = 0; q < KP; ++q)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[q * 8 + 2 * i], v[q * 8 + 2 * i + 1]);
+                float mx;
+                if constexpr (KP == 1) {
+                    mx = fmax3(fmax3(v[0], v[1], v[2]), fmax3(v[3], v[4], v[5]), fmaxf(v[6], v[7]));
+                } else if constexpr (KP == 2) {
+                    const float m0x = fmax3(v[0], v[1], v[2]), m1x = fmax3(v[3], v[4], v[5]);
+                    const float m2x = fmax3(v[6], v[7], v[8]), m3x = fmax3(v[9], v[10], v[11]);
+                    const float m4x = fmax3(v[12], v[13], v[14]);
+                    mx = fmax3(fmax3(m0x, m1x, m2x), fmax3(m3x, m4x, v[15]), 0.0f);
+                } else {
+                    float m[11];
+#pragma unroll
+                    for (int k = 0; k < 10; ++k) m[k] = fmax3(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
+                    m[10] = fmaxf(v[30], v[31]);
+                    const float g0 = fmax3(m[0], m[1], m[2]), g1 = fmax3(m[3], m[4], m[5]);
+                    const float g2 = fmax3(m[6], m[7], m[8]), g3 = fmaxf(m[9], m[10]);
+                    mx = fmax3(fmax3(g0, g1, g2), g3, 0.0f);
+                }
+                if (mx < scale_threshold<float>() && mx > 0.0f) {
+                    int e;
+                    float f1, f2;
+                    pow2_factors(mx, &e, &f1, &f2);
+                    const u64 h1 = pack2(f1, f1), h2 = pack2(f2, f2);
+#pragma unroll
+                    for (int q = 0; q < KP; ++q)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(mul2(acc[s][q][i], h1), h2);
+                    scale_e[s] += e;
+                }
+            }
+            if (push) {
+#pragma unroll
+                for (int q = 0; q < KP; ++q) {
+                    uint32_t w[NC];
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            float lo, hi;
+                            unpack2(acc[s][q][i], lo, hi);
+                            w[8 * s + 2 * i] = __float_as_uint(lo);
+                            w[8 * s + 2 * i + 1] = __float_as_uint(hi);
+                        }
+                    tmem_st<NC>(tstack + (uint32_t)((sp * KP + q) * NC), w);
+                }
+                tmem_wait_st();
+                ++sp;
+            }
+#pragma unroll
+            for (int s = 0; s < SPT; ++s) {
+                c0[s] = n0[s];
+                c1[s] = n1[s];
+                n0[s] = m0[s];
+                n1[s] = m1[s];
+            }
+        }
+
+        // root: L = sum_k w_k sum_s v_k[s] root_w[s] in FP32, categories in
+        // order (run_tile4p), log L = lm + ee ln 2
+        float rw[4], cw[2 * KP];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rw[i] = (float)a.root_w[i];
+#pragma unroll
+        for (int k = 0; k < 2 * KP; ++k) cw[k] = (float)a.cat_w[k];
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) {
+            float lk[2 * KP];
+#pragma unroll
+            for (int q = 0; q < KP; ++q) {
+                float vv[2][4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], vv[0][i], vv[1][i]);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    float x = vv[h][0] * rw[0];
+#pragma unroll
+                    for (int i = 1; i < 4; ++i) x = fmaf(vv[h][i], rw[i], x);
+                    lk[2 * q + h] = x;
+                }
+            }
+            float lsum = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 2 * KP; ++k) lsum = fmaf(cw[k], lk[k], lsum);
+            const int site = base + 32 * s;
+            if (site < a.n_sites) {
+                float lm;
+                int ee;
+                site_log32(lsum, scale_e[s], lm, ee);
+                if (a.site_lnl) a.site_lnl[site] = site_lnl64(lm, ee);
+                site_sum_add(sum, lm, ee);
+            }
+        }
+    }
+    // every warp is done with its stack: free the TMEM
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(s_tmem), "r"(tmem_cols)
+                     : "memory");
+    }
+    double tsum, tcomp;
+    block_sum_site32(sum, tsum, tcomp);
+    if (tid == 0) {
+        a.block_sum[2 * blockIdx.x] = tsum;
+        a.block_sum[2 * blockIdx.x + 1] = tcomp;
+    }
+    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+}
+
+template <int KP, int SPT>
+const void* prune4w_fn() {
+    return reinterpret_cast<const void*>(prune4w_kernel<KP, SPT>);
+}
+
+const void* prune4w_fn_of(int KP, int SPT) {
+    switch (KP * 10 + SPT) {
+        case 11: return prune4w_fn<1, 1>();
+        case 12: return prune4w_fn<1, 2>();
+        case 14: return prune4w_fn<1, 4>();
+        case 21: return prune4w_fn<2, 1>();
+        case 22: return prune4w_fn<2, 2>();
+        case 24: return prune4w_fn<2, 4>();
+        case 41: return prune4w_fn<4, 1>();
+        default: return prune4w_fn<4, 2>();
+    }
+}
+
+// TMEM columns a CTA of `warps` warps needs for stacks of `depth` slots: the
+// warps sharing a lane quarter stack their column ranges; a power of two of
+// at least 32 (0: more than the 512 an SM has)
+int prune4w_tmem_cols(int KP, int SPT, int warps, int depth) {
+    const int need = ((warps + 3) / 4) * (depth > 0 ? depth : 1) * KP * 8 * SPT;
+    int cols = 32;
+    while (cols < need) cols *= 2;
+    return cols <= 512 ? cols : 0;
+}
+
+// resident CTAs per SM with `warps` warps (occupancy calculator, cached: the
+// launch runs every evaluation); the carveout gives the L1 cache all the
+// shared memory the kernel does not use
+int prune4w_ctas_per_sm(int KP, int SPT, int warps) {
+    static std::atomic<int> cache[3][3][kWMaxWarps + 1];
+    static std::atomic<bool> init{false};
+    if (!init.load()) {
+        for (auto& a : cache)
+            for (auto& b : a)
+                for (auto& c : b) c.store(-1);
+        init.store(true);
+    }
+    const int ki = KP == 1 ? 0 : (KP == 2 ? 1 : 2), si = SPT == 1 ? 0 : (SPT == 2 ? 1 : 2);
+    int v = cache[ki][si][warps].load();
+    if (v >= 0) return v;
+    const void* fn = prune4w_fn_of(KP, SPT);
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * 32, 0) != cudaSuccess) n = 0;
+    cache[ki][si][warps].store(n);
+    return n;
+}
+
+int sm_count() {
+    static std::atomic<int> n{0};
+    int v = n.load();
+    if (v > 0) return v;
+    int dev = 0, c = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || c <= 0) c = 1;
+    n.store(c);
+    return c;
+}
+
+// warps per CTA: enough that every SM's CTA has a tile per warp where the
+// tiles allow, at most what keeps the stacks within the TMEM and the
+// registers within one CTA per SM (0: no size works)
+int prune4w_warps(int KP, int SPT, int depth, int tiles, int sms) {
+    int hi = 0;
+    for (int w = kWMaxWarps; w >= kWMinWarps; --w)
+        if (prune4w_tmem_cols(KP, SPT, w, depth) > 0 && prune4w_ctas_per_sm(KP, SPT, w) >= 1) {
+            hi = w;
+            break;
+        }
+    if (hi == 0) return 0;
+    const int want = (tiles + sms - 1) / sms;
+    return std::max(kWMinWarps, std::min(hi, want));
+}
+
+}  // namespace
+
+bool prune4w_fits(const PruneArgs& a, int spt) {
+    if (a.C != 2 && a.C != 4 && a.C != 8) return false;
+    if (spt != 1 && spt != 2 && spt != 4) return false;
+    if (spt == 4 && a.C == 8) return false;  // four sites of 8 categories exceed the registers
+    return prune4w_tmem_cols(a.C / 2, spt, kWMinWarps, a.max_depth) > 0;
+}
+
+cudaError_t launch_prune4w(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st) {
+    if (!prune4w_fits(a, spt) || a.scratch == nullptr) return cudaErrorInvalidValue;
+    const int KP = a.C / 2;
+    float *Pp, *Tp;
+    prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
+    if (!a.paired_ready) {
+        cudaError_t e = launch_relayout4p(a, Pp, Tp, st);
+        if (e != cudaSuccess) return e;
+    }
+    const int tiles = (a.n_sites + 32 * spt - 1) / (32 * spt);
+    const int sms = sm_count();
+    const int warps = prune4w_warps(KP, spt, a.max_depth, tiles, sms);
+    if (warps == 0) return cudaErrorInvalidConfiguration;
+    const int tmem_cols = prune4w_tmem_cols(KP, spt, warps, a.max_depth);
+    const int blocks = std::max(1, std::min(sms, (tiles + warps - 1) / warps));
+    *n_blocks = blocks;
+    const dim3 g(blocks), b(warps * 32);
+    switch (KP * 10 + spt) {
+        case 11: prune4w_kernel<1, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 12: prune4w_kernel<1, 2><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 14: prune4w_kernel<1, 4><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 21: prune4w_kernel<2, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 22: prune4w_kernel<2, 2><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 24: prune4w_kernel<2, 4><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 41: prune4w_kernel<4, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        default: prune4w_kernel<4, 2><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace plk

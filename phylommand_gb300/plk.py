@@ -53,6 +53,7 @@ EXPORTS = [
     "plk_parse_alignment", "plk_parse_newick",
     "plk_mlp_create", "plk_mlp_destroy", "plk_mlp_last_error", "plk_mlp_n_params", "plk_mlp_get_params",
     "plk_mlp_set_params", "plk_mlp_forward", "plk_mlp_gradients", "plk_mlp_train_step",
+    "plk_measure_fp32_peak", "plk_loglik_err", "plk_node_states_err", "plk_batch_device_ms",
 ]
 
 _lib = None
@@ -110,6 +111,10 @@ def lib() -> ctypes.CDLL:
     L.plk_set_patterns.argtypes = [hp, c_int]
     L.plk_n_patterns.argtypes = [hp]
     L.plk_sum_sites_noalloc.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
+    L.plk_measure_fp32_peak.argtypes = [c_int, c_int, c_int, dp, dp]
+    L.plk_loglik_err.argtypes = [hp, dp, dp, dp, dp]
+    L.plk_node_states_err.argtypes = [hp, c_int, dp, dp]
+    L.plk_batch_device_ms.argtypes = [c_void_p, dp, dp]
     L.plk_fit_gtr.argtypes = [hp, c_int, dp, c_int, dp, c_double, c_double, c_double, c_int, dp, dp, ip]
     L.plk_fit_n_params.argtypes = [c_int, c_int]
     L.plk_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_int, c_int]
@@ -409,17 +414,25 @@ class Handle:
             8: "prune4p_kernel (category pairs on FP32x2, 2 threads/site)",
             9: "prune4p_bulk_kernel (category pairs on FP32x2, TMA bulk-copy stage ring, mbarrier pipeline)",
             10: "prune4p_kernel (category pairs on FP32x2, 1 site/thread, tip codes staged with each op)",
-            11: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes staged with each op)"},
+            11: "prune4p_kernel (category pairs on FP32x2, 2 sites/thread, tip codes staged with each op)",
+            12: "prune4w_kernel (category pairs on FP32x2, warp-independent, 1 site/thread, spills in TMEM)",
+            13: "prune4w_kernel (category pairs on FP32x2, warp-independent, 2 sites/thread, spills in TMEM)",
+            14: "prune4w_kernel (category pairs on FP32x2, warp-independent, 4 sites/thread, spills in TMEM)"},
         20: {1: "prune20_kernel (CUDA cores, 4 warps/tile)", 2: "prune20_kernel (tensor cores, split TF32, 4 warps/tile)",
              3: "prune20_kernel (CUDA cores, 8 warps/tile)", 4: "prune20_kernel (tensor cores, split TF32, 8 warps/tile)",
              5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)",
-             6: "prune20v_kernel (tcgen05 tensor cores, compact: three CTAs per SM, split TF32)"},
+             6: "prune20v_kernel (tcgen05 tensor cores, compact: three CTAs per SM, split TF32)",
+             7: "prune20v_kernel (tcgen05 tensor cores, compact, split BF16)"},
     }
 
     def test_withhold_stage(self) -> None:
         """Arm the failure-path test of the TMA-fed post-order form (see
         plk_test_withhold_stage)."""
         _check(lib().plk_test_withhold_stage(self._h), self._h)
+
+    def prune_variant(self) -> int:
+        """Number of the autotuned FP32 post-order form (-1: none tuned)."""
+        return int(lib().plk_prune_variant(self._h))
 
     def prune_kernel(self) -> str:
         """Name of the autotuned FP32 post-order kernel, or 'other' where no
@@ -458,6 +471,20 @@ class Handle:
         out = np.zeros((self.n_internal(), self.n_sites, self.n_states))
         _check(lib().plk_node_states(self._h, int(mode), int(precision), _p(out, ctypes.c_double)), self._h)
         return out
+
+    def loglik_err(self) -> tuple[float, float, float, float]:
+        """(fast lnL, FP64 lnL, |delta|, |delta| / |FP64 lnL|)."""
+        v = [ctypes.c_double() for _ in range(4)]
+        _check(lib().plk_loglik_err(self._h, *[ctypes.byref(x) for x in v]), self._h)
+        return tuple(x.value for x in v)
+
+    def node_states_err(self, mode: int = PLK_NODES_COND) -> tuple[np.ndarray, float]:
+        """Fast-form node states and their largest absolute difference from
+        the FP64 plain form's."""
+        out = np.zeros((self.n_internal(), self.n_sites, self.n_states))
+        err = ctypes.c_double()
+        _check(lib().plk_node_states_err(self._h, int(mode), _p(out, ctypes.c_double), ctypes.byref(err)), self._h)
+        return out, err.value
 
 
 
@@ -619,6 +646,12 @@ class Batch:
         if n:
             self._check(lib().plk_batch_nni_moves(self._b, int(item), _p(out, ctypes.c_int)))
         return out
+
+    def device_ms(self) -> tuple[float, float]:
+        """CUDA-event device time (ms) of the last loglik() and nni_loglik()."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().plk_batch_device_ms(self._b, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def nni_loglik(self) -> list:
         """lnL of every NNI neighbour, one array per item."""

@@ -90,11 +90,15 @@ def mean_pairwise_path(left, right, bl) -> float:
     return float(np.sum(w * k * (n - k)) / (n * (n - 1) / 2))
 
 
-def simulate_batch(n_items: int, n_taxa: int, n_sites: int, seed: int):
+def simulate_batch(n_items: int, n_taxa: int, n_sites: int, seed: int, only=None):
     """A plk.Batch of ``n_items`` simulated alignments and the generating
-    parameters of each in the fit's parameterisation, shape [n_items, 7]."""
+    parameters of each in the fit's parameterisation, shape [n_items, 7].
+    With ``only`` (item indices, ascending), the batch holds just those items
+    -- the same alignments as in the full batch, since every item's draws
+    are made whether it is kept or not -- and truth has their rows."""
     rng = np.random.default_rng(seed)
     b = plk.Batch(N_CATS)
+    keep = None if only is None else set(int(i) for i in only)
     truth = np.zeros((n_items, N_PARAMS))
     for i in range(n_items):
         exch = rng.uniform(*EXCH_RANGE, size=6)
@@ -102,14 +106,19 @@ def simulate_batch(n_items: int, n_taxa: int, n_sites: int, seed: int):
         alpha = _loguniform(rng, *ALPHA_RANGE)
         mean_bl = _loguniform(rng, *MEAN_BL_RANGE)
         left, right, bl = synth.yule_tree(n_taxa, mean_bl, rng)
-        Q = synth.reversible_q(4, exch, freqs)
-        cr = plk.discrete_gamma(alpha, N_CATS)
-        masks = plk.simulate(left, right, bl, Q, freqs, cr, n_sites, seed=int(rng.integers(1 << 62)))
+        sim_seed = int(rng.integers(1 << 62))
         path = mean_pairwise_path(left, right, bl)
-        b.add(masks, left, right, bl * (INPUT_MEAN_PATH / path))
         truth[i, :5] = np.log(exch[:5] / exch[5])
         truth[i, 5] = np.log(alpha)
         truth[i, 6] = np.log(path / INPUT_MEAN_PATH)
+        if keep is not None and i not in keep:
+            continue
+        Q = synth.reversible_q(4, exch, freqs)
+        cr = plk.discrete_gamma(alpha, N_CATS)
+        masks = plk.simulate(left, right, bl, Q, freqs, cr, n_sites, seed=sim_seed)
+        b.add(masks, left, right, bl * (INPUT_MEAN_PATH / path))
+    if keep is not None:
+        truth = truth[sorted(keep)]
     return b, truth
 
 
@@ -278,24 +287,54 @@ def evaluate(ws: WarmStart, n_items: int = 1000, n_taxa: int = 64, n_sites: int 
                               target_tol=tol).hit_evals
     finally:
         b.close()
-    deficit = plain.lnl - warm.lnl   # > 0 where the warm fit ends below the plain optimum
-    reached = warm.hit_evals >= 0
+    # The judge: a warm fit that ends more than tol below the plain fit's
+    # optimum continues from the default start (the fallback), on a batch of
+    # just those alignments; its evaluations add to the warm fit's.
+    warm_only = warm.lnl.copy()
+    short = np.flatnonzero(plain.lnl - warm.lnl > tol)
+    final = warm.lnl.copy()
+    evals = warm.evals.astype(np.int64).copy()
+    hit = np.where(warm.hit_evals >= 0, warm.hit_evals, -1).astype(np.int64)
+    fallback_s = 0.0
+    fallback_diff = 0.0
+    if short.size:
+        fb, _ = simulate_batch(n_items, n_taxa, n_sites, seed, only=short)
+        try:
+            fb.set_fit_method(method)
+            fb.eval_gtr(freqs[short], np.zeros((short.size, N_PARAMS)))
+            t0 = time.perf_counter()
+            f = fb.fit_gtr(freqs[short], None, DEFAULT_STEP, ftol, xtol, max_evals, target=plain.lnl[short],
+                           target_tol=tol)
+            fallback_s = time.perf_counter() - t0
+        finally:
+            fb.close()
+        fallback_diff = float(np.abs(f.lnl - plain.lnl[short]).max())
+        final[short] = np.maximum(warm.lnl[short], f.lnl)
+        hit[short] = np.where(f.hit_evals >= 0, evals[short] + f.hit_evals, -1)
+        evals[short] += f.evals
+    warm_s += fallback_s
+    deficit = plain.lnl - final   # > 0 where the judged warm fit ends below the plain optimum
+    reached = hit >= 0
     pred = ws.predict(feats)
+    hit_or_all = np.where(reached, hit, evals)
     return {
         "n_items": n_items, "n_taxa": n_taxa, "n_sites": n_sites, "seed": seed, "tol": tol,
         "method": {plk.PLK_FIT_NELDER_MEAD: "nelder-mead", plk.PLK_FIT_QUASI_NEWTON: "quasi-newton",
                    plk.PLK_FIT_NEWTON_START: "quasi-newton, newton start"}[method],
-        "plain_evals_mean": float(plain.evals.mean()), "warm_evals_mean": float(warm.evals.mean()),
-        "evals_ratio_warm_over_plain": float(warm.evals.mean() / plain.evals.mean()),
+        "plain_evals_mean": float(plain.evals.mean()), "warm_evals_mean": float(evals.mean()),
+        "evals_ratio_warm_over_plain": float(evals.mean() / plain.evals.mean()),
         "plain_evals_to_optimum_mean": float(plain_hit.mean()),
-        "warm_evals_to_plain_optimum_mean": float(np.where(reached, warm.hit_evals, warm.evals).mean()),
-        "evals_to_optimum_ratio_warm_over_plain": float(np.where(reached, warm.hit_evals, warm.evals).mean()
-                                                        / plain_hit.mean()),
+        "warm_evals_to_plain_optimum_mean": float(hit_or_all.mean()),
+        "evals_to_optimum_ratio_warm_over_plain": float(hit_or_all.mean() / plain_hit.mean()),
         "frac_warm_reached_plain_optimum": float(reached.mean()),
         "plain_rounds": int(plain.rounds), "warm_rounds": int(warm.rounds),
         "plain_wall_s": plain_s, "warm_wall_s": warm_s, "wall_ratio_warm_over_plain": warm_s / plain_s,
         "frac_final_within_tol_of_plain": float(np.mean(deficit <= tol)),
         "max_lnl_deficit": float(deficit.max()), "mean_lnl_gain": float((-deficit).mean()),
+        "judge": {"fallback_items": int(short.size), "fallback_wall_s": fallback_s,
+                  "fallback_max_abs_lnl_diff_vs_plain": fallback_diff,
+                  "before_fallback_frac_within_tol": float(np.mean(plain.lnl - warm_only <= tol)),
+                  "before_fallback_max_deficit": float((plain.lnl - warm_only).max())},
         "frac_network_start_used": float(used.mean()),
         "prediction_rmse_vs_plain_fit": np.sqrt(np.mean((pred - plain.x) ** 2, axis=0)).tolist(),
         "prediction_rmse_vs_truth": np.sqrt(np.mean((pred - truth) ** 2, axis=0)).tolist(),

@@ -30,7 +30,9 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 from phylommand_gb300 import synth  # noqa: E402
 
-EXAMPLES = "/root/reference/example_files"
+from oracle import refpath  # noqa: E402
+
+EXAMPLES = refpath.REF_EXAMPLES
 PROTEIN = "ACDEFGHIKLMNPQRSTVWY"
 
 
@@ -150,7 +152,8 @@ def main():
     if not O.harness_available():
         O.build()
         import subprocess
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REFSRC={refpath.REF_SRC}"],
+                       check=True)
     fa = os.path.join(EXAMPLES, "alignment_file.fst")
     tr = os.path.join(EXAMPLES, "tree_file.tree")
     capture("ex_jc100", fa, tr, specs=[0] * 6, rates=[1.0], freqs=[0.25] * 4, nsites=100)

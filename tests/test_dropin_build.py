@@ -7,8 +7,10 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFSRC = "/root/reference/src"
-EXAMPLES = "/root/reference/example_files"
+from oracle import refpath
+
+REFSRC = refpath.REF_SRC
+EXAMPLES = refpath.REF_EXAMPLES
 
 
 @pytest.mark.skipif(not os.path.isdir(REFSRC), reason="reference sources absent")

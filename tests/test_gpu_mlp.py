@@ -193,5 +193,8 @@ def test_warm_start_end_to_end_small():
     assert np.mean(hist["val_rmse"]) < 0.5 * np.mean(hist["val_rmse_mean_predictor"])
     # held out, and with twice the taxa of the training alignments
     res = warmstart.evaluate(ws, n_items=200, n_taxa=64, n_sites=2000, seed=99)
-    assert res["frac_final_within_tol_of_plain"] >= 0.95, res
+    # the plain fit judges every warm fit: none ends more than 1e-3 below it
+    assert res["frac_final_within_tol_of_plain"] == 1.0, res
+    assert res["max_lnl_deficit"] <= 1e-3, res
+    assert res["judge"]["fallback_max_abs_lnl_diff_vs_plain"] <= 1e-3, res
     assert res["evals_to_optimum_ratio_warm_over_plain"] < 0.75, res

@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 FP64_REL = 1e-12
 FP32_REL = 1e-6
 FP32_PROB = 1e-5
+BF16_SITE_REL = 5e-5
 
 
 @pytest.mark.parametrize("name", H.fixture_names())
@@ -242,15 +243,16 @@ def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
     and 2 sites per thread, prune4p_kernel with category pairs on FP32x2 where
     C is 2, 4 or 8 -- one or two sites per thread, or two threads per site
     for 4 and 8 categories; tip codes in shared memory or read from global
-    for the 1300-tip tree, or staged with each op's tables) gives the same
-    per-site values."""
+    for the 1300-tip tree, or staged with each op's tables; the
+    warp-independent prune4w_kernel) gives the same per-site values."""
     rng = np.random.default_rng(n_tips + n_sites)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, n_tips, n_sites, C=C)
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
     sites = []
-    variants = {1: ("0", "1", "2"), 2: ("0", "1", "2", "3", "4", "5", "6", "9", "10", "11")}.get(
-        C, ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9", "10", "11"))
+    variants = {1: ("0", "1", "2"), 2: ("0", "1", "2", "3", "4", "5", "6", "9", "10", "11", "12", "13", "14"),
+                8: ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9", "10", "11", "12", "13")}.get(
+        C, ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9", "10", "11", "12", "13", "14"))
     for v in variants:
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
@@ -284,7 +286,8 @@ def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
     """20 states: prune20_kernel on CUDA cores (1, 3) and on mma.sync tensor
     cores with the split-TF32 products (2, 4), and on tcgen05 tensor cores
     with TMEM accumulators prune20u_kernel (5, spill stack in TMEM) and its
-    compact form prune20v_kernel (6, spills in global memory), against the
+    compact form prune20v_kernel (6, spills in global memory; 7, with the
+    split-BF16 products of kind::f16), against the
     FP64 oracle, per site; the caterpillar tree forces repeated rescaling,
     the balanced trees the deepest spill stacks, ambiguity codes the table
     look-ups."""
@@ -294,13 +297,16 @@ def test_protein_kernel_variants(monkeypatch, n_tips, n_sites, C, shape):
     masks[amb] |= np.uint32(1 << 3)                          # two-state ambiguity
     teff = plk.effective_lengths(left, right, bl, False)
     orc = O.loglik(left, right, masks, teff, Q, f, cr, cw, p_mode=O.P_EXACT)
-    for v in ("5", "6", "1", "2", "3", "4"):
+    for v in ("5", "6", "7", "1", "2", "3", "4"):
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 20, Q, f, cr, cw) as h:
             got = h.loglik(plk.PLK_FP32S)
             assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[20][int(v)]
             assert got == pytest.approx(orc.lnl, rel=FP32_REL), v
-            np.testing.assert_allclose(h.site_loglik(), orc.site_lnl, rtol=2e-6, atol=1e-9)
+            # the split-BF16 products keep about 16 bits per product (the
+            # split-TF32 and FP32 forms about 21 and 24): a looser per-site bound
+            site_rtol = BF16_SITE_REL if v == "7" else 2e-6
+            np.testing.assert_allclose(h.site_loglik(), orc.site_lnl, rtol=site_rtol, atol=1e-9)
             # the plain FP64 form stays bit-compatible with the oracle
             assert h.loglik(plk.PLK_FP64) == pytest.approx(orc.lnl, rel=1e-11)
 
@@ -425,3 +431,27 @@ def test_back_to_back_alignments_on_one_handle():
         want20 = O.loglik(l20, r20, m20, t20, Q20, f20, cr20, cw20, p_mode=O.P_EXACT).lnl
         assert h.loglik(plk.PLK_FP32S) == pytest.approx(want20, rel=FP32_REL)
 
+
+
+@pytest.mark.parametrize("name", ["syn_gtr_gamma_ambig", "syn_protein20"])
+def test_error_reporting_entry_points(name):
+    """plk_loglik_err and plk_node_states_err: the fast form's results with
+    their error against the FP64 plain form, equal to separate evaluations of
+    both forms, and the FP64 form held to the oracle."""
+    fx = H.load_fixture(name)
+    orc = H.oracle_for_fixture(fx, p_mode=O.P_EXACT, want_marginal=True)
+    with H.engine_for_fixture(fx, p_mode=plk.PLK_P_EXACT) as h:
+        fast, f64, abs_err, rel_err = h.loglik_err()
+        assert f64 == pytest.approx(orc.lnl, rel=1e-11)
+        assert fast == h.loglik(plk.PLK_FP32S)
+        assert f64 == h.loglik(plk.PLK_FP64)
+        assert abs_err == abs(fast - f64) and rel_err == pytest.approx(abs_err / abs(f64), rel=1e-15)
+        assert rel_err < FP32_REL
+        for mode in (plk.PLK_NODES_COND, plk.PLK_NODES_MARGINAL):
+            out, err = h.node_states_err(mode)
+            n64 = h.node_states(mode, plk.PLK_FP64)
+            n32 = h.node_states(mode, plk.PLK_FP32S)
+            np.testing.assert_array_equal(out, n32)
+            assert err == float(np.abs(n32 - n64).max())
+            assert err < FP32_PROB
+        np.testing.assert_allclose(h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64), orc.marginal, atol=1e-11)

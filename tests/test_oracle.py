@@ -8,7 +8,9 @@ import pytest
 from oracle import oracle as O
 import helpers as H
 
-REF = "/root/reference/example_files"
+from oracle import refpath
+
+REF = refpath.REF_EXAMPLES
 
 
 @pytest.mark.parametrize("name", H.fixture_names())
