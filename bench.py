@@ -496,7 +496,8 @@ def run_protein(args):
                 "7": "prune20v_bf16_kernel_protein_64x20k"}
     clocks = ClockSampler(0)
     clocks.start()
-    for v in ("1", "2", "3", "4", "5", "6", "7", "fp64", "auto"):
+    forms = ("1", "2", "3", "4", "5", "6", "7", "fp64", "auto") if args.form is None else (args.form,)
+    for v in forms:
         if v in ("auto", "fp64"):
             os.environ.pop("PLK_PRUNE_VARIANT", None)
         else:
@@ -535,6 +536,10 @@ def run_protein(args):
                 res[v]["ncu"] = prof
     clk = clocks.stop()
     os.environ.pop("PLK_PRUNE_VARIANT", None)
+    if args.form is not None:  # one form only (e.g. for a profile of its kernel)
+        print(json.dumps({"metric": "lnL evals/s (20 states)", "form": args.form, "variants": res, "clocks": clk}),
+              flush=True)
+        return
     best = res["auto"]
     tuned = str(best["variant"])
     prof = load_profile(profiles.get(tuned, "")) or {}
@@ -725,6 +730,7 @@ def main():
     ap.add_argument("--nni-sample", type=int, default=24)
     ap.add_argument("--ws-train", type=int, default=20000)
     ap.add_argument("--ws-eval", type=int, default=1000)
+    ap.add_argument("--form", default=None, help="protein workload: time only this 20-state form (1-7, fp64, auto)")
     args = ap.parse_args()
     if args.workload == "nni":
         run_nni(args)

@@ -52,12 +52,74 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
     return d;
 }
 
-// one category pair of a node's paired P(t) block: rows j = 0..3, each the
-// pairs of states i = 0..3 (P points at the node's block)
-__device__ __forceinline__ void load_p_pair(const u64* __restrict__ P, int q, u64 (&r)[4][4]) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) ldg_v4(P + (q * 4 + j) * 4, r[j][0], r[j][1], r[j][2], r[j][3]);
+__device__ __forceinline__ void lds_v2(uint32_t addr, u64& a, u64& b) {
+    asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];\n" : "=l"(a), "=l"(b) : "r"(addr));
 }
+__device__ __forceinline__ int4 lds_int4(uint32_t addr) {
+    int4 v;
+    asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];\n" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ int2 lds_int2(uint32_t addr) {
+    int2 v;
+    asm volatile("ld.shared.v2.s32 {%0, %1}, [%2];\n" : "=r"(v.x), "=r"(v.y) : "r"(addr));
+    return v;
+}
+
+// Where the paired tables and the ops are read: TS = 0 global memory through
+// the read-only L1 path, TS = 1 shared memory (32-bit addresses).
+//   p_pair(node, q, r): one category pair of a node's paired P(t) block, rows
+//     j = 0..3, each the pairs of states i = 0..3;
+//   tip(tip, q, code, out): pair q of the tip table row of a code
+//     ([pair][half][code][state in the half][2]);
+//   op(o): the op's e0, e1 and s0, s1, push.
+template <int KP, int TS>
+struct Tables;
+
+template <int KP>
+struct Tables<KP, 0> {
+    const u64* P;
+    const u64* T;
+    const Op* ops;
+    __device__ __forceinline__ void p_pair(int node, int q, u64 (&r)[4][4]) const {
+        const u64* b = P + (size_t)node * KP * 16 + q * 16;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ldg_v4(b + j * 4, r[j][0], r[j][1], r[j][2], r[j][3]);
+    }
+    __device__ __forceinline__ void tip(int t, int q, int code, u64 (&out)[4]) const {
+        const u64* b = T + (size_t)t * KP * 64 + (q * 2 * kCodes + code) * 2;
+        ldg_v2(b, out[0], out[1]);
+        ldg_v2(b + kCodes * 2, out[2], out[3]);
+    }
+    __device__ __forceinline__ void op(int o, int4& ea, int4& sb) const {
+        ea = __ldg(reinterpret_cast<const int4*>(ops + o));
+        sb = __ldg(reinterpret_cast<const int4*>(ops + o) + 1);
+    }
+    __device__ __forceinline__ int2 sources(int o) const { return __ldg(reinterpret_cast<const int2*>(&ops[o].s0)); }
+};
+
+template <int KP>
+struct Tables<KP, 1> {
+    uint32_t P, T, ops;  // shared-memory addresses
+    __device__ __forceinline__ void p_pair(int node, int q, u64 (&r)[4][4]) const {
+        const uint32_t b = P + (uint32_t)node * (KP * 128) + q * 128;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            lds_v2(b + j * 32, r[j][0], r[j][1]);
+            lds_v2(b + j * 32 + 16, r[j][2], r[j][3]);
+        }
+    }
+    __device__ __forceinline__ void tip(int t, int q, int code, u64 (&out)[4]) const {
+        const uint32_t b = T + (uint32_t)t * (KP * 512) + q * 512 + (uint32_t)code * 16;
+        lds_v2(b, out[0], out[1]);
+        lds_v2(b + 256, out[2], out[3]);
+    }
+    __device__ __forceinline__ void op(int o, int4& ea, int4& sb) const {
+        ea = lds_int4(ops + (uint32_t)o * 32);
+        sb = lds_int4(ops + (uint32_t)o * 32 + 16);
+    }
+    __device__ __forceinline__ int2 sources(int o) const { return lds_int2(ops + (uint32_t)o * 32 + 16); }
+};
 
 // out[i] = sum_j r[j][i] x[j], j ascending, the first term a product (the
 // order of mv4p)
@@ -70,13 +132,6 @@ __device__ __forceinline__ void mv_pair(const u64 (&r)[4][4], const u64 (&x)[4],
         acc = fma2(x[3], r[3][i], acc);
         out[i] = acc;
     }
-}
-
-// a tip child's message for pair q: the tip table row of this site's code; T
-// points at the tip's paired block [pair][half][code][state in the half][2]
-__device__ __forceinline__ void tip_pair(const u64* __restrict__ T, int q, int code, u64 (&out)[4]) {
-    ldg_v2(T + ((q * 2 + 0) * kCodes + code) * 2, out[0], out[1]);
-    ldg_v2(T + ((q * 2 + 1) * kCodes + code) * 2, out[2], out[3]);
 }
 
 // ---- the spill stack in tensor memory ------------------------------------
@@ -150,10 +205,10 @@ __device__ __forceinline__ int ldg_code_na(const uint8_t* p) {
 
 // this thread's tip codes (SPT sites) of op o's children (0 where a child is
 // no tip); col[s] points at site s's column of the code matrix
-template <int SPT>
-__device__ __forceinline__ void op_codes(const Op* __restrict__ ops, int o, const uint8_t* const (&col)[SPT],
-                                         int stride, int (&c0)[SPT], int (&c1)[SPT]) {
-    const int2 sv = __ldg(reinterpret_cast<const int2*>(&ops[o].s0));
+template <int SPT, class Tab>
+__device__ __forceinline__ void op_codes(const Tab& tab, int o, const uint8_t* const (&col)[SPT], int stride,
+                                         int (&c0)[SPT], int (&c1)[SPT]) {
+    const int2 sv = tab.sources(o);
 #pragma unroll
     for (int s = 0; s < SPT; ++s) {
         c0[s] = sv.x >= 0 ? ldg_code_na(col[s] + (size_t)sv.x * stride) : 0;
@@ -171,7 +226,9 @@ __host__ __device__ constexpr int prune4w_maxnreg(int KP, int SPT) {
 // x gridDim.x + blockIdx.x and T the grid's warps, so that the tiles of a
 // last, partial round fall on every SM alike.  tmem_cols: the CTA's TMEM
 // allocation (a power of two >= 32 holding every warp's stack).
-template <int KP, int SPT>
+// TS = 1: the CTA first copies the tree's paired P(t) and tip tables into
+// shared memory and reads them there (trees whose tables fit).
+template <int KP, int SPT, int TS>
 __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a, const float* __restrict__ Pp,
                                                                      const float* __restrict__ Tp, int tmem_cols) {
     constexpr int NC = 8 * SPT;  // TMEM columns of one category pair of a slot
@@ -179,9 +236,29 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
     const int nthr = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int n_wtiles = (a.n_sites + 32 * SPT - 1) / (32 * SPT);
     const int total_warps = (nthr >> 5) * gridDim.x;
-    const u64* __restrict__ P2 = reinterpret_cast<const u64*>(Pp);
-    const u64* __restrict__ T2 = reinterpret_cast<const u64*>(Tp);
-    const Op* __restrict__ ops = a.ops;
+    extern __shared__ __align__(16) unsigned char wtab[];
+    Tables<KP, TS> tab;
+    if constexpr (TS) {
+        // [P(t) of every node][tip tables of every tip][ops], 16 bytes per
+        // thread and step
+        const size_t pb = (size_t)a.n_nodes * KP * 128, tb = (size_t)a.n_tips * KP * 512;
+        const size_t ob = (size_t)a.n_ops * sizeof(Op);
+        const uint4* gp = reinterpret_cast<const uint4*>(Pp);
+        const uint4* gt = reinterpret_cast<const uint4*>(Tp);
+        const uint4* go = reinterpret_cast<const uint4*>(a.ops);
+        uint4* sp4 = reinterpret_cast<uint4*>(wtab);
+        for (size_t i = threadIdx.x; i < pb / 16; i += blockDim.x) sp4[i] = __ldg(gp + i);
+        for (size_t i = threadIdx.x; i < tb / 16; i += blockDim.x) sp4[pb / 16 + i] = __ldg(gt + i);
+        for (size_t i = threadIdx.x; i < ob / 16; i += blockDim.x) sp4[(pb + tb) / 16 + i] = __ldg(go + i);
+        const uint32_t base = static_cast<uint32_t>(__cvta_generic_to_shared(wtab));
+        tab.P = base;
+        tab.T = base + (uint32_t)pb;
+        tab.ops = base + (uint32_t)(pb + tb);
+    } else {
+        tab.P = reinterpret_cast<const u64*>(Pp);
+        tab.T = reinterpret_cast<const u64*>(Tp);
+        tab.ops = a.ops;
+    }
     const int n_ops = a.n_ops;
     const int depth = a.max_depth > 0 ? a.max_depth : 1;
     if (warp == 0) {
@@ -218,19 +295,15 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
         int sp = 0;
         // codes of ops o (c0, c1) and o + 1 (n0, n1)
         int c0[SPT] = {}, c1[SPT] = {}, n0[SPT] = {}, n1[SPT] = {};
-        if (n_ops > 0) op_codes<SPT>(ops, 0, col, stride, c0, c1);
-        if (n_ops > 1) op_codes<SPT>(ops, 1, col, stride, n0, n1);
+        if (n_ops > 0) op_codes<SPT>(tab, 0, col, stride, c0, c1);
+        if (n_ops > 1) op_codes<SPT>(tab, 1, col, stride, n0, n1);
         for (int o = 0; o < n_ops; ++o) {
             int m0[SPT] = {}, m1[SPT] = {};
-            if (o + 2 < n_ops) op_codes<SPT>(ops, o + 2, col, stride, m0, m1);
+            if (o + 2 < n_ops) op_codes<SPT>(tab, o + 2, col, stride, m0, m1);
             // the op (32 bytes, 32-byte aligned): node, rank, e0, e1 | s0, s1, push, pad
-            const int4 oa = __ldg(reinterpret_cast<const int4*>(ops + o));
-            const int4 ob = __ldg(reinterpret_cast<const int4*>(ops + o) + 1);
+            int4 oa, ob;
+            tab.op(o, oa, ob);
             const int e0 = oa.z, e1 = oa.w, s0 = ob.x, s1 = ob.y, push = ob.z;
-            const u64* __restrict__ P0 = P2 + (size_t)(e0 >= 0 ? e0 : 0) * KP * 16;
-            const u64* __restrict__ P1 = P2 + (size_t)(e1 >= 0 ? e1 : 0) * KP * 16;
-            const u64* __restrict__ T0 = T2 + (size_t)(s0 >= 0 ? s0 : 0) * KP * 64;
-            const u64* __restrict__ T1 = T2 + (size_t)(s1 >= 0 ? s1 : 0) * KP * 64;
             if (s0 == kSrcPop) --sp;
 #pragma unroll
             for (int q = 0; q < KP; ++q) {
@@ -239,10 +312,10 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
                 u64 d1[SPT][4];
                 if (s1 >= 0) {
 #pragma unroll
-                    for (int s = 0; s < SPT; ++s) tip_pair(T1, q, c1[s] & (kCodes - 1), d1[s]);
+                    for (int s = 0; s < SPT; ++s) tab.tip(s1, q, c1[s] & (kCodes - 1), d1[s]);
                 } else if (s1 == kSrcAcc) {
                     u64 r[4][4];
-                    load_p_pair(P1, q, r);
+                    tab.p_pair(e1, q, r);
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
                 } else {
@@ -255,13 +328,13 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
                         u64 d0[4];
-                        tip_pair(T0, q, c0[s] & (kCodes - 1), d0);
+                        tab.tip(s0, q, c0[s] & (kCodes - 1), d0);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
                     }
                 } else {
                     u64 r[4][4];
-                    load_p_pair(P0, q, r);
+                    tab.p_pair(e0, q, r);
                     if (s0 == kSrcPop) {
                         uint32_t w[NC];
                         tmem_ld<NC>(tstack + (uint32_t)((sp * KP + q) * NC), w);
@@ -405,23 +478,41 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
     if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
-template <int KP, int SPT>
+template <int KP, int SPT, int TS>
 const void* prune4w_fn() {
-    return reinterpret_cast<const void*>(prune4w_kernel<KP, SPT>);
+    return reinterpret_cast<const void*>(prune4w_kernel<KP, SPT, TS>);
 }
 
-const void* prune4w_fn_of(int KP, int SPT) {
+const void* prune4w_fn_of(int KP, int SPT, int TS) {
+    if (TS) {
+        switch (KP * 10 + SPT) {
+            case 11: return prune4w_fn<1, 1, 1>();
+            case 12: return prune4w_fn<1, 2, 1>();
+            case 14: return prune4w_fn<1, 4, 1>();
+            case 21: return prune4w_fn<2, 1, 1>();
+            case 22: return prune4w_fn<2, 2, 1>();
+            case 24: return prune4w_fn<2, 4, 1>();
+            case 41: return prune4w_fn<4, 1, 1>();
+            default: return prune4w_fn<4, 2, 1>();
+        }
+    }
     switch (KP * 10 + SPT) {
-        case 11: return prune4w_fn<1, 1>();
-        case 12: return prune4w_fn<1, 2>();
-        case 14: return prune4w_fn<1, 4>();
-        case 21: return prune4w_fn<2, 1>();
-        case 22: return prune4w_fn<2, 2>();
-        case 24: return prune4w_fn<2, 4>();
-        case 41: return prune4w_fn<4, 1>();
-        default: return prune4w_fn<4, 2>();
+        case 11: return prune4w_fn<1, 1, 0>();
+        case 12: return prune4w_fn<1, 2, 0>();
+        case 14: return prune4w_fn<1, 4, 0>();
+        case 21: return prune4w_fn<2, 1, 0>();
+        case 22: return prune4w_fn<2, 2, 0>();
+        case 24: return prune4w_fn<2, 4, 0>();
+        case 41: return prune4w_fn<4, 1, 0>();
+        default: return prune4w_fn<4, 2, 0>();
     }
 }
+
+// shared memory of the TS = 1 form: the tree's paired tables
+size_t prune4w_table_bytes(const PruneArgs& a) {
+    return (size_t)a.n_nodes * (a.C / 2) * 128 + (size_t)a.n_tips * (a.C / 2) * 512 + (size_t)a.n_ops * sizeof(Op);
+}
+constexpr size_t kWMaxTable = kMaxSmem - 8 * 1024;
 
 // TMEM columns a CTA of `warps` warps needs for stacks of `depth` slots: the
 // warps sharing a lane quarter stack their column ranges; a power of two of
@@ -436,7 +527,14 @@ int prune4w_tmem_cols(int KP, int SPT, int warps, int depth) {
 // resident CTAs per SM with `warps` warps (occupancy calculator, cached: the
 // launch runs every evaluation); the carveout gives the L1 cache all the
 // shared memory the kernel does not use
-int prune4w_ctas_per_sm(int KP, int SPT, int warps) {
+int prune4w_ctas_per_sm(int KP, int SPT, int TS, int warps, size_t smem) {
+    if (TS) {  // sized per launch (the tables), not cached
+        const void* fn = prune4w_fn_of(KP, SPT, 1);
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * 32, smem) != cudaSuccess) n = 0;
+        return n;
+    }
     static std::atomic<int> cache[3][3][kWMaxWarps + 1];
     static std::atomic<bool> init{false};
     if (!init.load()) {
@@ -448,7 +546,7 @@ int prune4w_ctas_per_sm(int KP, int SPT, int warps) {
     const int ki = KP == 1 ? 0 : (KP == 2 ? 1 : 2), si = SPT == 1 ? 0 : (SPT == 2 ? 1 : 2);
     int v = cache[ki][si][warps].load();
     if (v >= 0) return v;
-    const void* fn = prune4w_fn_of(KP, SPT);
+    const void* fn = prune4w_fn_of(KP, SPT, 0);
     cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * 32, 0) != cudaSuccess) n = 0;
@@ -469,11 +567,12 @@ int sm_count() {
 
 // warps per CTA: enough that every SM's CTA has a tile per warp where the
 // tiles allow, at most what keeps the stacks within the TMEM and the
-// registers within one CTA per SM (0: no size works)
-int prune4w_warps(int KP, int SPT, int depth, int tiles, int sms) {
+// registers (and, for TS = 1, the tables) within one CTA per SM (0: no size
+// works)
+int prune4w_warps(int KP, int SPT, int TS, size_t smem, int depth, int tiles, int sms) {
     int hi = 0;
     for (int w = kWMaxWarps; w >= kWMinWarps; --w)
-        if (prune4w_tmem_cols(KP, SPT, w, depth) > 0 && prune4w_ctas_per_sm(KP, SPT, w) >= 1) {
+        if (prune4w_tmem_cols(KP, SPT, w, depth) > 0 && prune4w_ctas_per_sm(KP, SPT, TS, w, smem) >= 1) {
             hi = w;
             break;
         }
@@ -484,15 +583,16 @@ int prune4w_warps(int KP, int SPT, int depth, int tiles, int sms) {
 
 }  // namespace
 
-bool prune4w_fits(const PruneArgs& a, int spt) {
+bool prune4w_fits(const PruneArgs& a, int spt, int ts) {
     if (a.C != 2 && a.C != 4 && a.C != 8) return false;
     if (spt != 1 && spt != 2 && spt != 4) return false;
     if (spt == 4 && a.C == 8) return false;  // four sites of 8 categories exceed the registers
+    if (ts && prune4w_table_bytes(a) > kWMaxTable) return false;
     return prune4w_tmem_cols(a.C / 2, spt, kWMinWarps, a.max_depth) > 0;
 }
 
-cudaError_t launch_prune4w(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st) {
-    if (!prune4w_fits(a, spt) || a.scratch == nullptr) return cudaErrorInvalidValue;
+cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int* n_blocks, cudaStream_t st) {
+    if (!prune4w_fits(a, spt, ts) || a.scratch == nullptr) return cudaErrorInvalidValue;
     const int KP = a.C / 2;
     float *Pp, *Tp;
     prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
@@ -500,23 +600,37 @@ cudaError_t launch_prune4w(const PruneArgs& a, int spt, int* n_blocks, cudaStrea
         cudaError_t e = launch_relayout4p(a, Pp, Tp, st);
         if (e != cudaSuccess) return e;
     }
+    const size_t smem = ts ? prune4w_table_bytes(a) : 0;
     const int tiles = (a.n_sites + 32 * spt - 1) / (32 * spt);
     const int sms = sm_count();
-    const int warps = prune4w_warps(KP, spt, a.max_depth, tiles, sms);
+    const int warps = prune4w_warps(KP, spt, ts, smem, a.max_depth, tiles, sms);
     if (warps == 0) return cudaErrorInvalidConfiguration;
     const int tmem_cols = prune4w_tmem_cols(KP, spt, warps, a.max_depth);
     const int blocks = std::max(1, std::min(sms, (tiles + warps - 1) / warps));
     *n_blocks = blocks;
     const dim3 g(blocks), b(warps * 32);
+    if (ts) {
+        switch (KP * 10 + spt) {
+            case 11: prune4w_kernel<1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 12: prune4w_kernel<1, 2, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 14: prune4w_kernel<1, 4, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 21: prune4w_kernel<2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 22: prune4w_kernel<2, 2, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 24: prune4w_kernel<2, 4, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 41: prune4w_kernel<4, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            default: prune4w_kernel<4, 2, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+        }
+        return cudaGetLastError();
+    }
     switch (KP * 10 + spt) {
-        case 11: prune4w_kernel<1, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 12: prune4w_kernel<1, 2><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 14: prune4w_kernel<1, 4><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 21: prune4w_kernel<2, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 22: prune4w_kernel<2, 2><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 24: prune4w_kernel<2, 4><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 41: prune4w_kernel<4, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        default: prune4w_kernel<4, 2><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 11: prune4w_kernel<1, 1, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 12: prune4w_kernel<1, 2, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 14: prune4w_kernel<1, 4, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 21: prune4w_kernel<2, 1, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 22: prune4w_kernel<2, 2, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 24: prune4w_kernel<2, 4, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 41: prune4w_kernel<4, 1, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        default: prune4w_kernel<4, 2, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
     }
     return cudaGetLastError();
 }
