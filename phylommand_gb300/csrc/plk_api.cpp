@@ -447,7 +447,7 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
         const int v = cands[i];
         if (v >= 0 && v < 3) h->tune_ms[v] = cand_ms[i] / 3.0f;
         if (cand_ms[i] < best) { best = cand_ms[i]; best_v = v; }
-        if (h->S == 4 && v >= 10 && v <= 17 && cand_ms[i] < best_staged) {
+        if (h->S == 4 && v >= 10 && v <= 18 && cand_ms[i] < best_staged) {
             best_staged = cand_ms[i];
             best_staged_v = v;
         }
@@ -475,7 +475,7 @@ plk_status autotune_prune(plk_handle* h, PruneArgs a, const std::vector<int>& ca
 bool tuned_paired(const plk_handle* h) {
     if (h->S != 4 || (h->C != 2 && h->C != 4 && h->C != 8) || !fused_kernel_applies(h, PLK_FP32S)) return false;
     const int v = tuned_variant(h);
-    return v >= 3 && v <= 17;
+    return v >= 3 && v <= 18;
 }
 
 // Re-arms the arrival counters of the passes' in-kernel totals (zero between
@@ -560,8 +560,9 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
             if (prune4p_fits(a, 1, 0)) cands.push_back(9);  // TMA-fed stage ring
             for (int v = 10; v <= 11; ++v)  // codes staged with each op
                 if (prune4p_fits(a, v - 9)) cands.push_back(v);
-            for (int v = 12; v <= 17; ++v)  // warp-independent: 1/2/4 sites per thread, tables via L1 or smem
-                if (prune4w_fits(a, (v == 12 || v == 15) ? 1 : ((v == 14 || v == 17) ? 4 : 2), v >= 15 ? 1 : 0))
+            for (int v = 12; v <= 18; ++v)  // warp-independent: 1/2/4 sites per thread, tables via L1 or smem
+                if (prune4w_fits(a, (v == 12 || v == 15) ? 1 : ((v == 14 || v == 17) ? 4 : 2), v >= 15 ? 1 : 0,
+                                 v == 18 ? 2 : 1))
                     cands.push_back(v);
             plk_status s = autotune_prune(h, a, cands);
             if (s != PLK_OK) return s;

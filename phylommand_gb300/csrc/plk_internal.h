@@ -217,7 +217,8 @@ struct PruneArgs {
     // 10/11 = prune4p_kernel with 1/2 sites per thread and each op's tip
     // codes staged with its tables, 12/13/14 = prune4w_kernel (warp-
     // independent, nothing staged) with 1/2/4 sites per thread, 15/16/17 =
-    // the same with 1/2/4 sites per thread and the tables in shared memory.
+    // the same with 1/2/4 sites per thread and the tables in shared memory,
+    // 18 = two sites per thread pair, each thread half of the pairs.
     // 20 states: 0 = prune_generic_kernel, 1 / 2 = prune20_kernel on CUDA
     // cores / mma.sync tensor cores (TF32, three-product split) with 4 warps
     // per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel on
@@ -288,8 +289,9 @@ cudaError_t launch_relayout4p(const PruneArgs& a, float* Pp, float* Tp, cudaStre
 // reading the paired layouts of prune4p's scratch through L1, spills in
 // tensor memory; C = 2, 4 or 8.
 // ts = 1: the tree's tables copied into shared memory first (when they fit).
-bool prune4w_fits(const PruneArgs& a, int spt, int ts = 0);
-cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int* n_blocks, cudaStream_t st);
+// tps = 2: two threads per site, each with half of the category pairs.
+bool prune4w_fits(const PruneArgs& a, int spt, int ts = 0, int tps = 1);
+cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int tps, int* n_blocks, cudaStream_t st);
 // Staged 4-state FP32 kernel (plk_prune4s.cu): spt sites per thread.
 bool prune4s_fits(const PruneArgs& a, int spt);
 cudaError_t launch_prune4s(const PruneArgs& a, int spt, int* n_blocks, cudaStream_t st);

@@ -625,10 +625,10 @@ cudaError_t launch_prune(const PruneArgs& a, int S, int precision, bool store, i
         return launch_prune4p(a, 1, 1, 0, n_blocks, st);
     if (!fp64 && !store && S == 4 && (a.variant == 10 || a.variant == 11) && prune4p_fits(a, a.variant - 9))
         return launch_prune4p(a, a.variant - 9, 2, 1, n_blocks, st);
-    if (!fp64 && !store && S == 4 && a.variant >= 12 && a.variant <= 17) {
+    if (!fp64 && !store && S == 4 && a.variant >= 12 && a.variant <= 18) {
         const int spt = (a.variant == 12 || a.variant == 15) ? 1 : ((a.variant == 14 || a.variant == 17) ? 4 : 2);
-        const int ts = a.variant >= 15 ? 1 : 0;
-        if (prune4w_fits(a, spt, ts)) return launch_prune4w(a, spt, ts, n_blocks, st);
+        const int ts = a.variant >= 15 ? 1 : 0, tps = a.variant == 18 ? 2 : 1;
+        if (prune4w_fits(a, spt, ts, tps)) return launch_prune4w(a, spt, ts, tps, n_blocks, st);
     }
     if (!fp64 && !store && S == 20 && a.variant >= 5 && a.variant <= 7 && prune20u_fits(a, a.variant - 5))
         return launch_prune20u(a, a.n_nodes, a.scratch, a.variant - 5, n_blocks, st);

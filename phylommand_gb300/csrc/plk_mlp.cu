@@ -2,11 +2,11 @@
 // hand-written kernels (absent in the reference, whose optimiser always starts
 // from fixed values, src/treeator.cpp:612-615).
 //
-//  gemm_bf16_kernel  C[M x N] = sum_k A(m, k) B(n, k) with BF16 operands read
+//  gemm_tc_kernel    C[M x N] = sum_k A(m, k) B(n, k) with BF16 operands read
 //                    through arbitrary strides (so one kernel serves X W^T,
-//                    dZ W and dZ^T A), FP32 accumulation on the tensor cores
-//                    (mma.sync m16n8k16), fused epilogue: + bias, ReLU, ReLU
-//                    mask of the backward pass, FP32 and/or BF16 stores.
+//                    dZ W and dZ^T A), FP32 accumulation in tensor memory
+//                    (tcgen05.mma kind::f16), fused epilogue: + bias, ReLU,
+//                    ReLU mask of the backward pass, FP32 and/or BF16 stores.
 //  loss_kernel       mean squared error over the real outputs and its
 //                    gradient (BF16) for the backward GEMMs.
 //  colsum_kernel     bias gradients.
@@ -28,8 +28,6 @@ namespace plk {
 
 namespace {
 
-constexpr int kTM = 64, kTN = 32, kTK = 16;  // block tile; 4 warps of 16 x 32
-
 inline int pad16(int x) { return (x + 15) & ~15; }
 inline int pad64(int x) { return (x + 63) & ~63; }
 
@@ -47,68 +45,6 @@ struct GemmArgs {
     __nv_bfloat16* Cb;           // bf16 out or null
     long long ldc;
 };
-
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    const uint32_t l = (uint32_t)__bfloat16_as_ushort(lo), h = (uint32_t)__bfloat16_as_ushort(hi);
-    return l | (h << 16);
-}
-
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(GemmArgs g) {
-    __shared__ __nv_bfloat16 As[kTM][kTK + 8];
-    __shared__ __nv_bfloat16 Bs[kTN][kTK + 8];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int gid = lane >> 2, tq = lane & 3;
-    const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
-    float acc[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[j][q] = 0.f;
-    const __nv_bfloat16 zero = __float2bfloat16(0.f);
-    for (int k0 = 0; k0 < g.K; k0 += kTK) {
-        for (int i = tid; i < kTM * kTK; i += 128) {
-            const int r = i / kTK, c = i % kTK, m = m0 + r, k = k0 + c;
-            As[r][c] = (m < g.M && k < g.K) ? g.A[m * g.sa_m + k * g.sa_k] : zero;
-        }
-        for (int i = tid; i < kTN * kTK; i += 128) {
-            const int r = i / kTK, c = i % kTK, n = n0 + r, k = k0 + c;
-            Bs[r][c] = (n < g.N && k < g.K) ? g.B[n * g.sb_n + k * g.sb_k] : zero;
-        }
-        __syncthreads();
-        const int r0 = warp * 16;
-        uint32_t a[4];
-        a[0] = pack2(As[r0 + gid][2 * tq], As[r0 + gid][2 * tq + 1]);
-        a[1] = pack2(As[r0 + gid + 8][2 * tq], As[r0 + gid + 8][2 * tq + 1]);
-        a[2] = pack2(As[r0 + gid][2 * tq + 8], As[r0 + gid][2 * tq + 9]);
-        a[3] = pack2(As[r0 + gid + 8][2 * tq + 8], As[r0 + gid + 8][2 * tq + 9]);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int nn = j * 8 + gid;
-            const uint32_t b0 = pack2(Bs[nn][2 * tq], Bs[nn][2 * tq + 1]);
-            const uint32_t b1 = pack2(Bs[nn][2 * tq + 8], Bs[nn][2 * tq + 9]);
-            asm volatile(
-                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                "{%0,%1,%2,%3};\n"
-                : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
-                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int m = m0 + warp * 16 + gid + (q >= 2 ? 8 : 0);
-            const int n = n0 + j * 8 + 2 * tq + (q & 1);
-            if (m >= g.M || n >= g.N) continue;
-            float v = acc[j][q];
-            if (g.bias) v += g.bias[n];
-            if (g.relu) v = fmaxf(v, 0.f);
-            if (g.mask && !(__bfloat162float(g.mask[m * g.smask_m + n]) > 0.f)) v = 0.f;
-            if (g.Cf) g.Cf[m * g.ldc + n] = v;
-            if (g.Cb) g.Cb[m * g.ldc + n] = __float2bfloat16(v);
-        }
-}
 
 // loss = mean over rows < n_rows and columns < n_out of (y - t)^2;
 // dY = 2 (y - t) / (n_rows n_out) as BF16, zero in the padding
@@ -165,9 +101,162 @@ __global__ void to_bf16_padded(const float* x, int rows, int cols, __nv_bfloat16
     out[i] = __float2bfloat16((r < rows && c < cols) ? x[r * cols + c] : 0.f);
 }
 
+// ---------------------------------------------------------------------------
+// The same GEMM on Blackwell's fifth-generation tensor cores: a CTA computes a
+// 128 x 64 tile of C with tcgen05.mma.kind::f16 (BF16 operands, FP32
+// accumulator in TMEM), K in chunks of 64 staged in shared memory in the
+// K-major canonical layout without swizzle (8-row x 16-byte core matrices:
+// 16 bytes = 8 BF16 along K; A: 128 rows, 2 KB between K-adjacent core
+// matrices; B: 64 rows, 1 KB), four MMAs of K = 16 per chunk issued by one
+// thread and completed through an mbarrier (a bounded wait: one that runs
+// out turns the tile's outputs NaN, so the loss shows it).  The operands are
+// gathered through the same arbitrary strides as gemm_bf16_kernel (rows and
+// K beyond the matrix read as zero); the epilogue reads each thread's TMEM
+// lane (its row) and applies the same bias / ReLU / mask.
+// ---------------------------------------------------------------------------
+constexpr int kGM = 128, kGN = 64, kGK = 64;
+constexpr uint32_t kGIdesc = (1u << 4)            // D: F32
+                             | (1u << 7)          // A: BF16
+                             | (1u << 10)         // B: BF16
+                             | ((kGN >> 3) << 17)  // N
+                             | ((kGM >> 4) << 24); // M
+constexpr int kGWaitLimit = 1 << 20;
+
+__device__ __forceinline__ uint64_t g_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__global__ void __launch_bounds__(128, 1) gemm_tc_kernel(GemmArgs g) {
+    __shared__ __align__(128) __nv_bfloat16 As[kGM * kGK];  // [K group 8][row 128][8]
+    __shared__ __align__(128) __nv_bfloat16 Bs[kGN * kGK];  // [K group 8][row 64][8]
+    __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * kGM, n0 = blockIdx.x * kGN;
+    const uint32_t mbar = static_cast<uint32_t>(__cvta_generic_to_shared(&s_mbar));
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         static_cast<uint32_t>(__cvta_generic_to_shared(&s_tmem))),
+                     "r"(kGN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_fail = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = s_tmem;
+    const uint32_t a_base = static_cast<uint32_t>(__cvta_generic_to_shared(As));
+    const uint32_t b_base = static_cast<uint32_t>(__cvta_generic_to_shared(Bs));
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    uint32_t phase = 0;
+    for (int k0 = 0; k0 < g.K; k0 += kGK) {
+        // element (row r, column c) of a chunk at [c / 8][r][c % 8]
+        for (int i = tid; i < kGM * kGK; i += 128) {
+            const int r = i / kGK, c = i % kGK, m = m0 + r, k = k0 + c;
+            As[((c >> 3) * kGM + r) * 8 + (c & 7)] = (m < g.M && k < g.K) ? g.A[m * g.sa_m + k * g.sa_k] : zero;
+        }
+        for (int i = tid; i < kGN * kGK; i += 128) {
+            const int r = i / kGK, c = i % kGK, n = n0 + r, k = k0 + c;
+            Bs[((c >> 3) * kGN + r) * 8 + (c & 7)] = (n < g.N && k < g.K) ? g.B[n * g.sb_n + k * g.sb_k] : zero;
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the rows -> the tensor cores
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int ks = 0; ks < kGK / 16; ++ks) {
+                const uint64_t ad = g_smem_desc(a_base + ks * 2 * (kGM * 16), kGM * 16, 128);
+                const uint64_t bd = g_smem_desc(b_base + ks * 2 * (kGN * 16), kGN * 16, 128);
+                const uint32_t accum = (k0 > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(kGIdesc), "r"(accum));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                         : "memory");
+        }
+        // the chunk's MMAs done: the accumulator is current and the staged
+        // operands may be overwritten (bounded wait)
+        bool done = false;
+        for (int it = 0; it < kGWaitLimit && !done; ++it) {
+            uint32_t ok;
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                "selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(mbar), "r"(phase)
+                : "memory");
+            done = ok != 0;
+        }
+        if (!done) s_fail = 1;
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (s_fail) {
+            // the MMAs whose completion was not seen get one more bounded
+            // wait before the CTA gives up their TMEM and operands
+            for (int it = 0; it < kGWaitLimit; ++it) {
+                uint32_t ok;
+                asm volatile(
+                    "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                    "selp.u32 %0, 1, 0, p;\n}\n"
+                    : "=r"(ok)
+                    : "r"(mbar), "r"(phase ^ 1u)
+                    : "memory");
+                if (ok) break;
+            }
+            break;
+        }
+    }
+    // epilogue: this thread's row m0 + 32 warp + lane is its TMEM lane
+    uint32_t r[kGN];
+    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll
+    for (int c = 0; c < kGN / 16; ++c)
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(r[16 * c + 0]), "=r"(r[16 * c + 1]), "=r"(r[16 * c + 2]), "=r"(r[16 * c + 3]),
+              "=r"(r[16 * c + 4]), "=r"(r[16 * c + 5]), "=r"(r[16 * c + 6]), "=r"(r[16 * c + 7]),
+              "=r"(r[16 * c + 8]), "=r"(r[16 * c + 9]), "=r"(r[16 * c + 10]), "=r"(r[16 * c + 11]),
+              "=r"(r[16 * c + 12]), "=r"(r[16 * c + 13]), "=r"(r[16 * c + 14]), "=r"(r[16 * c + 15])
+            : "r"(taddr + 16 * c)
+            : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    const int m = m0 + 32 * warp + lane;
+    const bool fail = s_fail != 0;
+    if (m < g.M) {
+#pragma unroll
+        for (int c = 0; c < kGN; ++c) {
+            const int n = n0 + c;
+            if (n >= g.N) break;
+            float v = fail ? __int_as_float(0x7fc00000) : __uint_as_float(r[c]);
+            if (g.bias) v += g.bias[n];
+            if (g.relu) v = fmaxf(v, 0.f);
+            if (g.mask && !(__bfloat162float(g.mask[m * g.smask_m + n]) > 0.f)) v = 0.f;
+            if (g.Cf) g.Cf[m * g.ldc + n] = v;
+            if (g.Cb) g.Cb[m * g.ldc + n] = __float2bfloat16(v);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kGN) : "memory");
+    }
+}
+
 cudaError_t gemm(const GemmArgs& g, cudaStream_t st) {
-    dim3 grid((g.N + kTN - 1) / kTN, (g.M + kTM - 1) / kTM);
-    gemm_bf16_kernel<<<grid, 128, 0, st>>>(g);
+    dim3 grid((g.N + kGN - 1) / kGN, (g.M + kGM - 1) / kGM);
+    gemm_tc_kernel<<<grid, 128, 0, st>>>(g);
     return cudaGetLastError();
 }
 

@@ -217,8 +217,10 @@ __device__ __forceinline__ void op_codes(const Tab& tab, int o, const uint8_t* c
 }
 
 // The register budget of a thread: one CTA of 32 x warps threads per SM.
-__host__ __device__ constexpr int prune4w_maxnreg(int KP, int SPT) {
-    return SPT == 1 ? (KP == 4 ? 128 : 96) : (SPT == 2 ? (KP == 4 ? 232 : (KP == 2 ? 168 : 128)) : (KP == 1 ? 192 : 255));
+__host__ __device__ constexpr int prune4w_maxnreg(int KP, int SPT, int TPS) {
+    return TPS == 2 ? (KP == 4 ? 168 : 124)
+                    : (SPT == 1 ? (KP == 4 ? 128 : 96)
+                                : (SPT == 2 ? (KP == 4 ? 232 : (KP == 2 ? 168 : 128)) : (KP == 1 ? 192 : 255)));
 }
 
 // One CTA per SM (the launch keeps the occupancy at one), blockDim.x / 32
@@ -228,13 +230,21 @@ __host__ __device__ constexpr int prune4w_maxnreg(int KP, int SPT) {
 // allocation (a power of two >= 32 holding every warp's stack).
 // TS = 1: the CTA first copies the tree's paired P(t) and tip tables into
 // shared memory and reads them there (trees whose tables fit).
-template <int KP, int SPT, int TS>
-__global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a, const float* __restrict__ Pp,
-                                                                     const float* __restrict__ Tp, int tmem_cols) {
-    constexpr int NC = 8 * SPT;  // TMEM columns of one category pair of a slot
+// TPS = 2: the two lanes 2i, 2i + 1 share sites, each holding half of the
+// category pairs (they exchange their maxima for the rescale, and the even
+// lane adds up the root in category order, so the bits are those of TPS = 1);
+// a warp tile is 16 x SPT sites.
+template <int KP, int SPT, int TS, int TPS>
+__global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneArgs a, const float* __restrict__ Pp,
+                                                                          const float* __restrict__ Tp, int tmem_cols) {
+    constexpr int NC = 8 * SPT;     // TMEM columns of one category pair of a slot
+    constexpr int KPT = KP / TPS;   // category pairs per thread
+    constexpr int WS = 32 / TPS;    // sites per warp and site index s
     __shared__ uint32_t s_tmem;
     const int nthr = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int n_wtiles = (a.n_sites + 32 * SPT - 1) / (32 * SPT);
+    const int half = TPS == 2 ? (lane & 1) : 0;
+    const int q0 = half * KPT;      // this thread's first pair
+    const int n_wtiles = (a.n_sites + WS * SPT - 1) / (WS * SPT);
     const int total_warps = (nthr >> 5) * gridDim.x;
     extern __shared__ __align__(16) unsigned char wtab[];
     Tables<KP, TS> tab;
@@ -273,22 +283,22 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     // this warp's stack: its lanes, its column range
     const uint32_t tstack =
-        s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * depth * KP * NC);
+        s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * depth * KPT * NC);
     SiteSum32 sum;
     const int stride = a.site_stride;
     const u64 one2 = pack2(1.0f, 1.0f);
     for (int wtile = warp * gridDim.x + blockIdx.x; wtile < n_wtiles; wtile += total_warps) {
-        const int base = wtile * 32 * SPT + lane;  // site s of the thread: base + 32 s
+        const int base = wtile * WS * SPT + (TPS == 2 ? lane >> 1 : lane);  // site s: base + WS s
         const uint8_t* col[SPT];
 #pragma unroll
-        for (int s = 0; s < SPT; ++s) col[s] = a.codes + min(base + 32 * s, stride - 1);
-        u64 acc[SPT][KP][4];
+        for (int s = 0; s < SPT; ++s) col[s] = a.codes + min(base + WS * s, stride - 1);
+        u64 acc[SPT][KPT][4];
         int scale_e[SPT];
 #pragma unroll
         for (int s = 0; s < SPT; ++s) {
             scale_e[s] = 0;
 #pragma unroll
-            for (int q = 0; q < KP; ++q)
+            for (int q = 0; q < KPT; ++q)
 #pragma unroll
                 for (int i = 0; i < 4; ++i) acc[s][q][i] = one2;
         }
@@ -306,16 +316,17 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
             const int e0 = oa.z, e1 = oa.w, s0 = ob.x, s1 = ob.y, push = ob.z;
             if (s0 == kSrcPop) --sp;
 #pragma unroll
-            for (int q = 0; q < KP; ++q) {
+            for (int q = 0; q < KPT; ++q) {
+                const int qg = q0 + q;  // the pair in the tables
                 // the second child's messages first: they read the running
                 // vector, which the products then overwrite
                 u64 d1[SPT][4];
                 if (s1 >= 0) {
 #pragma unroll
-                    for (int s = 0; s < SPT; ++s) tab.tip(s1, q, c1[s] & (kCodes - 1), d1[s]);
+                    for (int s = 0; s < SPT; ++s) tab.tip(s1, qg, c1[s] & (kCodes - 1), d1[s]);
                 } else if (s1 == kSrcAcc) {
                     u64 r[4][4];
-                    tab.p_pair(e1, q, r);
+                    tab.p_pair(e1, qg, r);
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
                 } else {
@@ -328,16 +339,16 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
                         u64 d0[4];
-                        tab.tip(s0, q, c0[s] & (kCodes - 1), d0);
+                        tab.tip(s0, qg, c0[s] & (kCodes - 1), d0);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
                     }
                 } else {
                     u64 r[4][4];
-                    tab.p_pair(e0, q, r);
+                    tab.p_pair(e0, qg, r);
                     if (s0 == kSrcPop) {
                         uint32_t w[NC];
-                        tmem_ld<NC>(tstack + (uint32_t)((sp * KP + q) * NC), w);
+                        tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
                         tmem_wait_ld();
 #pragma unroll
                         for (int s = 0; s < SPT; ++s) {
@@ -363,16 +374,16 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
 #pragma unroll
             for (int s = 0; s < SPT; ++s) {
                 // the node maximum (three-input max: the same value as the
-                // fmaxf chain of run_tile4p)
-                float v[KP * 8];
+                // fmaxf chain of run_tile4p; TPS = 2: with the partner's)
+                float v[KPT * 8];
 #pragma unroll
-                for (int q = 0; q < KP; ++q)
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[q * 8 + 2 * i], v[q * 8 + 2 * i + 1]);
                 float mx;
-                if constexpr (KP == 1) {
+                if constexpr (KPT == 1) {
                     mx = fmax3(fmax3(v[0], v[1], v[2]), fmax3(v[3], v[4], v[5]), fmaxf(v[6], v[7]));
-                } else if constexpr (KP == 2) {
+                } else if constexpr (KPT == 2) {
                     const float m0x = fmax3(v[0], v[1], v[2]), m1x = fmax3(v[3], v[4], v[5]);
                     const float m2x = fmax3(v[6], v[7], v[8]), m3x = fmax3(v[9], v[10], v[11]);
                     const float m4x = fmax3(v[12], v[13], v[14]);
@@ -386,13 +397,14 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
                     const float g2 = fmax3(m[6], m[7], m[8]), g3 = fmaxf(m[9], m[10]);
                     mx = fmax3(fmax3(g0, g1, g2), g3, 0.0f);
                 }
+                if constexpr (TPS == 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
                 if (mx < scale_threshold<float>() && mx > 0.0f) {
                     int e;
                     float f1, f2;
                     pow2_factors(mx, &e, &f1, &f2);
                     const u64 h1 = pack2(f1, f1), h2 = pack2(f2, f2);
 #pragma unroll
-                    for (int q = 0; q < KP; ++q)
+                    for (int q = 0; q < KPT; ++q)
 #pragma unroll
                         for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(mul2(acc[s][q][i], h1), h2);
                     scale_e[s] += e;
@@ -400,7 +412,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
             }
             if (push) {
 #pragma unroll
-                for (int q = 0; q < KP; ++q) {
+                for (int q = 0; q < KPT; ++q) {
                     uint32_t w[NC];
 #pragma unroll
                     for (int s = 0; s < SPT; ++s)
@@ -411,7 +423,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
                             w[8 * s + 2 * i] = __float_as_uint(lo);
                             w[8 * s + 2 * i + 1] = __float_as_uint(hi);
                         }
-                    tmem_st<NC>(tstack + (uint32_t)((sp * KP + q) * NC), w);
+                    tmem_st<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
                 }
                 tmem_wait_st();
                 ++sp;
@@ -434,9 +446,9 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
         for (int k = 0; k < 2 * KP; ++k) cw[k] = (float)a.cat_w[k];
 #pragma unroll
         for (int s = 0; s < SPT; ++s) {
-            float lk[2 * KP];
+            float lk[2 * KP];  // this thread's categories first (the even lane's are 0 .. 2 KPT - 1)
 #pragma unroll
-            for (int q = 0; q < KP; ++q) {
+            for (int q = 0; q < KPT; ++q) {
                 float vv[2][4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], vv[0][i], vv[1][i]);
@@ -448,11 +460,15 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
                     lk[2 * q + h] = x;
                 }
             }
+            if constexpr (TPS == 2) {
+#pragma unroll
+                for (int k = 0; k < 2 * KPT; ++k) lk[2 * KPT + k] = __shfl_xor_sync(0xffffffffu, lk[k], 1);
+            }
             float lsum = 0.0f;
 #pragma unroll
             for (int k = 0; k < 2 * KP; ++k) lsum = fmaf(cw[k], lk[k], lsum);
-            const int site = base + 32 * s;
-            if (site < a.n_sites) {
+            const int site = base + WS * s;
+            if (site < a.n_sites && half == 0) {
                 float lm;
                 int ee;
                 site_log32(lsum, scale_e[s], lm, ee);
@@ -478,12 +494,13 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT)) prune4w_kernel(PruneArgs a
     if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
 }
 
-template <int KP, int SPT, int TS>
+template <int KP, int SPT, int TS, int TPS = 1>
 const void* prune4w_fn() {
-    return reinterpret_cast<const void*>(prune4w_kernel<KP, SPT, TS>);
+    return reinterpret_cast<const void*>(prune4w_kernel<KP, SPT, TS, TPS>);
 }
 
-const void* prune4w_fn_of(int KP, int SPT, int TS) {
+const void* prune4w_fn_of(int KP, int SPT, int TS, int TPS = 1) {
+    if (TPS == 2) return KP == 2 ? prune4w_fn<2, 2, 1, 2>() : prune4w_fn<4, 2, 1, 2>();
     if (TS) {
         switch (KP * 10 + SPT) {
             case 11: return prune4w_fn<1, 1, 1>();
@@ -517,8 +534,8 @@ constexpr size_t kWMaxTable = kMaxSmem - 8 * 1024;
 // TMEM columns a CTA of `warps` warps needs for stacks of `depth` slots: the
 // warps sharing a lane quarter stack their column ranges; a power of two of
 // at least 32 (0: more than the 512 an SM has)
-int prune4w_tmem_cols(int KP, int SPT, int warps, int depth) {
-    const int need = ((warps + 3) / 4) * (depth > 0 ? depth : 1) * KP * 8 * SPT;
+int prune4w_tmem_cols(int KP, int SPT, int warps, int depth, int TPS = 1) {
+    const int need = ((warps + 3) / 4) * (depth > 0 ? depth : 1) * (KP / TPS) * 8 * SPT;
     int cols = 32;
     while (cols < need) cols *= 2;
     return cols <= 512 ? cols : 0;
@@ -527,9 +544,9 @@ int prune4w_tmem_cols(int KP, int SPT, int warps, int depth) {
 // resident CTAs per SM with `warps` warps (occupancy calculator, cached: the
 // launch runs every evaluation); the carveout gives the L1 cache all the
 // shared memory the kernel does not use
-int prune4w_ctas_per_sm(int KP, int SPT, int TS, int warps, size_t smem) {
+int prune4w_ctas_per_sm(int KP, int SPT, int TS, int warps, size_t smem, int TPS = 1) {
     if (TS) {  // sized per launch (the tables), not cached
-        const void* fn = prune4w_fn_of(KP, SPT, 1);
+        const void* fn = prune4w_fn_of(KP, SPT, 1, TPS);
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * 32, smem) != cudaSuccess) n = 0;
@@ -569,10 +586,10 @@ int sm_count() {
 // tiles allow, at most what keeps the stacks within the TMEM and the
 // registers (and, for TS = 1, the tables) within one CTA per SM (0: no size
 // works)
-int prune4w_warps(int KP, int SPT, int TS, size_t smem, int depth, int tiles, int sms) {
+int prune4w_warps(int KP, int SPT, int TS, int TPS, size_t smem, int depth, int tiles, int sms) {
     int hi = 0;
     for (int w = kWMaxWarps; w >= kWMinWarps; --w)
-        if (prune4w_tmem_cols(KP, SPT, w, depth) > 0 && prune4w_ctas_per_sm(KP, SPT, TS, w, smem) >= 1) {
+        if (prune4w_tmem_cols(KP, SPT, w, depth, TPS) > 0 && prune4w_ctas_per_sm(KP, SPT, TS, w, smem, TPS) >= 1) {
             hi = w;
             break;
         }
@@ -583,16 +600,19 @@ int prune4w_warps(int KP, int SPT, int TS, size_t smem, int depth, int tiles, in
 
 }  // namespace
 
-bool prune4w_fits(const PruneArgs& a, int spt, int ts) {
+bool prune4w_fits(const PruneArgs& a, int spt, int ts, int tps) {
     if (a.C != 2 && a.C != 4 && a.C != 8) return false;
     if (spt != 1 && spt != 2 && spt != 4) return false;
+    if (tps == 2 && (a.C == 2 || spt != 2 || !ts)) return false;  // instantiated: two sites, shared tables
+    if (tps == 2)
+        return prune4w_table_bytes(a) <= kWMaxTable && prune4w_tmem_cols(a.C / 2, spt, kWMinWarps, a.max_depth, 2) > 0;
     if (spt == 4 && a.C == 8) return false;  // four sites of 8 categories exceed the registers
     if (ts && prune4w_table_bytes(a) > kWMaxTable) return false;
     return prune4w_tmem_cols(a.C / 2, spt, kWMinWarps, a.max_depth) > 0;
 }
 
-cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int* n_blocks, cudaStream_t st) {
-    if (!prune4w_fits(a, spt, ts) || a.scratch == nullptr) return cudaErrorInvalidValue;
+cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int tps, int* n_blocks, cudaStream_t st) {
+    if (!prune4w_fits(a, spt, ts, tps) || a.scratch == nullptr) return cudaErrorInvalidValue;
     const int KP = a.C / 2;
     float *Pp, *Tp;
     prune4p_scratch_parts(a.scratch, a.n_nodes, a.C, &Pp, &Tp);
@@ -601,36 +621,42 @@ cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int* n_blocks, c
         if (e != cudaSuccess) return e;
     }
     const size_t smem = ts ? prune4w_table_bytes(a) : 0;
-    const int tiles = (a.n_sites + 32 * spt - 1) / (32 * spt);
+    const int ws = 32 / tps * spt;  // sites per warp tile
+    const int tiles = (a.n_sites + ws - 1) / ws;
     const int sms = sm_count();
-    const int warps = prune4w_warps(KP, spt, ts, smem, a.max_depth, tiles, sms);
+    const int warps = prune4w_warps(KP, spt, ts, tps, smem, a.max_depth, tiles, sms);
     if (warps == 0) return cudaErrorInvalidConfiguration;
-    const int tmem_cols = prune4w_tmem_cols(KP, spt, warps, a.max_depth);
+    const int tmem_cols = prune4w_tmem_cols(KP, spt, warps, a.max_depth, tps);
     const int blocks = std::max(1, std::min(sms, (tiles + warps - 1) / warps));
     *n_blocks = blocks;
     const dim3 g(blocks), b(warps * 32);
+    if (tps == 2) {
+        if (KP == 2) prune4w_kernel<2, 2, 1, 2><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols);
+        else prune4w_kernel<4, 2, 1, 2><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols);
+        return cudaGetLastError();
+    }
     if (ts) {
         switch (KP * 10 + spt) {
-            case 11: prune4w_kernel<1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 12: prune4w_kernel<1, 2, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 14: prune4w_kernel<1, 4, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 21: prune4w_kernel<2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 22: prune4w_kernel<2, 2, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 24: prune4w_kernel<2, 4, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 41: prune4w_kernel<4, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            default: prune4w_kernel<4, 2, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 11: prune4w_kernel<1, 1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 12: prune4w_kernel<1, 2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 14: prune4w_kernel<1, 4, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 21: prune4w_kernel<2, 1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 22: prune4w_kernel<2, 2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 24: prune4w_kernel<2, 4, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            case 41: prune4w_kernel<4, 1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
+            default: prune4w_kernel<4, 2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
         }
         return cudaGetLastError();
     }
     switch (KP * 10 + spt) {
-        case 11: prune4w_kernel<1, 1, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 12: prune4w_kernel<1, 2, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 14: prune4w_kernel<1, 4, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 21: prune4w_kernel<2, 1, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 22: prune4w_kernel<2, 2, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 24: prune4w_kernel<2, 4, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 41: prune4w_kernel<4, 1, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        default: prune4w_kernel<4, 2, 0><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 11: prune4w_kernel<1, 1, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 12: prune4w_kernel<1, 2, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 14: prune4w_kernel<1, 4, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 21: prune4w_kernel<2, 1, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 22: prune4w_kernel<2, 2, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 24: prune4w_kernel<2, 4, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        case 41: prune4w_kernel<4, 1, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
+        default: prune4w_kernel<4, 2, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
     }
     return cudaGetLastError();
 }

@@ -420,7 +420,8 @@ class Handle:
             14: "prune4w_kernel (category pairs on FP32x2, warp-independent, 4 sites/thread, spills in TMEM)",
             15: "prune4w_kernel (category pairs on FP32x2, warp-independent, 1 site/thread, tables in shared memory)",
             16: "prune4w_kernel (category pairs on FP32x2, warp-independent, 2 sites/thread, tables in shared memory)",
-            17: "prune4w_kernel (category pairs on FP32x2, warp-independent, 4 sites/thread, tables in shared memory)"},
+            17: "prune4w_kernel (category pairs on FP32x2, warp-independent, 4 sites/thread, tables in shared memory)",
+            18: "prune4w_kernel (category pairs on FP32x2, warp-independent, 2 sites per 2 threads, tables in shared memory)"},
         20: {1: "prune20_kernel (CUDA cores, 4 warps/tile)", 2: "prune20_kernel (tensor cores, split TF32, 4 warps/tile)",
              3: "prune20_kernel (CUDA cores, 8 warps/tile)", 4: "prune20_kernel (tensor cores, split TF32, 8 warps/tile)",
              5: "prune20u_kernel (tcgen05 tensor cores, TMEM accumulators, split TF32)",

@@ -255,7 +255,7 @@ def test_fp32_kernel_variants_agree(monkeypatch, n_tips, n_sites, C):
         C, ("0", "1", "2", "3", "4", "5", "6", "7", "8", "9", "10", "11", "12", "13", "14"))
     n_nodes = 2 * n_tips - 1
     if C > 1 and n_nodes * (C // 2) * 128 + n_tips * (C // 2) * 512 + (n_tips - 1) * 32 <= 219 * 1024:
-        variants = variants + ("15", "16") + (("17",) if C < 8 else ())  # the tables fit in shared memory
+        variants = variants + ("15", "16") + (("17",) if C < 8 else ()) + (("18",) if C > 2 else ())  # tables fit
     for v in variants:
         monkeypatch.setenv("PLK_PRUNE_VARIANT", v)
         with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
