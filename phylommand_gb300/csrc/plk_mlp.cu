@@ -107,14 +107,14 @@ __global__ void to_bf16_padded(const float* x, int rows, int cols, __nv_bfloat16
 // accumulator in TMEM), K in chunks of 64 staged in shared memory in the
 // K-major canonical layout without swizzle (8-row x 16-byte core matrices:
 // 16 bytes = 8 BF16 along K; A: 128 rows, 2 KB between K-adjacent core
-// matrices; B: 64 rows, 1 KB), four MMAs of K = 16 per chunk issued by one
+// matrices; B: 32 rows, 512 bytes), four MMAs of K = 16 per chunk issued by one
 // thread and completed through an mbarrier (a bounded wait: one that runs
 // out turns the tile's outputs NaN, so the loss shows it).  The operands are
 // gathered through the same arbitrary strides as gemm_bf16_kernel (rows and
 // K beyond the matrix read as zero); the epilogue reads each thread's TMEM
 // lane (its row) and applies the same bias / ReLU / mask.
 // ---------------------------------------------------------------------------
-constexpr int kGM = 128, kGN = 64, kGK = 64;
+constexpr int kGM = 128, kGN = 32, kGK = 64;  // N = 32: more CTAs for the network's small GEMMs
 constexpr uint32_t kGIdesc = (1u << 4)            // D: F32
                              | (1u << 7)          // A: BF16
                              | (1u << 10)         // B: BF16
@@ -129,7 +129,7 @@ __device__ __forceinline__ uint64_t g_smem_desc(uint32_t addr, uint32_t lbo, uin
 
 __global__ void __launch_bounds__(128, 1) gemm_tc_kernel(GemmArgs g) {
     __shared__ __align__(128) __nv_bfloat16 As[kGM * kGK];  // [K group 8][row 128][8]
-    __shared__ __align__(128) __nv_bfloat16 Bs[kGN * kGK];  // [K group 8][row 64][8]
+    __shared__ __align__(128) __nv_bfloat16 Bs[kGN * kGK];  // [K group 8][row 32][8]
     __shared__ __align__(8) uint64_t s_mbar;
     __shared__ uint32_t s_tmem;
     __shared__ int s_fail;

@@ -314,59 +314,115 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
             int4 oa, ob;
             tab.op(o, oa, ob);
             const int e0 = oa.z, e1 = oa.w, s0 = ob.x, s1 = ob.y, push = ob.z;
-            if (s0 == kSrcPop) --sp;
+            // the three shapes the op program has (build_program) with their
+            // branches taken once per op; anything else (one child) below
+            if (s0 >= 0 && s1 >= 0) {  // two tips
 #pragma unroll
-            for (int q = 0; q < KPT; ++q) {
-                const int qg = q0 + q;  // the pair in the tables
-                // the second child's messages first: they read the running
-                // vector, which the products then overwrite
-                u64 d1[SPT][4];
-                if (s1 >= 0) {
-#pragma unroll
-                    for (int s = 0; s < SPT; ++s) tab.tip(s1, qg, c1[s] & (kCodes - 1), d1[s]);
-                } else if (s1 == kSrcAcc) {
-                    u64 r[4][4];
-                    tab.p_pair(e1, qg, r);
-#pragma unroll
-                    for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
-                } else {
-#pragma unroll
-                    for (int s = 0; s < SPT; ++s)
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) d1[s][i] = one2;
-                }
-                if (s0 >= 0) {
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
-                        u64 d0[4];
-                        tab.tip(s0, qg, c0[s] & (kCodes - 1), d0);
+                        u64 d0[4], d1[4];
+                        tab.tip(s1, q0 + q, c1[s] & (kCodes - 1), d1);
+                        tab.tip(s0, q0 + q, c0[s] & (kCodes - 1), d0);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[i]);
+                    }
+            } else if (s0 == kSrcAcc && s1 >= 0) {  // the running vector and a tip
+#pragma unroll
+                for (int q = 0; q < KPT; ++q) {
+                    u64 r[4][4];
+                    tab.p_pair(e0, q0 + q, r);
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) {
+                        u64 d0[4], d1[4];
+                        tab.tip(s1, q0 + q, c1[s] & (kCodes - 1), d1);
+                        mv_pair(r, acc[s][q], d0);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[i]);
+                    }
+                }
+            } else if (s0 == kSrcPop && s1 == kSrcAcc) {  // the popped vector and the running one
+                --sp;
+#pragma unroll
+                for (int q = 0; q < KPT; ++q) {
+                    u64 d1[SPT][4];
+                    {
+                        u64 r[4][4];
+                        tab.p_pair(e1, q0 + q, r);
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
+                    }
+                    u64 r[4][4];
+                    tab.p_pair(e0, q0 + q, r);
+                    uint32_t w[NC];
+                    tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) {
+                        u64 x[4], d0[4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            x[i] = pack2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
+                        mv_pair(r, x, d0);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
                     }
-                } else {
-                    u64 r[4][4];
-                    tab.p_pair(e0, qg, r);
-                    if (s0 == kSrcPop) {
-                        uint32_t w[NC];
-                        tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
-                        tmem_wait_ld();
+                }
+            } else {
+                if (s0 == kSrcPop) --sp;
+#pragma unroll
+                for (int q = 0; q < KPT; ++q) {
+                    const int qg = q0 + q;  // the pair in the tables
+                    // the second child's messages first: they read the running
+                    // vector, which the products then overwrite
+                    u64 d1[SPT][4];
+                    if (s1 >= 0) {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) tab.tip(s1, qg, c1[s] & (kCodes - 1), d1[s]);
+                    } else if (s1 == kSrcAcc) {
+                        u64 r[4][4];
+                        tab.p_pair(e1, qg, r);
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
+                    } else {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s)
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) d1[s][i] = one2;
+                    }
+                    if (s0 >= 0) {
 #pragma unroll
                         for (int s = 0; s < SPT; ++s) {
-                            u64 x[4], d0[4];
-#pragma unroll
-                            for (int i = 0; i < 4; ++i)
-                                x[i] = pack2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
-                            mv_pair(r, x, d0);
+                            u64 d0[4];
+                            tab.tip(s0, qg, c0[s] & (kCodes - 1), d0);
 #pragma unroll
                             for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
                         }
                     } else {
+                        u64 r[4][4];
+                        tab.p_pair(e0, qg, r);
+                        if (s0 == kSrcPop) {
+                            uint32_t w[NC];
+                            tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
+                            tmem_wait_ld();
 #pragma unroll
-                        for (int s = 0; s < SPT; ++s) {
-                            u64 d0[4];
-                            mv_pair(r, acc[s][q], d0);
+                            for (int s = 0; s < SPT; ++s) {
+                                u64 x[4], d0[4];
 #pragma unroll
-                            for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                                for (int i = 0; i < 4; ++i)
+                                    x[i] = pack2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
+                                mv_pair(r, x, d0);
+#pragma unroll
+                                for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                            }
+                        } else {
+#pragma unroll
+                            for (int s = 0; s < SPT; ++s) {
+                                u64 d0[4];
+                                mv_pair(r, acc[s][q], d0);
+#pragma unroll
+                                for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                            }
                         }
                     }
                 }
