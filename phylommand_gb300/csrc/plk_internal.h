@@ -242,7 +242,8 @@ struct PruneArgs {
     // P(t) kernel): prune4p skips its relayout
     int paired_ready;
     // test of the failure path (plk_test_withhold_stage): the TMA-fed form
-    // never stages its first op, so its bounded waits run out
+    // never stages its first op, the shared-table form never copies its
+    // tables, so their bounded waits run out
     int withhold_first_stage;
 };
 // Fused 20-state FP32 kernels (plk_prune20.cu): mode 1 = CUDA cores, 2 =

@@ -6,11 +6,12 @@
 // 128-taxon x 100,000-site benchmark that staging, the barrier and the
 // generic op decoding cost more instructions than the arithmetic itself.
 // Here a warp walks the op list alone, over 32 x SPT sites:
-//  * a thread carries SPT sites (lane + 32 s of the warp's tile), so every
-//    P(t) row it loads feeds the products of SPT sites, and the SPT sites'
-//    independent products hide the latency of the next loads;
-//  * P(t) pairs and tip tables are read where the P(t) kernel wrote them
-//    (the paired layouts of plk_prune4p.cuh), through the read-only L1 path,
+//  * a thread carries SPT adjacent sites (SPT lane + s of the warp's tile),
+//    so every P(t) row it loads feeds the products of SPT sites, the SPT
+//    sites' independent products hide the latency of the next loads, and one
+//    load of SPT bytes brings a child's tip codes for all of them;
+//  * TS = 0: P(t) pairs and tip tables are read where the P(t) kernel wrote
+//    them (the paired layouts of plk_prune4p.cuh), through the read-only L1 path,
 //    which the launch gives all of the SM's unified memory that the kernel
 //    does not use as shared memory (none): a P(t) row of an op is the same
 //    address in every lane (one broadcast load of 32 bytes feeds two packed
@@ -20,6 +21,9 @@
 //  * the tip codes of op o + 2 are loaded while op o computes (a register
 //    ring, not allocated in L1), so their L2 / DRAM latency hides behind two
 //    ops of arithmetic;
+//  * TS = 1 (trees whose tables fit): the CTA first brings the paired tables
+//    and the op list into shared memory with bulk copies (cp.async.bulk on
+//    one mbarrier, a bounded wait) and reads them there;
 //  * every branch on the op's shape is uniform across the warp, and no CTA
 //    barrier stands between ops; one CTA per SM, its warp count chosen per
 //    launch so that every warp has a tile.
@@ -38,6 +42,7 @@ namespace {
 
 constexpr int kWMinWarps = 4;
 constexpr int kWMaxWarps = 24;
+constexpr uint32_t kWChunk = 16384;  // bytes per bulk copy of the TS = 1 prologue
 
 __device__ __forceinline__ void ldg_v4(const u64* p, u64& a, u64& b, u64& c, u64& d) {
     asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];\n" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
@@ -203,17 +208,30 @@ __device__ __forceinline__ int ldg_code_na(const uint8_t* p) {
     return (int)v;
 }
 
-// this thread's tip codes (SPT sites) of op o's children (0 where a child is
-// no tip); col[s] points at site s's column of the code matrix
-template <int SPT, class Tab>
-__device__ __forceinline__ void op_codes(const Tab& tab, int o, const uint8_t* const (&col)[SPT], int stride,
-                                         int (&c0)[SPT], int (&c1)[SPT]) {
-    const int2 sv = tab.sources(o);
-#pragma unroll
-    for (int s = 0; s < SPT; ++s) {
-        c0[s] = sv.x >= 0 ? ldg_code_na(col[s] + (size_t)sv.x * stride) : 0;
-        c1[s] = sv.y >= 0 ? ldg_code_na(col[s] + (size_t)sv.y * stride) : 0;
+// this thread's tip codes (SPT adjacent sites, one load of SPT bytes) of op
+// o's children (0 where a child is no tip); colp points at the thread's first
+// site in the code matrix
+template <int SPT>
+__device__ __forceinline__ int ldg_codes_na(const uint8_t* p) {
+    if constexpr (SPT == 1) {
+        unsigned short v;
+        asm volatile("ld.global.nc.L1::no_allocate.u8 %0, [%1];\n" : "=h"(v) : "l"(p));
+        return (int)v;
+    } else if constexpr (SPT == 2) {
+        unsigned short v;
+        asm volatile("ld.global.nc.L1::no_allocate.u16 %0, [%1];\n" : "=h"(v) : "l"(p));
+        return (int)v;
+    } else {
+        int v;
+        asm volatile("ld.global.nc.L1::no_allocate.u32 %0, [%1];\n" : "=r"(v) : "l"(p));
+        return v;
     }
+}
+template <int SPT, class Tab>
+__device__ __forceinline__ void op_codes(const Tab& tab, int o, const uint8_t* colp, int stride, int& c0, int& c1) {
+    const int2 sv = tab.sources(o);
+    c0 = sv.x >= 0 ? ldg_codes_na<SPT>(colp + (size_t)sv.x * stride) : 0;
+    c1 = sv.y >= 0 ? ldg_codes_na<SPT>(colp + (size_t)sv.y * stride) : 0;
 }
 
 // The register budget of a thread: one CTA of 32 x warps threads per SM.
@@ -247,23 +265,44 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
     const int n_wtiles = (a.n_sites + WS * SPT - 1) / (WS * SPT);
     const int total_warps = (nthr >> 5) * gridDim.x;
     extern __shared__ __align__(16) unsigned char wtab[];
+    __shared__ __align__(8) uint64_t s_bar;
     Tables<KP, TS> tab;
     if constexpr (TS) {
-        // [P(t) of every node][tip tables of every tip][ops], 16 bytes per
-        // thread and step
-        const size_t pb = (size_t)a.n_nodes * KP * 128, tb = (size_t)a.n_tips * KP * 512;
-        const size_t ob = (size_t)a.n_ops * sizeof(Op);
-        const uint4* gp = reinterpret_cast<const uint4*>(Pp);
-        const uint4* gt = reinterpret_cast<const uint4*>(Tp);
-        const uint4* go = reinterpret_cast<const uint4*>(a.ops);
-        uint4* sp4 = reinterpret_cast<uint4*>(wtab);
-        for (size_t i = threadIdx.x; i < pb / 16; i += blockDim.x) sp4[i] = __ldg(gp + i);
-        for (size_t i = threadIdx.x; i < tb / 16; i += blockDim.x) sp4[pb / 16 + i] = __ldg(gt + i);
-        for (size_t i = threadIdx.x; i < ob / 16; i += blockDim.x) sp4[(pb + tb) / 16 + i] = __ldg(go + i);
+        // [P(t) of every node][tip tables of every tip][ops] by bulk copies
+        // (cp.async.bulk, 16-byte aligned, sizes multiples of 16) that one
+        // thread issues in chunks, completing on one mbarrier; the TMEM
+        // allocation below overlaps them
+        const uint32_t pb = (uint32_t)a.n_nodes * KP * 128, tb = (uint32_t)a.n_tips * KP * 512;
+        const uint32_t ob = (uint32_t)a.n_ops * (uint32_t)sizeof(Op);
         const uint32_t base = static_cast<uint32_t>(__cvta_generic_to_shared(wtab));
+        const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(&s_bar));
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(pb + tb + ob)
+                         : "memory");
+            if (!a.withhold_first_stage) {
+                const unsigned char* src[3] = {reinterpret_cast<const unsigned char*>(Pp),
+                                               reinterpret_cast<const unsigned char*>(Tp),
+                                               reinterpret_cast<const unsigned char*>(a.ops)};
+                const uint32_t len[3] = {pb, tb, ob};
+                uint32_t dst = base;
+                for (int k = 0; k < 3; ++k) {
+                    for (uint32_t off = 0; off < len[k]; off += kWChunk) {
+                        const uint32_t n = min(kWChunk, len[k] - off);
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                                dst + off),
+                            "l"(src[k] + off), "r"(n), "r"(bar)
+                            : "memory");
+                    }
+                    dst += len[k];
+                }
+            }
+        }
         tab.P = base;
-        tab.T = base + (uint32_t)pb;
-        tab.ops = base + (uint32_t)(pb + tb);
+        tab.T = base + pb;
+        tab.ops = base + pb + tb;
     } else {
         tab.P = reinterpret_cast<const u64*>(Pp);
         tab.T = reinterpret_cast<const u64*>(Tp);
@@ -281,17 +320,27 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // TS = 1: the tables have landed (a bounded wait; one that runs out
+    // leaves this thread's sum NaN, so the evaluation reports a non-finite
+    // value, after a second bounded wait for copies still in flight)
+    bool tables_ok = true;
+    if constexpr (TS) {
+        const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(&s_bar));
+        if (!mbar_try_wait_bounded(bar, 0)) {
+            tables_ok = false;
+            if (!a.withhold_first_stage) mbar_try_wait_bounded(bar, 0);
+        }
+    }
     // this warp's stack: its lanes, its column range
     const uint32_t tstack =
         s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * depth * KPT * NC);
     SiteSum32 sum;
     const int stride = a.site_stride;
     const u64 one2 = pack2(1.0f, 1.0f);
-    for (int wtile = warp * gridDim.x + blockIdx.x; wtile < n_wtiles; wtile += total_warps) {
-        const int base = wtile * WS * SPT + (TPS == 2 ? lane >> 1 : lane);  // site s: base + WS s
-        const uint8_t* col[SPT];
-#pragma unroll
-        for (int s = 0; s < SPT; ++s) col[s] = a.codes + min(base + WS * s, stride - 1);
+    if (!tables_ok) site_sum_add(sum, __int_as_float(0x7fc00000), 0);
+    for (int wtile = warp * gridDim.x + blockIdx.x; tables_ok && wtile < n_wtiles; wtile += total_warps) {
+        const int base = wtile * WS * SPT + (TPS == 2 ? lane >> 1 : lane) * SPT;  // site s: base + s
+        const uint8_t* colp = a.codes + min(base, stride - SPT);
         u64 acc[SPT][KPT][4];
         int scale_e[SPT];
 #pragma unroll
@@ -304,12 +353,12 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
         }
         int sp = 0;
         // codes of ops o (c0, c1) and o + 1 (n0, n1)
-        int c0[SPT] = {}, c1[SPT] = {}, n0[SPT] = {}, n1[SPT] = {};
-        if (n_ops > 0) op_codes<SPT>(tab, 0, col, stride, c0, c1);
-        if (n_ops > 1) op_codes<SPT>(tab, 1, col, stride, n0, n1);
+        int c0 = 0, c1 = 0, n0 = 0, n1 = 0;
+        if (n_ops > 0) op_codes<SPT>(tab, 0, colp, stride, c0, c1);
+        if (n_ops > 1) op_codes<SPT>(tab, 1, colp, stride, n0, n1);
         for (int o = 0; o < n_ops; ++o) {
-            int m0[SPT] = {}, m1[SPT] = {};
-            if (o + 2 < n_ops) op_codes<SPT>(tab, o + 2, col, stride, m0, m1);
+            int m0 = 0, m1 = 0;
+            if (o + 2 < n_ops) op_codes<SPT>(tab, o + 2, colp, stride, m0, m1);
             // the op (32 bytes, 32-byte aligned): node, rank, e0, e1 | s0, s1, push, pad
             int4 oa, ob;
             tab.op(o, oa, ob);
@@ -322,8 +371,8 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
                         u64 d0[4], d1[4];
-                        tab.tip(s1, q0 + q, c1[s] & (kCodes - 1), d1);
-                        tab.tip(s0, q0 + q, c0[s] & (kCodes - 1), d0);
+                        tab.tip(s1, q0 + q, (c1 >> (8 * s)) & (kCodes - 1), d1);
+                        tab.tip(s0, q0 + q, (c0 >> (8 * s)) & (kCodes - 1), d0);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[i]);
                     }
@@ -335,7 +384,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
                         u64 d0[4], d1[4];
-                        tab.tip(s1, q0 + q, c1[s] & (kCodes - 1), d1);
+                        tab.tip(s1, q0 + q, (c1 >> (8 * s)) & (kCodes - 1), d1);
                         mv_pair(r, acc[s][q], d0);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[i]);
@@ -378,7 +427,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                     u64 d1[SPT][4];
                     if (s1 >= 0) {
 #pragma unroll
-                        for (int s = 0; s < SPT; ++s) tab.tip(s1, qg, c1[s] & (kCodes - 1), d1[s]);
+                        for (int s = 0; s < SPT; ++s) tab.tip(s1, qg, (c1 >> (8 * s)) & (kCodes - 1), d1[s]);
                     } else if (s1 == kSrcAcc) {
                         u64 r[4][4];
                         tab.p_pair(e1, qg, r);
@@ -394,7 +443,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
 #pragma unroll
                         for (int s = 0; s < SPT; ++s) {
                             u64 d0[4];
-                            tab.tip(s0, qg, c0[s] & (kCodes - 1), d0);
+                            tab.tip(s0, qg, (c0 >> (8 * s)) & (kCodes - 1), d0);
 #pragma unroll
                             for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
                         }
@@ -484,13 +533,10 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                 tmem_wait_st();
                 ++sp;
             }
-#pragma unroll
-            for (int s = 0; s < SPT; ++s) {
-                c0[s] = n0[s];
-                c1[s] = n1[s];
-                n0[s] = m0[s];
-                n1[s] = m1[s];
-            }
+            c0 = n0;
+            c1 = n1;
+            n0 = m0;
+            n1 = m1;
         }
 
         // root: L = sum_k w_k sum_s v_k[s] root_w[s] in FP32, categories in
@@ -523,7 +569,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
             float lsum = 0.0f;
 #pragma unroll
             for (int k = 0; k < 2 * KP; ++k) lsum = fmaf(cw[k], lk[k], lsum);
-            const int site = base + WS * s;
+            const int site = base + s;
             if (site < a.n_sites && half == 0) {
                 float lm;
                 int ee;

@@ -360,17 +360,20 @@ def test_site_patterns(S, n_tips, n_sites, C):
     np.testing.assert_allclose(res[True][3], res[False][3], rtol=1e-6)
 
 
-def test_withheld_stage_times_out_and_the_handle_recovers(monkeypatch):
-    """Failure path of the TMA-fed post-order form: with its first stage
-    withheld every bounded mbarrier wait runs out, the evaluation reports
-    PLK_ERR_NUMERIC, and the next evaluation on the same handle is exact."""
+@pytest.mark.parametrize("variant", [9, 16])
+def test_withheld_stage_times_out_and_the_handle_recovers(monkeypatch, variant):
+    """Failure path of the TMA-fed post-order forms (the staged ring of
+    variant 9, the bulk table copy of the shared-table variant 16): with the
+    copies withheld every bounded mbarrier wait runs out, the evaluation
+    reports PLK_ERR_NUMERIC, and the next evaluation on the same handle is
+    exact."""
     import time
     rng = np.random.default_rng(77)
     left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 24, 700, C=4)
-    monkeypatch.setenv("PLK_PRUNE_VARIANT", "9")
+    monkeypatch.setenv("PLK_PRUNE_VARIANT", str(variant))
     with _engine(left, right, bl, masks, 4, Q, f, cr, cw) as h:
         good = h.loglik(plk.PLK_FP32S)
-        assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[4][9]
+        assert h.prune_kernel() == plk.Handle.PRUNE_KERNELS[4][variant]
         h.test_withhold_stage()
         t0 = time.perf_counter()
         with pytest.raises(plk.PlkError) as err:
