@@ -144,38 +144,51 @@ __device__ __forceinline__ void site_sum_add(SiteSum32& a, float lm, int ee) {
     a.ee += ee;
 }
 
-// Block total of the threads' SiteSum32 as a compensated FP64 pair (s, c),
-// valid in thread 0: FP32 TwoSum and integer sums within each warp, FP64 from
-// the warp totals on.  All threads of the block must call it.
-__device__ inline void block_sum_site32(SiteSum32 a, double& s, double& c) {
+// Block total of the threads' SiteSum32, valid in thread 0: FP32 TwoSum and
+// integer sums only, within each warp and then across the warps (GB300's
+// FP64 pipe would make a chain of FP64 shuffle steps the longest part of a
+// short pass).  All threads of the block must call it.
+__device__ inline SiteSum32 block_sum_site32f(SiteSum32 a) {
     warp_two_sum_f(a.hi, a.lo);
-    const int esum = __reduce_add_sync(0xffffffffu, a.ee);
-    __shared__ double r_s[32], r_c[32];
+    a.ee = __reduce_add_sync(0xffffffffu, a.ee);
+    __shared__ float r_h[32], r_l[32];
+    __shared__ int r_e[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();  // an earlier call may still be reading r_s / r_c
+    __syncthreads();  // an earlier call may still be reading r_h / r_l / r_e
     if (lane == 0) {
-        double ws, we;
-        two_sum((double)esum * 0.69314718055994530942, (double)a.hi, ws, we);
-        r_s[warp] = ws;
-        r_c[warp] = we + (double)a.lo;
+        r_h[warp] = a.hi;
+        r_l[warp] = a.lo;
+        r_e[warp] = a.ee;
     }
     __syncthreads();
-    s = 0.0;
-    c = 0.0;
+    SiteSum32 t;
     if (warp == 0) {
         const int nw = blockDim.x >> 5;
-        s = lane < nw ? r_s[lane] : 0.0;
-        c = lane < nw ? r_c[lane] : 0.0;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const double os = __shfl_down_sync(0xffffffffu, s, off);
-            const double oc = __shfl_down_sync(0xffffffffu, c, off);
-            double ns, e;
-            two_sum(s, os, ns, e);
-            s = ns;
-            c = c + oc + e;
-        }
+        t.hi = lane < nw ? r_h[lane] : 0.0f;
+        t.lo = lane < nw ? r_l[lane] : 0.0f;
+        t.ee = lane < nw ? r_e[lane] : 0;
+        warp_two_sum_f(t.hi, t.lo);
+        t.ee = __reduce_add_sync(0xffffffffu, t.ee);
     }
+    return t;
+}
+
+// The same total as a compensated FP64 pair (s, c) in thread 0 (0 elsewhere):
+// sum = ee ln 2 + hi + lo.
+__device__ inline void block_sum_site32(SiteSum32 a, double& s, double& c) {
+    const SiteSum32 t = block_sum_site32f(a);
+    s = 0.0;
+    c = 0.0;
+    if (threadIdx.x == 0) {
+        two_sum((double)t.ee * 0.69314718055994530942, (double)t.hi, s, c);
+        c += (double)t.lo;
+    }
+}
+
+// A block's SiteSum32 record in the 16 bytes of its block-sum pair:
+// (hi, lo, ee, 0) as one 16-byte store by thread 0.
+__device__ __forceinline__ void store_site_record(double* bs, int block, const SiteSum32& t) {
+    reinterpret_cast<float4*>(bs)[block] = make_float4(t.hi, t.lo, __int_as_float(t.ee), 0.0f);
 }
 
 // Compensated sum of the n (sum, compensation) pairs of bs by one CTA:
@@ -194,6 +207,7 @@ __device__ inline double cta_sum_pairs(const double* bs, int n) {
         }
 #pragma unroll
         for (int q = 0; q < U; ++q) {
+            if (base + q * (int)blockDim.x + (int)threadIdx.x >= n) break;  // past the end: nothing to fold
             double ns, e;
             two_sum(s, v[q].x, ns, e);
             s = ns;
@@ -221,6 +235,35 @@ __device__ inline void finish_grid_sum(const double* bs, unsigned* counter, doub
     const double t = cta_sum_pairs(bs, (int)gridDim.x);
     if (threadIdx.x == 0) {
         *out = t;
+        *counter = 0u;
+    }
+}
+
+// The same epilogue for grids whose CTAs each stored a SiteSum32 record
+// (store_site_record): the last CTA folds the records in index order with
+// FP32 TwoSum and integer sums and writes ee ln 2 + hi + lo as one FP64 value.
+__device__ inline void finish_grid_sum32(const double* bs, unsigned* counter, double* out) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const float4* rec = reinterpret_cast<const float4*>(bs);
+    SiteSum32 a;
+    for (int i = (int)threadIdx.x; i < (int)gridDim.x; i += (int)blockDim.x) {
+        const float4 v = __ldcg(rec + i);
+        float ns, e;
+        two_sum_f(a.hi, v.x, ns, e);
+        a.hi = ns;
+        a.lo = __fadd_rn(a.lo, __fadd_rn(v.y, e));
+        a.ee += __float_as_int(v.z);
+    }
+    const SiteSum32 t = block_sum_site32f(a);
+    if (threadIdx.x == 0) {
+        *out = fma((double)t.ee, 0.69314718055994530942, (double)t.hi + (double)t.lo);
         *counter = 0u;
     }
 }

@@ -389,12 +389,8 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
             a.site_lnl[site] = site_lnl64(lm, ee);
             site_sum_add(sum, lm, ee);
         }
-        double s, c;
-        block_sum_site32(sum, s, c);
-        if (threadIdx.x == 0) {
-            a.block_sum[2 * blockIdx.x] = s;
-            a.block_sum[2 * blockIdx.x + 1] = c;
-        }
+        const SiteSum32 bsum = block_sum_site32f(sum);
+        if (threadIdx.x == 0) store_site_record(a.block_sum, blockIdx.x, bsum);
     } else {
         // ---- root: sum_k w_k sum_s L[s] * root_w[s]
         double lsum = 0.0;
@@ -450,7 +446,10 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
             }
         }
     }
-    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    if (a.grid_done) {  // FP32: SiteSum32 records; FP64: compensated pairs
+        if constexpr (std::is_same<T, float>::value) finish_grid_sum32(a.block_sum, a.grid_done, a.lnl_out);
+        else finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    }
 }
 
 }  // namespace

@@ -505,13 +505,9 @@ __global__ void __launch_bounds__(kThreads) combine20_kernel(const float* __rest
         site_lnl[site] = site_lnl64(lm, ee);
         site_sum_add(sum, lm, ee);
     }
-    double s, c;
-    block_sum_site32(sum, s, c);
-    if (threadIdx.x == 0) {
-        block_sum[2 * blockIdx.x] = s;
-        block_sum[2 * blockIdx.x + 1] = c;
-    }
-    if (grid_done) finish_grid_sum(block_sum, grid_done, lnl_out);
+    const SiteSum32 bsum = block_sum_site32f(sum);
+    if (threadIdx.x == 0) store_site_record(block_sum, blockIdx.x, bsum);
+    if (grid_done) finish_grid_sum32(block_sum, grid_done, lnl_out);
 }
 
 size_t smem20_bytes(const PruneArgs& a, int mode) {

@@ -782,14 +782,12 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         if (a.site_lnl) a.site_lnl[site] = site_lnl64(lm, ee);
         site_sum_add(sum, lm, ee);
     }
-    double bs, bc;
-    block_sum_site32(sum, bs, bc);
+    const SiteSum32 bsum = block_sum_site32f(sum);
     if (tid == 0) {
-        a.block_sum[2 * blockIdx.x] = bs;
-        a.block_sum[2 * blockIdx.x + 1] = bc;
+        store_site_record(a.block_sum, blockIdx.x, bsum);
         a.tile_done[blockIdx.x] = 0u;  // re-armed for the next launch
     }
-    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    if (a.grid_done) finish_grid_sum32(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 int tmem_cols_for(const PruneArgs& a, int form) {

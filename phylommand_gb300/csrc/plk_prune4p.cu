@@ -64,13 +64,9 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_kernel(PruneArgs a, con
     j.max_depth = a.max_depth;
     SiteSum32 sum;
     run_tile4p<KP, SPT, CODES, TPS>(j, sm, sum);
-    double tsum, tcomp;
-    block_sum_site32(sum, tsum, tcomp);
-    if (threadIdx.x == 0) {
-        a.block_sum[2 * blockIdx.x] = tsum;
-        a.block_sum[2 * blockIdx.x + 1] = tcomp;
-    }
-    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    const SiteSum32 bsum = block_sum_site32f(sum);
+    if (threadIdx.x == 0) store_site_record(a.block_sum, blockIdx.x, bsum);
+    if (a.grid_done) finish_grid_sum32(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 // The TMA-fed form (run_tile4p_bulk): one site per thread, codes from global.
@@ -107,13 +103,9 @@ __global__ void __launch_bounds__(kPruneThreads) prune4p_bulk_kernel(PruneArgs a
     j.max_depth = a.max_depth;
     SiteSum32 sum;
     run_tile4p_bulk<KP>(j, sm, bars, &s_abort, sum, a.withhold_first_stage != 0);
-    double tsum, tcomp;
-    block_sum_site32(sum, tsum, tcomp);
-    if (threadIdx.x == 0) {
-        a.block_sum[2 * blockIdx.x] = tsum;
-        a.block_sum[2 * blockIdx.x + 1] = tcomp;
-    }
-    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    const SiteSum32 bsum = block_sum_site32f(sum);
+    if (threadIdx.x == 0) store_site_record(a.block_sum, blockIdx.x, bsum);
+    if (a.grid_done) finish_grid_sum32(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 template <int KP>

@@ -45,13 +45,9 @@ __global__ void __launch_bounds__(kPruneThreads) prune4s_kernel(PruneArgs a) {
     j.max_depth = a.max_depth;
     SiteSum32 sum;
     run_tile<CM, SPT, CODES_SMEM>(j, sm, sum);
-    double tsum, tcomp;
-    block_sum_site32(sum, tsum, tcomp);
-    if (threadIdx.x == 0) {
-        a.block_sum[2 * blockIdx.x] = tsum;
-        a.block_sum[2 * blockIdx.x + 1] = tcomp;
-    }
-    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    const SiteSum32 bsum = block_sum_site32f(sum);
+    if (threadIdx.x == 0) store_site_record(a.block_sum, blockIdx.x, bsum);
+    if (a.grid_done) finish_grid_sum32(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 template <int CM, int SPT, bool CODES_SMEM>

@@ -34,6 +34,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 namespace plk {
 using namespace dev;
@@ -44,11 +47,23 @@ constexpr int kWMinWarps = 4;
 constexpr int kWMaxWarps = 24;
 constexpr uint32_t kWChunk = 16384;  // bytes per bulk copy of the TS = 1 prologue
 
-__device__ __forceinline__ void ldg_v4(const u64* p, u64& a, u64& b, u64& c, u64& d) {
-    asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];\n" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+// FP32 lane pairs as float2, multiplied on the packed FP32x2 path
+// (fma.rn.f32x2 / mul.rn.f32x2 through __ffma2_rn / __fmul2_rn)
+typedef float2 f2;
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ f2 pk2(float lo, float hi) { return make_float2(lo, hi); }
+__device__ __forceinline__ void unpack2(f2 v, float& lo, float& hi) {
+    lo = v.x;
+    hi = v.y;
 }
-__device__ __forceinline__ void ldg_v2(const u64* p, u64& a, u64& b) {
-    asm("ld.global.nc.v2.u64 {%0, %1}, [%2];\n" : "=l"(a), "=l"(b) : "l"(p));
+__device__ __forceinline__ void ldg_v4(const f2* p, f2& a, f2& b, f2& c, f2& d) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+        : "=f"(a.x), "=f"(a.y), "=f"(b.x), "=f"(b.y), "=f"(c.x), "=f"(c.y), "=f"(d.x), "=f"(d.y)
+        : "l"(p));
+}
+__device__ __forceinline__ void ldg_v2(const f2* p, f2& a, f2& b) {
+    asm("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];\n" : "=f"(a.x), "=f"(a.y), "=f"(b.x), "=f"(b.y) : "l"(p));
 }
 // three-input maximum (PTX ISA 8.8+, sm_100+): the same value as two fmaxf
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
@@ -57,8 +72,8 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
     return d;
 }
 
-__device__ __forceinline__ void lds_v2(uint32_t addr, u64& a, u64& b) {
-    asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];\n" : "=l"(a), "=l"(b) : "r"(addr));
+__device__ __forceinline__ void lds_v2(uint32_t addr, f2& a, f2& b) {
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];\n" : "=f"(a.x), "=f"(a.y), "=f"(b.x), "=f"(b.y) : "r"(addr));
 }
 __device__ __forceinline__ int4 lds_int4(uint32_t addr) {
     int4 v;
@@ -83,16 +98,16 @@ struct Tables;
 
 template <int KP>
 struct Tables<KP, 0> {
-    const u64* P;
-    const u64* T;
+    const f2* P;
+    const f2* T;
     const Op* ops;
-    __device__ __forceinline__ void p_pair(int node, int q, u64 (&r)[4][4]) const {
-        const u64* b = P + (size_t)node * KP * 16 + q * 16;
+    __device__ __forceinline__ void p_pair(int node, int q, f2 (&r)[4][4]) const {
+        const f2* b = P + (size_t)node * KP * 16 + q * 16;
 #pragma unroll
         for (int j = 0; j < 4; ++j) ldg_v4(b + j * 4, r[j][0], r[j][1], r[j][2], r[j][3]);
     }
-    __device__ __forceinline__ void tip(int t, int q, int code, u64 (&out)[4]) const {
-        const u64* b = T + (size_t)t * KP * 64 + (q * 2 * kCodes + code) * 2;
+    __device__ __forceinline__ void tip(int t, int q, int code, f2 (&out)[4]) const {
+        const f2* b = T + (size_t)t * KP * 64 + (q * 2 * kCodes + code) * 2;
         ldg_v2(b, out[0], out[1]);
         ldg_v2(b + kCodes * 2, out[2], out[3]);
     }
@@ -106,7 +121,7 @@ struct Tables<KP, 0> {
 template <int KP>
 struct Tables<KP, 1> {
     uint32_t P, T, ops;  // shared-memory addresses
-    __device__ __forceinline__ void p_pair(int node, int q, u64 (&r)[4][4]) const {
+    __device__ __forceinline__ void p_pair(int node, int q, f2 (&r)[4][4]) const {
         const uint32_t b = P + (uint32_t)node * (KP * 128) + q * 128;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -114,7 +129,7 @@ struct Tables<KP, 1> {
             lds_v2(b + j * 32 + 16, r[j][2], r[j][3]);
         }
     }
-    __device__ __forceinline__ void tip(int t, int q, int code, u64 (&out)[4]) const {
+    __device__ __forceinline__ void tip(int t, int q, int code, f2 (&out)[4]) const {
         const uint32_t b = T + (uint32_t)t * (KP * 512) + q * 512 + (uint32_t)code * 16;
         lds_v2(b, out[0], out[1]);
         lds_v2(b + 256, out[2], out[3]);
@@ -128,10 +143,10 @@ struct Tables<KP, 1> {
 
 // out[i] = sum_j r[j][i] x[j], j ascending, the first term a product (the
 // order of mv4p)
-__device__ __forceinline__ void mv_pair(const u64 (&r)[4][4], const u64 (&x)[4], u64 (&out)[4]) {
+__device__ __forceinline__ void mv_pair(const f2 (&r)[4][4], const f2 (&x)[4], f2 (&out)[4]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        u64 acc = mul2(x[0], r[0][i]);
+        f2 acc = mul2(x[0], r[0][i]);
         acc = fma2(x[1], r[1][i], acc);
         acc = fma2(x[2], r[2][i], acc);
         acc = fma2(x[3], r[3][i], acc);
@@ -304,8 +319,8 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
         tab.T = base + pb;
         tab.ops = base + pb + tb;
     } else {
-        tab.P = reinterpret_cast<const u64*>(Pp);
-        tab.T = reinterpret_cast<const u64*>(Tp);
+        tab.P = reinterpret_cast<const f2*>(Pp);
+        tab.T = reinterpret_cast<const f2*>(Tp);
         tab.ops = a.ops;
     }
     const int n_ops = a.n_ops;
@@ -336,12 +351,12 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
         s_tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)((warp >> 2) * depth * KPT * NC);
     SiteSum32 sum;
     const int stride = a.site_stride;
-    const u64 one2 = pack2(1.0f, 1.0f);
+    const f2 one2 = pk2(1.0f, 1.0f);
     if (!tables_ok) site_sum_add(sum, __int_as_float(0x7fc00000), 0);
     for (int wtile = warp * gridDim.x + blockIdx.x; tables_ok && wtile < n_wtiles; wtile += total_warps) {
         const int base = wtile * WS * SPT + (TPS == 2 ? lane >> 1 : lane) * SPT;  // site s: base + s
         const uint8_t* colp = a.codes + min(base, stride - SPT);
-        u64 acc[SPT][KPT][4];
+        f2 acc[SPT][KPT][4];
         int scale_e[SPT];
 #pragma unroll
         for (int s = 0; s < SPT; ++s) {
@@ -370,7 +385,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                 for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
-                        u64 d0[4], d1[4];
+                        f2 d0[4], d1[4];
                         tab.tip(s1, q0 + q, (c1 >> (8 * s)) & (kCodes - 1), d1);
                         tab.tip(s0, q0 + q, (c0 >> (8 * s)) & (kCodes - 1), d0);
 #pragma unroll
@@ -379,11 +394,11 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
             } else if (s0 == kSrcAcc && s1 >= 0) {  // the running vector and a tip
 #pragma unroll
                 for (int q = 0; q < KPT; ++q) {
-                    u64 r[4][4];
+                    f2 r[4][4];
                     tab.p_pair(e0, q0 + q, r);
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
-                        u64 d0[4], d1[4];
+                        f2 d0[4], d1[4];
                         tab.tip(s1, q0 + q, (c1 >> (8 * s)) & (kCodes - 1), d1);
                         mv_pair(r, acc[s][q], d0);
 #pragma unroll
@@ -392,29 +407,38 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                 }
             } else if (s0 == kSrcPop && s1 == kSrcAcc) {  // the popped vector and the running one
                 --sp;
+                // the popped slot's loads go out first (after the stores of
+                // earlier pushes), the running vector's messages cover them
+                tmem_wait_st();
+                uint32_t w[KPT][NC];
+#pragma unroll
+                for (int q = 0; q < KPT; ++q) tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w[q]);
+                f2 d1[SPT][KPT][4];
 #pragma unroll
                 for (int q = 0; q < KPT; ++q) {
-                    u64 d1[SPT][4];
-                    {
-                        u64 r[4][4];
-                        tab.p_pair(e1, q0 + q, r);
+                    f2 r[4][4];
+                    tab.p_pair(e1, q0 + q, r);
 #pragma unroll
-                        for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
-                    }
-                    u64 r[4][4];
+                    for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s][q]);
+                }
+                tmem_wait_ld();
+#pragma unroll
+                for (int q = 0; q < KPT; ++q)
+#pragma unroll
+                    for (int k = 0; k < NC; ++k) asm volatile("" : "+r"(w[q][k]));  // no use ahead of the wait
+#pragma unroll
+                for (int q = 0; q < KPT; ++q) {
+                    f2 r[4][4];
                     tab.p_pair(e0, q0 + q, r);
-                    uint32_t w[NC];
-                    tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
-                    tmem_wait_ld();
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
-                        u64 x[4], d0[4];
+                        f2 x[4], d0[4];
 #pragma unroll
                         for (int i = 0; i < 4; ++i)
-                            x[i] = pack2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
+                            x[i] = pk2(__uint_as_float(w[q][8 * s + 2 * i]), __uint_as_float(w[q][8 * s + 2 * i + 1]));
                         mv_pair(r, x, d0);
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
+                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][q][i]);
                     }
                 }
             } else {
@@ -424,12 +448,12 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                     const int qg = q0 + q;  // the pair in the tables
                     // the second child's messages first: they read the running
                     // vector, which the products then overwrite
-                    u64 d1[SPT][4];
+                    f2 d1[SPT][4];
                     if (s1 >= 0) {
 #pragma unroll
                         for (int s = 0; s < SPT; ++s) tab.tip(s1, qg, (c1 >> (8 * s)) & (kCodes - 1), d1[s]);
                     } else if (s1 == kSrcAcc) {
-                        u64 r[4][4];
+                        f2 r[4][4];
                         tab.p_pair(e1, qg, r);
 #pragma unroll
                         for (int s = 0; s < SPT; ++s) mv_pair(r, acc[s][q], d1[s]);
@@ -442,24 +466,25 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                     if (s0 >= 0) {
 #pragma unroll
                         for (int s = 0; s < SPT; ++s) {
-                            u64 d0[4];
+                            f2 d0[4];
                             tab.tip(s0, qg, (c0 >> (8 * s)) & (kCodes - 1), d0);
 #pragma unroll
                             for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
                         }
                     } else {
-                        u64 r[4][4];
+                        f2 r[4][4];
                         tab.p_pair(e0, qg, r);
                         if (s0 == kSrcPop) {
                             uint32_t w[NC];
+                            tmem_wait_st();
                             tmem_ld<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
                             tmem_wait_ld();
 #pragma unroll
                             for (int s = 0; s < SPT; ++s) {
-                                u64 x[4], d0[4];
+                                f2 x[4], d0[4];
 #pragma unroll
                                 for (int i = 0; i < 4; ++i)
-                                    x[i] = pack2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
+                                    x[i] = pk2(__uint_as_float(w[8 * s + 2 * i]), __uint_as_float(w[8 * s + 2 * i + 1]));
                                 mv_pair(r, x, d0);
 #pragma unroll
                                 for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
@@ -467,7 +492,7 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                         } else {
 #pragma unroll
                             for (int s = 0; s < SPT; ++s) {
-                                u64 d0[4];
+                                f2 d0[4];
                                 mv_pair(r, acc[s][q], d0);
 #pragma unroll
                                 for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(d0[i], d1[s][i]);
@@ -476,61 +501,92 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
                     }
                 }
             }
+            // a quick exact test first (TPS = 1, two or more pairs): when the
+            // maximum of the first pair's eight values reaches the threshold
+            // so does the node maximum, and no rescale follows; only when
+            // some lane of the warp falls short does the warp take the full
+            // maximum below, with the decision and factors it always had
+            bool full_test = true;
+            if constexpr (TPS == 1 && KPT >= 2) {
+                bool near = false;
 #pragma unroll
-            for (int s = 0; s < SPT; ++s) {
-                // the node maximum (three-input max: the same value as the
-                // fmaxf chain of run_tile4p; TPS = 2: with the partner's)
-                float v[KPT * 8];
-#pragma unroll
-                for (int q = 0; q < KPT; ++q)
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[q * 8 + 2 * i], v[q * 8 + 2 * i + 1]);
-                float mx;
-                if constexpr (KPT == 1) {
-                    mx = fmax3(fmax3(v[0], v[1], v[2]), fmax3(v[3], v[4], v[5]), fmaxf(v[6], v[7]));
-                } else if constexpr (KPT == 2) {
-                    const float m0x = fmax3(v[0], v[1], v[2]), m1x = fmax3(v[3], v[4], v[5]);
-                    const float m2x = fmax3(v[6], v[7], v[8]), m3x = fmax3(v[9], v[10], v[11]);
-                    const float m4x = fmax3(v[12], v[13], v[14]);
-                    mx = fmax3(fmax3(m0x, m1x, m2x), fmax3(m3x, m4x, v[15]), 0.0f);
-                } else {
-                    float m[11];
-#pragma unroll
-                    for (int k = 0; k < 10; ++k) m[k] = fmax3(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
-                    m[10] = fmaxf(v[30], v[31]);
-                    const float g0 = fmax3(m[0], m[1], m[2]), g1 = fmax3(m[3], m[4], m[5]);
-                    const float g2 = fmax3(m[6], m[7], m[8]), g3 = fmaxf(m[9], m[10]);
-                    mx = fmax3(fmax3(g0, g1, g2), g3, 0.0f);
+                for (int s = 0; s < SPT; ++s) {
+                    const f2* a0 = acc[s][0];
+                    const float pm = fmax3(fmax3(a0[0].x, a0[0].y, a0[1].x), fmax3(a0[1].y, a0[2].x, a0[2].y),
+                                           fmaxf(a0[3].x, a0[3].y));
+                    near |= !(pm >= scale_threshold<float>());
                 }
-                if constexpr (TPS == 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-                if (mx < scale_threshold<float>() && mx > 0.0f) {
-                    int e;
-                    float f1, f2;
-                    pow2_factors(mx, &e, &f1, &f2);
-                    const u64 h1 = pack2(f1, f1), h2 = pack2(f2, f2);
+                full_test = __any_sync(0xffffffffu, near);
+            }
+            if (full_test) {
+#pragma unroll
+                for (int s = 0; s < SPT; ++s) {
+                    // the node maximum (three-input max: the same value as the
+                    // fmaxf chain of run_tile4p; TPS = 2: with the partner's)
+                    float v[KPT * 8];
 #pragma unroll
                     for (int q = 0; q < KPT; ++q)
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(mul2(acc[s][q][i], h1), h2);
-                    scale_e[s] += e;
+                        for (int i = 0; i < 4; ++i) unpack2(acc[s][q][i], v[q * 8 + 2 * i], v[q * 8 + 2 * i + 1]);
+                    float mx;
+                    if constexpr (KPT == 1) {
+                        mx = fmax3(fmax3(v[0], v[1], v[2]), fmax3(v[3], v[4], v[5]), fmaxf(v[6], v[7]));
+                    } else if constexpr (KPT == 2) {
+                        const float m0x = fmax3(v[0], v[1], v[2]), m1x = fmax3(v[3], v[4], v[5]);
+                        const float m2x = fmax3(v[6], v[7], v[8]), m3x = fmax3(v[9], v[10], v[11]);
+                        const float m4x = fmax3(v[12], v[13], v[14]);
+                        mx = fmax3(fmax3(m0x, m1x, m2x), fmax3(m3x, m4x, v[15]), 0.0f);
+                    } else {
+                        float m[11];
+#pragma unroll
+                        for (int k = 0; k < 10; ++k) m[k] = fmax3(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
+                        m[10] = fmaxf(v[30], v[31]);
+                        const float g0 = fmax3(m[0], m[1], m[2]), g1 = fmax3(m[3], m[4], m[5]);
+                        const float g2 = fmax3(m[6], m[7], m[8]), g3 = fmaxf(m[9], m[10]);
+                        mx = fmax3(fmax3(g0, g1, g2), g3, 0.0f);
+                    }
+                    if constexpr (TPS == 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+                    if (mx < scale_threshold<float>() && mx > 0.0f) {
+                        int e;
+                        float g1, g2;
+                        pow2_factors(mx, &e, &g1, &g2);
+                        const f2 h1 = pk2(g1, g1), h2 = pk2(g2, g2);
+#pragma unroll
+                        for (int q = 0; q < KPT; ++q)
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) acc[s][q][i] = mul2(mul2(acc[s][q][i], h1), h2);
+                        scale_e[s] += e;
+                    }
                 }
             }
             if (push) {
+                // the slot's columns, all pairs (KPT x NC), leave in as few
+                // instructions as fit; the wait for them stands before the
+                // next pop's loads
+                uint32_t w[KPT * NC];
 #pragma unroll
-                for (int q = 0; q < KPT; ++q) {
-                    uint32_t w[NC];
+                for (int q = 0; q < KPT; ++q)
 #pragma unroll
                     for (int s = 0; s < SPT; ++s)
 #pragma unroll
                         for (int i = 0; i < 4; ++i) {
                             float lo, hi;
                             unpack2(acc[s][q][i], lo, hi);
-                            w[8 * s + 2 * i] = __float_as_uint(lo);
-                            w[8 * s + 2 * i + 1] = __float_as_uint(hi);
+                            w[q * NC + 8 * s + 2 * i] = __float_as_uint(lo);
+                            w[q * NC + 8 * s + 2 * i + 1] = __float_as_uint(hi);
                         }
-                    tmem_st<NC>(tstack + (uint32_t)((sp * KPT + q) * NC), w);
+                const uint32_t ta = tstack + (uint32_t)(sp * KPT * NC);
+                if constexpr (KPT * NC <= 32) {
+                    tmem_st<KPT * NC>(ta, w);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < KPT; ++q) {
+                        uint32_t wq[NC];
+#pragma unroll
+                        for (int k = 0; k < NC; ++k) wq[k] = w[q * NC + k];
+                        tmem_st<NC>(ta + (uint32_t)(q * NC), wq);
+                    }
                 }
-                tmem_wait_st();
                 ++sp;
             }
             c0 = n0;
@@ -579,7 +635,8 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
             }
         }
     }
-    // every warp is done with its stack: free the TMEM
+    // every warp is done with its stack (its stores complete): free the TMEM
+    tmem_wait_st();
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) {
@@ -587,13 +644,9 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(s_tmem), "r"(tmem_cols)
                      : "memory");
     }
-    double tsum, tcomp;
-    block_sum_site32(sum, tsum, tcomp);
-    if (tid == 0) {
-        a.block_sum[2 * blockIdx.x] = tsum;
-        a.block_sum[2 * blockIdx.x + 1] = tcomp;
-    }
-    if (a.grid_done) finish_grid_sum(a.block_sum, a.grid_done, a.lnl_out);
+    const SiteSum32 bsum = block_sum_site32f(sum);
+    if (tid == 0) store_site_record(a.block_sum, blockIdx.x, bsum);
+    if (a.grid_done) finish_grid_sum32(a.block_sum, a.grid_done, a.lnl_out);
 }
 
 template <int KP, int SPT, int TS, int TPS = 1>
@@ -647,11 +700,25 @@ int prune4w_tmem_cols(int KP, int SPT, int warps, int depth, int TPS = 1) {
 // launch runs every evaluation); the carveout gives the L1 cache all the
 // shared memory the kernel does not use
 int prune4w_ctas_per_sm(int KP, int SPT, int TS, int warps, size_t smem, int TPS = 1) {
-    if (TS) {  // sized per launch (the tables), not cached
+    if (TS) {  // sized per launch (the tables): cached per device, kernel, warps and bytes
         const void* fn = prune4w_fn_of(KP, SPT, 1, TPS);
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        static std::mutex mu;
+        static std::map<std::tuple<int, const void*, int, size_t>, int> occ;
+        static std::map<std::pair<int, const void*>, size_t> attr;  // the largest dynamic size allowed so far
+        std::lock_guard<std::mutex> lock(mu);
+        size_t& allowed = attr[std::make_pair(dev, fn)];
+        if (smem > allowed) {
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+            allowed = smem;
+        }
+        const auto key = std::make_tuple(dev, fn, warps, smem);
+        const auto it = occ.find(key);
+        if (it != occ.end()) return it->second;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * 32, smem) != cudaSuccess) n = 0;
+        occ[key] = n;
         return n;
     }
     static std::atomic<int> cache[3][3][kWMaxWarps + 1];
