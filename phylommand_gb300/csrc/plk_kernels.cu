@@ -209,7 +209,72 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
     }
 }
 
+// P(t) of the eigen form for 4 states, eight (node, category) matrices per
+// warp: lane 4 w + r of a warp holds row r of matrix w.  GB300 retires a
+// warp-wide FP64 instruction at a small fraction of the FP32 rate whatever
+// the number of active lanes, so the one-matrix-per-CTA kernel spent most
+// of its time in FP64 instructions with 4 or 16 of 32 lanes busy.  Here
+// every FP64 instruction works on 32 lanes, with the operations and their
+// order of pmat_kernel (p_kind 1), so P(t) and the tip tables keep their
+// bits: e_m = exp(lambda_m t) (lane m of the matrix), X[r][m] = L[r][m] e_m,
+// P[r][j] = fma over m ascending from 0, tips summed over the allowed
+// states j ascending.
+__global__ void __launch_bounds__(128) pmat4_eigen_kernel(DeviceModel m) {
+    const int lane = threadIdx.x & 31;
+    const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;  // (node, category)
+    const int r = lane & 3;
+    const int n_items = m.n_nodes * m.C;
+    const bool live = item < n_items;
+    const int it = live ? item : n_items - 1;  // lanes past the end repeat the last item, store nothing
+    const int v = it / m.C, k = it % m.C;
+    const double t = __dmul_rn(m.t_eff[v], m.cat_rate[k]);
+    const double e_own = exp(m.eig_lam[r] * t);
+    double e[4];
+#pragma unroll
+    for (int mm = 0; mm < 4; ++mm) e[mm] = __shfl_sync(0xffffffffu, e_own, (lane & ~3) | mm);
+    double x[4], p[4];
+#pragma unroll
+    for (int mm = 0; mm < 4; ++mm) x[mm] = m.eig_L[r * 4 + mm] * e[mm];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        double acc = 0.0;
+#pragma unroll
+        for (int mm = 0; mm < 4; ++mm) acc = fma(x[mm], m.eig_R[mm * 4 + j], acc);
+        p[j] = acc;
+    }
+    if (!live) return;
+    const size_t base = (size_t)it * 16 + r * 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        m.P64[base + j] = p[j];
+        m.P32[base + j] = (float)p[j];
+        if (m.P32p) m.P32p[(size_t)v * m.C * 16 + paired_p_index(k, r, j)] = (float)p[j];
+    }
+    if (v < m.n_tips) {
+        const size_t tb = (size_t)it * m.n_codes * 4;
+        for (int c = 0; c < m.n_codes; ++c) {
+            const uint32_t mask = m.code_mask ? m.code_mask[c] : (uint32_t)c;
+            double acc = 0.0;
+            bool first = true;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if ((mask >> j) & 1u) {
+                    acc = first ? p[j] : __dadd_rn(acc, p[j]);
+                    first = false;
+                }
+            m.tip64[tb + (size_t)c * 4 + r] = acc;
+            m.tip32[tb + (size_t)c * 4 + r] = (float)acc;
+            if (m.tip32p) m.tip32p[(size_t)v * m.C * kCodes * 4 + paired_tip_index(k, c, r)] = (float)acc;
+        }
+    }
+}
+
 cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st) {
+    if (m.S == 4 && p_kind == 1 && m.B20 == nullptr) {
+        const int lanes = m.n_nodes * m.C * 4;
+        pmat4_eigen_kernel<<<(lanes + 127) / 128, 128, 0, st>>>(m);
+        return cudaGetLastError();
+    }
     const int SS = m.S * m.S;
     const size_t smem = sizeof(double) * (size_t)(3 * SS);
     const int threads = SS >= 256 ? 256 : (SS >= 64 ? 64 : 32);

@@ -28,6 +28,9 @@
 // padded so that no more CTAs fit on an SM than its 512 columns serve, so an
 // allocation never waits.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "plk_device.cuh"
 #include "plk_internal.h"
@@ -570,8 +573,25 @@ __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
 //   * tip codes read from global memory one op ahead instead of staged.
 // BF: the split-BF16 products (kind::f16) instead of split TF32: smaller A
 // operands and B images (four CTAs per SM), six MMAs per child message.
+// the op record o (32 bytes, 32-byte aligned) through the read-only path: the
+// same address in every thread
+__device__ __forceinline__ Op ldg_op(const Op* ops, int o) {
+    const int4 x = __ldg(reinterpret_cast<const int4*>(ops + o));
+    const int4 y = __ldg(reinterpret_cast<const int4*>(ops + o) + 1);
+    Op op;
+    op.node = x.x;
+    op.rank = x.y;
+    op.e0 = x.z;
+    op.e1 = x.w;
+    op.s0 = y.x;
+    op.s1 = y.y;
+    op.push = y.z;
+    op.pad = y.w;
+    return op;
+}
+
 template <int NCS, bool BF>
-__global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
+__global__ void __launch_bounds__(kThreads, BF ? 5 : 3) prune20v_kernel(P20UArgs g) {
     constexpr int APART = BF ? kAPartB : kAPart5;
     constexpr int AOPER = 2 * APART;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -588,7 +608,13 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     unsigned char* acc_op = smem;                // A operand of the running vector
     unsigned char* pop_op = smem + AOPER;        // A operand of a vector popped from the stack
     unsigned char* stages = smem + 2 * AOPER + kAGroup;  // after the zero group
+    // the op list: in shared memory (split TF32), or read through L1 (split
+    // BF16, whose CTAs fit five to an SM only without it)
     Op* s_ops = reinterpret_cast<Op*>(stages + 2 * 2 * cb);
+    auto load_op = [&](int o) -> Op {
+        if constexpr (BF) return ldg_op(a.ops, o);
+        else return s_ops[o];
+    };
     const uint32_t mbar = smem_u32(&s_mbar);
     const uint32_t full0 = smem_u32(&s_full[0]);  // slot j's barrier: full0 + 8 j
     const int site = tile0 + tid;
@@ -610,7 +636,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         s_abort = 0;
     }
     if (tid < kS) s_rw[tid] = (float)a.root_w[tid];
-    for (int i = tid; i < a.n_ops; i += kThreads) s_ops[i] = a.ops[i];
+    if constexpr (!BF)
+        for (int i = tid; i < a.n_ops; i += kThreads) s_ops[i] = a.ops[i];
     // both A operands and the zero group after them: every column an MMA
     // reads is finite from the start
     for (int i = tid; i < (2 * AOPER + kAGroup) / 16; i += kThreads)
@@ -620,14 +647,23 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
     tc_fence_after();
     const uint32_t tmem = s_tmem;
     const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
-    if (tid == 0) bulk_stage20<BF>(stages, s_ops[0], k, g, full0);
+    if (tid == 0) bulk_stage20<BF>(stages, load_op(0), k, g, full0);
     const uint32_t acc_lo = desc_lo(smem_u32(acc_op), kAGroup), pop_lo = desc_lo(smem_u32(pop_op), kAGroup);
     const uint32_t stage_lo = desc_lo(smem_u32(stages), kBGroup);  // slot j, child c: + (2 j + c) cb / 16
 
     auto code_of = [&](int src) -> int {
-        return (src >= 0 && has_code) ? (int)__ldg(a.codes + (size_t)src * a.site_stride + site) : 0;
+        if (src < 0 || !has_code) return 0;
+        unsigned short v;  // not allocated in L1, which keeps the op list
+        asm volatile("ld.global.nc.L1::no_allocate.u8 %0, [%1];\n"
+                     : "=h"(v)
+                     : "l"(a.codes + (size_t)src * a.site_stride + site));
+        return (int)v;
     };
-    int c0 = code_of(s_ops[0].s0), c1 = code_of(s_ops[0].s1);
+    // the op records of ops o, o + 1 and o + 2: each is read two ops before
+    // its own, so no decision of an op waits on a load
+    Op op = load_op(0);
+    Op nx = a.n_ops > 1 ? load_op(1) : op;
+    int c0 = code_of(op.s0), c1 = code_of(op.s1);
     float m0[kS], m1[kS], pre[kS];
     int e_site = 0, sp = 0;
     uint32_t phase = 0;
@@ -639,12 +675,11 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
             lost = o;
             s_abort = 1;
         }
-        const Op op = s_ops[o];
         const bool has_next = o + 1 < a.n_ops;
+        const Op nn = o + 2 < a.n_ops ? load_op(o + 2) : nx;
         int n0 = 0, n1 = 0;
         bool next_pops = false;
         if (has_next) {
-            const Op nx = s_ops[o + 1];
             n0 = code_of(nx.s0);
             n1 = code_of(nx.s1);
             next_pops = nx.s0 == kSrcPop;
@@ -661,7 +696,7 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         // the slot op o-1 used: its MMAs completed and its tip rows were read
         // before the barrier
         if (tid == 0 && has_next)
-            bulk_stage20<BF>(stages + ((o + 1) & 1) * 2 * cb, s_ops[o + 1], k, g, full0 + 8 * ((o + 1) & 1));
+            bulk_stage20<BF>(stages + ((o + 1) & 1) * 2 * cb, nx, k, g, full0 + 8 * ((o + 1) & 1));
         // the vector the next op pops (this op does not push when the next pops)
         if (next_pops) {
 #pragma unroll
@@ -725,6 +760,8 @@ __global__ void __launch_bounds__(kThreads, 3) prune20v_kernel(P20UArgs g) {
         }
         c0 = n0;
         c1 = n1;
+        op = nx;
+        nx = nn;
     }
     // every issued stage was waited for, unless a wait ran out: give that
     // copy one more bounded wait before the shared memory is given up
@@ -805,8 +842,9 @@ int child_bytes_for(const PruneArgs& a, int form) {
 
 size_t smem20u_bytes(const PruneArgs& a, int form) {
     const size_t ops = ((size_t)a.n_ops * sizeof(Op) + 15) & ~(size_t)15;
+    // the split-BF16 compact form reads the op list through L1
     if (form == 1) return (size_t)2 * kAOperand5 + kAGroup + (size_t)2 * 2 * child_bytes_for(a, form) + ops;
-    if (form == 2) return (size_t)2 * kAOperandB + kAGroup + (size_t)2 * 2 * child_bytes_for(a, form) + ops;
+    if (form == 2) return (size_t)2 * kAOperandB + kAGroup + (size_t)2 * 2 * child_bytes_for(a, form);
     return (size_t)2 * kAOperand + (size_t)3 * 2 * child_bytes_for(a, form) + ops + (size_t)a.n_tips * kTile;
 }
 
@@ -837,6 +875,59 @@ size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes) {
     const size_t cl = (((size_t)a.C * a.n_sites * sizeof(float) + 255) & ~(size_t)255) +
                       (((size_t)a.C * a.n_sites * sizeof(int) + 255) & ~(size_t)255);
     return ((ps + 255) & ~(size_t)255) + ((ts + 255) & ~(size_t)255) + cl + spill_bytes(a);
+}
+
+// The dynamic shared memory of a launch of `ctas` chains: its own bytes,
+// padded until an SM holds no more CTAs than (1) its TMEM serves (max_ctas)
+// and (2) the fewest that still run the grid in the fewest rounds.  Every
+// chain of a round takes about as long, so 628 chains at 4 per SM (608 in a
+// first round, 20 in a second) take twice as long as at 5 per SM in one, and
+// at 3 per SM (456 and 172) the two rounds are shorter than at 4.  Cached per
+// device, kernel, bytes and grid: the attribute and occupancy calls cost
+// microseconds of host time per launch.
+static cudaError_t pick_ctas_per_sm(void (*kern)(P20UArgs), size_t base, int max_ctas, int ctas, size_t* smem_out) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void*, size_t, int, int>, size_t> cache;
+    static std::map<std::pair<int, const void*>, size_t> allowed;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(dev, reinterpret_cast<const void*>(kern), base, max_ctas, ctas);
+    const auto hit = cache.find(key);
+    size_t& allow = allowed[std::make_pair(dev, reinterpret_cast<const void*>(kern))];
+    auto set_attr = [&](size_t bytes) -> cudaError_t {
+        if (bytes <= allow) return cudaSuccess;
+        const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e == cudaSuccess) allow = bytes;
+        return e;
+    };
+    if (hit != cache.end()) {
+        *smem_out = hit->second;
+        return set_attr(hit->second);
+    }
+    auto occupancy = [&](size_t bytes, int* occ) -> cudaError_t {
+        const cudaError_t e = set_attr(bytes);
+        if (e != cudaSuccess) return e;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, kThreads, bytes);
+    };
+    int occ = 0;
+    cudaError_t e = occupancy(base, &occ);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    const int most = std::min(occ, max_ctas);
+    const int rounds = (ctas + sms * most - 1) / (sms * most);
+    const int target = std::max(1, std::min(most, (ctas + sms * rounds - 1) / (sms * rounds)));
+    size_t smem = base;
+    while (occ > target) {
+        smem += 1024;
+        if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+        if ((e = occupancy(smem, &occ)) != cudaSuccess) return e;
+    }
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    cache[key] = smem;
+    *smem_out = smem;
+    return cudaSuccess;
 }
 
 cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int form, int* n_blocks,
@@ -878,21 +969,10 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
         kern = ncs == 20 ? prune20v_kernel<20, true> : ncs == 24 ? prune20v_kernel<24, true>
                                                                  : prune20v_kernel<0, true>;
     }
-    // pad the shared memory until no more CTAs fit on an SM than its TMEM serves
-    const int max_ctas = 512 / g.tmem_cols;
-    size_t smem = smem20u_bytes(a, form);
-    int occ = 0;
-    for (;;) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, smem);
-        if (e != cudaSuccess) return e;
-        if (occ <= max_ctas) break;
-        smem += 4096;
-        if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    }
-    if (occ < 1) return cudaErrorInvalidConfiguration;
     dim3 grid((a.n_sites + kTile - 1) / kTile, a.C);
+    size_t smem = 0;
+    const cudaError_t pe = pick_ctas_per_sm(kern, smem20u_bytes(a, form), 512 / g.tmem_cols, (int)(grid.x * grid.y), &smem);
+    if (pe != cudaSuccess) return pe;
     kern<<<grid, kThreads, smem, st>>>(g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
