@@ -99,7 +99,12 @@ plk_status plk_set_alignment(plk_handle* h, int n_tips, int n_sites, int n_state
 /* The same with one byte per cell (bit s = state s allowed), for alphabets
  * of at most 8 states: a quarter of the host-to-device traffic.  For <= 4
  * states without site patterns the bytes go to the device as they are and are
- * encoded there; otherwise they are widened on the host first. */
+ * encoded there; otherwise they are widened on the host first.  With 4 states
+ * and at least 16,384 sites the bytes are the codes themselves: they are
+ * copied in place in site chunks (PLK_STREAM_CHUNKS, default 2; 0 turns this
+ * off) and the next FP32 evaluation starts while they land.  As with every
+ * upload from pinned memory, the copy is asynchronous: keep the buffer
+ * unchanged until the next evaluation has returned. */
 plk_status plk_set_alignment8(plk_handle* h, int n_tips, int n_sites, int n_states,
                               const uint8_t* masks);
 

@@ -127,6 +127,7 @@ struct plk_handle {
     // pinned arena of small host-to-device uploads, and the event after the
     // last copy out of it; a pinned word for the tip-check flag
     char* arena = nullptr;
+    char* arena_dev = nullptr;  // the arena's device address (mapped)
     size_t arena_off = 0;
     cudaEvent_t arena_done = nullptr;
     int* h_flag = nullptr;
@@ -138,12 +139,22 @@ struct plk_handle {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t main_done = nullptr, codes_ready = nullptr;
     bool codes_pending = false;
+    // a streamed alignment (byte masks, 4 states): the masks are copied in
+    // place as codes in chunks of chunk_sites sites, each chunk followed by a
+    // 4-byte copy of the alignment's generation (flag_gen, from the pinned
+    // ring h_gen) into d_arrive[chunk]; a warp-independent pass starts
+    // before the last chunk lands and waits per tile
+    bool codes_streamed = false;
+    int chunk_sites = 0;
+    DevBuf d_arrive;
+    int* h_gen = nullptr;
     ~plk_handle() {
         for (auto& s : evs)
             for (auto& e : s.e) cudaEventDestroy(e);
         if (arena) cudaFreeHost(arena);
         if (arena_done) cudaEventDestroy(arena_done);
         if (h_flag) cudaFreeHost(h_flag);
+        if (h_gen) cudaFreeHost(h_gen);
         if (main_done) cudaEventDestroy(main_done);
         if (codes_ready) cudaEventDestroy(codes_ready);
     }
@@ -169,11 +180,31 @@ plk_status cuda_fail(plk_handle* h, cudaError_t e, const char* what) {
     } while (0)
 
 constexpr size_t kArenaBytes = 1 << 20;
+// streamed alignments (plk_set_alignment8, 4 states): from this many sites
+// on, in this many chunks; the pinned ring of generations the arrival flags
+// are copied from
+constexpr int kStreamMinSites = 16384;
+constexpr int kStreamChunks = 16;  // at most; 2 by default (PLK_STREAM_CHUNKS)
+constexpr int kGenRing = 256;
+
+// The handle's pinned upload arena, mapped into the device's address space.
+cudaError_t ensure_arena(plk_handle* h) {
+    if (h->arena) return cudaSuccess;
+    cudaError_t e = cudaHostAlloc(&h->arena, kArenaBytes, cudaHostAllocMapped);
+    if (e != cudaSuccess) return e;
+    void* dev = nullptr;
+    if ((e = cudaHostGetDevicePointer(&dev, h->arena, 0)) != cudaSuccess) return e;
+    h->arena_dev = static_cast<char*>(dev);
+    if ((e = cudaEventCreateWithFlags(&h->arena_done, cudaEventDisableTiming)) != cudaSuccess) return e;
+    h->arena_off = 0;
+    return cudaSuccess;
+}
 
 // Host-to-device upload of v into b on the handle's stream.  Small arrays go
-// through the handle's pinned arena, so the copy is asynchronous (a pageable
-// copy stages synchronously); the arena starts over once the event after its
-// last copy has completed.  Larger arrays are copied from pageable memory.
+// through the handle's pinned arena and are copied by a kernel that reads
+// the mapped arena (asynchronous, and never queued behind a large DMA copy);
+// the arena starts over once the event after its last copy has completed.
+// Larger arrays are copied from pageable memory.
 template <typename T>
 cudaError_t upload(plk_handle* h, DevBuf& b, const std::vector<T>& v) {
     cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
@@ -181,11 +212,7 @@ cudaError_t upload(plk_handle* h, DevBuf& b, const std::vector<T>& v) {
     if (v.empty()) return cudaSuccess;
     const size_t bytes = sizeof(T) * v.size();
     if (bytes > kArenaBytes) return cudaMemcpyAsync(b.p, v.data(), bytes, cudaMemcpyHostToDevice, h->stream);
-    if (!h->arena) {
-        if ((e = cudaMallocHost(&h->arena, kArenaBytes)) != cudaSuccess) return e;
-        if ((e = cudaEventCreateWithFlags(&h->arena_done, cudaEventDisableTiming)) != cudaSuccess) return e;
-        h->arena_off = 0;
-    }
+    if ((e = ensure_arena(h)) != cudaSuccess) return e;
     if (h->arena_off + bytes > kArenaBytes) {
         if ((e = cudaEventSynchronize(h->arena_done)) != cudaSuccess) return e;
         h->arena_off = 0;
@@ -193,7 +220,7 @@ cudaError_t upload(plk_handle* h, DevBuf& b, const std::vector<T>& v) {
     char* src = h->arena + h->arena_off;
     std::memcpy(src, v.data(), bytes);
     h->arena_off = (h->arena_off + bytes + 15) & ~(size_t)15;
-    if ((e = cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) return e;
+    if ((e = launch_arena_copy(b.p, h->arena_dev + (src - h->arena), bytes, h->stream)) != cudaSuccess) return e;
     return cudaEventRecord(h->arena_done, h->stream);
 }
 
@@ -233,11 +260,7 @@ cudaError_t upload_group(plk_handle* h, DevBuf& block, std::initializer_list<Upl
         return cudaSuccess;
     }
     if (total == 0) return cudaSuccess;
-    if (!h->arena) {
-        if ((e = cudaMallocHost(&h->arena, kArenaBytes)) != cudaSuccess) return e;
-        if ((e = cudaEventCreateWithFlags(&h->arena_done, cudaEventDisableTiming)) != cudaSuccess) return e;
-        h->arena_off = 0;
-    }
+    if ((e = ensure_arena(h)) != cudaSuccess) return e;
     h->arena_off = (h->arena_off + 255) & ~(size_t)255;
     if (h->arena_off + total > kArenaBytes) {
         if ((e = cudaEventSynchronize(h->arena_done)) != cudaSuccess) return e;
@@ -250,7 +273,7 @@ cudaError_t upload_group(plk_handle* h, DevBuf& block, std::initializer_list<Upl
         off += (q.bytes + 255) & ~(size_t)255;
     }
     h->arena_off += total;
-    if ((e = cudaMemcpyAsync(block.p, src, total, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) return e;
+    if ((e = launch_arena_copy(block.p, h->arena_dev + (src - h->arena), total, h->stream)) != cudaSuccess) return e;
     return cudaEventRecord(h->arena_done, h->stream);
 }
 
@@ -489,9 +512,16 @@ void clear_counters(plk_handle* h) {
 // Runs the post-order pass (P(t) already built); store != null asks for the
 // conditional vectors of every internal node in *store.
 plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* after_prune = nullptr) {
+    // a streamed alignment's codes: a tuned warp-independent FP32 pass starts
+    // while they land and waits per tile; every other pass after all of them
+    bool streamed = false;
     if (h->codes_pending) {  // the tip codes come from the copy stream
-        PLK_CUDA(h, cudaStreamWaitEvent(h->stream, h->codes_ready, 0), "cudaStreamWaitEvent");
-        h->codes_pending = false;
+        const int v = tuned_variant(h);
+        streamed = h->codes_streamed && precision == PLK_FP32S && store == nullptr && v >= 12 && v <= 18;
+        if (!streamed) {
+            PLK_CUDA(h, cudaStreamWaitEvent(h->stream, h->codes_ready, 0), "cudaStreamWaitEvent");
+            h->codes_pending = false;
+        }
     }
     const size_t tsz = precision == PLK_FP64 ? sizeof(double) : sizeof(float);
     const size_t vec_bytes = (size_t)h->post.size() * h->C * h->n_sites * h->S * tsz;
@@ -569,8 +599,17 @@ plk_status run_prune(plk_handle* h, int precision, void** store, cudaEvent_t* af
         }
         a.variant = h->variant;
     }
+    if (streamed && a.variant >= 12 && a.variant <= 18) {
+        a.arrive = h->d_arrive.as<int>();
+        a.arrive_gen = h->flag_gen;
+        a.chunk_sites = h->chunk_sites;
+    }
     int nb = 0;
     const cudaError_t le = launch_prune(a, h->S, precision, store != nullptr, &nb, h->stream);
+    if (streamed) {  // the rest of the copy stream (the empty-cell check) before anything after the pass
+        PLK_CUDA(h, cudaStreamWaitEvent(h->stream, h->codes_ready, 0), "cudaStreamWaitEvent");
+        h->codes_pending = false;
+    }
     if (le != cudaSuccess) {
         clear_counters(h);  // a launch that failed part-way may leave arrivals counted
         return cuda_fail(h, le, "post-order kernel launch");
@@ -674,6 +713,7 @@ plk_status set_alignment_impl(plk_handle* h, int n_tips, int n_sites, int n_stat
         PLK_CUDA(h, cudaStreamWaitEvent(h->stream, h->codes_ready, 0), "cudaStreamWaitEvent");
         h->codes_pending = false;
     }
+    h->codes_streamed = false;
     h->n_sites_full = n_sites;
     h->site_pattern.clear();
     h->pattern_w.clear();
@@ -738,16 +778,64 @@ plk_status set_alignment_impl(plk_handle* h, int n_tips, int n_sites, int n_stat
         }
         if (!h->h_flag) PLK_CUDA(h, cudaMallocHost(&h->h_flag, sizeof(int)), "allocate flag");
         h->flag_gen = h->flag_gen == 0x7fffffff ? 1 : h->flag_gen + 1;
+        // byte masks of 4 states are the codes themselves (the passes mask a
+        // code to its low four bits): copied in place in chunks, with an
+        // arrival flag per chunk, once the alignment is large enough for the
+        // pass to overlap the copy
+        // PLK_STREAM_CHUNKS: the number of chunks (0: no streaming).  Two
+        // measured best on 128 x 100,000 end to end (164 us a step against
+        // 178 unstreamed, 172 with three chunks or four, 187 with eight: each
+        // chunk costs two API calls of host time before the pass is launched)
+        int chunks = 2;
+        if (const char* e = getenv("PLK_STREAM_CHUNKS")) chunks = std::max(0, std::min(kStreamChunks, atoi(e)));
+        const bool stream_codes = masks8 != nullptr && n_states == 4 && n_sites >= kStreamMinSites && chunks > 0;
+        int n_chunks = 0;
+        if (stream_codes) {
+            const int want = std::min(chunks, (n_sites + 127) / 128);
+            h->chunk_sites = ((n_sites + want - 1) / want + 127) / 128 * 128;  // whole 128-site tiles
+            n_chunks = (n_sites + h->chunk_sites - 1) / h->chunk_sites;
+            if (h->d_arrive.bytes < sizeof(int) * kStreamChunks) {  // zero once: generations count from 1
+                PLK_CUDA(h, h->d_arrive.ensure(sizeof(int) * kStreamChunks), "allocate arrival flags");
+                PLK_CUDA(h, cudaMemsetAsync(h->d_arrive.p, 0, sizeof(int) * kStreamChunks, h->stream),
+                         "clear arrival flags");
+            }
+            if (!h->h_gen) PLK_CUDA(h, cudaMallocHost(&h->h_gen, sizeof(int) * kGenRing), "allocate generations");
+        }
         // the copy stream starts after all work already on the main stream
         // (earlier passes still reading the masks or codes, the flag clear)
         PLK_CUDA(h, cudaEventRecord(h->main_done, h->stream), "cudaEventRecord");
         PLK_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->main_done, 0), "cudaStreamWaitEvent");
-        PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks8 ? (const void*)masks8 : (const void*)masks, n_cells * eb,
-                                    cudaMemcpyHostToDevice, h->copy_stream),
-                 "upload masks");
-        PLK_CUDA(h, launch_encode_small(h->d_mask_raw.p, eb, n_tips, n_sites, code_stride(n_sites), all,
-                                        h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->flag_gen, h->copy_stream),
-                 "encode kernel launch");
+        if (stream_codes) {
+            // a ring slot of the pinned generations: its last reader (the
+            // copy kGenRing alignments ago) is done once the copy stream has
+            // drained, which is waited for when the ring wraps
+            const int slot = h->flag_gen % kGenRing;
+            if (slot == 0) PLK_CUDA(h, cudaStreamSynchronize(h->copy_stream), "drain copy stream");
+            h->h_gen[slot] = h->flag_gen;
+            const size_t stride = (size_t)code_stride(n_sites);
+            for (int c = 0; c < n_chunks; ++c) {
+                const size_t s0 = (size_t)c * h->chunk_sites;
+                const size_t w = std::min((size_t)h->chunk_sites, (size_t)n_sites - s0);
+                PLK_CUDA(h, cudaMemcpy2DAsync(h->d_codes.as<uint8_t>() + s0, stride, masks8 + s0, (size_t)n_sites, w,
+                                              (size_t)n_tips, cudaMemcpyHostToDevice, h->copy_stream),
+                         "upload masks");
+                PLK_CUDA(h, cudaMemcpyAsync(h->d_arrive.as<int>() + c, h->h_gen + slot, sizeof(int),
+                                            cudaMemcpyHostToDevice, h->copy_stream),
+                         "arrival flag");
+            }
+            PLK_CUDA(h, launch_check_codes(h->d_codes.as<uint8_t>(), n_tips, n_sites, (int)stride, all,
+                                           h->d_flag.as<int>(), h->flag_gen, h->copy_stream),
+                     "check kernel launch");
+        } else {
+            PLK_CUDA(h, cudaMemcpyAsync(h->d_mask_raw.p, masks8 ? (const void*)masks8 : (const void*)masks,
+                                        n_cells * eb, cudaMemcpyHostToDevice, h->copy_stream),
+                     "upload masks");
+            PLK_CUDA(h, launch_encode_small(h->d_mask_raw.p, eb, n_tips, n_sites, code_stride(n_sites), all,
+                                            h->d_codes.as<uint8_t>(), h->d_flag.as<int>(), h->flag_gen,
+                                            h->copy_stream),
+                     "encode kernel launch");
+        }
+        h->codes_streamed = stream_codes;
         // the empty-cell flag comes back with the next result fetch (no wait
         // here); the code table is the identity, so none is uploaded (the
         // P(t) kernel takes the code as the state set)

@@ -183,6 +183,13 @@ struct DeviceModel {
 };
 // p_kind: 0 taylor20, 1 eigen (reversible), 2 series (non-reversible)
 cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st);
+// copies bytes (both addresses 16-byte aligned) from mapped pinned host
+// memory with loads over the host link instead of a DMA copy
+cudaError_t launch_arena_copy(void* dst, const void* src_mapped, size_t bytes, cudaStream_t st);
+// the empty-cell check of byte masks copied in place as codes (the streamed
+// alignment): *bad = gen when a cell of sites < n_sites allows no state
+cudaError_t launch_check_codes(const uint8_t* codes, int n_tips, int n_sites, int stride, uint32_t all, int* bad,
+                               int gen, cudaStream_t st);
 
 struct PruneArgs {
     const Op* ops;
@@ -245,6 +252,13 @@ struct PruneArgs {
     // never stages its first op, the shared-table form never copies its
     // tables, so their bounded waits run out
     int withhold_first_stage;
+    // streamed tip codes (plk_set_alignment8, 4 states): the codes of sites
+    // [c chunk_sites, (c + 1) chunk_sites) have landed once arrive[c] holds
+    // arrive_gen.  The warp-independent forms wait for their tile's chunk
+    // (bounded); null for every other launch, which runs after all chunks.
+    const int* arrive;
+    int arrive_gen;
+    int chunk_sites;
 };
 // Fused 20-state FP32 kernels (plk_prune20.cu): mode 1 = CUDA cores, 2 =
 // tensor cores.  Launches the relayout, the pass and the per-site combine

@@ -804,6 +804,70 @@ cudaError_t launch_encode_small(const void* masks, int elem_bytes, int n_tips, i
     return cudaGetLastError();
 }
 
+// Copies bytes from mapped pinned host memory (the handle's upload arena)
+// into device memory with loads over the host link, not a DMA copy: a small
+// upload then never queues behind a large host-to-device copy (a streamed
+// alignment's chunks) on the copy engines.
+__global__ void arena_copy_kernel(unsigned char* __restrict__ dst, const unsigned char* __restrict__ src,
+                                  size_t bytes) {
+    const size_t n16 = bytes / 16;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, step = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = t; i < n16; i += step)
+        reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
+    for (size_t i = n16 * 16 + t; i < bytes; i += step) dst[i] = src[i];
+}
+
+cudaError_t launch_arena_copy(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes == 0) return cudaSuccess;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) != 0 || (reinterpret_cast<uintptr_t>(src) & 15) != 0)
+        return cudaErrorInvalidValue;
+    size_t blocks = (bytes / 16 + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 64) blocks = 64;
+    arena_copy_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<unsigned char*>(dst),
+                                                        static_cast<const unsigned char*>(src), bytes);
+    return cudaGetLastError();
+}
+
+// The empty-cell check of the streamed alignment: 16 codes of a row per
+// thread (rows are code_stride bytes, 16-byte aligned), sites past n_sites
+// ignored.
+__global__ void check_codes_kernel(const uint4* __restrict__ codes, int n_tips, int n_sites, int vec_per_row,
+                                   uint32_t all4, int* __restrict__ bad, int gen) {
+    int any_bad = 0;
+    const size_t n_vec = (size_t)n_tips * vec_per_row;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_vec; i += (size_t)gridDim.x * blockDim.x) {
+        const int first = (int)(i % vec_per_row) * 16;  // the vector's first site
+        uint4 v = codes[i];
+        v.x &= all4;
+        v.y &= all4;
+        v.z &= all4;
+        v.w &= all4;
+        uint32_t z[4] = {(v.x - 0x01010101u) & ~v.x, (v.y - 0x01010101u) & ~v.y, (v.z - 0x01010101u) & ~v.z,
+                         (v.w - 0x01010101u) & ~v.w};
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const int valid = min(max(n_sites - (first + 4 * w), 0), 4);  // bytes of this word within the row
+            const uint32_t keep = valid >= 4 ? 0xffffffffu : ((1u << (8 * valid)) - 1u);
+            any_bad |= (z[w] & keep & 0x80808080u) != 0;
+        }
+    }
+    if (__any_sync(0xffffffffu, any_bad) && (threadIdx.x & 31) == 0) *reinterpret_cast<volatile int*>(bad) = gen;
+}
+
+cudaError_t launch_check_codes(const uint8_t* codes, int n_tips, int n_sites, int stride, uint32_t all, int* bad,
+                               int gen, cudaStream_t st) {
+    if (stride % 16 != 0 || (reinterpret_cast<uintptr_t>(codes) & 15) != 0) return cudaErrorInvalidValue;
+    const size_t n_vec = (size_t)n_tips * (stride / 16);
+    size_t blocks = (n_vec + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    const uint32_t all4 = (all & 0xffu) * 0x01010101u;
+    check_codes_kernel<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const uint4*>(codes), n_tips, n_sites,
+                                                         stride / 16, all4, bad, gen);
+    return cudaGetLastError();
+}
+
 // sum_i w_i x_i with TwoSum compensation in one CTA (site patterns: x = the
 // pattern lnL, w = its number of sites)
 __global__ void __launch_bounds__(1024) weighted_sum_kernel(const double* __restrict__ x,

@@ -216,32 +216,52 @@ __device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[N]) {
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 
-// a tip code, loaded without allocating in L1 (which holds the tables)
-__device__ __forceinline__ int ldg_code_na(const uint8_t* p) {
-    unsigned short v;
-    asm volatile("ld.global.nc.L1::no_allocate.u8 %0, [%1];\n" : "=h"(v) : "l"(p));
-    return (int)v;
-}
-
-// this thread's tip codes (SPT adjacent sites, one load of SPT bytes) of op
-// o's children (0 where a child is no tip); colp points at the thread's first
-// site in the code matrix
+// this thread's tip codes (SPT adjacent sites, one load of SPT bytes),
+// loaded without allocating in L1 (which holds the tables).  Plain (coherent)
+// loads, not the read-only path: a streamed alignment's codes land while the
+// pass runs (a warp reads its tile's codes only after their arrival flag).
 template <int SPT>
 __device__ __forceinline__ int ldg_codes_na(const uint8_t* p) {
     if constexpr (SPT == 1) {
         unsigned short v;
-        asm volatile("ld.global.nc.L1::no_allocate.u8 %0, [%1];\n" : "=h"(v) : "l"(p));
+        asm volatile("ld.global.L1::no_allocate.u8 %0, [%1];\n" : "=h"(v) : "l"(p));
         return (int)v;
     } else if constexpr (SPT == 2) {
         unsigned short v;
-        asm volatile("ld.global.nc.L1::no_allocate.u16 %0, [%1];\n" : "=h"(v) : "l"(p));
+        asm volatile("ld.global.L1::no_allocate.u16 %0, [%1];\n" : "=h"(v) : "l"(p));
         return (int)v;
     } else {
         int v;
-        asm volatile("ld.global.nc.L1::no_allocate.u32 %0, [%1];\n" : "=r"(v) : "l"(p));
+        asm volatile("ld.global.L1::no_allocate.u32 %0, [%1];\n" : "=r"(v) : "l"(p));
         return v;
     }
 }
+
+// The arrival of a streamed tile's codes: arrive[c] reaching gen (written by a
+// copy after the chunk's copy on the alignment's copy stream).  Every lane
+// reads the flag with acquire semantics, so its code loads that follow see
+// the chunk.  Bounded: false after kArriveLimitNs of waiting.
+constexpr unsigned long long kArriveLimitNs = 2000000000ull;  // 2 s: far above any chunk's copy time
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ bool wait_arrival(const int* flag, int gen) {
+    if (ld_acquire_gpu(flag) == gen) return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        __nanosleep(256);
+        if (ld_acquire_gpu(flag) == gen) return true;
+        if (global_ns() - t0 > kArriveLimitNs) return false;
+    }
+}
+
 template <int SPT, class Tab>
 __device__ __forceinline__ void op_codes(const Tab& tab, int o, const uint8_t* colp, int stride, int& c0, int& c1) {
     const int2 sv = tab.sources(o);
@@ -354,6 +374,13 @@ __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneA
     const f2 one2 = pk2(1.0f, 1.0f);
     if (!tables_ok) site_sum_add(sum, __int_as_float(0x7fc00000), 0);
     for (int wtile = warp * gridDim.x + blockIdx.x; tables_ok && wtile < n_wtiles; wtile += total_warps) {
+        if (a.arrive) {  // a streamed alignment: this tile's chunk of codes first (the test hook withholds it)
+            const int want = a.withhold_first_stage ? (a.arrive_gen ^ 0x40000000) : a.arrive_gen;
+            if (!wait_arrival(a.arrive + (wtile * WS * SPT) / a.chunk_sites, want)) {
+                site_sum_add(sum, __int_as_float(0x7fc00000), 0);  // NaN: the evaluation reports a numeric error
+                continue;
+            }
+        }
         const int base = wtile * WS * SPT + (TPS == 2 ? lane >> 1 : lane) * SPT;  // site s: base + s
         const uint8_t* colp = a.codes + min(base, stride - SPT);
         f2 acc[SPT][KPT][4];

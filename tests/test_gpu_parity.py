@@ -461,3 +461,66 @@ def test_error_reporting_entry_points(name):
             assert err == float(np.abs(n32 - n64).max())
             assert err < FP32_PROB
         np.testing.assert_allclose(h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64), orc.marginal, atol=1e-11)
+
+
+@pytest.mark.parametrize("variant", [None, "13", "16"])
+def test_streamed_byte_alignment_matches_the_32bit_path(monkeypatch, variant):
+    """plk_set_alignment8 with 4 states and at least 16,384 sites copies the
+    masks in place as codes, in chunks each followed by an arrival flag; a
+    warp-independent pass starts while they land and waits per tile.  Every
+    evaluation after a fresh alignment gives the bits of the 32-bit path,
+    whose codes are encoded before the pass."""
+    rng = np.random.default_rng(31)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 40, 20000, C=4)
+    if variant:
+        monkeypatch.setenv("PLK_PRUNE_VARIANT", variant)
+    res = []
+    for m in (masks.astype(np.uint32), masks.astype(np.uint8)):
+        with _engine(left, right, bl, m, 4, Q, f, cr, cw) as h:
+            vals = []
+            for _ in range(3):  # a fresh alignment each time (the first one tunes the form)
+                h.set_alignment(m, 4)
+                vals.append(h.loglik(plk.PLK_FP32S))
+            res.append((vals, h.site_loglik(), h.prune_kernel()))
+    np.testing.assert_array_equal(res[0][1], res[1][1])  # every FP32 form: the same per-site bits
+    if res[0][2] == res[1][2]:  # the same form (the tuner may pick another on timing noise)
+        assert res[0][0] == res[1][0]
+    else:
+        assert res[0][0] == pytest.approx(res[1][0], rel=1e-12)
+
+
+def test_streamed_alignment_reports_an_empty_cell(monkeypatch):
+    """The empty-cell check of a streamed alignment runs on the copy stream
+    beside the pass and still turns a cell that allows no state (here the
+    last site of a row) into PLK_ERR_TIP, as the encoded path does."""
+    rng = np.random.default_rng(32)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 24, 17000, C=4)
+    m8 = masks.astype(np.uint8)
+    m8[5, 16999] = 0
+    monkeypatch.setenv("PLK_PRUNE_VARIANT", "16")
+    with _engine(left, right, bl, m8, 4, Q, f, cr, cw) as h:
+        with pytest.raises(plk.PlkError) as err:
+            h.loglik(plk.PLK_FP32S)
+        assert err.value.status == plk.PLK_ERR_TIP
+
+
+def test_streamed_arrival_wait_times_out_and_the_handle_recovers(monkeypatch):
+    """Failure path of the per-tile arrival wait: with the arrival withheld
+    (the test hook waits for a generation no copy writes) every tile's
+    bounded wait runs out, the evaluation reports PLK_ERR_NUMERIC, and the
+    next evaluation on the same handle is exact."""
+    import time
+    rng = np.random.default_rng(33)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 24, 17000, C=4)
+    monkeypatch.setenv("PLK_PRUNE_VARIANT", "13")  # tables through L1: no table copy to withhold first
+    m8 = masks.astype(np.uint8)
+    with _engine(left, right, bl, m8, 4, Q, f, cr, cw) as h:
+        good = h.loglik(plk.PLK_FP32S)
+        h.set_alignment(m8, 4)
+        h.test_withhold_stage()
+        t0 = time.perf_counter()
+        with pytest.raises(plk.PlkError) as err:
+            h.loglik(plk.PLK_FP32S)
+        assert err.value.status == plk.PLK_ERR_NUMERIC
+        assert time.perf_counter() - t0 < 120.0
+        assert h.loglik(plk.PLK_FP32S) == good
