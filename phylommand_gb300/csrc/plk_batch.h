@@ -59,7 +59,7 @@ struct BatchDev {
     // NNI
     const NniMoveDev* moves;
     const long long* unit_move_off;  // [n_units] offset of each unit's per-move partials
-    double* unit_move_sums;          // [sum over units of n_moves][2]
+    double* unit_move_sums;          // [sum over units of n_moves][2]: 16-byte SiteSum32 records (store_site_record)
     double* nni_out;                 // [sum over items of n_moves]
     const int* move_item;            // [total moves] item of each output move
     int total_moves, scratch_int;    // scratch_int: max internal nodes of any item

@@ -187,8 +187,8 @@ __device__ inline void block_sum_site32(SiteSum32 a, double& s, double& c) {
 
 // A block's SiteSum32 record in the 16 bytes of its block-sum pair:
 // (hi, lo, ee, 0) as one 16-byte store by thread 0.
-__device__ __forceinline__ void store_site_record(double* bs, int block, const SiteSum32& t) {
-    reinterpret_cast<float4*>(bs)[block] = make_float4(t.hi, t.lo, __int_as_float(t.ee), 0.0f);
+__device__ __forceinline__ void store_site_record(double* bs, size_t slot, const SiteSum32& t) {
+    reinterpret_cast<float4*>(bs)[slot] = make_float4(t.hi, t.lo, __int_as_float(t.ee), 0.0f);
 }
 
 // Compensated sum of the n (sum, compensation) pairs of bs by one CTA:

@@ -251,7 +251,10 @@ template <int CM, bool CODES_SMEM>
 __global__ void __launch_bounds__(kPruneThreads, 3) batch_nni_kernel(BatchDev b) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ int s_unit;
-    __shared__ double s_red[kPruneThreads / 32][32][2];
+    // per warp and move of a round: the warp's mantissa-log sum (FP32 TwoSum
+    // pair) and exponent sum
+    __shared__ float s_rh[kPruneThreads / 32][32], s_rl[kPruneThreads / 32][32];
+    __shared__ int s_re[kPruneThreads / 32][32];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const size_t vec_slice = (size_t)b.scratch_int * b.C * TILE;
     const size_t int_slice = (size_t)b.scratch_int * TILE;
@@ -313,44 +316,51 @@ __global__ void __launch_bounds__(kPruneThreads, 3) batch_nni_kernel(BatchDev b)
                 warp_two_sum_f(hi, lo);
                 const int esum = __reduce_add_sync(0xffffffffu, ee);
                 if (lane == 0) {
-                    s_red[warp][mi][0] = (double)esum * 0.69314718055994530942 + (double)hi;
-                    s_red[warp][mi][1] = (double)lo;
+                    s_rh[warp][mi] = hi;
+                    s_rl[warp][mi] = lo;
+                    s_re[warp][mi] = esum;
                 }
             }
             __syncthreads();
             if (tid < mcount) {
-                double s = 0.0, c = 0.0;
+                // the warps in order, FP32 TwoSum and integer sums (FP64
+                // chains here cost GB300 tens of cycles per instruction),
+                // stored as the move's 16-byte record of this tile
+                SiteSum32 t;
                 for (int w = 0; w < kPruneThreads / 32; ++w) {
-                    double ns, e;
-                    two_sum(s, s_red[w][tid][0], ns, e);
-                    s = ns;
-                    c += s_red[w][tid][1] + e;
+                    float ns, e;
+                    two_sum_f(t.hi, s_rh[w][tid], ns, e);
+                    t.hi = ns;
+                    t.lo = __fadd_rn(t.lo, __fadd_rn(s_rl[w][tid], e));
+                    t.ee += s_re[w][tid];
                 }
-                b.unit_move_sums[2 * (out_off + m0 + tid)] = s;
-                b.unit_move_sums[2 * (out_off + m0 + tid) + 1] = c;
+                store_site_record(b.unit_move_sums, (size_t)(out_off + m0 + tid), t);
             }
             __syncthreads();
         }
     }
 }
 
-// one thread per (item, move): sum its tiles in site order
+// one thread per (item, move): fold its tiles' records in site order (FP32
+// TwoSum, integer exponents), lnL = ee ln 2 + hi + lo in FP64 at the end
 __global__ void batch_nni_reduce_kernel(BatchDev b) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= b.total_moves) return;
     const int item = b.move_item[g];
     const BatchItemDev it = b.items[item];
     const int m = g - it.move_out_off;
-    double s = 0.0, c = 0.0;
+    const float4* rec = reinterpret_cast<const float4*>(b.unit_move_sums);
+    SiteSum32 t;
     for (int q = b.item_unit_ptr[item]; q < b.item_unit_ptr[item + 1]; ++q) {
         const int u = b.item_units[q];
-        const double* p = b.unit_move_sums + 2 * (b.unit_move_off[u] + m);
-        double ns, e;
-        two_sum(s, p[0], ns, e);
-        s = ns;
-        c += p[1] + e;
+        const float4 v = rec[b.unit_move_off[u] + m];
+        float ns, e;
+        two_sum_f(t.hi, v.x, ns, e);
+        t.hi = ns;
+        t.lo = __fadd_rn(t.lo, __fadd_rn(v.y, e));
+        t.ee += __float_as_int(v.z);
     }
-    b.nni_out[g] = s + c;
+    b.nni_out[g] = fma((double)t.ee, 0.69314718055994530942, (double)t.hi + (double)t.lo);
 }
 
 // ---------------------------------------------------------------------------
