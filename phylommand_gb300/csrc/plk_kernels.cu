@@ -220,6 +220,9 @@ __global__ void pmat_kernel(DeviceModel m, int p_kind) {
 // P[r][j] = fma over m ascending from 0, tips summed over the allowed
 // states j ascending.
 __global__ void __launch_bounds__(128) pmat4_eigen_kernel(DeviceModel m) {
+    // the post-order pass after it may be scheduled now (it waits for this
+    // kernel's completion before reading the tables)
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     const int lane = threadIdx.x & 31;
     const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;  // (node, category)
     const int r = lane & 3;

@@ -290,6 +290,9 @@ __host__ __device__ constexpr int prune4w_maxnreg(int KP, int SPT, int TPS) {
 template <int KP, int SPT, int TS, int TPS>
 __global__ void __maxnreg__(prune4w_maxnreg(KP, SPT, TPS)) prune4w_kernel(PruneArgs a, const float* __restrict__ Pp,
                                                                           const float* __restrict__ Tp, int tmem_cols) {
+    // the kernel before this one in the stream (P(t), which writes the
+    // tables) has completed and its writes are visible
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
     constexpr int NC = 8 * SPT;     // TMEM columns of one category pair of a slot
     constexpr int KPT = KP / TPS;   // category pairs per thread
     constexpr int WS = 32 / TPS;    // sites per warp and site index s
@@ -825,36 +828,27 @@ cudaError_t launch_prune4w(const PruneArgs& a, int spt, int ts, int tps, int* n_
     const int tmem_cols = prune4w_tmem_cols(KP, spt, warps, a.max_depth, tps);
     const int blocks = std::max(1, std::min(sms, (tiles + warps - 1) / warps));
     *n_blocks = blocks;
-    const dim3 g(blocks), b(warps * 32);
-    if (tps == 2) {
-        if (KP == 2) prune4w_kernel<2, 2, 1, 2><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols);
-        else prune4w_kernel<4, 2, 1, 2><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols);
-        return cudaGetLastError();
-    }
-    if (ts) {
-        switch (KP * 10 + spt) {
-            case 11: prune4w_kernel<1, 1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 12: prune4w_kernel<1, 2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 14: prune4w_kernel<1, 4, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 21: prune4w_kernel<2, 1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 22: prune4w_kernel<2, 2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 24: prune4w_kernel<2, 4, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            case 41: prune4w_kernel<4, 1, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-            default: prune4w_kernel<4, 2, 1, 1><<<g, b, smem, st>>>(a, Pp, Tp, tmem_cols); break;
-        }
-        return cudaGetLastError();
-    }
-    switch (KP * 10 + spt) {
-        case 11: prune4w_kernel<1, 1, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 12: prune4w_kernel<1, 2, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 14: prune4w_kernel<1, 4, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 21: prune4w_kernel<2, 1, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 22: prune4w_kernel<2, 2, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 24: prune4w_kernel<2, 4, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        case 41: prune4w_kernel<4, 1, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-        default: prune4w_kernel<4, 2, 0, 1><<<g, b, 0, st>>>(a, Pp, Tp, tmem_cols); break;
-    }
-    return cudaGetLastError();
+    // launched with programmatic stream serialization: the CTAs may be
+    // scheduled while the P(t) kernel before them finishes (it lets its
+    // dependents launch at its start); the kernel waits for it
+    // (griddepcontrol.wait) before reading anything it wrote
+    const void* fn = prune4w_fn_of(KP, spt, ts, tps);
+    PruneArgs args_a = a;
+    const float* args_p = Pp;
+    const float* args_t = Tp;
+    int args_cols = tmem_cols;
+    void* args[] = {&args_a, &args_p, &args_t, &args_cols};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(warps * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 }  // namespace plk
