@@ -40,6 +40,9 @@ __device__ __forceinline__ float tf32_rna_dev(float x) {
 }
 
 __global__ void pmat_kernel(DeviceModel m, int p_kind) {
+    // a pass launched after it with programmatic stream serialization may be
+    // scheduled now (it waits for this kernel's completion before reading)
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     const int v = blockIdx.x / m.C, k = blockIdx.x % m.C;
     const int S = m.S, SS = S * S;
     extern __shared__ double pm_smem[];

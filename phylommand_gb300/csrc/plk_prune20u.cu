@@ -410,6 +410,7 @@ __device__ __forceinline__ void bulk_stage20(unsigned char* dst, const Op& op, i
 }
 
 __global__ void __launch_bounds__(kThreads, 1) prune20u_kernel(P20UArgs g) {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");  // the kernel before it (P(t)) has completed
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t s_mbar;
     __shared__ uint32_t s_tmem;
@@ -592,6 +593,7 @@ __device__ __forceinline__ Op ldg_op(const Op* ops, int o) {
 
 template <int NCS, bool BF>
 __global__ void __launch_bounds__(kThreads, BF ? 5 : 3) prune20v_kernel(P20UArgs g) {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");  // the kernel before it (P(t)) has completed
     constexpr int APART = BF ? kAPartB : kAPart5;
     constexpr int AOPER = 2 * APART;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -973,8 +975,21 @@ cudaError_t launch_prune20u(const PruneArgs& a, int n_nodes, void* scratch, int 
     size_t smem = 0;
     const cudaError_t pe = pick_ctas_per_sm(kern, smem20u_bytes(a, form), 512 / g.tmem_cols, (int)(grid.x * grid.y), &smem);
     if (pe != cudaSuccess) return pe;
-    kern<<<grid, kThreads, smem, st>>>(g);
-    cudaError_t e = cudaGetLastError();
+    // programmatic stream serialization: the CTAs may be scheduled while the
+    // P(t) kernel before them finishes; the kernels wait for it
+    // (griddepcontrol.wait) before reading anything it wrote
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, g);
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (form >= 1 && a.tile_done) {  // combined in the kernel
         *n_blocks = (int)grid.x;
