@@ -11,11 +11,10 @@
 //    sites' independent products hide the latency of the next loads, and one
 //    load of SPT bytes brings a child's tip codes for all of them;
 //  * TS = 0: P(t) pairs and tip tables are read where the P(t) kernel wrote
-//    them (the paired layouts of plk_prune4p.cuh), through the read-only L1 path,
-//    which the launch gives all of the SM's unified memory that the kernel
-//    does not use as shared memory (none): a P(t) row of an op is the same
-//    address in every lane (one broadcast load of 32 bytes feeds two packed
-//    FMAs per site), a tip-table load gathers each lane's code row;
+//    them (the paired layouts of plk_prune4p.cuh), through the read-only L1
+//    path: a P(t) row of an op is the same address in every lane (one
+//    broadcast load of 32 bytes feeds two packed FMAs per site), a tip-table
+//    load gathers each lane's code row;
 //  * spilled vectors sit in tensor memory (tcgen05.st / tcgen05.ld, one
 //    instruction per category pair and op), not in shared memory;
 //  * the tip codes of op o + 2 are loaded while op o computes (a register
@@ -26,10 +25,18 @@
 //    one mbarrier, a bounded wait) and reads them there;
 //  * every branch on the op's shape is uniform across the warp, and no CTA
 //    barrier stands between ops; one CTA per SM, its warp count chosen per
-//    launch so that every warp has a tile.
+//    launch so that every warp has a tile;
+//  * the rescale test first takes the maximum of one category pair; only when
+//    a lane of the warp falls below the threshold does the warp take the full
+//    maximum (the same decision and factors);
+//  * a streamed alignment's codes land while the pass runs: a warp waits
+//    (bounded) for its tile's chunk flag before its walk;
+//  * the launch overlaps the P(t) kernel before it (programmatic stream
+//    serialization; griddepcontrol.wait before any read of its tables).
 // The arithmetic is run_tile4p's (plk_prune4p.cuh) in the same order -- every
 // product, rescale and root sum on fma.rn.f32x2 / mul.rn.f32x2 lanes -- so the
-// per-site results are the bits of prune4s and prune4p.
+// per-site results are the bits of prune4s and prune4p; the sites' sum is the
+// FP32 record epilogue of every FP32 form (block_sum_site32f).
 #include "plk_prune4p.cuh"
 
 #include <algorithm>
