@@ -197,10 +197,12 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * applies (FP64, other state counts, more than 8 categories). */
 int plk_prune_variant(const plk_handle* h);
 /* Test of the failure path: the next FP32 evaluation that runs one of the
- * mbarrier-driven post-order forms -- the TMA-fed 4-state form (candidate 9)
- * or the tcgen05 20-state forms (candidates 5 and 6) -- withholds the first stage
- * (respectively the first MMA commit) of every tile, so every bounded
- * mbarrier wait of that launch runs out; the tiles' sites come out NaN, the
+ * mbarrier-driven post-order forms -- the TMA-fed 4-state form (candidate 9),
+ * the shared-table warp-independent forms (15-18: their table copy), the
+ * tcgen05 20-state forms (5-7: the first MMA commit) -- withholds the first
+ * stage of every tile or CTA, so every bounded mbarrier wait of that launch
+ * runs out; with a streamed alignment the warp-independent forms (12-18) wait
+ * for an arrival no copy writes.  The tiles' sites come out NaN, the
  * evaluation fails with PLK_ERR_NUMERIC, and the handle stays usable.  No
  * effect on the other forms. */
 plk_status plk_test_withhold_stage(plk_handle* h);
