@@ -188,13 +188,18 @@ plk_status plk_kernel_times(plk_handle* h, double* ms_out, int* n_evals, int res
  * threads per site (each takes half of the category pairs; codes from global
  * memory / staged), 9 = prune4p_bulk_kernel (TMA-fed stage ring), 10 / 11 =
  * prune4p_kernel with 1 / 2 sites per thread and each op's tip codes staged
- * with its tables two ops ahead (the fast forms when the codes exceed L2).  20
- * states: 1 / 2 = prune20_kernel on CUDA cores / mma.sync tensor cores with
- * 4 warps per tile, 3 / 4 = the same with 8 warps, 5 = prune20u_kernel
- * (tcgen05 tensor cores, TMEM accumulators, spill stack in TMEM), 6 =
- * prune20v_kernel (its compact form: three CTAs per SM, spills in global
- * memory).  -1 = not tuned yet or another kernel
- * applies (FP64, other state counts, more than 8 categories). */
+ * with its tables two ops ahead (the fast forms when the codes exceed L2),
+ * 12 / 13 / 14 = prune4w_kernel (every warp walks the op list alone over its
+ * own 32 x 1 / 2 / 4 sites, tables through L1, spill stack in TMEM), 15 / 16
+ * / 17 = the same with the tree's tables in shared memory, 18 = two threads
+ * per site pair with the tables in shared memory.  20 states: 1 / 2 =
+ * prune20_kernel on CUDA cores / mma.sync tensor cores with 4 warps per tile,
+ * 3 / 4 = the same with 8 warps, 5 = prune20u_kernel (tcgen05 tensor cores,
+ * TMEM accumulators, spill stack in TMEM), 6 = prune20v_kernel (its compact
+ * form: spills in global memory, split TF32), 7 = the compact form with
+ * split-BF16 products (tcgen05 kind::f16, five CTAs per SM).  -1 = not tuned
+ * yet or another kernel applies (FP64, other state counts, more than 8
+ * categories). */
 int plk_prune_variant(const plk_handle* h);
 /* Test of the failure path: the next FP32 evaluation that runs one of the
  * mbarrier-driven post-order forms -- the TMA-fed 4-state form (candidate 9),
