@@ -183,6 +183,9 @@ struct DeviceModel {
 };
 // p_kind: 0 taylor20, 1 eigen (reversible), 2 series (non-reversible)
 cudaError_t launch_pmat(const DeviceModel& m, int p_kind, cudaStream_t st);
+// unique id of the current CUDA context (0 when it cannot be had): launch
+// set-up caches key on it, since a device reset resets kernel attributes
+unsigned long long current_ctx_id();
 // copies bytes (both addresses 16-byte aligned) from mapped pinned host
 // memory with loads over the host link instead of a DMA copy
 cudaError_t launch_arena_copy(void* dst, const void* src_mapped, size_t bytes, cudaStream_t st);

@@ -101,38 +101,44 @@ std::mutex g_setup_mu;
 double* g_partials_addr[kMaxDevices] = {nullptr};
 unsigned long long g_partials_ctx[kMaxDevices] = {0};  // the context the address belongs to (0: unknown)
 
+}  // namespace
+
+namespace plk {
+
 // Unique id of the current context (cuCtxGetId, fetched through the
 // runtime's driver entry points), 0 when it cannot be had.  A device reset
 // destroys the primary context and the next runtime call makes a new one
-// with a new id, in which the array may sit at another address.  Called
-// under g_setup_mu.
+// with a new id, in which device symbols may sit at other addresses and a
+// kernel's attributes are back at their defaults.  Thread-safe.
 unsigned long long current_ctx_id() {
     typedef CUresult (*GetCurrent)(CUcontext*);
     typedef CUresult (*GetId)(CUcontext, unsigned long long*);
-    static GetCurrent get_current = nullptr;
-    static GetId get_id = nullptr;
-    static bool looked_up = false;
-    if (!looked_up) {
-        looked_up = true;
-        void* f = nullptr;
+    struct Fns {
+        GetCurrent get_current = nullptr;
+        GetId get_id = nullptr;
+    };
+    static const Fns fns = [] {  // looked up once (thread-safe initialisation)
+        Fns f;
+        void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            get_current = reinterpret_cast<GetCurrent>(f);
-        f = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            f.get_current = reinterpret_cast<GetCurrent>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            get_id = reinterpret_cast<GetId>(f);
-    }
-    if (!get_current || !get_id) return 0;
+            f.get_id = reinterpret_cast<GetId>(p);
+        return f;
+    }();
+    if (!fns.get_current || !fns.get_id) return 0;
     CUcontext ctx = nullptr;
     unsigned long long id = 0;
-    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
-    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    if (fns.get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+    if (fns.get_id(ctx, &id) != CUDA_SUCCESS) return 0;
     return id;
 }
 
-}  // namespace
+}  // namespace plk
 
 extern "C" plk_status plk_sum_sites_noalloc(const double* d_site_lnl, int n_sites, double* d_lnl_out,
                                             void* cuda_stream) {
@@ -154,7 +160,7 @@ extern "C" plk_status plk_sum_sites_noalloc(const double* d_site_lnl, int n_site
         // reset): resolve the device address of the array with that device
         // current (host code cannot use the symbol itself)
         std::lock_guard<std::mutex> lock(g_setup_mu);
-        const unsigned long long ctx = current_ctx_id();
+        const unsigned long long ctx = plk::current_ctx_id();
         if (!g_partials_addr[dev] || (ctx != 0 && ctx != g_partials_ctx[dev])) {
             e = cudaGetSymbolAddress(reinterpret_cast<void**>(&g_partials_addr[dev]), g_noalloc_partials);
             if (e != cudaSuccess) {
@@ -163,7 +169,7 @@ extern "C" plk_status plk_sum_sites_noalloc(const double* d_site_lnl, int n_site
                                                            cudaGetErrorString(e));
             }
             // the id of the context the runtime just used (made, after a reset)
-            g_partials_ctx[dev] = ctx != 0 ? ctx : current_ctx_id();
+            g_partials_ctx[dev] = ctx != 0 ? ctx : plk::current_ctx_id();
         }
         partials = g_partials_addr[dev];
     }

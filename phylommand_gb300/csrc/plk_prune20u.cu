@@ -885,19 +885,20 @@ size_t prune20u_scratch_bytes(const PruneArgs& a, int n_nodes) {
 // chain of a round takes about as long, so 628 chains at 4 per SM (608 in a
 // first round, 20 in a second) take twice as long as at 5 per SM in one, and
 // at 3 per SM (456 and 172) the two rounds are shorter than at 4.  Cached per
-// device, kernel, bytes and grid: the attribute and occupancy calls cost
+// device, context, kernel, bytes and grid: the attribute and occupancy calls cost
 // microseconds of host time per launch.
 static cudaError_t pick_ctas_per_sm(void (*kern)(P20UArgs), size_t base, int max_ctas, int ctas, size_t* smem_out) {
     static std::mutex mu;
-    static std::map<std::tuple<int, const void*, size_t, int, int>, size_t> cache;
-    static std::map<std::pair<int, const void*>, size_t> allowed;
+    static std::map<std::tuple<int, unsigned long long, const void*, size_t, int, int>, size_t> cache;
+    static std::map<std::tuple<int, unsigned long long, const void*>, size_t> allowed;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    const unsigned long long ctx = current_ctx_id();  // a device reset starts the caches over
     std::lock_guard<std::mutex> lock(mu);
-    const auto key = std::make_tuple(dev, reinterpret_cast<const void*>(kern), base, max_ctas, ctas);
+    const auto key = std::make_tuple(dev, ctx, reinterpret_cast<const void*>(kern), base, max_ctas, ctas);
     const auto hit = cache.find(key);
-    size_t& allow = allowed[std::make_pair(dev, reinterpret_cast<const void*>(kern))];
+    size_t& allow = allowed[std::make_tuple(dev, ctx, reinterpret_cast<const void*>(kern))];
     auto set_attr = [&](size_t bytes) -> cudaError_t {
         if (bytes <= allow) return cudaSuccess;
         const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

@@ -737,20 +737,21 @@ int prune4w_tmem_cols(int KP, int SPT, int warps, int depth, int TPS = 1) {
 // launch runs every evaluation); the carveout gives the L1 cache all the
 // shared memory the kernel does not use
 int prune4w_ctas_per_sm(int KP, int SPT, int TS, int warps, size_t smem, int TPS = 1) {
-    if (TS) {  // sized per launch (the tables): cached per device, kernel, warps and bytes
+    if (TS) {  // sized per launch (the tables): cached per device, context, kernel, warps and bytes
         const void* fn = prune4w_fn_of(KP, SPT, 1, TPS);
         int dev = 0;
         cudaGetDevice(&dev);
+        const unsigned long long ctx = current_ctx_id();  // a device reset starts the caches over
         static std::mutex mu;
-        static std::map<std::tuple<int, const void*, int, size_t>, int> occ;
-        static std::map<std::pair<int, const void*>, size_t> attr;  // the largest dynamic size allowed so far
+        static std::map<std::tuple<int, unsigned long long, const void*, int, size_t>, int> occ;
+        static std::map<std::tuple<int, unsigned long long, const void*>, size_t> attr;  // the largest size allowed
         std::lock_guard<std::mutex> lock(mu);
-        size_t& allowed = attr[std::make_pair(dev, fn)];
+        size_t& allowed = attr[std::make_tuple(dev, ctx, fn)];
         if (smem > allowed) {
             if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
             allowed = smem;
         }
-        const auto key = std::make_tuple(dev, fn, warps, smem);
+        const auto key = std::make_tuple(dev, ctx, fn, warps, smem);
         const auto it = occ.find(key);
         if (it != occ.end()) return it->second;
         int n = 0;
