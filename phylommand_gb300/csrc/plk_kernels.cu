@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
         T d0[CM][4], d1[CM][4];
         // ---- first child vector
         if (op.s0 >= 0) {
-            const int code = codes[(size_t)op.s0 * a.site_stride + cs];
+            const int code = codes[(size_t)op.s0 * a.site_stride + cs] & (kCodes - 1);  // streamed codes: raw bytes
 #pragma unroll
             for (int k = 0; k < CM; ++k)
                 if (k < C) {
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kPruneThreads) prune4_kernel(PruneArgs a) {
         }
         // ---- second child vector
         if (op.s1 >= 0) {
-            const int code = codes[(size_t)op.s1 * a.site_stride + cs];
+            const int code = codes[(size_t)op.s1 * a.site_stride + cs] & (kCodes - 1);
 #pragma unroll
             for (int k = 0; k < CM; ++k)
                 if (k < C) {
@@ -546,7 +546,8 @@ __device__ __forceinline__ void child_vec_generic(const GenericArgs& g, int v, i
     const PruneArgs& a = g.a;
     const int S = g.S, C = a.C;
     if (v < g.n_tips) {
-        const int code = a.codes[(size_t)v * a.site_stride + cs];
+        int code = a.codes[(size_t)v * a.site_stride + cs];
+        if (S <= 4) code &= (1 << S) - 1;  // state sets (a streamed alignment's codes are the caller's bytes)
         const T* tv = static_cast<const T*>(a.tipT) + (((size_t)v * C + k) * a.n_codes + code) * S;
         for (int i = 0; i < S; ++i) out[i] = tv[i];
         return;
@@ -970,7 +971,8 @@ __global__ void __launch_bounds__(128) preorder_kernel(PreorderArgs a) {
                 for (int s = 0; s < S; ++s) o[s] = (r == a.n_int - 1) ? (T)a.root_w[s] : ou[s];
                 if (w >= 0) {
                     if (w < a.n_tips) {
-                        const int code = a.codes[(size_t)w * a.site_stride + site];
+                        int code = a.codes[(size_t)w * a.site_stride + site];
+                        if (S <= 4) code &= (1 << S) - 1;  // state sets (streamed codes are the caller's bytes)
                         const T* tv = tipT + (((size_t)w * C + k) * a.n_codes + code) * S;
                         for (int i = 0; i < S; ++i) dw[i] = tv[i];
                     } else {

@@ -524,3 +524,28 @@ def test_streamed_arrival_wait_times_out_and_the_handle_recovers(monkeypatch):
         assert err.value.status == plk.PLK_ERR_NUMERIC
         assert time.perf_counter() - t0 < 120.0
         assert h.loglik(plk.PLK_FP32S) == good
+
+
+def test_streamed_masks_with_bits_past_the_alphabet():
+    """Bits past the 4 states in a byte mask mean nothing (the encoded path
+    drops them), but a streamed alignment's codes are the caller's bytes, so
+    every reader masks them: the FP32 and FP64 lnL, the per-site values and
+    the node states (post-order FP64 and the pre-order marginals) carry the
+    bits of the 32-bit path."""
+    rng = np.random.default_rng(34)
+    left, right, bl, masks, Q, f, cr, cw = _random_case(rng, 30, 17000, C=4)
+    out = []
+    for m in (masks.astype(np.uint32), (masks.astype(np.uint8) | np.uint8(0xF0))):
+        with _engine(left, right, bl, m, 4, Q, f, cr, cw) as h:
+            r = [h.loglik(plk.PLK_FP32S)]
+            h.set_alignment(m, 4)  # streamed again (the first evaluation tuned the form)
+            r.append(h.loglik(plk.PLK_FP32S))
+            r.append(h.site_loglik())
+            r.append(h.loglik(plk.PLK_FP64))
+            r.append(h.node_states(plk.PLK_NODES_COND, plk.PLK_FP64))
+            r.append(h.node_states(plk.PLK_NODES_MARGINAL, plk.PLK_FP64))
+            out.append(r)
+    a, b = out
+    assert a[0] == b[0] and a[1] == b[1] and a[3] == b[3]
+    for x, y in zip(a[2:], b[2:]):
+        np.testing.assert_array_equal(x, y)
