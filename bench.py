@@ -213,6 +213,18 @@ def measure_fp32_peak(device: int):
     return best
 
 
+def measure_fp64_peak(device: int):
+    """The FP64 multiply-add rate of this GPU, measured by the library's
+    microbenchmark (fma.rn.f64 chains over 4 CTAs per SM, CUDA events):
+    TFLOP/s, or None when it fails."""
+    import ctypes
+    from phylommand_gb300 import plk
+    t, ms = ctypes.c_double(), ctypes.c_double()
+    if plk.lib().plk_measure_fp32_peak(device, 2, 1 << 10, ctypes.byref(t), ctypes.byref(ms)) == 0:
+        return t.value
+    return None
+
+
 def required_bytes(w, C: int, grid_blocks: int) -> int:
     """Bytes one fused post-order pass must move through HBM: the 1-byte tip
     codes (rows padded to 16 bytes), the paired P(t) and tip tables it reads,
@@ -290,9 +302,15 @@ def run_ours(args, world, rank, local):
         h.loglik_async(plk.PLK_FP64)
     h.loglik_result()
     steps64 = max(3, args.steps // 2)
+    # (the engine's per-kernel events are on here: about 2 us each against a
+    # 4 ms step)
+    h.set_profiling(True)
     ms64 = reduce_max(world, time_steps(h, stream, flush, steps64, plk.PLK_FP64), dev)
+    kern64, n64 = h.kernel_times(reset=True)
+    h.set_profiling(False)
     lnl64_timed = h.loglik_result()
     value64 = world * steps64 / (ms64 / 1e3)
+    fp64_peak = measure_fp64_peak(local)
 
     # end to end through the C ABI with host buffers: upload the alignment,
     # tree and model from pinned host memory, evaluate, read the lnL back
@@ -403,6 +421,8 @@ def run_ours(args, world, rank, local):
     hbm_peak, _, peak_src = load_peaks()
     flops_per_launch = algorithmic_flops_per_site(w.n_tips, w.n_states, C) * w.n_sites
     prune_ms = kern_ms[1] / max(n_evals, 1)
+    post64_ms = kern64[1] / max(n64, 1)
+    fp64_achieved = flops_per_launch / (post64_ms / 1e3) / 1e12
     grid = (w.n_sites + 127) // 128
     req = required_bytes(w, C, grid)
     fp32_achieved = flops_per_launch / (prune_ms / 1e3) / 1e12
@@ -444,7 +464,15 @@ def run_ours(args, world, rank, local):
                           "peak_source": "measured: plk_measure_fp32_peak (fma.rn.f32x2 and fma.rn.f32 chains, "
                                          "4 CTAs per SM, CUDA events), the larger"},
         "fp64_plain_form": {"value": value64, "unit": "evals/s", "ms_per_step": ms64 / steps64, "steps": steps64,
-                            "e2e": e2e64_value},
+                            "e2e": e2e64_value, "postorder_ms": post64_ms,
+                            "roofline_fp64": {
+                                "bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                                "frac": (fp64_achieved / fp64_peak) if fp64_peak else None,
+                                "peak_source": "measured: plk_measure_fp32_peak(packed = 2), fma.rn.f64 chains over "
+                                               "4 CTAs per SM, CUDA events",
+                                "note": "the plain form multiplies and adds separately in the reference's operation "
+                                        "order, one FP64 instruction per flop, so the FP64 issue rate caps it at half "
+                                        "of this FMA peak"}},
         "cpu_baseline": {"value": cpu_value, "unit": "evals/s", "cores": 1, "kind": "port",
                          "sample": f"{sample} of {w.n_sites} sites, P(t) rebuilt per (site, edge, category) by the "
                                    f"reference's Taylor-plus-20-squarings, scaled linearly to all sites"},

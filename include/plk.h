@@ -472,10 +472,11 @@ plk_status plk_effective_lengths(int n_nodes, const int* left, const int* right,
  * No counterpart in the reference (which has no GPU path).  Measures the FP32
  * multiply-add rate of `device`: every thread of a grid of 4 CTAs per SM runs
  * independent fma.rn.f32 chains (packed = 0) or fma.rn.f32x2 chains
- * (packed = 1) for `iters` iterations of 64 lane-FMAs, timed with CUDA events
- * after a warm-up launch.  Writes TFLOP/s (2 flops per lane-FMA) and the
- * launch time in ms (ms_out may be NULL).  1 <= iters <= 2^24.  The
- * post-order passes' FP32 roofline is quoted against this number. */
+ * (packed = 1), or fma.rn.f64 chains (packed = 2: the FP64 rate), for
+ * `iters` iterations of 64 lane-FMAs, timed with CUDA events after a warm-up
+ * launch.  Writes TFLOP/s (2 flops per lane-FMA) and the launch time in ms
+ * (ms_out may be NULL).  1 <= iters <= 2^24.  The post-order passes' FP32
+ * roofline, and the FP64 plain form's, are quoted against these numbers. */
 plk_status plk_measure_fp32_peak(int device, int packed, int iters, double* tflops_out, double* ms_out);
 
 /* ---- allocation-free entry point ----------------------------------------------

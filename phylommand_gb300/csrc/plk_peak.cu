@@ -1,5 +1,6 @@
 // plk_measure_fp32_peak: the FP32 multiply-add rate this GPU sustains, the
-// denominator of the post-order passes' FP32 roofline.
+// denominator of the post-order passes' FP32 roofline (packed = 2: the FP64
+// rate, the denominator of the FP64 plain form's).
 //
 // Every thread runs kChains independent multiply-add chains (enough to cover
 // the pipe latency with a few warps per scheduler), either as scalar
@@ -70,10 +71,29 @@ __global__ void __launch_bounds__(kPeakThreads) fp32_peak_kernel(int iters, floa
     }
 }
 
+// FP64 multiply-adds: 2 kChains independent fma.rn.f64 chains per thread,
+// the lane-FMA count per iteration of the FP32 forms
+__global__ void __launch_bounds__(kPeakThreads) fp64_peak_kernel(int iters, double b, double c, double* sink,
+                                                                 int flag) {
+    double a[2 * kChains];
+#pragma unroll
+    for (int k = 0; k < 2 * kChains; ++k) a[k] = (double)(threadIdx.x + k);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int k = 0; k < 2 * kChains; ++k) a[k] = __fma_rn(a[k], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 2 * kChains; ++k) s += a[k];
+    if (flag == 12345) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 
 extern "C" plk_status plk_measure_fp32_peak(int device, int packed, int iters, double* tflops_out, double* ms_out) {
-    if (tflops_out == nullptr || iters < 1 || iters > (1 << 24))
+    if (tflops_out == nullptr || iters < 1 || iters > (1 << 24) || packed < 0 || packed > 2)
         return plk::report_error(PLK_ERR_ARG, "plk_measure_fp32_peak: bad arguments");
     int n_dev = 0;
     if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev == 0)
@@ -90,7 +110,8 @@ extern "C" plk_status plk_measure_fp32_peak(int device, int packed, int iters, d
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     auto launch = [&](int n) {
-        if (packed) fp32_peak_kernel<true><<<blocks, kPeakThreads, 0, st>>>(n, 0.999f, 1e-3f, nullptr, 0);
+        if (packed == 2) fp64_peak_kernel<<<blocks, kPeakThreads, 0, st>>>(n, 0.999, 1e-3, nullptr, 0);
+        else if (packed) fp32_peak_kernel<true><<<blocks, kPeakThreads, 0, st>>>(n, 0.999f, 1e-3f, nullptr, 0);
         else fp32_peak_kernel<false><<<blocks, kPeakThreads, 0, st>>>(n, 0.999f, 1e-3f, nullptr, 0);
     };
     launch(iters / 8 + 1);  // warm-up
