@@ -519,6 +519,7 @@ def run_protein(args):
     flops_per_eval = algorithmic_flops_per_site(w.n_tips, S, C) * w.n_sites
     hbm_peak, bf16_peak, peak_src = load_peaks()
     fp32_peak = measure_fp32_peak(0)
+    fp64_peak = measure_fp64_peak(0)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
     res = {}
@@ -567,6 +568,7 @@ def run_protein(args):
                       "achieved_tflops": tflops,
                       "frac_of_fp32_peak": tflops / fp32_peak if fp32_peak else None,
                       "frac_of_bf16_dense_peak": tflops / bf16_peak,
+                      "frac_of_fp64_peak": (tflops / fp64_peak) if (v == "fp64" and fp64_peak) else None,
                       "rel_err_vs_fp64_oracle": abs(lnl - orc.lnl) / abs(orc.lnl),
                       "abs_err_vs_fp64_oracle": abs(lnl - orc.lnl)}
             if v == "auto":
