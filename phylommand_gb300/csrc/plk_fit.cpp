@@ -2,7 +2,7 @@
 //
 // The reference maximises lnL with NLopt's LN_NELDERMEAD and no stopping
 // criteria (src/treeator.cpp:791-805, objective opt_function at :1122-1129).
-// NLopt is not part of this build; NelderMead below is written from Nelder &
+// libplk does not link NLopt; NelderMead below is written from Nelder &
 // Mead (1965), "A simplex method for function minimization", with the usual
 // coefficients (reflection 1, expansion 2, contraction 1/2, shrink 1/2) and
 // explicit stopping rules.  It is a state machine that asks for one point at
