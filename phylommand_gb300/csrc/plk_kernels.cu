@@ -256,7 +256,25 @@ __global__ void __launch_bounds__(128) pmat4_eigen_kernel(DeviceModel m) {
         m.P32[base + j] = (float)p[j];
         if (m.P32p) m.P32p[(size_t)v * m.C * 16 + paired_p_index(k, r, j)] = (float)p[j];
     }
-    if (v < m.n_tips) {
+    if (v < m.n_tips && m.code_mask == nullptr && m.n_codes == kCodes) {
+        // the 16 state sets themselves as codes: every mask known at compile
+        // time, so the 16 sums are straight-line and independent
+        const size_t tb = (size_t)it * kCodes * 4;
+#pragma unroll
+        for (int c = 0; c < kCodes; ++c) {
+            double acc = 0.0;
+            bool first = true;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if ((c >> j) & 1) {
+                    acc = first ? p[j] : __dadd_rn(acc, p[j]);
+                    first = false;
+                }
+            m.tip64[tb + (size_t)c * 4 + r] = acc;
+            m.tip32[tb + (size_t)c * 4 + r] = (float)acc;
+            if (m.tip32p) m.tip32p[(size_t)v * m.C * kCodes * 4 + paired_tip_index(k, c, r)] = (float)acc;
+        }
+    } else if (v < m.n_tips) {
         const size_t tb = (size_t)it * m.n_codes * 4;
         for (int c = 0; c < m.n_codes; ++c) {
             const uint32_t mask = m.code_mask ? m.code_mask[c] : (uint32_t)c;
